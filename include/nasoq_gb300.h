@@ -1,0 +1,156 @@
+/*
+ * nasoq_gb300.h -- C ABI of the GB300 supernodal LDL^T (Bunch-Kaufman)
+ * factorization, supernodal solves and GMRES refinement.
+ *
+ * Plain pointers and sizes only.  Host buffers stay owned by the caller;
+ * device memory is owned by the plan.  Every function returns an int status
+ * (NQG_OK == 0; negative values are errors, positive values are warnings),
+ * mirroring the int returns of the reference API instead of exceptions.
+ *
+ * The C++ drop-in classes nasoq::SolverSettings and nasoq::Nasoq
+ * (include/nasoq/QP/linear_solver_wrapper.h, include/nasoq/nasoq.h) are
+ * implemented on top of these entry points.
+ */
+#ifndef NASOQ_GB300_H
+#define NASOQ_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define NQG_OK 0
+#define NQG_WARN_ZERO_PIVOT 1     /* factor finished; a pivot block was exactly singular */
+#define NQG_WARN_NONFINITE 2      /* factor finished; a non-finite value appeared */
+#define NQG_ERR_ARG (-1)          /* invalid argument */
+#define NQG_ERR_CUDA (-2)         /* a CUDA call failed (no device, out of memory, ...) */
+#define NQG_ERR_SYMBOLIC (-3)     /* ordering / supernode analysis failed */
+#define NQG_ERR_STATE (-4)        /* call out of order (e.g. solve before factor) */
+#define NQG_ERR_TIMEOUT (-5)      /* a bounded device-side wait gave up */
+#define NQG_ERR_SIZE (-6)         /* problem exceeds a fixed capacity */
+
+#define NQG_FP64 0                /* factor stored and computed in FP64 */
+#define NQG_FP32 1                /* factor in FP32, refinement residuals in FP64 */
+
+typedef struct nqg_settings {
+  int precision;        /* NQG_FP64 or NQG_FP32 */
+  int req_ref_iter;     /* GMRES restarts (reference SolverSettings::req_ref_iter) */
+  int max_inner_iter;   /* GMRES inner steps (reference max_inner_iter) */
+  double tol_abs;       /* GMRES absolute tolerance (reference tol_abs) */
+  double tol_rel;       /* GMRES relative tolerance (reference tol_rel) */
+  double reg_diag;      /* diagonal perturbation (reference reg_diag) */
+  int regularization;   /* 1: |a_jj| < reg_diag -> a_jj = reg_diag (reference find_perturbation) */
+  int n_relax[3];       /* supernode relaxation (reference n_relax) */
+  double z_relax[3];    /* supernode relaxation (reference z_relax) */
+} nqg_settings;
+
+/* Reference defaults (src/QP/linear_solver_wrapper.cpp:205-244). */
+void nqg_default_settings(nqg_settings *s);
+
+/* Human-readable text of a status code. */
+const char *nqg_status_str(int status);
+
+/* ---- symbolic analysis (host only, no GPU needed) ----------------------- */
+typedef struct nqg_symbolic nqg_symbolic;
+
+typedef struct nqg_symbolic_info {
+  int n, nsuper, max_sup_wid, max_col;
+  int64_t ssize;        /* length of the row-list array */
+  int64_t xsize;        /* number of factor values */
+  double metis_seconds, total_seconds;
+} nqg_symbolic_info;
+
+/* Replaces symbolic_analysis_lin_solve (src/symbolic/symbolic_phase.cpp:167)
+ * as called by SolverSettings::symbolic_analysis
+ * (src/QP/linear_solver_wrapper.cpp:396-536): METIS ordering, etree,
+ * column counts, weighted postorder, relaxed supernodes, supernodal row
+ * structure.  A is lower-stored CSC (sorted, diagonal first).  extra_cols
+ * (nullable, n ints) flags columns kept as single-column supernodes. */
+int nqg_symbolic_create(int n, const int *Ap, const int *Ai, const int *extra_cols, const int n_relax[3],
+                        const double z_relax[3], nqg_symbolic **out);
+int nqg_symbolic_get_info(const nqg_symbolic *sym, nqg_symbolic_info *info);
+/* Copies the arrays out (any pointer may be NULL).  Sizes: perm, iperm,
+ * parent, colcount, col2sup, extra_cols: n; super: nsuper+1; sparent: nsuper;
+ * lpi: nsuper+1 (row-list start per supernode); ls: ssize; colp: n+1 (value
+ * offset per column, reference L->p). */
+int nqg_symbolic_export(const nqg_symbolic *sym, int *perm, int *iperm, int *parent, int *colcount, int *super,
+                        int *sparent, int *col2sup, int64_t *lpi, int *ls, int64_t *colp, int *extra_cols);
+void nqg_symbolic_destroy(nqg_symbolic *sym);
+
+/* ---- numeric plan (GPU) -------------------------------------------------- */
+typedef struct nqg_plan nqg_plan;
+
+typedef struct nqg_timings {
+  double factor_ms, solve_ms, refine_ms;  /* last call, device time */
+  int num_ref_iter;                        /* Arnoldi steps of the last refinement */
+  int num_pivot_supernodes;                /* supernodes whose columns BK permuted */
+  int num_2x2;                             /* 2x2 pivot blocks in the factor */
+  double last_residual;                    /* preconditioned residual norm at exit */
+} nqg_timings;
+
+/* Symbolic analysis + device upload of the matrix (replaces
+ * SolverSettings::symbolic_analysis, src/QP/linear_solver_wrapper.cpp:396).
+ * A: lower CSC, n columns, values Ax; the perturbation rule of the settings
+ * is applied to a private copy.  Allocates all device memory of the plan. */
+int nqg_plan_create(int n, const int *Ap, const int *Ai, const double *Ax, const int *extra_cols,
+                    const nqg_settings *settings, nqg_plan **out);
+int nqg_plan_destroy(nqg_plan *plan);
+/* Work on the given CUDA stream (cudaStream_t passed as void*; NULL = the
+ * plan's own stream). */
+int nqg_set_stream(nqg_plan *plan, void *stream);
+int nqg_get_symbolic(const nqg_plan *plan, const nqg_symbolic **sym);
+
+/* Replace all matrix values (same pattern as at creation); host buffer.
+ * The perturbation rule is re-applied. */
+int nqg_set_values(nqg_plan *plan, const double *Ax);
+/* Overwrite `count` entries of the CSC value array (indices into Ax) in both
+ * the factorization and the refinement copies of the matrix (the edit that
+ * SolverSettings::add_del_matrix_qp applies to A_ord,
+ * src/QP/linear_solver_wrapper.cpp:1020-1137). */
+int nqg_edit_values(nqg_plan *plan, int count, const int64_t *idx, const double *vals);
+
+/* Full numeric factorization (replaces ldl_left_sn_02_v2,
+ * src/ldl/Serial_blocked_ldl_02_2.cpp:18-183, and the reorder_matrix that
+ * follows it, src/QP/linear_solver_wrapper.cpp:1432-1460). */
+int nqg_factor(nqg_plan *plan);
+/* Partial refactorization of `count` supernodes, which must be closed under
+ * "ancestor of a listed supernode" as the SoMod marking produces (replaces
+ * update_ldl_left_sn_02_v2, src/ldl/Serial_update_ldl.cpp:18-277). */
+int nqg_refactor(nqg_plan *plan, int count, const int *snodes);
+
+/* Visibility masks for the masked solve of the QP mode (reference
+ * visible_sn / extra_cols as passed to
+ * solve_phase_ldl_blocked_parallel_permuted_update, src/linear_solver/
+ * solve_phase.cpp:133-161).  NULL = everything visible. */
+int nqg_set_visibility(nqg_plan *plan, const uint8_t *visible_sn, const uint8_t *hidden_col);
+
+/* Solve K x = rhs with host buffers: permute, supernodal forward / diagonal /
+ * backward solve, then GMRES refinement on the unperturbed matrix, unpermute
+ * (replaces SolverSettings::solve_only, src/QP/linear_solver_wrapper.cpp:
+ * 1300-1404, with pmgmres_ldlt_auto(_update), src/gmres/mgmres.cpp:1015-1421). */
+int nqg_solve(nqg_plan *plan, const double *rhs, double *x);
+/* Same with device buffers (n doubles each, may alias). */
+int nqg_solve_device(nqg_plan *plan, const double *d_rhs, double *d_x);
+/* Only the LDL^T solve of an ordered vector in place on the device
+ * (reference solve_phase_ldl_blocked_parallel, src/linear_solver/
+ * solve_phase.cpp:88-111). */
+int nqg_ldlt_solve_ordered_device(nqg_plan *plan, double *d_x_ord);
+/* y = K x in the original ordering with the unperturbed matrix, device
+ * buffers (reference spmv_csc_sym_one_int, src/matrixVector/spmv_CSC.cpp:26). */
+int nqg_spmv_device(nqg_plan *plan, const double *d_x, double *d_y);
+
+int nqg_get_timings(const nqg_plan *plan, nqg_timings *t);
+/* Copies the current factor to host buffers (any may be NULL): values
+ * (xsize doubles), d (2n: diagonal, then 2x2 sub-diagonals), perm (n, the
+ * combined fill-reducing + pivoting permutation), ls (ssize, row lists after
+ * pivoting). */
+int nqg_get_factor(const nqg_plan *plan, double *values, double *d, int *perm, int *ls);
+/* Device error word of the last factor/solve (bit flags, 0 = clean). */
+int nqg_get_device_status(const nqg_plan *plan, int *status_bits);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

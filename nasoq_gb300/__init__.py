@@ -1,0 +1,239 @@
+"""nasoq_gb300: supernodal Bunch-Kaufman LDL^T, supernodal solves and GMRES
+refinement for sparse symmetric-indefinite (KKT) systems on one GB300 GPU.
+
+This module is a thin ctypes binding of the C ABI in include/nasoq_gb300.h
+(built in-tree as nasoq_gb300/libnasoq_gb300.so by nasoq_gb300.build).  There
+is no CPU fallback: every numeric call runs the CUDA kernels, and importing
+the binding without the built library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnasoq_gb300.so")
+
+NQG_OK = 0
+NQG_FP64 = 0
+NQG_FP32 = 1
+
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+
+
+class Settings(C.Structure):
+    _fields_ = [("precision", C.c_int), ("req_ref_iter", C.c_int), ("max_inner_iter", C.c_int),
+                ("tol_abs", C.c_double), ("tol_rel", C.c_double), ("reg_diag", C.c_double),
+                ("regularization", C.c_int), ("n_relax", C.c_int * 3), ("z_relax", C.c_double * 3)]
+
+
+class SymbolicInfo(C.Structure):
+    _fields_ = [("n", C.c_int), ("nsuper", C.c_int), ("max_sup_wid", C.c_int), ("max_col", C.c_int),
+                ("ssize", C.c_int64), ("xsize", C.c_int64), ("metis_seconds", C.c_double),
+                ("total_seconds", C.c_double)]
+
+
+class Timings(C.Structure):
+    _fields_ = [("factor_ms", C.c_double), ("solve_ms", C.c_double), ("refine_ms", C.c_double),
+                ("num_ref_iter", C.c_int), ("num_pivot_supernodes", C.c_int), ("num_2x2", C.c_int),
+                ("last_residual", C.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libnasoq_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run `python -m nasoq_gb300.build` first")
+    L = C.CDLL(LIB_PATH)
+    L.nqg_default_settings.argtypes = [C.POINTER(Settings)]
+    L.nqg_default_settings.restype = None
+    L.nqg_status_str.argtypes = [C.c_int]
+    L.nqg_status_str.restype = C.c_char_p
+    L.nqg_symbolic_create.argtypes = [C.c_int, _i32p, _i32p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.POINTER(C.c_void_p)]
+    L.nqg_symbolic_get_info.argtypes = [C.c_void_p, C.POINTER(SymbolicInfo)]
+    L.nqg_symbolic_export.argtypes = [C.c_void_p] + [C.c_void_p] * 11
+    L.nqg_symbolic_destroy.argtypes = [C.c_void_p]
+    L.nqg_symbolic_destroy.restype = None
+    L.nqg_plan_create.argtypes = [C.c_int, _i32p, _i32p, _f64p, C.c_void_p, C.POINTER(Settings),
+                                  C.POINTER(C.c_void_p)]
+    L.nqg_plan_destroy.argtypes = [C.c_void_p]
+    L.nqg_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+    L.nqg_get_symbolic.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+    L.nqg_set_values.argtypes = [C.c_void_p, _f64p]
+    L.nqg_edit_values.argtypes = [C.c_void_p, C.c_int, _i64p, _f64p]
+    L.nqg_factor.argtypes = [C.c_void_p]
+    L.nqg_refactor.argtypes = [C.c_void_p, C.c_int, _i32p]
+    L.nqg_set_visibility.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.nqg_solve.argtypes = [C.c_void_p, _f64p, _f64p]
+    L.nqg_solve_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.nqg_ldlt_solve_ordered_device.argtypes = [C.c_void_p, C.c_void_p]
+    L.nqg_spmv_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.nqg_get_timings.argtypes = [C.c_void_p, C.POINTER(Timings)]
+    L.nqg_get_factor.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.nqg_get_device_status.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
+    _lib = L
+    return L
+
+
+class NasoqError(RuntimeError):
+    pass
+
+
+def _check(rc, what):
+    if rc < 0:
+        raise NasoqError(f"{what}: {lib().nqg_status_str(rc).decode()} ({rc})")
+    return rc
+
+
+def default_settings(**kw) -> Settings:
+    s = Settings()
+    lib().nqg_default_settings(C.byref(s))
+    for k, v in kw.items():
+        if k in ("n_relax", "z_relax"):
+            getattr(s, k)[:] = v
+        else:
+            setattr(s, k, v)
+    return s
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class Symbolic:
+    """Host symbolic analysis (no GPU needed)."""
+
+    def __init__(self, n, Ap, Ai, extra_cols=None, n_relax=(4, 16, 48), z_relax=(0.8, 0.1, 0.05)):
+        L = lib()
+        Ap = np.ascontiguousarray(Ap, np.int32)
+        Ai = np.ascontiguousarray(Ai, np.int32)
+        ex = None if extra_cols is None else np.ascontiguousarray(extra_cols, np.int32)
+        nr = (C.c_int * 3)(*n_relax)
+        zr = (C.c_double * 3)(*z_relax)
+        h = C.c_void_p()
+        _check(L.nqg_symbolic_create(int(n), Ap, Ai, _ptr(ex), C.cast(nr, C.c_void_p), C.cast(zr, C.c_void_p),
+                                     C.byref(h)), "symbolic analysis")
+        self._h = h
+        self._own = True
+        self._load()
+
+    @classmethod
+    def _wrap(cls, handle):
+        self = cls.__new__(cls)
+        self._h = handle
+        self._own = False
+        self._load()
+        return self
+
+    def _load(self):
+        L = lib()
+        info = SymbolicInfo()
+        L.nqg_symbolic_get_info(self._h, C.byref(info))
+        self.info = info
+        n, ns = info.n, info.nsuper
+        a = {k: np.zeros(n, np.int32) for k in ("perm", "iperm", "parent", "colcount", "col2sup", "extra_cols")}
+        a["super"] = np.zeros(ns + 1, np.int32)
+        a["sparent"] = np.zeros(ns, np.int32)
+        a["lpi"] = np.zeros(ns + 1, np.int64)
+        a["ls"] = np.zeros(max(info.ssize, 1), np.int32)
+        a["colp"] = np.zeros(n + 1, np.int64)
+        L.nqg_symbolic_export(self._h, *[_ptr(a[k]) for k in ("perm", "iperm", "parent", "colcount", "super",
+                                                              "sparent", "col2sup", "lpi", "ls", "colp",
+                                                              "extra_cols")])
+        a["ls"] = a["ls"][:info.ssize]
+        self.__dict__.update(a)
+
+    def __del__(self):
+        if getattr(self, "_own", False) and getattr(self, "_h", None):
+            lib().nqg_symbolic_destroy(self._h)
+            self._h = None
+
+
+class Plan:
+    """A factorization plan on the GPU (symbolic analysis + device buffers)."""
+
+    def __init__(self, n, Ap, Ai, Ax, extra_cols=None, settings: Settings | None = None, **kw):
+        L = lib()
+        self.n = int(n)
+        self.Ap = np.ascontiguousarray(Ap, np.int32)
+        self.Ai = np.ascontiguousarray(Ai, np.int32)
+        Ax = np.ascontiguousarray(Ax, np.float64)
+        ex = None if extra_cols is None else np.ascontiguousarray(extra_cols, np.int32)
+        self.settings = settings if settings is not None else default_settings(**kw)
+        h = C.c_void_p()
+        _check(L.nqg_plan_create(self.n, self.Ap, self.Ai, Ax, _ptr(ex), C.byref(self.settings), C.byref(h)),
+               "plan create")
+        self._h = h
+        sh = C.c_void_p()
+        L.nqg_get_symbolic(h, C.byref(sh))
+        self.symbolic = Symbolic._wrap(sh)
+
+    def factor(self):
+        return _check(lib().nqg_factor(self._h), "factor")
+
+    def refactor(self, snodes):
+        sn = np.ascontiguousarray(snodes, np.int32)
+        return _check(lib().nqg_refactor(self._h, len(sn), sn), "refactor")
+
+    def set_values(self, Ax):
+        _check(lib().nqg_set_values(self._h, np.ascontiguousarray(Ax, np.float64)), "set values")
+
+    def edit_values(self, idx, vals):
+        idx = np.ascontiguousarray(idx, np.int64)
+        vals = np.ascontiguousarray(vals, np.float64)
+        _check(lib().nqg_edit_values(self._h, len(idx), idx, vals), "edit values")
+
+    def set_visibility(self, visible_sn=None, hidden_col=None):
+        v = None if visible_sn is None else np.ascontiguousarray(visible_sn, np.uint8)
+        hd = None if hidden_col is None else np.ascontiguousarray(hidden_col, np.uint8)
+        _check(lib().nqg_set_visibility(self._h, _ptr(v), _ptr(hd)), "set visibility")
+
+    def solve(self, rhs):
+        rhs = np.ascontiguousarray(rhs, np.float64)
+        x = np.empty(self.n, np.float64)
+        _check(lib().nqg_solve(self._h, rhs, x), "solve")
+        return x
+
+    def solve_device(self, d_rhs_ptr, d_x_ptr):
+        _check(lib().nqg_solve_device(self._h, C.c_void_p(d_rhs_ptr), C.c_void_p(d_x_ptr)), "solve")
+
+    def set_stream(self, stream_ptr):
+        _check(lib().nqg_set_stream(self._h, C.c_void_p(stream_ptr)), "set stream")
+
+    def timings(self) -> Timings:
+        t = Timings()
+        lib().nqg_get_timings(self._h, C.byref(t))
+        return t
+
+    def factor_arrays(self):
+        s = self.symbolic
+        vals = np.zeros(max(s.info.xsize, 1), np.float64)
+        d = np.zeros(2 * self.n, np.float64)
+        perm = np.zeros(self.n, np.int32)
+        ls = np.zeros(max(s.info.ssize, 1), np.int32)
+        _check(lib().nqg_get_factor(self._h, _ptr(vals), _ptr(d), _ptr(perm), _ptr(ls)), "get factor")
+        return vals[:s.info.xsize], d, perm, ls[:s.info.ssize]
+
+    def device_status(self):
+        v = C.c_int(0)
+        lib().nqg_get_device_status(self._h, C.byref(v))
+        return v.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().nqg_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

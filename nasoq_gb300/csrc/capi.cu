@@ -1,0 +1,579 @@
+// extern "C" entry points of include/nasoq_gb300.h: plan construction (host
+// symbolic analysis, level schedule, update work lists, device uploads) and
+// the factor / solve calls.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "plan.hpp"
+
+using namespace nqg;
+
+struct nqg_symbolic {
+  Symbolic sym;
+};
+struct nqg_plan {
+  Plan P;
+};
+
+extern "C" void nqg_default_settings(nqg_settings *s) {
+  if (!s) return;
+  s->precision = NQG_FP64;
+  s->req_ref_iter = 2;
+  s->max_inner_iter = 2;
+  s->tol_abs = 1e-15;
+  s->tol_rel = 1e-15;
+  s->reg_diag = 1e-8;
+  s->regularization = 1;
+  s->n_relax[0] = 4;
+  s->n_relax[1] = 16;
+  s->n_relax[2] = 48;
+  s->z_relax[0] = 0.8;
+  s->z_relax[1] = 0.1;
+  s->z_relax[2] = 0.05;
+}
+
+extern "C" const char *nqg_status_str(int st) {
+  switch (st) {
+    case NQG_OK: return "ok";
+    case NQG_WARN_ZERO_PIVOT: return "factorization met an exactly singular pivot block";
+    case NQG_WARN_NONFINITE: return "factorization produced a non-finite value";
+    case NQG_ERR_ARG: return "invalid argument";
+    case NQG_ERR_CUDA: return "CUDA error";
+    case NQG_ERR_SYMBOLIC: return "symbolic analysis failed";
+    case NQG_ERR_STATE: return "call out of order";
+    case NQG_ERR_TIMEOUT: return "device wait timed out";
+    case NQG_ERR_SIZE: return "problem exceeds a fixed capacity";
+    default: return "unknown status";
+  }
+}
+
+static bool check_lower_csc(int n, const int *Ap, const int *Ai) {
+  if (n < 0 || (n > 0 && (!Ap || !Ai))) return false;
+  if (n == 0) return true;
+  if (Ap[0] != 0) return false;
+  for (int j = 0; j < n; ++j) {
+    // every column stores its diagonal first (reference find_perturbation and
+    // set_diags address A->x[A->p[j]] as the diagonal)
+    if (Ap[j + 1] <= Ap[j] || Ai[Ap[j]] != j) return false;
+    for (int q = Ap[j]; q < Ap[j + 1]; ++q) {
+      if (Ai[q] < j || Ai[q] >= n) return false;
+      if (q > Ap[j] && Ai[q] <= Ai[q - 1]) return false;
+    }
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// symbolic only
+extern "C" int nqg_symbolic_create(int n, const int *Ap, const int *Ai, const int *extra_cols, const int n_relax[3],
+                                   const double z_relax[3], nqg_symbolic **out) {
+  if (!out || !check_lower_csc(n, Ap, Ai)) return NQG_ERR_ARG;
+  *out = nullptr;
+  Csc A;
+  A.n = n;
+  A.p.assign(Ap, Ap + n + 1);
+  A.i.assign(Ai, Ai + Ap[n]);
+  int nr[3] = {4, 16, 48};
+  double zr[3] = {0.8, 0.1, 0.05};
+  if (n_relax) std::copy(n_relax, n_relax + 3, nr);
+  if (z_relax) std::copy(z_relax, z_relax + 3, zr);
+  auto *h = new (std::nothrow) nqg_symbolic;
+  if (!h) return NQG_ERR_SIZE;
+  std::string err = analyze(A, extra_cols, nr, zr, h->sym);
+  if (!err.empty()) {
+    delete h;
+    return NQG_ERR_SYMBOLIC;
+  }
+  *out = h;
+  return NQG_OK;
+}
+
+static void fill_info(const Symbolic &S, nqg_symbolic_info *info) {
+  info->n = S.n;
+  info->nsuper = S.nsuper;
+  info->max_sup_wid = S.max_sup_wid;
+  info->max_col = S.max_col;
+  info->ssize = S.nsuper > 0 ? S.lpi[S.nsuper] : 0;
+  info->xsize = S.xsize;
+  info->metis_seconds = S.metis_seconds;
+  info->total_seconds = S.total_seconds;
+}
+
+extern "C" int nqg_symbolic_get_info(const nqg_symbolic *h, nqg_symbolic_info *info) {
+  if (!h || !info) return NQG_ERR_ARG;
+  fill_info(h->sym, info);
+  return NQG_OK;
+}
+
+static void export_sym(const Symbolic &S, int *perm, int *iperm, int *parent, int *colcount, int *super, int *sparent,
+                       int *col2sup, int64_t *lpi, int *ls, int64_t *colp, int *extra) {
+  const int n = S.n, ns = S.nsuper;
+  if (perm) std::copy(S.perm.begin(), S.perm.end(), perm);
+  if (iperm) std::copy(S.iperm.begin(), S.iperm.end(), iperm);
+  if (parent) std::copy(S.parent.begin(), S.parent.end(), parent);
+  if (colcount) std::copy(S.colcount.begin(), S.colcount.end(), colcount);
+  if (super) std::copy(S.super.begin(), S.super.begin() + ns + 1, super);
+  if (sparent) std::copy(S.sparent.begin(), S.sparent.end(), sparent);
+  if (col2sup) std::copy(S.col2sup.begin(), S.col2sup.end(), col2sup);
+  if (lpi) std::copy(S.lpi.begin(), S.lpi.end(), lpi);
+  if (ls && ns > 0) std::copy(S.ls.begin(), S.ls.begin() + S.lpi[ns], ls);
+  if (colp) std::copy(S.colp.begin(), S.colp.begin() + n + 1, colp);
+  if (extra) std::copy(S.extra_cols.begin(), S.extra_cols.end(), extra);
+}
+
+extern "C" int nqg_symbolic_export(const nqg_symbolic *h, int *perm, int *iperm, int *parent, int *colcount,
+                                   int *super, int *sparent, int *col2sup, int64_t *lpi, int *ls, int64_t *colp,
+                                   int *extra_cols) {
+  if (!h) return NQG_ERR_ARG;
+  export_sym(h->sym, perm, iperm, parent, colcount, super, sparent, col2sup, lpi, ls, colp, extra_cols);
+  return NQG_OK;
+}
+
+extern "C" void nqg_symbolic_destroy(nqg_symbolic *h) { delete h; }
+
+// ---------------------------------------------------------------------------
+// plan construction helpers
+
+// Supernode levels (leaves 0), descendant pairs from the elimination-tree
+// reach of every supernode, and the 64x64 update tiles of each pair.
+static void build_schedule(Plan &P) {
+  Symbolic &S = P.sym;
+  const int ns = S.nsuper;
+  P.level_of.assign(ns, 0);
+  int maxlev = 0;
+  for (int s = 0; s < ns; ++s) {
+    int p = S.sparent[s];
+    if (p >= 0) P.level_of[p] = std::max(P.level_of[p], P.level_of[s] + 1);
+    maxlev = std::max(maxlev, P.level_of[s]);
+  }
+  P.levels.assign(ns > 0 ? maxlev + 1 : 0, {});
+  for (int s = 0; s < ns; ++s) P.levels[P.level_of[s]].push_back(s);
+  P.level_off.assign(P.levels.size() + 1, 0);
+  for (size_t l = 0; l < P.levels.size(); ++l) P.level_off[l + 1] = P.level_off[l] + (int)P.levels[l].size();
+  // pairs
+  std::vector<int> mark(ns, 0), stack, lst;
+  P.pair_ptr.assign(ns + 1, 0);
+  P.pair_d.clear();
+  P.pair_lb.clear();
+  P.pair_ub.clear();
+  P.tile_ptr.assign(ns + 1, 0);
+  P.tiles.clear();
+  for (int s = 0; s < ns; ++s) {
+    ereach_sn(S, P.Uord, s, S.sparent, mark, stack, lst);
+    const int c1 = S.super[s], c2 = S.super[s + 1];
+    for (int d : lst) {
+      const int *rows = S.ls.data() + S.lpi[d];
+      const int nr = (int)(S.lpi[d + 1] - S.lpi[d]);
+      int lb = (int)(std::lower_bound(rows, rows + nr, c1) - rows);
+      int ub = (int)(std::lower_bound(rows, rows + nr, c2) - rows) - 1;
+      if (lb >= nr || ub < lb) continue;  // no overlap (cannot happen for a true reach)
+      P.pair_d.push_back(d);
+      P.pair_lb.push_back(lb);
+      P.pair_ub.push_back(ub);
+      for (int ri = lb; ri < nr; ri += UPD_TM)
+        for (int cj = lb; cj <= ub; cj += UPD_TN)
+          if (ri + UPD_TM - 1 >= cj) P.tiles.push_back(UpdTile{s, d, ri, cj, ub});
+    }
+    P.pair_ptr[s + 1] = (int)P.pair_d.size();
+    P.tile_ptr[s + 1] = (int64_t)P.tiles.size();
+  }
+}
+
+template <class T> static int dev_alloc_copy(Plan &P, T **dst, const T *src, size_t count) {
+  NQG_CUDA(cudaMalloc(dst, std::max<size_t>(count, 1) * sizeof(T)));
+  if (count) NQG_CUDA(cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice));
+  return NQG_OK;
+}
+
+// Full CSR (both triangles) of K with the refinement values; map_lo/map_hi
+// give, for every lower-CSC entry, its positions in the CSR (hi = -1 on the
+// diagonal).
+static void build_full_csr(const Csc &K, const std::vector<double> &xv, std::vector<int> &Rp, std::vector<int> &Rj,
+                           std::vector<double> &Rx, std::vector<int64_t> &mlo, std::vector<int64_t> &mhi) {
+  const int n = K.n;
+  Rp.assign(n + 1, 0);
+  for (int j = 0; j < n; ++j)
+    for (int q = K.p[j]; q < K.p[j + 1]; ++q) {
+      int i = K.i[q];
+      Rp[i + 1]++;
+      if (i != j) Rp[j + 1]++;
+    }
+  for (int i = 0; i < n; ++i) Rp[i + 1] += Rp[i];
+  Rj.resize(Rp[n]);
+  Rx.resize(Rp[n]);
+  mlo.assign(K.nnz(), -1);
+  mhi.assign(K.nnz(), -1);
+  std::vector<int> pos(Rp.begin(), Rp.end() - 1);
+  // entries of row i: columns j <= i come from column j (lower), in increasing j;
+  // columns j > i come from column i itself.  Visit columns in order.
+  for (int j = 0; j < n; ++j)
+    for (int q = K.p[j]; q < K.p[j + 1]; ++q) {
+      int i = K.i[q];
+      int t = pos[i]++;
+      Rj[t] = j;
+      Rx[t] = xv[q];
+      mlo[q] = t;
+    }
+  for (int j = 0; j < n; ++j)
+    for (int q = K.p[j]; q < K.p[j + 1]; ++q) {
+      int i = K.i[q];
+      if (i == j) continue;
+      int t = pos[j]++;
+      Rj[t] = i;
+      Rx[t] = xv[q];
+      mhi[q] = t;
+    }
+}
+
+static int upload_plan(Plan &P) {
+  Symbolic &S = P.sym;
+  const int n = P.n, ns = S.nsuper;
+  if (!P.own_stream) NQG_CUDA(cudaStreamCreateWithFlags(&P.own_stream, cudaStreamNonBlocking));
+  P.stream = P.own_stream;
+  NQG_CUDA(cudaEventCreate(&P.ev0));
+  NQG_CUDA(cudaEventCreate(&P.ev1));
+  int rc;
+  if ((rc = dev_alloc_copy(P, &P.d_super, S.super.data(), S.super.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_col2sup, S.col2sup.data(), S.col2sup.size()))) return rc;
+  P.ssize = ns > 0 ? S.lpi[ns] : 0;
+  if ((rc = dev_alloc_copy(P, &P.d_ls, S.ls.data(), (size_t)P.ssize))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_ls_sym, S.ls.data(), (size_t)P.ssize))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_lpi, S.lpi.data(), S.lpi.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_lpx, S.lpx.data(), S.lpx.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_Kp, P.K.p.data(), P.K.p.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_Ki, P.K.i.data(), P.K.i.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_Kx, P.K.x.data(), P.K.x.size()))) return rc;
+  std::vector<int> Rp, Rj;
+  std::vector<double> Rx;
+  std::vector<int64_t> mlo, mhi;
+  build_full_csr(P.K, P.Kx_spmv, Rp, Rj, Rx, mlo, mhi);
+  if ((rc = dev_alloc_copy(P, &P.d_Rp, Rp.data(), Rp.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_Rj, Rj.data(), Rj.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_Rx, Rx.data(), Rx.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_map_lo, mlo.data(), mlo.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_map_hi, mhi.data(), mhi.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_perm, S.perm.data(), S.perm.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_iperm, S.iperm.data(), S.iperm.size()))) return rc;
+  NQG_CUDA(cudaMalloc(&P.d_locperm, std::max(n, 1) * sizeof(int)));
+  NQG_CUDA(cudaMalloc(&P.d_perm_tmp, std::max(n, 1) * sizeof(int)));
+  NQG_CUDA(cudaMalloc(&P.d_L, (size_t)S.xsize * P.val_size()));
+  NQG_CUDA(cudaMalloc(&P.d_D, (size_t)std::max(2 * n, 2) * P.val_size()));
+  NQG_CUDA(cudaMemset(P.d_L, 0, (size_t)S.xsize * P.val_size()));
+  NQG_CUDA(cudaMemset(P.d_D, 0, (size_t)std::max(2 * n, 2) * P.val_size()));
+  if ((rc = dev_alloc_copy(P, &P.d_tiles, P.tiles.data(), P.tiles.size()))) return rc;
+  std::vector<int> ps(P.pair_d.size());
+  for (int s = 0; s < ns; ++s)
+    for (int q = P.pair_ptr[s]; q < P.pair_ptr[s + 1]; ++q) ps[q] = s;
+  if ((rc = dev_alloc_copy(P, &P.d_pair_s, ps.data(), ps.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_pair_d, P.pair_d.data(), P.pair_d.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_pair_lb, P.pair_lb.data(), P.pair_lb.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_pair_ub, P.pair_ub.data(), P.pair_ub.size()))) return rc;
+  std::vector<int> lvflat;
+  for (auto &lv : P.levels) lvflat.insert(lvflat.end(), lv.begin(), lv.end());
+  if ((rc = dev_alloc_copy(P, &P.d_targets_lv, lvflat.data(), lvflat.size()))) return rc;
+  NQG_CUDA(cudaMalloc(&P.d_pivoted, std::max(2 * ns, 2)));
+  NQG_CUDA(cudaMemset(P.d_pivoted, 0, std::max(2 * ns, 2)));
+  NQG_CUDA(cudaMalloc(&P.d_visible, std::max(ns, 1)));
+  NQG_CUDA(cudaMalloc(&P.d_hidden, std::max(n, 1)));
+  NQG_CUDA(cudaMalloc(&P.d_status, sizeof(int)));
+  NQG_CUDA(cudaMemset(P.d_status, 0, sizeof(int)));
+  P.mr_cap = std::max(P.set.max_inner_iter, 8);
+  const size_t nn = std::max(n, 1);
+  NQG_CUDA(cudaMalloc(&P.d_xo, nn * sizeof(double)));
+  NQG_CUDA(cudaMalloc(&P.d_bo, nn * sizeof(double)));
+  NQG_CUDA(cudaMalloc(&P.d_r, nn * sizeof(double)));
+  NQG_CUDA(cudaMalloc(&P.d_w, nn * sizeof(double)));
+  NQG_CUDA(cudaMalloc(&P.d_in, nn * sizeof(double)));
+  NQG_CUDA(cudaMalloc(&P.d_out, nn * sizeof(double)));
+  NQG_CUDA(cudaMalloc(&P.d_V, (size_t)(P.mr_cap + 1) * nn * sizeof(double)));
+  NQG_CUDA(cudaMalloc(&P.d_scal, (64 + 512) * sizeof(double)));
+  return NQG_OK;
+}
+
+static void free_plan(Plan &P) {
+  void *ptrs[] = {P.d_super, P.d_col2sup, P.d_ls, P.d_ls_sym, P.d_lpi, P.d_lpx, P.d_Kp, P.d_Ki, P.d_Kx,
+                  P.d_Rp, P.d_Rj, P.d_Rx, P.d_map_lo, P.d_map_hi, P.d_perm, P.d_iperm, P.d_locperm,
+                  P.d_perm_tmp, P.d_L, P.d_D, P.d_tiles, P.d_tile_list, P.d_targets, P.d_pair_s, P.d_pair_d,
+                  P.d_pair_lb, P.d_pair_ub, P.d_targets_lv, P.d_pivoted, P.d_visible, P.d_hidden, P.d_status,
+                  P.d_xo, P.d_bo, P.d_r, P.d_w, P.d_in, P.d_out, P.d_V, P.d_scal};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (P.ev0) cudaEventDestroy(P.ev0);
+  if (P.ev1) cudaEventDestroy(P.ev1);
+  if (P.own_stream) cudaStreamDestroy(P.own_stream);
+}
+
+// Perturbation of tiny diagonals (reference find_perturbation,
+// src/QP/linear_solver_wrapper.cpp:352-363): the factorization sees
+// reg_diag, the refinement matrix sees 0 there (set_diags(0), :1524-1533).
+static void apply_perturbation(Plan &P) {
+  P.pert_idx.clear();
+  P.Kx_spmv = P.K.x;
+  if (P.set.regularization != 1) return;
+  for (int j = 0; j < P.n; ++j) {
+    int q = P.K.p[j];
+    if (q >= P.K.p[j + 1]) continue;
+    if (std::abs(P.K.x[q]) < P.set.reg_diag) {
+      P.K.x[q] = P.set.reg_diag;
+      P.Kx_spmv[q] = 0.0;
+      P.pert_idx.push_back(q);
+    }
+  }
+}
+
+extern "C" int nqg_plan_create(int n, const int *Ap, const int *Ai, const double *Ax, const int *extra_cols,
+                               const nqg_settings *settings, nqg_plan **out) {
+  if (!out || !check_lower_csc(n, Ap, Ai) || (n > 0 && !Ax)) return NQG_ERR_ARG;
+  *out = nullptr;
+  auto *h = new (std::nothrow) nqg_plan;
+  if (!h) return NQG_ERR_SIZE;
+  Plan &P = h->P;
+  if (settings) P.set = *settings;
+  else nqg_default_settings(&P.set);
+  if (P.set.precision != NQG_FP64 && P.set.precision != NQG_FP32) {
+    delete h;
+    return NQG_ERR_ARG;
+  }
+  P.n = n;
+  P.K.n = n;
+  P.K.p.assign(Ap, Ap + n + 1);
+  P.K.i.assign(Ai, Ai + Ap[n]);
+  P.K.x.assign(Ax, Ax + Ap[n]);
+  apply_perturbation(P);
+  std::string err = analyze(P.K, extra_cols, P.set.n_relax, P.set.z_relax, P.sym);
+  if (!err.empty()) {
+    P.last_error = err;
+    delete h;
+    return NQG_ERR_SYMBOLIC;
+  }
+  {
+    Csc pat = P.K;
+    pat.x.clear();
+    sym_permute(pat, P.sym.iperm, nullptr, &P.Uord);
+  }
+  build_schedule(P);
+  int rc = upload_plan(P);
+  if (rc) {
+    free_plan(P);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return NQG_OK;
+}
+
+extern "C" int nqg_plan_destroy(nqg_plan *h) {
+  if (!h) return NQG_ERR_ARG;
+  free_plan(h->P);
+  delete h;
+  return NQG_OK;
+}
+
+extern "C" int nqg_set_stream(nqg_plan *h, void *stream) {
+  if (!h) return NQG_ERR_ARG;
+  h->P.stream = stream ? (cudaStream_t)stream : h->P.own_stream;
+  return NQG_OK;
+}
+
+extern "C" int nqg_get_symbolic(const nqg_plan *h, const nqg_symbolic **sym) {
+  if (!h || !sym) return NQG_ERR_ARG;
+  // nqg_symbolic is layout-compatible with its single Symbolic member
+  *sym = reinterpret_cast<const nqg_symbolic *>(&h->P.sym);
+  return NQG_OK;
+}
+
+extern "C" int nqg_set_values(nqg_plan *h, const double *Ax) {
+  if (!h || (!Ax && h->P.n > 0)) return NQG_ERR_ARG;
+  Plan &P = h->P;
+  P.K.x.assign(Ax, Ax + P.K.nnz());
+  apply_perturbation(P);
+  NQG_CUDA(cudaMemcpyAsync(P.d_Kx, P.K.x.data(), P.K.x.size() * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  std::vector<int> Rp, Rj;
+  std::vector<double> Rx;
+  std::vector<int64_t> mlo, mhi;
+  build_full_csr(P.K, P.Kx_spmv, Rp, Rj, Rx, mlo, mhi);
+  NQG_CUDA(cudaMemcpyAsync(P.d_Rx, Rx.data(), Rx.size() * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  NQG_CUDA(cudaStreamSynchronize(P.stream));
+  P.factored = false;
+  return NQG_OK;
+}
+
+namespace {
+__global__ void k_edit(int count, const int64_t *idx, const double *vals, const int64_t *mlo, const int64_t *mhi,
+                       double *Kx, double *Rx) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+    int64_t q = idx[t];
+    double v = vals[t];
+    Kx[q] = v;
+    Rx[mlo[q]] = v;
+    if (mhi[q] >= 0) Rx[mhi[q]] = v;
+  }
+}
+}  // namespace
+
+extern "C" int nqg_edit_values(nqg_plan *h, int count, const int64_t *idx, const double *vals) {
+  if (!h || count < 0 || (count > 0 && (!idx || !vals))) return NQG_ERR_ARG;
+  Plan &P = h->P;
+  if (count == 0) return NQG_OK;
+  std::vector<double> kv(count), rv(count);
+  for (int t = 0; t < count; ++t) {
+    if (idx[t] < 0 || idx[t] >= P.K.nnz()) return NQG_ERR_ARG;
+    P.K.x[idx[t]] = vals[t];
+    P.Kx_spmv[idx[t]] = vals[t];
+  }
+  // staging: indices then values in the refinement workspace
+  int64_t *d_idx = reinterpret_cast<int64_t *>(P.d_w);
+  double *d_vals = P.d_r;
+  if ((size_t)count > (size_t)std::max(P.n, 1)) return NQG_ERR_SIZE;
+  NQG_CUDA(cudaMemcpyAsync(d_idx, idx, count * sizeof(int64_t), cudaMemcpyHostToDevice, P.stream));
+  NQG_CUDA(cudaMemcpyAsync(d_vals, vals, count * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  k_edit<<<std::min((count + 255) / 256, 1024), 256, 0, P.stream>>>(count, d_idx, d_vals, P.d_map_lo, P.d_map_hi,
+                                                                     P.d_Kx, P.d_Rx);
+  NQG_CUDA(cudaGetLastError());
+  NQG_CUDA(cudaStreamSynchronize(P.stream));
+  return NQG_OK;
+}
+
+static int finish_factor(Plan &P) {
+  int st = 0;
+  NQG_CUDA(cudaMemcpyAsync(&st, P.d_status, sizeof(int), cudaMemcpyDeviceToHost, P.stream));
+  NQG_CUDA(cudaStreamSynchronize(P.stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, P.ev0, P.ev1);
+  P.tm.factor_ms = ms;
+  if (st & ST_BOUNDS) {
+    P.last_error = "device index check failed during factorization";
+    return NQG_ERR_STATE;
+  }
+  if (st & ST_TIMEOUT) return NQG_ERR_TIMEOUT;
+  P.factored = true;
+  if (st & ST_NONFINITE) return NQG_WARN_NONFINITE;
+  if (st & ST_ZERO_PIVOT) return NQG_WARN_ZERO_PIVOT;
+  return NQG_OK;
+}
+
+extern "C" int nqg_factor(nqg_plan *h) {
+  if (!h) return NQG_ERR_ARG;
+  Plan &P = h->P;
+  NQG_CUDA(cudaMemsetAsync(P.d_status, 0, sizeof(int), P.stream));
+  NQG_CUDA(cudaEventRecord(P.ev0, P.stream));
+  int rc = dev_factor(P, nullptr);
+  if (rc < 0) return rc;
+  NQG_CUDA(cudaEventRecord(P.ev1, P.stream));
+  return finish_factor(P);
+}
+
+extern "C" int nqg_refactor(nqg_plan *h, int count, const int *snodes) {
+  if (!h || count < 0 || (count > 0 && !snodes)) return NQG_ERR_ARG;
+  Plan &P = h->P;
+  std::vector<int> sub(snodes, snodes + count);
+  NQG_CUDA(cudaMemsetAsync(P.d_status, 0, sizeof(int), P.stream));
+  NQG_CUDA(cudaEventRecord(P.ev0, P.stream));
+  int rc = dev_factor(P, &sub);
+  if (rc < 0) return rc;
+  NQG_CUDA(cudaEventRecord(P.ev1, P.stream));
+  return finish_factor(P);
+}
+
+extern "C" int nqg_set_visibility(nqg_plan *h, const uint8_t *visible_sn, const uint8_t *hidden_col) {
+  if (!h) return NQG_ERR_ARG;
+  Plan &P = h->P;
+  if (!visible_sn && !hidden_col) {
+    P.masked = false;
+    return NQG_OK;
+  }
+  const int ns = P.sym.nsuper;
+  std::vector<uint8_t> vis(ns, 1), hid(P.n, 0);
+  if (visible_sn) std::copy(visible_sn, visible_sn + ns, vis.begin());
+  if (hidden_col) std::copy(hidden_col, hidden_col + P.n, hid.begin());
+  NQG_CUDA(cudaMemcpyAsync(P.d_visible, vis.data(), ns, cudaMemcpyHostToDevice, P.stream));
+  NQG_CUDA(cudaMemcpyAsync(P.d_hidden, hid.data(), P.n, cudaMemcpyHostToDevice, P.stream));
+  NQG_CUDA(cudaStreamSynchronize(P.stream));
+  P.masked = true;
+  return NQG_OK;
+}
+
+extern "C" int nqg_solve_device(nqg_plan *h, const double *d_rhs, double *d_x) {
+  if (!h || !d_rhs || !d_x) return NQG_ERR_ARG;
+  Plan &P = h->P;
+  if (!P.factored) return NQG_ERR_STATE;
+  NQG_CUDA(cudaEventRecord(P.ev0, P.stream));
+  int rc = dev_solve(P, d_rhs, d_x);
+  if (rc) return rc;
+  NQG_CUDA(cudaEventRecord(P.ev1, P.stream));
+  NQG_CUDA(cudaEventSynchronize(P.ev1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, P.ev0, P.ev1);
+  P.tm.solve_ms = ms;
+  return NQG_OK;
+}
+
+extern "C" int nqg_solve(nqg_plan *h, const double *rhs, double *x) {
+  if (!h || (!rhs && h->P.n > 0) || (!x && h->P.n > 0)) return NQG_ERR_ARG;
+  Plan &P = h->P;
+  if (!P.factored) return NQG_ERR_STATE;
+  NQG_CUDA(cudaMemcpyAsync(P.d_in, rhs, P.n * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  int rc = nqg_solve_device(h, P.d_in, P.d_out);
+  if (rc) return rc;
+  NQG_CUDA(cudaMemcpyAsync(x, P.d_out, P.n * sizeof(double), cudaMemcpyDeviceToHost, P.stream));
+  NQG_CUDA(cudaStreamSynchronize(P.stream));
+  return NQG_OK;
+}
+
+extern "C" int nqg_ldlt_solve_ordered_device(nqg_plan *h, double *d_x_ord) {
+  if (!h || !d_x_ord) return NQG_ERR_ARG;
+  Plan &P = h->P;
+  if (!P.factored) return NQG_ERR_STATE;
+  return dev_ldlt_solve_ord(P, d_x_ord);
+}
+
+extern "C" int nqg_spmv_device(nqg_plan *h, const double *d_x, double *d_y) {
+  if (!h || !d_x || !d_y) return NQG_ERR_ARG;
+  return dev_spmv_orig(h->P, d_x, d_y);
+}
+
+extern "C" int nqg_get_timings(const nqg_plan *h, nqg_timings *t) {
+  if (!h || !t) return NQG_ERR_ARG;
+  *t = h->P.tm;
+  return NQG_OK;
+}
+
+extern "C" int nqg_get_factor(const nqg_plan *hc, double *values, double *d, int *perm, int *ls) {
+  if (!hc) return NQG_ERR_ARG;
+  Plan &P = const_cast<nqg_plan *>(hc)->P;
+  NQG_CUDA(cudaStreamSynchronize(P.stream));
+  const int n = P.n;
+  if (values) {
+    if (P.set.precision == NQG_FP32) {
+      std::vector<float> tmp(P.sym.xsize);
+      NQG_CUDA(cudaMemcpy(tmp.data(), P.d_L, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost));
+      for (size_t q = 0; q < tmp.size(); ++q) values[q] = tmp[q];
+    } else {
+      NQG_CUDA(cudaMemcpy(values, P.d_L, (size_t)P.sym.xsize * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+  }
+  if (d) {
+    if (P.set.precision == NQG_FP32) {
+      std::vector<float> tmp(2 * n);
+      NQG_CUDA(cudaMemcpy(tmp.data(), P.d_D, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost));
+      for (size_t q = 0; q < tmp.size(); ++q) d[q] = tmp[q];
+    } else {
+      NQG_CUDA(cudaMemcpy(d, P.d_D, (size_t)2 * n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+  }
+  if (perm) NQG_CUDA(cudaMemcpy(perm, P.d_perm, n * sizeof(int), cudaMemcpyDeviceToHost));
+  if (ls) NQG_CUDA(cudaMemcpy(ls, P.d_ls, P.ssize * sizeof(int), cudaMemcpyDeviceToHost));
+  return NQG_OK;
+}
+
+extern "C" int nqg_get_device_status(const nqg_plan *hc, int *bits) {
+  if (!hc || !bits) return NQG_ERR_ARG;
+  Plan &P = const_cast<nqg_plan *>(hc)->P;
+  NQG_CUDA(cudaMemcpy(bits, P.d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  return NQG_OK;
+}

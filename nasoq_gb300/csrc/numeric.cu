@@ -1,0 +1,833 @@
+// Supernodal LDL^T numeric factorization with Bunch-Kaufman pivoting inside
+// each supernode's diagonal block, level-scheduled on one GPU.
+//
+// Per level of the supernodal assembly tree (leaves first):
+//   1. k_update: every (target s, descendant d) Schur contribution
+//      L_d D_d L_d^T restricted to s, tiled 64x64, accumulated in registers
+//      and subtracted from s with atomics (reference left-looking loop,
+//      src/ldl/Serial_blocked_ldl_02_2.cpp:69-129);
+//   2. k_bk_*: Bunch-Kaufman on the diagonal block with explicit row swaps
+//      (LAPACK dsytrf('L') + reorder_after_sytrf, Sym_BLAS.cpp:128-196),
+//      then the panel column permutation (dlapmt), the unit triangular solve
+//      with L11^T (dtrsm) and the D^-1 scaling (blocked_2by2_solver,
+//      Sym_BLAS.cpp:492-529).
+// After all levels, k_row_reorder renames the rows of descendants that fall
+// into pivoted supernodes and re-sorts them (row_reordering,
+// Sym_BLAS.cpp:327-490), and k_perm_compose folds the pivots into the global
+// permutation (reorder_matrix, linear_solver_wrapper.cpp:1432-1460).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+
+#include "plan.hpp"
+
+namespace nqg {
+
+namespace {
+
+constexpr int BK_SMALL = 64;     // diagonal blocks up to this width live in shared memory
+constexpr int BK_THREADS = 128;
+constexpr int UPD_THREADS = 256;
+constexpr int UPD_KC = 16;
+
+__device__ __forceinline__ void flag_status(int *st, int bits) { atomicOr(st, bits); }
+
+template <class T> __device__ __forceinline__ T tabs(T v) { return v < T(0) ? -v : v; }
+
+// Block-wide argmax of |value| with the smallest index winning ties (the
+// LAPACK idamax convention).  Every thread passes its candidate; returns the
+// winner to all threads.  `sv`/`si` are shared scratch of blockDim/32 entries.
+template <class T>
+__device__ void block_argmax(T &v, int &idx, T *sv, int *si) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    T ov = __shfl_down_sync(0xffffffffu, v, o);
+    int oi = __shfl_down_sync(0xffffffffu, idx, o);
+    if (oi >= 0 && (idx < 0 || ov > v || (ov == v && oi < idx))) {
+      v = ov;
+      idx = oi;
+    }
+  }
+  __syncthreads();
+  if (lane == 0) {
+    sv[wid] = v;
+    si[wid] = idx;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    v = lane < nw ? sv[lane] : T(-1);
+    idx = lane < nw ? si[lane] : -1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      T ov = __shfl_down_sync(0xffffffffu, v, o);
+      int oi = __shfl_down_sync(0xffffffffu, idx, o);
+      if (oi >= 0 && (idx < 0 || ov > v || (ov == v && oi < idx))) {
+        v = ov;
+        idx = oi;
+      }
+    }
+    if (lane == 0) {
+      sv[0] = v;
+      si[0] = idx;
+    }
+  }
+  __syncthreads();
+  v = sv[0];
+  idx = si[0];
+  __syncthreads();
+}
+
+// Bunch-Kaufman (alpha = (1+sqrt(17))/8) on the w-by-w lower-stored block
+// `a` (column-major, leading dimension lda), leaving L in explicit form
+// (P A P^T = L D L^T): every interchange also swaps the two rows in all
+// previously computed columns.  On return a holds L with unit diagonal and
+// zeroed 2x2 sub-diagonals; D/E get the diagonal and 2x2 sub-diagonals;
+// perm[m] = original local column now at position m.
+template <class T>
+__device__ void bk_factor(T *a, int lda, int w, T *D, T *E, int *perm, int *status, bool *pivoted_out) {
+  __shared__ T red_v[32];
+  __shared__ int red_i[32];
+  __shared__ int s_kp, s_kstep, s_zero;
+  __shared__ T s_wk[BK_SMALL * 2];
+  const T alpha = (T)((1.0 + sqrt(17.0)) / 8.0);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  bool pivoted = false;
+  for (int m = tid; m < w; m += nt) perm[m] = m;
+  __syncthreads();
+  int k = 0;
+  while (k < w) {
+    // ---- pivot search on column k
+    T absakk = tabs(a[k + (size_t)k * lda]);
+    T cv = T(-1);
+    int ci = -1;
+    for (int i = k + 1 + tid; i < w; i += nt) {
+      T v = tabs(a[i + (size_t)k * lda]);
+      if (ci < 0 || v > cv) {
+        cv = v;
+        ci = i;
+      }
+    }
+    block_argmax(cv, ci, red_v, red_i);
+    T colmax = ci >= 0 ? cv : T(0);
+    int imax = ci;
+    int kp = k, kstep = 1, zero = 0;
+    if ((absakk >= colmax ? absakk : colmax) == T(0) || absakk != absakk) {
+      zero = 1;
+    } else if (absakk >= alpha * colmax) {
+      kp = k;
+    } else {
+      // rowmax: off-diagonal max of row/column imax inside the trailing block
+      T rv = T(-1);
+      int ri = -1;
+      for (int j = k + tid; j < w; j += nt) {
+        if (j == imax) continue;
+        T v = j < imax ? tabs(a[imax + (size_t)j * lda]) : tabs(a[j + (size_t)imax * lda]);
+        if (ri < 0 || v > rv) {
+          rv = v;
+          ri = j;
+        }
+      }
+      block_argmax(rv, ri, red_v, red_i);
+      T rowmax = rv;
+      if (absakk >= alpha * colmax * (colmax / rowmax)) {
+        kp = k;
+      } else if (tabs(a[imax + (size_t)imax * lda]) >= alpha * rowmax) {
+        kp = imax;
+      } else {
+        kp = imax;
+        kstep = 2;
+      }
+    }
+    if (tid == 0) {
+      s_kp = kp;
+      s_kstep = kstep;
+      s_zero = zero;
+    }
+    __syncthreads();
+    kp = s_kp;
+    kstep = s_kstep;
+    zero = s_zero;
+    const int kk = k + kstep - 1;
+    if (zero && tid == 0) flag_status(status, ST_ZERO_PIVOT);
+    // ---- symmetric interchange of kk and kp (kp > kk)
+    if (kp != kk) {
+      pivoted = true;
+      for (int i = kp + 1 + tid; i < w; i += nt) {
+        T t = a[i + (size_t)kk * lda];
+        a[i + (size_t)kk * lda] = a[i + (size_t)kp * lda];
+        a[i + (size_t)kp * lda] = t;
+      }
+      for (int j = kk + 1 + tid; j < kp; j += nt) {
+        T t = a[j + (size_t)kk * lda];
+        a[j + (size_t)kk * lda] = a[kp + (size_t)j * lda];
+        a[kp + (size_t)j * lda] = t;
+      }
+      // rows kk and kp of the columns to the left of the current pivot
+      // (for a 2x2 pivot this includes column k: LAPACK swaps A(k+1,k), A(kp,k))
+      const int ncols_left = kstep == 2 ? k + 1 : k;
+      for (int c = tid; c < ncols_left; c += nt) {
+        T t = a[kk + (size_t)c * lda];
+        a[kk + (size_t)c * lda] = a[kp + (size_t)c * lda];
+        a[kp + (size_t)c * lda] = t;
+      }
+      if (tid == 0) {
+        T t = a[kk + (size_t)kk * lda];
+        a[kk + (size_t)kk * lda] = a[kp + (size_t)kp * lda];
+        a[kp + (size_t)kp * lda] = t;
+        int pt = perm[kk];
+        perm[kk] = perm[kp];
+        perm[kp] = pt;
+      }
+    }
+    __syncthreads();
+    // ---- elimination
+    if (kstep == 1) {
+      if (!zero) {
+        const T r1 = T(1) / a[k + (size_t)k * lda];
+        const int m = w - k - 1;
+        // trailing rank-1 update of the lower triangle, then scale the column
+        for (int e = tid; e < m * m; e += nt) {
+          int jj = e / m, ii = e % m;
+          if (ii < jj) continue;
+          int i = k + 1 + ii, j = k + 1 + jj;
+          a[i + (size_t)j * lda] -= r1 * a[j + (size_t)k * lda] * a[i + (size_t)k * lda];
+        }
+        __syncthreads();
+        for (int i = k + 1 + tid; i < w; i += nt) a[i + (size_t)k * lda] *= r1;
+      }
+      if (tid == 0) {
+        D[k] = a[k + (size_t)k * lda];
+        E[k] = T(0);
+      }
+    } else {
+      // 2x2 pivot on rows/cols k, k+1
+      T d21 = a[k + 1 + (size_t)k * lda];
+      T d11 = a[k + 1 + (size_t)(k + 1) * lda] / d21;
+      T d22 = a[k + (size_t)k * lda] / d21;
+      T t = T(1) / (d11 * d22 - T(1));
+      d21 = t / d21;
+      const int m = w - k - 2;
+      // multipliers for all trailing rows j (kept in shared or recomputed)
+      for (int base = 0; base < m; base += BK_SMALL) {
+        const int cnt = min(BK_SMALL, m - base);
+        for (int q = tid; q < cnt; q += nt) {
+          int j = k + 2 + base + q;
+          T ajk = a[j + (size_t)k * lda], ajk1 = a[j + (size_t)(k + 1) * lda];
+          s_wk[2 * q] = d21 * (d11 * ajk - ajk1);
+          s_wk[2 * q + 1] = d21 * (d22 * ajk1 - ajk);
+        }
+        __syncthreads();
+        // update columns j in [base, base+cnt): a(i,j) -= a(i,k) wk_j + a(i,k+1) wkp1_j, i >= j
+        for (int e = tid; e < cnt * m; e += nt) {
+          int q = e / m, ii = e % m;
+          int j = k + 2 + base + q, i = k + 2 + ii;
+          if (i < j) continue;
+          a[i + (size_t)j * lda] -= a[i + (size_t)k * lda] * s_wk[2 * q] + a[i + (size_t)(k + 1) * lda] * s_wk[2 * q + 1];
+        }
+        __syncthreads();
+        // multipliers of rows whose trailing updates are all done can be written:
+        // columns k, k+1 are read by later chunks (rows i >= j), so stage them.
+        for (int q = tid; q < cnt; q += nt) {
+          int j = k + 2 + base + q;
+          // keep the multiplier in the upper triangle slot (unused) temporarily
+          a[k + (size_t)j * lda] = s_wk[2 * q];
+          a[k + 1 + (size_t)j * lda] = s_wk[2 * q + 1];
+        }
+        __syncthreads();
+      }
+      for (int j = k + 2 + tid; j < w; j += nt) {
+        a[j + (size_t)k * lda] = a[k + (size_t)j * lda];
+        a[j + (size_t)(k + 1) * lda] = a[k + 1 + (size_t)j * lda];
+        a[k + (size_t)j * lda] = T(0);
+        a[k + 1 + (size_t)j * lda] = T(0);
+      }
+      if (tid == 0) {
+        D[k] = a[k + (size_t)k * lda];
+        D[k + 1] = a[k + 1 + (size_t)(k + 1) * lda];
+        E[k] = a[k + 1 + (size_t)k * lda];
+        E[k + 1] = T(0);
+        a[k + 1 + (size_t)k * lda] = T(0);
+      }
+    }
+    __syncthreads();
+    k += kstep;
+  }
+  for (int m = tid; m < w; m += nt) a[m + (size_t)m * lda] = T(1);
+  __syncthreads();
+  if (pivoted_out) *pivoted_out = pivoted;
+}
+
+// Block-wide OR of a per-thread flag.
+__device__ bool block_any(bool f) { return __syncthreads_or(f ? 1 : 0) != 0; }
+
+// Panel rows [w, nrow): columns permuted by perm, solved with the unit lower
+// L11^T and scaled by D^-1 (1x1: times 1/d; 2x2: Cramer's rule with
+// 1/det, the arithmetic of blocked_2by2_solver).  One thread per row.
+template <class T>
+__device__ void panel_solve_rows(T *Ls, int nrow, int w, const T *l11, int ld11, const T *D, const T *E,
+                                 const int *perm, T *rowbuf, int rb_ld, bool permute) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int r0 = w; r0 < nrow; r0 += nt) {
+    const int r = r0 + tid;
+    const bool act = r < nrow;
+    if (act) {
+      for (int j = 0; j < w; ++j) {
+        int src = permute ? perm[j] : j;
+        rowbuf[j * rb_ld + tid] = Ls[r + (size_t)src * nrow];
+      }
+      for (int j = 0; j < w; ++j) {
+        T x = rowbuf[j * rb_ld + tid];
+        for (int t = 0; t < j; ++t) x -= rowbuf[t * rb_ld + tid] * l11[j + (size_t)t * ld11];
+        rowbuf[j * rb_ld + tid] = x;
+      }
+      for (int j = 0; j < w; ++j) {
+        if (E[j] == T(0)) {
+          T inv = T(1) / D[j];
+          Ls[r + (size_t)j * nrow] = rowbuf[j * rb_ld + tid] * inv;
+        } else {
+          T s = E[j];
+          T det = D[j] * D[j + 1] - s * s;
+          T inv = T(1) / det;
+          T x1 = rowbuf[j * rb_ld + tid], x2 = rowbuf[(j + 1) * rb_ld + tid];
+          Ls[r + (size_t)j * nrow] = (x1 * D[j + 1] - x2 * s) * inv;
+          Ls[r + (size_t)(j + 1) * nrow] = (x2 * D[j] - x1 * s) * inv;
+          ++j;
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_zero_targets / k_assemble: reset the values of the supernodes being
+// factored and scatter the (perturbed) matrix entries into them.
+template <class T>
+__global__ void k_zero_targets(const int *targets, int ntargets, const int *super, const int64_t *lpi,
+                               const int64_t *lpx, T *L, T *D, int n) {
+  const int s = targets[blockIdx.x];
+  const int64_t beg = lpx[s], end = lpx[s + 1];
+  for (int64_t q = beg + threadIdx.x; q < end; q += blockDim.x) L[q] = T(0);
+  for (int c = super[s] + threadIdx.x; c < super[s + 1]; c += blockDim.x) {
+    D[c] = T(0);
+    D[n + c] = T(0);
+  }
+}
+
+__device__ __forceinline__ int lower_bound_i(const int *a, int len, int key) {
+  int lo = 0, hi = len;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (a[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <class T>
+__global__ void k_assemble(int n, const int *Kp, const int *Ki, const double *Kx, const int *iperm, const int *col2sup,
+                           const int *super, const int64_t *lpi, const int64_t *lpx, const int *ls, const uint8_t *mark,
+                           T *L, int *status) {
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  for (int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < n; j += warps) {
+    const int bj = iperm[j];
+    for (int q = Kp[j] + lane; q < Kp[j + 1]; q += 32) {
+      const int bi = iperm[Ki[q]];
+      const int c = min(bi, bj), r = max(bi, bj);
+      const int s = col2sup[c];
+      if (mark && !mark[s]) continue;
+      const int c0 = super[s], w = super[s + 1] - c0;
+      const int nrow = (int)(lpi[s + 1] - lpi[s]);
+      int pos;
+      if (r < c0 + w) {
+        pos = r - c0;
+      } else {
+        const int *rows = ls + lpi[s] + w;
+        pos = w + lower_bound_i(rows, nrow - w, r);
+        if (pos >= nrow || ls[lpi[s] + pos] != r) {
+          flag_status(status, ST_BOUNDS);
+          continue;
+        }
+      }
+      L[lpx[s] + (int64_t)(c - c0) * nrow + pos] = (T)Kx[q];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Schur update tiles.  C = (L_d D_d)[rows] * L_d[cols]^T, subtracted from the
+// target with atomics.  D_d is block diagonal with 1x1 and 2x2 blocks:
+// (L D)(:,t) = d_t L(:,t) + e_t L(:,t+1) + e_{t-1} L(:,t-1) with e the 2x2
+// sub-diagonals (zero outside 2x2 blocks), which is blocked_2by2_mult.
+template <class T>
+__global__ void __launch_bounds__(UPD_THREADS) k_update(const UpdTile *tiles, const int *tile_ids, int ntiles, int n,
+                                                       const int *super, const int64_t *lpi, const int64_t *lpx,
+                                                       const int *ls, T *L, const T *Dg, int *status) {
+  __shared__ T As[UPD_KC][UPD_TM + 1];
+  __shared__ T Bs[UPD_KC][UPD_TN + 1];
+  __shared__ T Raw[UPD_KC + 2][UPD_TM + 1];
+  __shared__ T dk[UPD_KC + 2], ek[UPD_KC + 2];
+  __shared__ int prow[UPD_TM], pcol[UPD_TN];
+  const int tid = threadIdx.x;
+  const UpdTile tl = tiles[tile_ids ? tile_ids[blockIdx.x] : blockIdx.x];
+  const int s = tl.s, d = tl.d;
+  const int c0 = super[d], wd = super[d + 1] - c0;
+  const int nrd = (int)(lpi[d + 1] - lpi[d]);
+  const int *rows_d = ls + lpi[d];
+  const T *Ld = L + lpx[d];
+  const int mrows = min(UPD_TM, nrd - tl.ri);
+  const int ncols = min(UPD_TN, tl.ub + 1 - tl.cj);
+  const int cs0 = super[s], ws = super[s + 1] - cs0;
+  const int nrs = (int)(lpi[s + 1] - lpi[s]);
+  const int *rows_s = ls + lpi[s];
+  T *Lt = L + lpx[s];
+  // target positions of the tile's rows and columns
+  for (int i = tid; i < UPD_TM; i += blockDim.x) {
+    int pos = -1;
+    if (i < mrows) {
+      int r = rows_d[tl.ri + i];
+      if (r < cs0 + ws) pos = r - cs0;
+      else {
+        pos = ws + lower_bound_i(rows_s + ws, nrs - ws, r);
+        if (pos >= nrs || rows_s[pos] != r) {
+          flag_status(status, ST_BOUNDS);
+          pos = -1;
+        }
+      }
+    }
+    prow[i] = pos;
+  }
+  for (int j = tid; j < UPD_TN; j += blockDim.x) {
+    int pos = -1;
+    if (j < ncols) {
+      pos = rows_d[tl.cj + j] - cs0;
+      if (pos < 0 || pos >= ws) {
+        flag_status(status, ST_BOUNDS);
+        pos = -1;
+      }
+    }
+    pcol[j] = pos;
+  }
+  const int tx = tid & 15, ty = tid >> 4;
+  T acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
+  for (int t0 = 0; t0 < wd; t0 += UPD_KC) {
+    __syncthreads();
+    // raw columns t0-1 .. t0+KC of the tile rows, plus D entries
+    for (int e = tid; e < (UPD_KC + 2) * UPD_TM; e += blockDim.x) {
+      int cc = e / UPD_TM, i = e % UPD_TM;
+      int t = t0 - 1 + cc;
+      T v = T(0);
+      if (t >= 0 && t < wd && i < mrows) v = Ld[(size_t)t * nrd + tl.ri + i];
+      Raw[cc][i] = v;
+    }
+    for (int cc = tid; cc < UPD_KC + 2; cc += blockDim.x) {
+      int t = t0 - 1 + cc;
+      dk[cc] = (t >= 0 && t < wd) ? Dg[c0 + t] : T(0);
+      ek[cc] = (t >= 0 && t < wd) ? Dg[n + c0 + t] : T(0);
+    }
+    for (int e = tid; e < UPD_KC * UPD_TN; e += blockDim.x) {
+      int cc = e / UPD_TN, j = e % UPD_TN;
+      int t = t0 + cc;
+      Bs[cc][j] = (t < wd && j < ncols) ? Ld[(size_t)t * nrd + tl.cj + j] : T(0);
+    }
+    __syncthreads();
+    for (int e = tid; e < UPD_KC * UPD_TM; e += blockDim.x) {
+      int cc = e / UPD_TM, i = e % UPD_TM;
+      // column t = t0+cc sits at Raw index cc+1
+      As[cc][i] = dk[cc + 1] * Raw[cc + 1][i] + ek[cc + 1] * Raw[cc + 2][i] + ek[cc] * Raw[cc][i];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int cc = 0; cc < UPD_KC; ++cc) {
+      T av[4], bv[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) av[a] = As[cc][ty * 4 + a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) bv[b] = Bs[cc][tx * 4 + b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int i = ty * 4 + a;
+    if (i >= mrows || prow[i] < 0) continue;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int j = tx * 4 + b;
+      if (j >= ncols || pcol[j] < 0) continue;
+      if (tl.ri + i < tl.cj + j) continue;  // lower part only
+      atomicAdd(&Lt[(size_t)pcol[j] * nrs + prow[i]], -acc[a][b]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Diagonal block BK + panel, one CTA per supernode.  SMALL: the block and a
+// row chunk of the panel are staged in shared memory.
+template <class T>
+__global__ void __launch_bounds__(BK_THREADS) k_bk_small(const int *targets, int n, const int *super,
+                                                         const int64_t *lpi, const int64_t *lpx, T *L, T *Dg,
+                                                         int *locperm, uint8_t *pivoted, int *status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *a = reinterpret_cast<T *>(smem_raw);                 // BK_SMALL * BK_SMALL
+  T *rowbuf = a + BK_SMALL * BK_SMALL;                     // BK_SMALL * BK_THREADS
+  __shared__ int perm[BK_SMALL];
+  const int s = targets[blockIdx.x];
+  const int c0 = super[s], w = super[s + 1] - c0;
+  const int nrow = (int)(lpi[s + 1] - lpi[s]);
+  T *Ls = L + lpx[s];
+  for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+    int c = e / w, r = e % w;
+    a[r + c * w] = r >= c ? Ls[r + (size_t)c * nrow] : T(0);
+  }
+  __syncthreads();
+  bool piv = false;
+  bk_factor(a, w, w, Dg + c0, Dg + n + c0, perm, status, &piv);
+  for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+    int c = e / w, r = e % w;
+    Ls[r + (size_t)c * nrow] = r >= c ? a[r + c * w] : T(0);
+  }
+  for (int m = threadIdx.x; m < w; m += blockDim.x) locperm[c0 + m] = perm[m];
+  if (threadIdx.x == 0) pivoted[s] = piv ? 1 : 0;
+  __syncthreads();
+  panel_solve_rows(Ls, nrow, w, a, w, Dg + c0, Dg + n + c0, perm, rowbuf, BK_THREADS, piv);
+  // non-finite check on D
+  bool bad = false;
+  for (int m = threadIdx.x; m < w; m += blockDim.x) {
+    T v = Dg[c0 + m];
+    if (!isfinite((double)v)) bad = true;
+  }
+  if (block_any(bad) && threadIdx.x == 0) flag_status(status, ST_NONFINITE);
+}
+
+// GENERIC: the diagonal block is factored in place in global memory; the
+// panel is permuted in place by following the permutation's cycles and
+// solved one row per thread.
+template <class T>
+__global__ void __launch_bounds__(256) k_bk_global(const int *targets, int n, const int *super, const int64_t *lpi,
+                                                   const int64_t *lpx, T *L, T *Dg, int *locperm, uint8_t *pivoted,
+                                                   int *cycle_buf, int *status) {
+  const int s = targets[blockIdx.x];
+  const int c0 = super[s], w = super[s + 1] - c0;
+  const int nrow = (int)(lpi[s + 1] - lpi[s]);
+  T *Ls = L + lpx[s];
+  int *perm = locperm + c0;
+  bool piv = false;
+  bk_factor(Ls, nrow, w, Dg + c0, Dg + n + c0, perm, status, &piv);
+  // zero the strict upper triangle (never referenced, kept at 0 like the reference)
+  for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+    int c = e / w, r = e % w;
+    if (r < c) Ls[r + (size_t)c * nrow] = T(0);
+  }
+  if (threadIdx.x == 0) pivoted[s] = piv ? 1 : 0;
+  __syncthreads();
+  const T *D = Dg + c0, *E = Dg + n + c0;
+  // cycle leaders of the column permutation new[j] = old[perm[j]]
+  int *lead = cycle_buf + c0;  // n-sized scratch, this supernode's slice
+  if (piv) {
+    for (int j = threadIdx.x; j < w; j += blockDim.x) {
+      // j leads its cycle if it is the smallest index on it
+      int q = perm[j], isl = 1;
+      int guard = 0;
+      while (q != j && guard++ <= w) {
+        if (q < j) {
+          isl = 0;
+          break;
+        }
+        q = perm[q];
+      }
+      lead[j] = isl;
+    }
+  }
+  __syncthreads();
+  for (int r = w + threadIdx.x; r < nrow; r += blockDim.x) {
+    T *row = Ls + r;  // element j at row[j*nrow]
+    if (piv) {
+      for (int j = 0; j < w; ++j) {
+        if (!lead[j] || perm[j] == j) continue;
+        // new[j] = old[perm[j]]: rotate along the cycle starting at j
+        T first = row[(size_t)j * nrow];
+        int cur = j, guard = 0;
+        while (guard++ <= w) {
+          int nx = perm[cur];
+          if (nx == j) {
+            row[(size_t)cur * nrow] = first;
+            break;
+          }
+          row[(size_t)cur * nrow] = row[(size_t)nx * nrow];
+          cur = nx;
+        }
+      }
+    }
+    for (int j = 0; j < w; ++j) {
+      T x = row[(size_t)j * nrow];
+      for (int t = 0; t < j; ++t) x -= row[(size_t)t * nrow] * Ls[j + (size_t)t * nrow];
+      row[(size_t)j * nrow] = x;
+    }
+    for (int j = 0; j < w; ++j) {
+      if (E[j] == T(0)) {
+        T inv = T(1) / D[j];
+        row[(size_t)j * nrow] *= inv;
+      } else {
+        T sd = E[j];
+        T det = D[j] * D[j + 1] - sd * sd;
+        T inv = T(1) / det;
+        T x1 = row[(size_t)j * nrow], x2 = row[(size_t)(j + 1) * nrow];
+        row[(size_t)j * nrow] = (x1 * D[j + 1] - x2 * sd) * inv;
+        row[(size_t)(j + 1) * nrow] = (x2 * D[j] - x1 * sd) * inv;
+        ++j;
+      }
+    }
+  }
+  bool bad = false;
+  for (int m = threadIdx.x; m < w; m += blockDim.x)
+    if (!isfinite((double)D[m])) bad = true;
+  if (block_any(bad) && threadIdx.x == 0) flag_status(status, ST_NONFINITE);
+}
+
+// ---------------------------------------------------------------------------
+// Row renaming after pivoting: for a (pivoted target s, descendant d) pair,
+// the rows of d in s's column range [lb, ub] are renamed through s's inverse
+// pivot permutation and re-sorted, moving d's value rows along.
+template <class T>
+__global__ void k_row_reorder(const int *pair_s, const int *pair_d, const int *pair_lb, const int *pair_ub, int npairs,
+                              const uint8_t *pivoted, const int *super, const int64_t *lpi, const int64_t *lpx,
+                              int *ls, const int *locperm, T *L, int *status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int pidx = blockIdx.x;
+  if (pidx >= npairs) return;
+  const int s = pair_s[pidx];
+  if (!pivoted[s]) return;
+  const int d = pair_d[pidx], lb = pair_lb[pidx], ub = pair_ub[pidx];
+  const int c0 = super[s], w = super[s + 1] - c0;
+  const int len = ub - lb + 1;
+  if (len <= 0) return;
+  int *dest = reinterpret_cast<int *>(smem_raw);   // len
+  int *inv = dest + len;                            // w
+  unsigned *bits = reinterpret_cast<unsigned *>(inv + w);  // (w+31)/32
+  int *wpre = reinterpret_cast<int *>(bits + (w + 31) / 32);  // (w+31)/32
+  __shared__ int s_lead_cnt;
+  const int nwords = (w + 31) / 32;
+  for (int m = threadIdx.x; m < w; m += blockDim.x) inv[locperm[c0 + m]] = m;
+  for (int q = threadIdx.x; q < nwords; q += blockDim.x) bits[q] = 0u;
+  __syncthreads();
+  int *rows = ls + lpi[d] + lb;
+  for (int e = threadIdx.x; e < len; e += blockDim.x) {
+    int r = rows[e] - c0;
+    if (r < 0 || r >= w) {
+      flag_status(status, ST_BOUNDS);
+      r = 0;
+    }
+    int nw = inv[r];
+    dest[e] = nw;  // temporarily the new local name
+    atomicOr(&bits[nw >> 5], 1u << (nw & 31));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int q = 0; q < nwords; ++q) {
+      wpre[q] = acc;
+      acc += __popc(bits[q]);
+    }
+    s_lead_cnt = acc;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < len; e += blockDim.x) {
+    int nw = dest[e];
+    int rank = wpre[nw >> 5] + __popc(bits[nw >> 5] & ((1u << (nw & 31)) - 1u));
+    dest[e] = rank;
+    rows[rank] = -1 - (c0 + nw);  // staged; fixed below
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < len; e += blockDim.x) rows[e] = -1 - rows[e];
+  // cycle leaders of the position permutation (reuse inv[] as flags)
+  __syncthreads();
+  int *leader = inv;
+  for (int e = threadIdx.x; e < len; e += blockDim.x) {
+    int q = dest[e];
+    int isl = q != e;
+    int guard = 0;
+    while (isl && q != e && guard++ <= len) {
+      if (q < e) isl = 0;
+      q = dest[q];
+    }
+    leader[e] = isl;
+  }
+  __syncthreads();
+  // move value rows: element at position e goes to dest[e]; one thread per column of d
+  const int wd = super[d + 1] - super[d];
+  const int nrd = (int)(lpi[d + 1] - lpi[d]);
+  T *Ld = L + lpx[d] + lb;
+  for (int c = threadIdx.x; c < wd; c += blockDim.x) {
+    T *col = Ld + (size_t)c * nrd;
+    for (int e = 0; e < len; ++e) {
+      if (!leader[e]) continue;
+      T carry = col[e];
+      int cur = dest[e];
+      int guard = 0;
+      while (guard++ <= len) {
+        T t = col[cur];
+        col[cur] = carry;
+        carry = t;
+        if (cur == e) break;
+        cur = dest[cur];
+      }
+    }
+  }
+}
+
+// perm_new[i] = perm[c0 + locperm[i - c0]] for columns of factored supernodes.
+__global__ void k_perm_compose(int n, const int *col2sup, const int *super, const uint8_t *mark,
+                               const uint8_t *pivoted, const int *locperm, const int *perm, int *perm_new) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int s = col2sup[i];
+    int v = perm[i];
+    if ((!mark || mark[s]) && pivoted[s]) {
+      int c0 = super[s];
+      v = perm[c0 + locperm[i]];
+    }
+    perm_new[i] = v;
+  }
+}
+
+__global__ void k_iperm(int n, const int *perm, int *iperm) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) iperm[perm[i]] = i;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host driver.
+template <class T> static int factor_impl(Plan &P, const std::vector<int> *subset) {
+  const int n = P.n;
+  const int ns = P.sym.nsuper;
+  cudaStream_t st = P.stream;
+  T *L = reinterpret_cast<T *>(P.d_L);
+  T *D = reinterpret_cast<T *>(P.d_D);
+  // marks and per-level target lists
+  std::vector<uint8_t> mark(ns, subset ? 0 : 1);
+  if (subset)
+    for (int s : *subset) {
+      if (s < 0 || s >= ns) return NQG_ERR_ARG;
+      mark[s] = 1;
+    }
+  std::vector<int> order;      // targets grouped by level
+  std::vector<int> lv_small_off, lv_small_cnt, lv_glob_off, lv_glob_cnt;
+  std::vector<int> tile_ids;
+  std::vector<int64_t> lv_tile_off, lv_tile_cnt;
+  const int nlev = (int)P.levels.size();
+  for (int l = 0; l < nlev; ++l) {
+    int so = (int)order.size();
+    for (int s : P.levels[l])
+      if (mark[s] && P.sym.super[s + 1] - P.sym.super[s] <= BK_SMALL) order.push_back(s);
+    int go = (int)order.size();
+    for (int s : P.levels[l])
+      if (mark[s] && P.sym.super[s + 1] - P.sym.super[s] > BK_SMALL) order.push_back(s);
+    lv_small_off.push_back(so);
+    lv_small_cnt.push_back(go - so);
+    lv_glob_off.push_back(go);
+    lv_glob_cnt.push_back((int)order.size() - go);
+    int64_t to = (int64_t)tile_ids.size();
+    for (int s : P.levels[l])
+      if (mark[s])
+        for (int64_t t = P.tile_ptr[s]; t < P.tile_ptr[s + 1]; ++t) tile_ids.push_back((int)t);
+    lv_tile_off.push_back(to);
+    lv_tile_cnt.push_back((int64_t)tile_ids.size() - to);
+  }
+  if (order.empty()) return NQG_OK;
+  if (order.size() > P.targets_cap) {
+    if (P.d_targets) cudaFree(P.d_targets);
+    P.targets_cap = std::max<size_t>(order.size(), 64);
+    NQG_CUDA(cudaMalloc(&P.d_targets, P.targets_cap * sizeof(int)));
+  }
+  if (tile_ids.size() > P.tile_list_cap) {
+    if (P.d_tile_list) cudaFree(P.d_tile_list);
+    P.tile_list_cap = std::max<size_t>(tile_ids.size(), 64);
+    NQG_CUDA(cudaMalloc(&P.d_tile_list, P.tile_list_cap * sizeof(int)));
+  }
+  NQG_CUDA(cudaMemcpyAsync(P.d_targets, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  if (!tile_ids.empty())
+    NQG_CUDA(cudaMemcpyAsync(P.d_tile_list, tile_ids.data(), tile_ids.size() * sizeof(int), cudaMemcpyHostToDevice,
+                             st));
+  uint8_t *d_mark = P.d_pivoted + ns;  // second half of the pivoted buffer holds the marks
+  NQG_CUDA(cudaMemcpyAsync(d_mark, mark.data(), ns, cudaMemcpyHostToDevice, st));
+  NQG_CUDA(cudaMemsetAsync(P.d_pivoted, 0, ns, st));
+  // reset + assemble
+  if (!subset) {
+    NQG_CUDA(cudaMemsetAsync(L, 0, (size_t)P.sym.xsize * sizeof(T), st));
+    NQG_CUDA(cudaMemsetAsync(D, 0, (size_t)2 * n * sizeof(T), st));
+  } else {
+    k_zero_targets<T><<<(unsigned)order.size(), 256, 0, st>>>(P.d_targets, (int)order.size(), P.d_super, P.d_lpi,
+                                                                P.d_lpx, L, D, n);
+  }
+  {
+    int blocks = std::min(std::max((n + 7) / 8, 1), 4096);
+    k_assemble<T><<<blocks, 256, 0, st>>>(n, P.d_Kp, P.d_Ki, P.d_Kx, P.d_iperm, P.d_col2sup, P.d_super, P.d_lpi,
+                                          P.d_lpx, P.d_ls, subset ? d_mark : nullptr, L, P.d_status);
+  }
+  const size_t smem_small = (size_t)(BK_SMALL * BK_SMALL + BK_SMALL * BK_THREADS) * sizeof(T);
+  static bool attr_set[2] = {false, false};
+  int ai = sizeof(T) == 8 ? 0 : 1;
+  if (!attr_set[ai]) {
+    NQG_CUDA(cudaFuncSetAttribute(k_bk_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_small));
+    attr_set[ai] = true;
+  }
+  for (int l = 0; l < nlev; ++l) {
+    if (lv_tile_cnt[l] > 0)
+      k_update<T><<<(unsigned)lv_tile_cnt[l], UPD_THREADS, 0, st>>>(P.d_tiles, P.d_tile_list + lv_tile_off[l],
+                                                                    (int)lv_tile_cnt[l], n, P.d_super, P.d_lpi,
+                                                                    P.d_lpx, P.d_ls, L, D, P.d_status);
+    if (lv_small_cnt[l] > 0)
+      k_bk_small<T><<<lv_small_cnt[l], BK_THREADS, smem_small, st>>>(P.d_targets + lv_small_off[l], n, P.d_super,
+                                                                      P.d_lpi, P.d_lpx, L, D, P.d_locperm,
+                                                                      P.d_pivoted, P.d_status);
+    if (lv_glob_cnt[l] > 0)
+      k_bk_global<T><<<lv_glob_cnt[l], 256, 0, st>>>(P.d_targets + lv_glob_off[l], n, P.d_super, P.d_lpi, P.d_lpx,
+                                                      L, D, P.d_locperm, P.d_pivoted, P.d_perm_tmp, P.d_status);
+  }
+  NQG_CUDA(cudaGetLastError());
+  // row renaming in descendants of pivoted supernodes
+  {
+    int64_t npairs = P.pair_d.size();
+    if (npairs > 0) {
+      int w = std::max(P.sym.max_sup_wid, 1);
+      size_t smem = (size_t)(w + w) * sizeof(int) + (size_t)2 * ((w + 31) / 32) * sizeof(int);
+      if (smem > 227 * 1024) return NQG_ERR_SIZE;
+      static size_t smem_set[2] = {0, 0};
+      if (smem > 48 * 1024 && smem > smem_set[ai]) {
+        NQG_CUDA(cudaFuncSetAttribute(k_row_reorder<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        smem_set[ai] = smem;
+      }
+      k_row_reorder<T><<<(unsigned)npairs, 128, smem, st>>>(P.d_pair_s, P.d_pair_d, P.d_pair_lb, P.d_pair_ub,
+                                                            (int)npairs, P.d_pivoted, P.d_super, P.d_lpi, P.d_lpx,
+                                                            P.d_ls, P.d_locperm, L, P.d_status);
+    }
+  }
+  {
+    int blocks = std::min((n + 255) / 256, 4096);
+    k_perm_compose<<<blocks, 256, 0, st>>>(n, P.d_col2sup, P.d_super, d_mark, P.d_pivoted, P.d_locperm, P.d_perm,
+                                           P.d_perm_tmp);
+    std::swap(P.d_perm, P.d_perm_tmp);
+    k_iperm<<<blocks, 256, 0, st>>>(n, P.d_perm, P.d_iperm);
+  }
+  NQG_CUDA(cudaGetLastError());
+  return NQG_OK;
+}
+
+int dev_factor(Plan &P, const std::vector<int> *subset) {
+  if (P.set.precision == NQG_FP32) return factor_impl<float>(P, subset);
+  return factor_impl<double>(P, subset);
+}
+
+}  // namespace nqg

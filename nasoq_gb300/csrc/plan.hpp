@@ -1,0 +1,113 @@
+// Plan object behind the C ABI: host symbolic structure, the supernode level
+// schedule, the update work lists, and every device buffer of one sparse
+// symmetric-indefinite system.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/nasoq_gb300.h"
+#include "symbolic.hpp"
+
+namespace nqg {
+
+// Device status bits (plan->d_status).
+enum : int {
+  ST_ZERO_PIVOT = 1,
+  ST_NONFINITE = 2,
+  ST_TIMEOUT = 4,
+  ST_BOUNDS = 8,
+};
+
+// One unit of Schur-update work: the TM x TN block of rows [ri, ri+TM) x
+// cols [cj, cj+TN) (positions in descendant d's row list, cols limited to
+// <= ub) of L_d D_d L_d^T, subtracted from target supernode s.
+struct UpdTile {
+  int s, d, ri, cj, ub;
+};
+
+constexpr int UPD_TM = 64;
+constexpr int UPD_TN = 64;
+
+template <class T> struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+};
+
+struct Plan {
+  // ---- configuration / host structure
+  nqg_settings set;
+  int n = 0;
+  Symbolic sym;
+  Csc K;                            // lower CSC, original ordering, values after perturbation
+  std::vector<double> Kx_spmv;      // same pattern, perturbed diagonals set to 0 (reference set_diags(0))
+  std::vector<int64_t> pert_idx;    // value indices of perturbed diagonals
+  Csc Uord;                         // upper pattern of the ordered matrix (reach computation)
+  std::vector<int> level_of;        // per supernode
+  std::vector<std::vector<int>> levels;
+  std::vector<int> pair_ptr;        // per supernode s: range of its descendant pairs
+  std::vector<int> pair_d, pair_lb, pair_ub;
+  std::vector<int64_t> tile_ptr;    // per supernode s: range of its update tiles
+  std::vector<UpdTile> tiles;
+  std::vector<int> wide;            // supernodes factored by the blocked kernel
+  int64_t ssize = 0;
+
+  // ---- device structure
+  cudaStream_t stream = nullptr, own_stream = nullptr;
+  int *d_super = nullptr, *d_col2sup = nullptr, *d_ls = nullptr, *d_ls_sym = nullptr;
+  int64_t *d_lpi = nullptr, *d_lpx = nullptr;
+  int *d_Kp = nullptr, *d_Ki = nullptr;
+  double *d_Kx = nullptr;           // factorization copy of K values
+  int *d_Rp = nullptr, *d_Rj = nullptr;  // full (both triangles) CSR of K for the SpMV
+  double *d_Rx = nullptr;
+  int64_t *d_map_lo = nullptr, *d_map_hi = nullptr;  // CSC value index -> CSR positions
+  int *d_perm = nullptr, *d_iperm = nullptr, *d_locperm = nullptr, *d_perm_tmp = nullptr;
+  void *d_L = nullptr;              // factor values (double or float)
+  void *d_D = nullptr;              // 2n: diagonal then 2x2 sub-diagonal
+  UpdTile *d_tiles = nullptr;
+  int *d_tile_list = nullptr;       // tile ids for a partial refactor
+  size_t tile_list_cap = 0;
+  int *d_targets = nullptr;         // supernode ids for per-level kernels
+  size_t targets_cap = 0;
+  int *d_pair_s = nullptr, *d_pair_d = nullptr, *d_pair_lb = nullptr, *d_pair_ub = nullptr;
+  int *d_targets_lv = nullptr;      // all supernodes grouped by level (solve kernels)
+  std::vector<int> level_off;       // offsets of each level in d_targets_lv
+  double *d_in = nullptr, *d_out = nullptr;  // host-buffer solve staging
+  uint8_t *d_pivoted = nullptr;     // 2*nsuper: [0,ns) BK permuted the supernode in the last factor,
+                                    // [ns,2ns) supernode is being factored by the current call
+  uint8_t *d_visible = nullptr, *d_hidden = nullptr;
+  bool masked = false;
+  int *d_status = nullptr;
+  // refinement workspace
+  double *d_xo = nullptr, *d_bo = nullptr, *d_r = nullptr, *d_V = nullptr, *d_w = nullptr, *d_scal = nullptr;
+  int mr_cap = 0;
+
+  bool factored = false;
+  nqg_timings tm{};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string last_error;
+
+  size_t val_size() const { return set.precision == NQG_FP32 ? sizeof(float) : sizeof(double); }
+};
+
+// numeric.cu
+int dev_factor(Plan &P, const std::vector<int> *subset);
+// solve.cu
+int dev_ldlt_solve_ord(Plan &P, double *d_x);
+int dev_spmv_ord(Plan &P, const double *d_x_ord, double *d_y_ord);
+int dev_spmv_orig(Plan &P, const double *d_x, double *d_y);
+int dev_solve(Plan &P, const double *d_rhs, double *d_x);
+int dev_assemble_upload(Plan &P);
+
+#define NQG_CUDA(call)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) {                                                             \
+      P.last_error = std::string(#call) + ": " + cudaGetErrorString(e_);                 \
+      return NQG_ERR_CUDA;                                                               \
+    }                                                                                    \
+  } while (0)
+
+}  // namespace nqg
