@@ -44,6 +44,12 @@ typedef struct nqg_settings {
   int regularization;   /* 1: |a_jj| < reg_diag -> a_jj = reg_diag (reference find_perturbation) */
   int n_relax[3];       /* supernode relaxation (reference n_relax) */
   double z_relax[3];    /* supernode relaxation (reference z_relax) */
+  /* FP32 factor only: diagonal entries smaller than this in magnitude are
+   * replaced by +-reg_diag_fp32 (sign kept, 0 -> +) in the matrix that is
+   * factored, bounding the element growth of block-restricted pivoting to
+   * what FP32 can carry; the refinement still works on the reference's
+   * matrix.  <= 0 selects 3e-4 * max|a_ij|. */
+  double reg_diag_fp32;
 } nqg_settings;
 
 /* Reference defaults (src/QP/linear_solver_wrapper.cpp:205-244). */
@@ -149,6 +155,41 @@ int nqg_get_timings(const nqg_plan *plan, nqg_timings *t);
 int nqg_get_factor(const nqg_plan *plan, double *values, double *d, int *perm, int *ls);
 /* Device error word of the last factor/solve (bit flags, 0 = clean). */
 int nqg_get_device_status(const nqg_plan *plan, int *status_bits);
+
+/* ---- QP solve (dual active-set NASOQ over the GPU LBL) ------------------- */
+typedef struct nqg_qp_settings {
+  int variant;          /* 0 Fixed, 1 AUTO, 2 Tuned, 3 PREDET (reference nasoq_mode) */
+  double eps_abs;       /* KKT tolerance (reference Nasoq::eps_abs) */
+  double diag_perturb;  /* KKT regularization (reference diag_perturb) */
+  double stop_tol;      /* refinement tolerance (reference stop_tol) */
+  int max_iter;         /* refinement iterations (reference max_iter) */
+  int max_iter_nas;     /* active-set iteration cap (reference max_iter_nas) */
+  int precision;        /* NQG_FP64 or NQG_FP32 factorization */
+} nqg_qp_settings;
+
+typedef struct nqg_qp_result {
+  int status;           /* reference nasoq_status: 1 Optimal, 2 Inaccurate, 3 NotConverged, 0 Infeasible */
+  int num_iter, active_size;
+  double objective, primal_obj, dual_obj;
+  double lag_res, cons_sat_norm, non_negativity_infn, complementarity_infn;
+  double total_seconds, factor_seconds;
+} nqg_qp_result;
+
+/* Defaults of the reference Nasoq object (src/nasoq.cpp:163-182). */
+void nqg_qp_default_settings(nqg_qp_settings *s);
+/* min 1/2 x'Hx + q'x  s.t.  A x = a,  B x <= b.  H: n-by-n lower CSC (diagonal
+ * first); A: meq-by-n CSC; B: mineq-by-n CSC (A/B pointers may be NULL when
+ * their row count is 0).  Outputs x (n), y (meq equality duals), z (mineq
+ * inequality duals), active_set (mineq ints, first result->active_size used).
+ * Replaces Nasoq(...) + Nasoq::solve() (src/nasoq.cpp:95-160, 656-710).
+ * With warm-start arrays (x0, z0, y0 and a list of n_as active constraints,
+ * all non-NULL) it replaces symbolic_QP + set_warm_start + numeric_QP
+ * (src/nasoq.cpp:413-436, 741-762). */
+int nqg_qp_solve(int n, const int *Hp, const int *Hi, const double *Hx, const double *q, int meq, const int *Ap,
+                 const int *Ai, const double *Ax, const double *a, int mineq, const int *Bp, const int *Bi,
+                 const double *Bx, const double *b, const nqg_qp_settings *settings, const double *x0,
+                 const double *z0, const double *y0, int n_as, const int *as0, double *x, double *y, double *z,
+                 int *active_set, nqg_qp_result *result);
 
 #ifdef __cplusplus
 }

@@ -29,7 +29,8 @@ _u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 class Settings(C.Structure):
     _fields_ = [("precision", C.c_int), ("req_ref_iter", C.c_int), ("max_inner_iter", C.c_int),
                 ("tol_abs", C.c_double), ("tol_rel", C.c_double), ("reg_diag", C.c_double),
-                ("regularization", C.c_int), ("n_relax", C.c_int * 3), ("z_relax", C.c_double * 3)]
+                ("regularization", C.c_int), ("n_relax", C.c_int * 3), ("z_relax", C.c_double * 3),
+                ("reg_diag_fp32", C.c_double)]
 
 
 class SymbolicInfo(C.Structure):
@@ -42,6 +43,19 @@ class Timings(C.Structure):
     _fields_ = [("factor_ms", C.c_double), ("solve_ms", C.c_double), ("refine_ms", C.c_double),
                 ("num_ref_iter", C.c_int), ("num_pivot_supernodes", C.c_int), ("num_2x2", C.c_int),
                 ("last_residual", C.c_double)]
+
+
+class QPSettings(C.Structure):
+    _fields_ = [("variant", C.c_int), ("eps_abs", C.c_double), ("diag_perturb", C.c_double),
+                ("stop_tol", C.c_double), ("max_iter", C.c_int), ("max_iter_nas", C.c_int), ("precision", C.c_int)]
+
+
+class QPResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("num_iter", C.c_int), ("active_size", C.c_int), ("objective", C.c_double),
+                ("primal_obj", C.c_double), ("dual_obj", C.c_double), ("lag_res", C.c_double),
+                ("cons_sat_norm", C.c_double), ("non_negativity_infn", C.c_double),
+                ("complementarity_infn", C.c_double), ("total_seconds", C.c_double),
+                ("factor_seconds", C.c_double)]
 
 
 _lib = None
@@ -82,6 +96,11 @@ def lib():
     L.nqg_get_timings.argtypes = [C.c_void_p, C.POINTER(Timings)]
     L.nqg_get_factor.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.nqg_get_device_status.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
+    L.nqg_qp_default_settings.argtypes = [C.POINTER(QPSettings)]
+    L.nqg_qp_default_settings.restype = None
+    L.nqg_qp_solve.argtypes = [C.c_int] + [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 4 + [C.c_int] + \
+        [C.c_void_p] * 4 + [C.POINTER(QPSettings), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(QPResult)]
     _lib = L
     return L
 
@@ -237,3 +256,50 @@ class Plan:
 
     def __del__(self):
         self.close()
+
+
+VARIANTS = {"fixed": 0, "auto": 1, "tuned": 2, "predet": 3}
+
+
+def qp_settings(**kw) -> QPSettings:
+    s = QPSettings()
+    lib().nqg_qp_default_settings(C.byref(s))
+    for k, v in kw.items():
+        if k == "variant" and isinstance(v, str):
+            v = VARIANTS[v.lower()]
+        setattr(s, k, v)
+    return s
+
+
+def qp_solve(H, q, A, b, Cm, d, settings: QPSettings | None = None, warm=None):
+    """Solves min 1/2 x'Hx + q'x s.t. A x = b, Cm x <= d with the NASOQ
+    active-set method on the GPU.  H, A, Cm are CSC objects with p/i/x
+    arrays (H lower-stored).  warm = (x0, z0, active_set[, y0]) starts from a
+    given point and active set.  Returns (x, y, z, active_set, QPResult)."""
+    L = lib()
+    n = int(H.ncol)
+    meq, mineq = int(A.nrow), int(Cm.nrow)
+    arr = lambda a, t: np.ascontiguousarray(a, t)
+    Hp, Hi, Hx, qv = arr(H.p, np.int32), arr(H.i, np.int32), arr(H.x, np.float64), arr(q, np.float64)
+    Ap, Ai, Ax, bv = arr(A.p, np.int32), arr(A.i, np.int32), arr(A.x, np.float64), arr(b, np.float64)
+    Cp, Ci, Cx, dv = arr(Cm.p, np.int32), arr(Cm.i, np.int32), arr(Cm.x, np.float64), arr(d, np.float64)
+    x = np.zeros(n)
+    y = np.zeros(max(meq, 1))
+    z = np.zeros(max(mineq, 1))
+    act = np.zeros(max(mineq, 1), np.int32)
+    res = QPResult()
+    st = settings if settings is not None else qp_settings()
+    x0 = z0 = y0 = as0 = None
+    nas = 0
+    if warm is not None:
+        x0 = arr(warm[0], np.float64)
+        z0 = arr(warm[1], np.float64)
+        as0 = arr(warm[2], np.int32)
+        nas = len(as0)
+        if len(warm) > 3 and warm[3] is not None:
+            y0 = arr(warm[3], np.float64)
+    rc = L.nqg_qp_solve(n, _ptr(Hp), _ptr(Hi), _ptr(Hx), _ptr(qv), meq, _ptr(Ap), _ptr(Ai), _ptr(Ax), _ptr(bv),
+                        mineq, _ptr(Cp), _ptr(Ci), _ptr(Cx), _ptr(dv), C.byref(st), _ptr(x0), _ptr(z0), _ptr(y0),
+                        nas, _ptr(as0), _ptr(x), _ptr(y), _ptr(z), _ptr(act), C.byref(res))
+    _check(rc, "qp solve")
+    return x, y[:meq], z[:mineq], act[:res.active_size].copy(), res

@@ -35,6 +35,7 @@ extern "C" void nqg_default_settings(nqg_settings *s) {
   s->z_relax[0] = 0.8;
   s->z_relax[1] = 0.1;
   s->z_relax[2] = 0.05;
+  s->reg_diag_fp32 = 0.0;
 }
 
 extern "C" const char *nqg_status_str(int st) {
@@ -314,14 +315,35 @@ static void free_plan(Plan &P) {
 static void apply_perturbation(Plan &P) {
   P.pert_idx.clear();
   P.Kx_spmv = P.K.x;
-  if (P.set.regularization != 1) return;
-  for (int j = 0; j < P.n; ++j) {
-    int q = P.K.p[j];
-    if (q >= P.K.p[j + 1]) continue;
-    if (std::abs(P.K.x[q]) < P.set.reg_diag) {
-      P.K.x[q] = P.set.reg_diag;
-      P.Kx_spmv[q] = 0.0;
-      P.pert_idx.push_back(q);
+  if (P.set.regularization == 1) {
+    for (int j = 0; j < P.n; ++j) {
+      int q = P.K.p[j];
+      if (q >= P.K.p[j + 1]) continue;
+      if (std::abs(P.K.x[q]) < P.set.reg_diag) {
+        P.K.x[q] = P.set.reg_diag;
+        P.Kx_spmv[q] = 0.0;
+        P.pert_idx.push_back(q);
+      }
+    }
+  }
+  // FP32 factor: a larger, sign-keeping floor on the diagonal of the matrix
+  // that is factored.  Pivots as small as the reference's 1e-8..1e-9
+  // regularization create element growth of 1e8..1e9 under block-restricted
+  // Bunch-Kaufman, beyond what FP32 values can carry; the refinement matrix
+  // (Kx_spmv) is left as the reference defines it.
+  if (P.set.precision == NQG_FP32) {
+    double tau = P.set.reg_diag_fp32;
+    if (tau <= 0) {
+      double amax = 0;
+      for (double v : P.Kx_spmv) amax = std::max(amax, std::abs(v));
+      tau = 3e-4 * (amax > 0 ? amax : 1.0);
+    }
+    P.reg32 = tau;
+    for (int j = 0; j < P.n; ++j) {
+      int q = P.K.p[j];
+      if (q >= P.K.p[j + 1]) continue;
+      double v = P.K.x[q];
+      if (std::abs(v) < tau) P.K.x[q] = v < 0 ? -tau : tau;
     }
   }
 }
@@ -335,7 +357,9 @@ extern "C" int nqg_plan_create(int n, const int *Ap, const int *Ai, const double
   Plan &P = h->P;
   if (settings) P.set = *settings;
   else nqg_default_settings(&P.set);
-  if (P.set.precision != NQG_FP64 && P.set.precision != NQG_FP32) {
+  // the refinement keeps its Hessenberg solution in 48 device scalar slots
+  if (P.set.precision != NQG_FP64 && P.set.precision != NQG_FP32 || P.set.max_inner_iter > 48 ||
+      P.set.max_inner_iter < 0 || P.set.req_ref_iter < 0) {
     delete h;
     return NQG_ERR_ARG;
   }

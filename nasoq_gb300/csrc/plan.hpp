@@ -44,6 +44,7 @@ struct Plan {
   Csc K;                            // lower CSC, original ordering, values after perturbation
   std::vector<double> Kx_spmv;      // same pattern, perturbed diagonals set to 0 (reference set_diags(0))
   std::vector<int64_t> pert_idx;    // value indices of perturbed diagonals
+  double reg32 = 0.0;               // diagonal floor of the FP32 factor
   Csc Uord;                         // upper pattern of the ordered matrix (reach computation)
   std::vector<int> level_of;        // per supernode
   std::vector<std::vector<int>> levels;

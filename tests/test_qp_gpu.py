@@ -1,0 +1,72 @@
+"""GPU parity of the NASOQ QP solve (Nasoq::solve(), src/nasoq.cpp:656-710)
+against the reference on its own known-answer problems (tests/1.json and
+data/*.yml with data/out_correct.csv) and on seeded QPs.
+
+The active-set loop is replayed with the same decisions, so status, the
+number of iterations and the final active set must be identical; primal and
+dual solutions agree to 1e-7 relative (the refinement-free PREDET settings of
+tests/1.json reach 1e-12), the objective to 1e-9 relative, and the KKT norms
+must meet eps_abs."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import nqa
+import nasoq_gb300 as nq
+from nasoq_gb300.problems import CSC
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+CASES = sorted(glob.glob(os.path.join(GOLD, "qp_*.nqa")))
+
+
+def load_qp(d):
+    n = len(d["in_Hp"]) - 1
+    meq, mineq = int(d["in_meq"][0]), int(d["in_mineq"][0])
+    H = CSC(n, n, d["in_Hp"], d["in_Hi"], d["in_Hx"])
+    A = CSC(meq, n, d["in_Ap"], d["in_Ai"], d["in_Ax"])
+    Cm = CSC(mineq, n, d["in_Cp"], d["in_Ci"], d["in_Cx"])
+    return H, d["in_q"], A, d["in_b"], Cm, d["in_d"]
+
+
+def run(d, precision=nq.NQG_FP64):
+    st = nq.qp_settings(variant=int(d["in_variant"][0]), eps_abs=float(d["in_eps_abs"][0]),
+                        diag_perturb=float(d["in_diag_perturb"][0]),
+                        max_iter=int(d["in_max_iter"][0]),
+                        stop_tol=float(d.get("in_stop_tol", [1e-15])[0]),
+                        max_iter_nas=int(d.get("in_max_iter_nas", [200000])[0]), precision=precision)
+    return nq.qp_solve(*load_qp(d), settings=st)
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", CASES, ids=os.path.basename)
+def test_qp_matches_reference(path):
+    d = nqa.load(path)
+    x, y, z, act, res = run(d)
+    assert res.status == int(d["out_status"][0])
+    assert res.num_iter == int(d["out_num_iter"][0])
+    assert sorted(act.tolist()) == sorted(d["out_active_set"].tolist())
+    assert rel(x, d["out_x"]) <= 1e-7
+    assert rel(z, d["out_z"]) <= 1e-7
+    if "out_y" in d:
+        assert rel(y, d["out_y"]) <= 1e-7
+    ob = float(d["out_objective"][0])
+    assert abs(res.objective - ob) <= 1e-9 * max(abs(ob), 1.0)
+    eps = float(d["in_eps_abs"][0])
+    assert res.cons_sat_norm <= eps and res.non_negativity_infn <= eps
+
+
+@pytest.mark.gpu
+def test_qp_test1json_known_answer():
+    """tests/1.json of the reference: x, y, z to Eigen's isApprox (1e-12)."""
+    d = nqa.load(os.path.join(GOLD, "qp_test1json.nqa"))
+    x, y, z, act, res = run(d)
+    assert res.status == 1 and res.num_iter == 23
+    assert rel(x, d["out_json_x"]) <= 1e-12
+    assert rel(z, d["out_json_z"]) <= 1e-12
