@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -154,8 +155,6 @@ static void build_schedule(Plan &P) {
   }
   P.levels.assign(ns > 0 ? maxlev + 1 : 0, {});
   for (int s = 0; s < ns; ++s) P.levels[P.level_of[s]].push_back(s);
-  P.level_off.assign(P.levels.size() + 1, 0);
-  for (size_t l = 0; l < P.levels.size(); ++l) P.level_off[l + 1] = P.level_off[l] + (int)P.levels[l].size();
   // pairs
   std::vector<int> mark(ns, 0), stack, lst;
   P.pair_ptr.assign(ns + 1, 0);
@@ -274,9 +273,22 @@ static int upload_plan(Plan &P) {
   if ((rc = dev_alloc_copy(P, &P.d_pair_d, P.pair_d.data(), P.pair_d.size()))) return rc;
   if ((rc = dev_alloc_copy(P, &P.d_pair_lb, P.pair_lb.data(), P.pair_lb.size()))) return rc;
   if ((rc = dev_alloc_copy(P, &P.d_pair_ub, P.pair_ub.data(), P.pair_ub.size()))) return rc;
+  // tuning overrides: width above which the blocked multi-CTA kernels take
+  // a supernode, and their panel width
+  if (const char *e = std::getenv("NASOQ_GB300_WIDE_MIN")) P.wide_min = std::max(1, std::atoi(e));
+  if (const char *e = std::getenv("NASOQ_GB300_WIDE_NB")) P.wide_nb = std::min(64, std::max(4, std::atoi(e)));
   std::vector<int> lvflat;
-  for (auto &lv : P.levels) lvflat.insert(lvflat.end(), lv.begin(), lv.end());
+  P.level_off.assign(P.levels.size() + 1, 0);
+  P.wide_lv.assign(P.levels.size(), {});
+  for (size_t l = 0; l < P.levels.size(); ++l) {
+    for (int s : P.levels[l]) {
+      if (S.super[s + 1] - S.super[s] > P.wide_min) P.wide_lv[l].push_back(s);
+      else lvflat.push_back(s);
+    }
+    P.level_off[l + 1] = (int)lvflat.size();
+  }
   if ((rc = dev_alloc_copy(P, &P.d_targets_lv, lvflat.data(), lvflat.size()))) return rc;
+  P.vis_host.assign(ns, 1);
   NQG_CUDA(cudaMalloc(&P.d_pivoted, std::max(2 * ns, 2)));
   NQG_CUDA(cudaMemset(P.d_pivoted, 0, std::max(2 * ns, 2)));
   NQG_CUDA(cudaMalloc(&P.d_visible, std::max(ns, 1)));
@@ -293,6 +305,19 @@ static int upload_plan(Plan &P) {
   NQG_CUDA(cudaMalloc(&P.d_out, nn * sizeof(double)));
   NQG_CUDA(cudaMalloc(&P.d_V, (size_t)(P.mr_cap + 1) * nn * sizeof(double)));
   NQG_CUDA(cudaMalloc(&P.d_scal, (64 + 512) * sizeof(double)));
+  {
+    int dev = 0;
+    NQG_CUDA(cudaGetDevice(&dev));
+    NQG_CUDA(cudaDeviceGetAttribute(&P.num_sms, cudaDevAttrMultiProcessorCount, dev));
+    int64_t wide_rows = 0;
+    for (int s = 0; s < ns; ++s)
+      if (S.super[s + 1] - S.super[s] > P.wide_min) wide_rows = std::max<int64_t>(wide_rows, S.lpi[s + 1] - S.lpi[s]);
+    if (wide_rows > 0) {
+      NQG_CUDA(cudaMalloc(&P.d_wide_W, (size_t)wide_rows * (P.wide_nb + 2) * P.val_size()));
+      NQG_CUDA(cudaMalloc(&P.d_wide_ctl, wide_ctl_bytes()));
+      NQG_CUDA(cudaMemset(P.d_wide_ctl, 0, wide_ctl_bytes()));
+    }
+  }
   return NQG_OK;
 }
 
@@ -301,7 +326,7 @@ static void free_plan(Plan &P) {
                   P.d_Rp, P.d_Rj, P.d_Rx, P.d_map_lo, P.d_map_hi, P.d_perm, P.d_iperm, P.d_locperm,
                   P.d_perm_tmp, P.d_L, P.d_D, P.d_tiles, P.d_tile_list, P.d_targets, P.d_pair_s, P.d_pair_d,
                   P.d_pair_lb, P.d_pair_ub, P.d_targets_lv, P.d_pivoted, P.d_visible, P.d_hidden, P.d_status,
-                  P.d_xo, P.d_bo, P.d_r, P.d_w, P.d_in, P.d_out, P.d_V, P.d_scal};
+                  P.d_xo, P.d_bo, P.d_r, P.d_w, P.d_in, P.d_out, P.d_V, P.d_scal, P.d_wide_W, P.d_wide_ctl};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (P.ev0) cudaEventDestroy(P.ev0);
@@ -515,6 +540,7 @@ extern "C" int nqg_set_visibility(nqg_plan *h, const uint8_t *visible_sn, const 
   std::vector<uint8_t> vis(ns, 1), hid(P.n, 0);
   if (visible_sn) std::copy(visible_sn, visible_sn + ns, vis.begin());
   if (hidden_col) std::copy(hidden_col, hidden_col + P.n, hid.begin());
+  P.vis_host = vis;
   NQG_CUDA(cudaMemcpyAsync(P.d_visible, vis.data(), ns, cudaMemcpyHostToDevice, P.stream));
   NQG_CUDA(cudaMemcpyAsync(P.d_hidden, hid.data(), P.n, cudaMemcpyHostToDevice, P.stream));
   NQG_CUDA(cudaStreamSynchronize(P.stream));

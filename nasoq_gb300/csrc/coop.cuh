@@ -1,0 +1,66 @@
+// Cooperative-launch helpers shared by the multi-CTA kernels of wide
+// supernodes: the control block and a bounded grid-wide barrier.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "plan.hpp"
+
+namespace nqg {
+
+struct WideCtl {
+  unsigned count;
+  unsigned gen;
+  int abort;
+  int kb;          // columns completed by the last panel launch
+  int pivoted;     // any interchange in this supernode
+  int pad[3];
+  double cval[2][1024];
+  int cidx[2][1024];
+  double rval[2][1024];
+  int ridx[2][1024];
+};
+
+constexpr long long SPIN_LIMIT = 1ll << 26;  // polls before a barrier gives up
+
+// Grid-wide barrier for a cooperative launch, sense-reversing on ctl->gen.
+// Returns false once any CTA has timed out (all CTAs then unwind).
+__device__ __forceinline__ bool grid_sync(WideCtl *ctl, int *status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned *vgen = &ctl->gen;
+    volatile int *vab = &ctl->abort;
+    unsigned my = *vgen;
+    __threadfence();
+    unsigned arrived = atomicAdd(&ctl->count, 1u);
+    if (arrived == gridDim.x - 1) {
+      ctl->count = 0;
+      __threadfence();
+      atomicAdd(&ctl->gen, 1u);
+    } else {
+      long long it = 0;
+      while (*vgen == my) {
+        if (*vab) {
+          ok = 0;
+          break;
+        }
+        if (++it > SPIN_LIMIT) {
+          atomicOr(status, ST_TIMEOUT);
+          atomicExch(&ctl->abort, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (*vab) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+
+}  // namespace nqg

@@ -729,11 +729,15 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
   const int nlev = (int)P.levels.size();
   for (int l = 0; l < nlev; ++l) {
     int so = (int)order.size();
-    for (int s : P.levels[l])
-      if (mark[s] && P.sym.super[s + 1] - P.sym.super[s] <= BK_SMALL) order.push_back(s);
+    for (int s : P.levels[l]) {
+      const int w = P.sym.super[s + 1] - P.sym.super[s];
+      if (mark[s] && w <= BK_SMALL && w <= P.wide_min) order.push_back(s);
+    }
     int go = (int)order.size();
-    for (int s : P.levels[l])
-      if (mark[s] && P.sym.super[s + 1] - P.sym.super[s] > BK_SMALL) order.push_back(s);
+    for (int s : P.levels[l]) {
+      const int w = P.sym.super[s + 1] - P.sym.super[s];
+      if (mark[s] && w > BK_SMALL && w <= P.wide_min) order.push_back(s);
+    }
     lv_small_off.push_back(so);
     lv_small_cnt.push_back(go - so);
     lv_glob_off.push_back(go);
@@ -745,8 +749,10 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
     lv_tile_off.push_back(to);
     lv_tile_cnt.push_back((int64_t)tile_ids.size() - to);
   }
-  if (order.empty()) return NQG_OK;
-  if (order.size() > P.targets_cap) {
+  bool any = false;
+  for (int s = 0; s < ns && !any; ++s) any = mark[s] != 0;
+  if (!any) return NQG_OK;
+  if (std::max<size_t>(order.size(), 1) > P.targets_cap) {
     if (P.d_targets) cudaFree(P.d_targets);
     P.targets_cap = std::max<size_t>(order.size(), 64);
     NQG_CUDA(cudaMalloc(&P.d_targets, P.targets_cap * sizeof(int)));
@@ -756,7 +762,8 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
     P.tile_list_cap = std::max<size_t>(tile_ids.size(), 64);
     NQG_CUDA(cudaMalloc(&P.d_tile_list, P.tile_list_cap * sizeof(int)));
   }
-  NQG_CUDA(cudaMemcpyAsync(P.d_targets, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  if (!order.empty())
+    NQG_CUDA(cudaMemcpyAsync(P.d_targets, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, st));
   if (!tile_ids.empty())
     NQG_CUDA(cudaMemcpyAsync(P.d_tile_list, tile_ids.data(), tile_ids.size() * sizeof(int), cudaMemcpyHostToDevice,
                              st));
@@ -768,8 +775,15 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
     NQG_CUDA(cudaMemsetAsync(L, 0, (size_t)P.sym.xsize * sizeof(T), st));
     NQG_CUDA(cudaMemsetAsync(D, 0, (size_t)2 * n * sizeof(T), st));
   } else {
-    k_zero_targets<T><<<(unsigned)order.size(), 256, 0, st>>>(P.d_targets, (int)order.size(), P.d_super, P.d_lpi,
-                                                                P.d_lpx, L, D, n);
+    // every supernode being refactored, staged in the permutation scratch
+    // buffer (n >= nsuper ints; its later users run after this kernel)
+    std::vector<int> all_marked;
+    for (int s = 0; s < ns; ++s)
+      if (mark[s]) all_marked.push_back(s);
+    NQG_CUDA(cudaMemcpyAsync(P.d_perm_tmp, all_marked.data(), all_marked.size() * sizeof(int),
+                             cudaMemcpyHostToDevice, st));
+    k_zero_targets<T><<<(unsigned)all_marked.size(), 256, 0, st>>>(P.d_perm_tmp, (int)all_marked.size(), P.d_super,
+                                                                   P.d_lpi, P.d_lpx, L, D, n);
   }
   {
     int blocks = std::min(std::max((n + 7) / 8, 1), 4096);
@@ -795,6 +809,12 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
     if (lv_glob_cnt[l] > 0)
       k_bk_global<T><<<lv_glob_cnt[l], 256, 0, st>>>(P.d_targets + lv_glob_off[l], n, P.d_super, P.d_lpi, P.d_lpx,
                                                       L, D, P.d_locperm, P.d_pivoted, P.d_perm_tmp, P.d_status);
+    for (int s : P.levels[l]) {
+      if (!mark[s] || P.sym.super[s + 1] - P.sym.super[s] <= P.wide_min) continue;
+      int rc = factor_wide<T>(P, s, L, D, P.wide_nb, reinterpret_cast<T *>(P.d_wide_W),
+                              reinterpret_cast<WideCtl *>(P.d_wide_ctl), P.num_sms);
+      if (rc) return rc;
+    }
   }
   NQG_CUDA(cudaGetLastError());
   // row renaming in descendants of pivoted supernodes

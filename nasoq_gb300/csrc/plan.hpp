@@ -73,8 +73,10 @@ struct Plan {
   int *d_targets = nullptr;         // supernode ids for per-level kernels
   size_t targets_cap = 0;
   int *d_pair_s = nullptr, *d_pair_d = nullptr, *d_pair_lb = nullptr, *d_pair_ub = nullptr;
-  int *d_targets_lv = nullptr;      // all supernodes grouped by level (solve kernels)
+  int *d_targets_lv = nullptr;      // narrow supernodes grouped by level (solve kernels)
   std::vector<int> level_off;       // offsets of each level in d_targets_lv
+  std::vector<std::vector<int>> wide_lv;  // wide supernodes of each level (multi-CTA solves)
+  std::vector<uint8_t> vis_host;    // host copy of the supernode visibility mask
   double *d_in = nullptr, *d_out = nullptr;  // host-buffer solve staging
   uint8_t *d_pivoted = nullptr;     // 2*nsuper: [0,ns) BK permuted the supernode in the last factor,
                                     // [ns,2ns) supernode is being factored by the current call
@@ -84,6 +86,12 @@ struct Plan {
   // refinement workspace
   double *d_xo = nullptr, *d_bo = nullptr, *d_r = nullptr, *d_V = nullptr, *d_w = nullptr, *d_scal = nullptr;
   int mr_cap = 0;
+  // wide supernodes (blocked cooperative BK)
+  void *d_wide_W = nullptr;         // panel buffer, max nrow x (nb+2)
+  void *d_wide_ctl = nullptr;       // barrier / reduction control block
+  int wide_nb = 64;
+  int wide_min = 256;               // supernodes wider than this use the blocked kernels
+  int num_sms = 0;
 
   bool factored = false;
   nqg_timings tm{};
@@ -93,8 +101,16 @@ struct Plan {
   size_t val_size() const { return set.precision == NQG_FP32 ? sizeof(float) : sizeof(double); }
 };
 
+
 // numeric.cu
 int dev_factor(Plan &P, const std::vector<int> *subset);
+// wide.cu
+struct WideCtl;
+size_t wide_ctl_bytes();
+template <class T> int factor_wide(Plan &P, int s, T *L, T *Dg, int nb, T *Wb, WideCtl *ctl, int num_sms);
+// solve_wide.cu
+template <class T> int solve_wide_fwd(Plan &P, int s, const T *L, double *x);
+template <class T> int solve_wide_bwd(Plan &P, int s, const T *L, double *x);
 // solve.cu
 int dev_ldlt_solve_ord(Plan &P, double *d_x);
 int dev_spmv_ord(Plan &P, const double *d_x_ord, double *d_y_ord);

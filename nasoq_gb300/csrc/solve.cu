@@ -209,16 +209,25 @@ template <class T> static int ldlt_solve_impl(Plan &P, double *x) {
     smem_set[ai][0] = smem;
   }
   const int nlev = (int)P.levels.size();
+  int rc;
   for (int l = 0; l < nlev; ++l) {
-    int cnt = (int)P.levels[l].size();
-    k_fwd<T><<<cnt, SV_THREADS, smem, st>>>(P.d_targets_lv + P.level_off[l], P.d_super, P.d_lpi, P.d_lpx, P.d_ls, L,
-                                             x, vis);
+    int cnt = P.level_off[l + 1] - P.level_off[l];
+    if (cnt > 0)
+      k_fwd<T><<<cnt, SV_THREADS, smem, st>>>(P.d_targets_lv + P.level_off[l], P.d_super, P.d_lpi, P.d_lpx, P.d_ls,
+                                               L, x, vis);
+    for (int s : P.wide_lv[l])
+      if (!P.masked || P.vis_host[s])
+        if ((rc = solve_wide_fwd<T>(P, s, L, x))) return rc;
   }
   k_dsolve<T><<<grid_for(P.n), 256, 0, st>>>(P.n, D, x, hid);
   for (int l = nlev - 1; l >= 0; --l) {
-    int cnt = (int)P.levels[l].size();
-    k_bwd<T><<<cnt, SV_THREADS, smem, st>>>(P.d_targets_lv + P.level_off[l], P.d_super, P.d_lpi, P.d_lpx, P.d_ls, L,
-                                             x, vis);
+    for (int s : P.wide_lv[l])
+      if (!P.masked || P.vis_host[s])
+        if ((rc = solve_wide_bwd<T>(P, s, L, x))) return rc;
+    int cnt = P.level_off[l + 1] - P.level_off[l];
+    if (cnt > 0)
+      k_bwd<T><<<cnt, SV_THREADS, smem, st>>>(P.d_targets_lv + P.level_off[l], P.d_super, P.d_lpi, P.d_lpx, P.d_ls,
+                                               L, x, vis);
   }
   NQG_CUDA(cudaGetLastError());
   return NQG_OK;
