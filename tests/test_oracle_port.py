@@ -1,0 +1,78 @@
+"""The oracle restatement is pinned to the reference: on every LBL golden
+fixture, run on the reference's own symbolic structure, it reproduces the
+reference's factor (values, D, combined permutation, row lists after pivoting)
+and solutions.  Runs on CPU only.
+
+The reference sets OpenBLAS to all cores for the factorization
+(SET_BLAS_THREAD(num_thread), src/QP/linear_solver_wrapper.cpp:626), and
+OpenBLAS partitions the larger dgemm/dsytrf calls by thread count, so the
+fixtures (made on an 8-core x86-64 host) are reproduced bit for bit with 8
+BLAS threads on x86-64; other hosts get a rounding-level tolerance."""
+import glob
+import os
+import platform
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+
+import nqa
+from oracle import port
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+FIXTURE_BLAS_THREADS = 8
+SAME_PLATFORM = platform.machine() == "x86_64"
+CASES = sorted(glob.glob(os.path.join(GOLD, "lbl_*.nqa")))
+
+
+def ref_sym(d):
+    n = len(d["in_rhs"])
+    sup = d["out_sym_super"]
+    c2s = d["out_sym_col2Sup"]
+    ip = d["out_sym_i_ptr"]
+    lpi = np.append(ip[sup[:-1]], ip[n]).astype(np.int64)
+    return SimpleNamespace(perm=d["out_sym_Perm"], super=sup, lpi=lpi, ls=d["out_sym_s"], colp=d["out_sym_p"],
+                           sparent=d["out_sym_sParent"], col2sup=c2s)
+
+
+def refine_matrix(d):
+    """Refinement values: the reference zeroes the perturbed diagonals (set_diags(0))."""
+    ax = d["in_Ax"].copy()
+    axp = d["out_Ax_perturbed"]
+    pert = ax != axp
+    ax[pert] = 0.0
+    return ax
+
+
+@pytest.mark.parametrize("path", CASES, ids=os.path.basename)
+def test_port_reproduces_reference_factor(path):
+    port.set_threads(FIXTURE_BLAS_THREADS)
+    d = nqa.load(path)
+    n = len(d["in_rhs"])
+    out = port.solve(n, d["in_Ap"], d["in_Ai"], d["out_Ax_perturbed"], refine_matrix(d), ref_sym(d), d["in_rhs"],
+                     req_ref_iter=0, want_factor=True)
+    assert np.array_equal(out["perm"], d["out_fac_Perm"])
+    assert np.array_equal(out["ls"], d["out_fac_s"])
+    if SAME_PLATFORM:
+        # same BLAS library and threads, same operation order: identical bits
+        assert np.array_equal(out["L"], d["out_valL"])
+        assert np.array_equal(out["D"], d["out_d_val"])
+    xr = d["out_x_noref"]
+    g = np.abs(d["out_valL"]).max()
+    assert np.linalg.norm(out["x"] - xr) <= max(1e-13, 1e-15 * g) * np.linalg.norm(xr)
+
+
+@pytest.mark.parametrize("path", CASES, ids=os.path.basename)
+def test_port_refined_solution(path):
+    port.set_threads(FIXTURE_BLAS_THREADS)
+    d = nqa.load(path)
+    n = len(d["in_rhs"])
+    rr = int(d.get("in_req_ref_iter", [2])[0])
+    mi = int(d.get("in_max_inner_iter", [2])[0])
+    out = port.solve(n, d["in_Ap"], d["in_Ai"], d["out_Ax_perturbed"], refine_matrix(d), ref_sym(d), d["in_rhs"],
+                     req_ref_iter=rr, max_inner_iter=mi)
+    xr = d["out_x"]
+    if not np.all(np.isfinite(xr)) or np.linalg.norm(xr) > 1e15:
+        pytest.skip("reference refinement diverges on this singular refinement matrix")
+    g = np.abs(d["out_valL"]).max()
+    assert np.linalg.norm(out["x"] - xr) <= max(1e-11, 1e-15 * g) * np.linalg.norm(xr)
