@@ -156,6 +156,30 @@ int nqg_get_factor(const nqg_plan *plan, double *values, double *d, int *perm, i
 /* Device error word of the last factor/solve (bit flags, 0 = clean). */
 int nqg_get_device_status(const nqg_plan *plan, int *status_bits);
 
+/* ---- measurement ----------------------------------------------------------
+ * Kernel classes timed with CUDA events on the plan's stream when profiling
+ * is on; alg_flops / alg_bytes are the algorithmic work of the launches
+ * (useful multiply-adds x 2, and bytes of factor values that must be read). */
+#define NQG_K_UPDATE 0          /* Schur updates between supernodes */
+#define NQG_K_WIDE_PANEL 1      /* wide supernode: BK panel */
+#define NQG_K_WIDE_TRAILING 2   /* wide supernode: trailing update */
+#define NQG_K_BK 3              /* narrow supernodes: BK + panel */
+#define NQG_K_SOLVE 4           /* forward / backward supernodal solves */
+#define NQG_K_SPMV 5            /* refinement residual SpMV */
+#define NQG_K_OTHER 6           /* assembly, row renaming, vector kernels */
+#define NQG_K_CLASSES 7
+typedef struct nqg_kernel_stats {
+  long long launches;
+  double total_ms;
+  double alg_flops;
+  double alg_bytes;
+} nqg_kernel_stats;
+int nqg_set_profiling(nqg_plan *plan, int on);
+/* Accumulated since profiling was switched on (synchronizes the stream). */
+int nqg_get_kernel_stats(nqg_plan *plan, int kernel_class, nqg_kernel_stats *stats);
+/* Number of kernels this plan launched since creation. */
+int nqg_get_launch_count(const nqg_plan *plan, long long *count);
+
 /* ---- QP solve (dual active-set NASOQ over the GPU LBL) ------------------- */
 typedef struct nqg_qp_settings {
   int variant;          /* 0 Fixed, 1 AUTO, 2 Tuned, 3 PREDET (reference nasoq_mode) */

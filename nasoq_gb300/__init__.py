@@ -45,6 +45,14 @@ class Timings(C.Structure):
                 ("last_residual", C.c_double)]
 
 
+class KernelStats(C.Structure):
+    _fields_ = [("launches", C.c_longlong), ("total_ms", C.c_double), ("alg_flops", C.c_double),
+                ("alg_bytes", C.c_double)]
+
+
+KERNEL_CLASSES = {"update": 0, "wide_panel": 1, "wide_trailing": 2, "bk": 3, "solve": 4, "spmv": 5, "other": 6}
+
+
 class QPSettings(C.Structure):
     _fields_ = [("variant", C.c_int), ("eps_abs", C.c_double), ("diag_perturb", C.c_double),
                 ("stop_tol", C.c_double), ("max_iter", C.c_int), ("max_iter_nas", C.c_int), ("precision", C.c_int)]
@@ -96,6 +104,9 @@ def lib():
     L.nqg_get_timings.argtypes = [C.c_void_p, C.POINTER(Timings)]
     L.nqg_get_factor.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.nqg_get_device_status.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
+    L.nqg_set_profiling.argtypes = [C.c_void_p, C.c_int]
+    L.nqg_get_kernel_stats.argtypes = [C.c_void_p, C.c_int, C.POINTER(KernelStats)]
+    L.nqg_get_launch_count.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
     L.nqg_qp_default_settings.argtypes = [C.POINTER(QPSettings)]
     L.nqg_qp_default_settings.restype = None
     L.nqg_qp_solve.argtypes = [C.c_int] + [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 4 + [C.c_int] + \
@@ -243,6 +254,23 @@ class Plan:
         ls = np.zeros(max(s.info.ssize, 1), np.int32)
         _check(lib().nqg_get_factor(self._h, _ptr(vals), _ptr(d), _ptr(perm), _ptr(ls)), "get factor")
         return vals[:s.info.xsize], d, perm, ls[:s.info.ssize]
+
+    def set_profiling(self, on=True):
+        _check(lib().nqg_set_profiling(self._h, 1 if on else 0), "set profiling")
+
+    def kernel_stats(self):
+        out = {}
+        for name, cls in KERNEL_CLASSES.items():
+            st = KernelStats()
+            _check(lib().nqg_get_kernel_stats(self._h, cls, C.byref(st)), "kernel stats")
+            out[name] = {"launches": st.launches, "total_ms": st.total_ms, "alg_flops": st.alg_flops,
+                         "alg_bytes": st.alg_bytes}
+        return out
+
+    def launch_count(self):
+        v = C.c_longlong(0)
+        lib().nqg_get_launch_count(self._h, C.byref(v))
+        return v.value
 
     def device_status(self):
         v = C.c_int(0)

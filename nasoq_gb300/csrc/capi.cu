@@ -161,6 +161,7 @@ static void build_schedule(Plan &P) {
   P.pair_d.clear();
   P.pair_lb.clear();
   P.pair_ub.clear();
+  P.pair_flops.clear();
   P.tile_ptr.assign(ns + 1, 0);
   P.tiles.clear();
   for (int s = 0; s < ns; ++s) {
@@ -175,6 +176,11 @@ static void build_schedule(Plan &P) {
       P.pair_d.push_back(d);
       P.pair_lb.push_back(lb);
       P.pair_ub.push_back(ub);
+      {
+        // useful multiply-adds: lower trapezoid of the (nr-lb) x (ub-lb+1) block, depth = width of d
+        const double m = nr - lb, nc = ub - lb + 1, wd = S.super[d + 1] - S.super[d];
+        P.pair_flops.push_back(2.0 * wd * (nc * m - nc * (nc - 1) / 2.0));
+      }
       for (int ri = lb; ri < nr; ri += UPD_TM)
         for (int cj = lb; cj <= ub; cj += UPD_TN)
           if (ri + UPD_TM - 1 >= cj) P.tiles.push_back(UpdTile{s, d, ri, cj, ub});
@@ -253,6 +259,7 @@ static int upload_plan(Plan &P) {
   std::vector<int64_t> mlo, mhi;
   build_full_csr(P.K, P.Kx_spmv, Rp, Rj, Rx, mlo, mhi);
   if ((rc = dev_alloc_copy(P, &P.d_Rp, Rp.data(), Rp.size()))) return rc;
+  P.nnzR = Rp.back();
   if ((rc = dev_alloc_copy(P, &P.d_Rj, Rj.data(), Rj.size()))) return rc;
   if ((rc = dev_alloc_copy(P, &P.d_Rx, Rx.data(), Rx.size()))) return rc;
   if ((rc = dev_alloc_copy(P, &P.d_map_lo, mlo.data(), mlo.size()))) return rc;
@@ -288,6 +295,7 @@ static int upload_plan(Plan &P) {
     P.level_off[l + 1] = (int)lvflat.size();
   }
   if ((rc = dev_alloc_copy(P, &P.d_targets_lv, lvflat.data(), lvflat.size()))) return rc;
+  P.lv_targets_host = lvflat;
   P.vis_host.assign(ns, 1);
   NQG_CUDA(cudaMalloc(&P.d_pivoted, std::max(2 * ns, 2)));
   NQG_CUDA(cudaMemset(P.d_pivoted, 0, std::max(2 * ns, 2)));
@@ -329,6 +337,8 @@ static void free_plan(Plan &P) {
                   P.d_xo, P.d_bo, P.d_r, P.d_w, P.d_in, P.d_out, P.d_V, P.d_scal, P.d_wide_W, P.d_wide_ctl};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  P.prof_collect();
+  for (cudaEvent_t e : P.ev_pool) cudaEventDestroy(e);
   if (P.ev0) cudaEventDestroy(P.ev0);
   if (P.ev1) cudaEventDestroy(P.ev1);
   if (P.own_stream) cudaStreamDestroy(P.own_stream);
@@ -483,6 +493,7 @@ extern "C" int nqg_edit_values(nqg_plan *h, int count, const int64_t *idx, const
   NQG_CUDA(cudaMemcpyAsync(d_vals, vals, count * sizeof(double), cudaMemcpyHostToDevice, P.stream));
   k_edit<<<std::min((count + 255) / 256, 1024), 256, 0, P.stream>>>(count, d_idx, d_vals, P.d_map_lo, P.d_map_hi,
                                                                      P.d_Kx, P.d_Rx);
+  P.nlaunch++;
   NQG_CUDA(cudaGetLastError());
   NQG_CUDA(cudaStreamSynchronize(P.stream));
   return NQG_OK;
@@ -625,5 +636,72 @@ extern "C" int nqg_get_device_status(const nqg_plan *hc, int *bits) {
   if (!hc || !bits) return NQG_ERR_ARG;
   Plan &P = const_cast<nqg_plan *>(hc)->P;
   NQG_CUDA(cudaMemcpy(bits, P.d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  return NQG_OK;
+}
+
+// ---- measurement -------------------------------------------------------------
+namespace nqg {
+cudaEvent_t Plan::prof_begin() {
+  if (!prof) return nullptr;
+  cudaEvent_t e;
+  if (!ev_pool.empty()) {
+    e = ev_pool.back();
+    ev_pool.pop_back();
+  } else if (cudaEventCreate(&e) != cudaSuccess) {
+    return nullptr;
+  }
+  cudaEventRecord(e, stream);
+  return e;
+}
+void Plan::prof_end(int cls, cudaEvent_t a, double flops, double bytes) {
+  if (!prof || !a) return;
+  cudaEvent_t e;
+  if (!ev_pool.empty()) {
+    e = ev_pool.back();
+    ev_pool.pop_back();
+  } else if (cudaEventCreate(&e) != cudaSuccess) {
+    return;
+  }
+  cudaEventRecord(e, stream);
+  prof_pending.push_back(ProfRec{cls, a, e, flops, bytes});
+  if (prof_pending.size() > 8192) prof_collect();
+}
+void Plan::prof_collect() {
+  if (prof_pending.empty()) return;
+  cudaStreamSynchronize(stream);
+  for (auto &r : prof_pending) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    auto &k = kstats[r.cls];
+    k.launches += 1;
+    k.total_ms += ms;
+    k.alg_flops += r.flops;
+    k.alg_bytes += r.bytes;
+    ev_pool.push_back(r.a);
+    ev_pool.push_back(r.b);
+  }
+  prof_pending.clear();
+}
+}  // namespace nqg
+
+extern "C" int nqg_set_profiling(nqg_plan *h, int on) {
+  if (!h) return NQG_ERR_ARG;
+  Plan &P = h->P;
+  P.prof_collect();
+  P.prof = on != 0;
+  for (auto &k : P.kstats) k = nqg_kernel_stats{};
+  return NQG_OK;
+}
+
+extern "C" int nqg_get_kernel_stats(nqg_plan *h, int cls, nqg_kernel_stats *st) {
+  if (!h || !st || cls < 0 || cls >= NQG_K_CLASSES) return NQG_ERR_ARG;
+  h->P.prof_collect();
+  *st = h->P.kstats[cls];
+  return NQG_OK;
+}
+
+extern "C" int nqg_get_launch_count(const nqg_plan *h, long long *count) {
+  if (!h || !count) return NQG_ERR_ARG;
+  *count = h->P.nlaunch;
   return NQG_OK;
 }

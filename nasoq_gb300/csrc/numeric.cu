@@ -784,11 +784,15 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
                              cudaMemcpyHostToDevice, st));
     k_zero_targets<T><<<(unsigned)all_marked.size(), 256, 0, st>>>(P.d_perm_tmp, (int)all_marked.size(), P.d_super,
                                                                    P.d_lpi, P.d_lpx, L, D, n);
+    P.nlaunch++;
   }
   {
     int blocks = std::min(std::max((n + 7) / 8, 1), 4096);
+    cudaEvent_t e0 = P.prof_begin();
     k_assemble<T><<<blocks, 256, 0, st>>>(n, P.d_Kp, P.d_Ki, P.d_Kx, P.d_iperm, P.d_col2sup, P.d_super, P.d_lpi,
                                           P.d_lpx, P.d_ls, subset ? d_mark : nullptr, L, P.d_status);
+    P.prof_end(NQG_K_OTHER, e0, 0.0, 0.0);
+    P.nlaunch++;
   }
   const size_t smem_small = (size_t)(BK_SMALL * BK_SMALL + BK_SMALL * BK_THREADS) * sizeof(T);
   static bool attr_set[2] = {false, false};
@@ -797,18 +801,43 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
     NQG_CUDA(cudaFuncSetAttribute(k_bk_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_small));
     attr_set[ai] = true;
   }
+  auto bk_flops = [&](int s) {
+    const double w = P.sym.super[s + 1] - P.sym.super[s], r = (double)(P.sym.lpi[s + 1] - P.sym.lpi[s]);
+    // sum_{k<w} (r-k)^2, the conventional factorization flop count of one supernode
+    return w * r * r - r * w * (w - 1) + (w - 1) * w * (2 * w - 1) / 6.0;
+  };
   for (int l = 0; l < nlev; ++l) {
-    if (lv_tile_cnt[l] > 0)
+    if (lv_tile_cnt[l] > 0) {
+      double fl = 0;
+      if (P.prof)
+        for (int s : P.levels[l])
+          if (mark[s])
+            for (int q = P.pair_ptr[s]; q < P.pair_ptr[s + 1]; ++q) fl += P.pair_flops[q];
+      cudaEvent_t e0 = P.prof_begin();
       k_update<T><<<(unsigned)lv_tile_cnt[l], UPD_THREADS, 0, st>>>(P.d_tiles, P.d_tile_list + lv_tile_off[l],
                                                                     (int)lv_tile_cnt[l], n, P.d_super, P.d_lpi,
                                                                     P.d_lpx, P.d_ls, L, D, P.d_status);
-    if (lv_small_cnt[l] > 0)
-      k_bk_small<T><<<lv_small_cnt[l], BK_THREADS, smem_small, st>>>(P.d_targets + lv_small_off[l], n, P.d_super,
-                                                                      P.d_lpi, P.d_lpx, L, D, P.d_locperm,
-                                                                      P.d_pivoted, P.d_status);
-    if (lv_glob_cnt[l] > 0)
-      k_bk_global<T><<<lv_glob_cnt[l], 256, 0, st>>>(P.d_targets + lv_glob_off[l], n, P.d_super, P.d_lpi, P.d_lpx,
-                                                      L, D, P.d_locperm, P.d_pivoted, P.d_perm_tmp, P.d_status);
+      P.prof_end(NQG_K_UPDATE, e0, fl, 0.0);
+      P.nlaunch++;
+    }
+    if (lv_small_cnt[l] + lv_glob_cnt[l] > 0) {
+      double fl = 0;
+      if (P.prof)
+        for (int q = lv_small_off[l]; q < lv_glob_off[l] + lv_glob_cnt[l]; ++q) fl += bk_flops(order[q]);
+      cudaEvent_t e0 = P.prof_begin();
+      if (lv_small_cnt[l] > 0) {
+        k_bk_small<T><<<lv_small_cnt[l], BK_THREADS, smem_small, st>>>(P.d_targets + lv_small_off[l], n, P.d_super,
+                                                                        P.d_lpi, P.d_lpx, L, D, P.d_locperm,
+                                                                        P.d_pivoted, P.d_status);
+        P.nlaunch++;
+      }
+      if (lv_glob_cnt[l] > 0) {
+        k_bk_global<T><<<lv_glob_cnt[l], 256, 0, st>>>(P.d_targets + lv_glob_off[l], n, P.d_super, P.d_lpi, P.d_lpx,
+                                                        L, D, P.d_locperm, P.d_pivoted, P.d_perm_tmp, P.d_status);
+        P.nlaunch++;
+      }
+      P.prof_end(NQG_K_BK, e0, fl, 0.0);
+    }
     for (int s : P.levels[l]) {
       if (!mark[s] || P.sym.super[s + 1] - P.sym.super[s] <= P.wide_min) continue;
       int rc = factor_wide<T>(P, s, L, D, P.wide_nb, reinterpret_cast<T *>(P.d_wide_W),
@@ -829,9 +858,12 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
         NQG_CUDA(cudaFuncSetAttribute(k_row_reorder<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         smem_set[ai] = smem;
       }
+      cudaEvent_t e0 = P.prof_begin();
       k_row_reorder<T><<<(unsigned)npairs, 128, smem, st>>>(P.d_pair_s, P.d_pair_d, P.d_pair_lb, P.d_pair_ub,
                                                             (int)npairs, P.d_pivoted, P.d_super, P.d_lpi, P.d_lpx,
                                                             P.d_ls, P.d_locperm, L, P.d_status);
+      P.prof_end(NQG_K_OTHER, e0, 0.0, 0.0);
+      P.nlaunch++;
     }
   }
   {
@@ -840,6 +872,7 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
                                            P.d_perm_tmp);
     std::swap(P.d_perm, P.d_perm_tmp);
     k_iperm<<<blocks, 256, 0, st>>>(n, P.d_perm, P.d_iperm);
+    P.nlaunch += 2;
   }
   NQG_CUDA(cudaGetLastError());
   return NQG_OK;

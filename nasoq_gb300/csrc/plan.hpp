@@ -75,6 +75,8 @@ struct Plan {
   int *d_pair_s = nullptr, *d_pair_d = nullptr, *d_pair_lb = nullptr, *d_pair_ub = nullptr;
   int *d_targets_lv = nullptr;      // narrow supernodes grouped by level (solve kernels)
   std::vector<int> level_off;       // offsets of each level in d_targets_lv
+  std::vector<int> lv_targets_host; // host copy of d_targets_lv
+  int64_t nnzR = 0;                 // entries of the full CSR used by the SpMV
   std::vector<std::vector<int>> wide_lv;  // wide supernodes of each level (multi-CTA solves)
   std::vector<uint8_t> vis_host;    // host copy of the supernode visibility mask
   double *d_in = nullptr, *d_out = nullptr;  // host-buffer solve staging
@@ -92,6 +94,23 @@ struct Plan {
   int wide_nb = 64;
   int wide_min = 256;               // supernodes wider than this use the blocked kernels
   int num_sms = 0;
+
+  // measurement: launch counter and per-class event timing
+  long long nlaunch = 0;
+  bool prof = false;
+  struct ProfRec {
+    int cls;
+    cudaEvent_t a, b;
+    double flops, bytes;
+  };
+  std::vector<ProfRec> prof_pending;
+  std::vector<cudaEvent_t> ev_pool;
+  nqg_kernel_stats kstats[NQG_K_CLASSES] = {};
+  std::vector<double> pair_flops;   // per descendant pair: useful Schur-update flops
+  // Brackets one launch (or one group of launches) of class `cls`.
+  cudaEvent_t prof_begin();
+  void prof_end(int cls, cudaEvent_t a, double flops, double bytes);
+  void prof_collect();
 
   bool factored = false;
   nqg_timings tm{};

@@ -210,24 +210,42 @@ template <class T> static int ldlt_solve_impl(Plan &P, double *x) {
   }
   const int nlev = (int)P.levels.size();
   int rc;
+  auto lvl_bytes = [&](int l) {
+    double b = 0;
+    if (P.prof)
+      for (int q = P.level_off[l]; q < P.level_off[l + 1]; ++q) {
+        int s = P.lv_targets_host[q];
+        b += (double)(P.sym.lpi[s + 1] - P.sym.lpi[s]) * (P.sym.super[s + 1] - P.sym.super[s]) * sizeof(T);
+      }
+    return b;
+  };
   for (int l = 0; l < nlev; ++l) {
     int cnt = P.level_off[l + 1] - P.level_off[l];
-    if (cnt > 0)
+    if (cnt > 0) {
+      cudaEvent_t e0 = P.prof_begin();
       k_fwd<T><<<cnt, SV_THREADS, smem, st>>>(P.d_targets_lv + P.level_off[l], P.d_super, P.d_lpi, P.d_lpx, P.d_ls,
                                                L, x, vis);
+      P.prof_end(NQG_K_SOLVE, e0, 0.0, lvl_bytes(l));
+      P.nlaunch++;
+    }
     for (int s : P.wide_lv[l])
       if (!P.masked || P.vis_host[s])
         if ((rc = solve_wide_fwd<T>(P, s, L, x))) return rc;
   }
   k_dsolve<T><<<grid_for(P.n), 256, 0, st>>>(P.n, D, x, hid);
+  P.nlaunch++;
   for (int l = nlev - 1; l >= 0; --l) {
     for (int s : P.wide_lv[l])
       if (!P.masked || P.vis_host[s])
         if ((rc = solve_wide_bwd<T>(P, s, L, x))) return rc;
     int cnt = P.level_off[l + 1] - P.level_off[l];
-    if (cnt > 0)
+    if (cnt > 0) {
+      cudaEvent_t e0 = P.prof_begin();
       k_bwd<T><<<cnt, SV_THREADS, smem, st>>>(P.d_targets_lv + P.level_off[l], P.d_super, P.d_lpi, P.d_lpx, P.d_ls,
                                                L, x, vis);
+      P.prof_end(NQG_K_SOLVE, e0, 0.0, lvl_bytes(l));
+      P.nlaunch++;
+    }
   }
   NQG_CUDA(cudaGetLastError());
   return NQG_OK;
@@ -240,7 +258,11 @@ int dev_ldlt_solve_ord(Plan &P, double *d_x) {
 
 int dev_spmv_ord(Plan &P, const double *xo, double *yo) {
   int blocks = std::max(1, std::min((P.n + 7) / 8, 8192));
+  cudaEvent_t e0 = P.prof_begin();
   k_spmv_ord<<<blocks, 256, 0, P.stream>>>(P.n, P.d_Rp, P.d_Rj, P.d_Rx, P.d_perm, P.d_iperm, xo, yo);
+  // values + column indices, row pointers, x gathered through iperm, y, perm/iperm
+  P.prof_end(NQG_K_SPMV, e0, 2.0 * P.nnzR, 12.0 * P.nnzR + 4.0 * (P.n + 1) + 24.0 * P.n);
+  P.nlaunch++;
   NQG_CUDA(cudaGetLastError());
   return NQG_OK;
 }
@@ -261,7 +283,9 @@ struct Gm {
   // dot into device slot, returns host value
   int dot(const double *a, const double *b, int slot, double &out) {
     k_dot_partial<<<DOT_BLOCKS, 256, 0, P.stream>>>(P.n, a, b, part);
+    P.nlaunch++;
     k_dot_final<<<1, 256, 0, P.stream>>>(part, DOT_BLOCKS, P.d_scal + slot);
+    P.nlaunch++;
     NQG_CUDA(cudaMemcpyAsync(&out, P.d_scal + slot, sizeof(double), cudaMemcpyDeviceToHost, P.stream));
     NQG_CUDA(cudaStreamSynchronize(P.stream));
     return NQG_OK;
@@ -294,6 +318,7 @@ static int gmres_refine(Plan &P, double *x, const double *b, int &itr_used, doub
   for (int itr = 0; itr < itr_max; ++itr) {
     if ((rc = dev_spmv_ord(P, x, r))) return rc;
     k_sub<<<grid_for(n), 256, 0, P.stream>>>(n, b, r);
+    P.nlaunch++;
     if ((rc = dev_ldlt_solve_ord(P, r))) return rc;
     double rr;
     if ((rc = g.dot(r, r, 0, rr))) return rc;
@@ -303,6 +328,7 @@ static int gmres_refine(Plan &P, double *x, const double *b, int &itr_used, doub
     if (itr == 0) rho_tol = rho * tol_rel;
     if ((rc = g.set_slot(1, rho))) return rc;
     k_scale_div<<<grid_for(n), 256, 0, P.stream>>>(n, P.d_scal + 1, r, V);
+    P.nlaunch++;
     gg[0] = rho;
     for (int i = 1; i <= mr; ++i) gg[i] = 0.0;
     for (auto &row : h) std::fill(row.begin(), row.end(), 0.0);
@@ -320,6 +346,7 @@ static int gmres_refine(Plan &P, double *x, const double *b, int &itr_used, doub
         if ((rc = g.dot(vk1, V + (size_t)j * n, 2, hj))) return rc;
         h[j][k] = hj;
         k_axpy<<<grid_for(n), 256, 0, P.stream>>>(n, P.d_scal + 2, -1.0, V + (size_t)j * n, vk1);
+        P.nlaunch++;
       }
       double hn2;
       if ((rc = g.dot(vk1, vk1, 0, hn2))) return rc;
@@ -330,6 +357,7 @@ static int gmres_refine(Plan &P, double *x, const double *b, int &itr_used, doub
           if ((rc = g.dot(vk1, V + (size_t)j * n, 2, ht))) return rc;
           h[j][k] = h[j][k] + ht;
           k_axpy<<<grid_for(n), 256, 0, P.stream>>>(n, P.d_scal + 2, -1.0, V + (size_t)j * n, vk1);
+          P.nlaunch++;
         }
         if ((rc = g.dot(vk1, vk1, 0, hn2))) return rc;
         h[k + 1][k] = std::sqrt(hn2);
@@ -337,6 +365,7 @@ static int gmres_refine(Plan &P, double *x, const double *b, int &itr_used, doub
       if (h[k + 1][k] != 0.0) {
         if ((rc = g.set_slot(1, h[k + 1][k]))) return rc;
         k_scale_div<<<grid_for(n), 256, 0, P.stream>>>(n, P.d_scal + 1, vk1, vk1);
+        P.nlaunch++;
       }
       if (0 < k) {
         for (int i = 0; i < k + 2; ++i) y[i] = h[i][k];
@@ -375,6 +404,7 @@ static int gmres_refine(Plan &P, double *x, const double *b, int &itr_used, doub
     }
     NQG_CUDA(cudaMemcpyAsync(P.d_scal + 8, y.data(), (k + 1) * sizeof(double), cudaMemcpyHostToDevice, P.stream));
     k_update_x<<<grid_for(n), 256, 0, P.stream>>>(n, k + 1, V, P.d_scal + 8, x);
+    P.nlaunch++;
     NQG_CUDA(cudaGetLastError());
     if (rho <= rho_tol && rho <= tol_abs) break;
   }
@@ -386,6 +416,7 @@ int dev_solve(Plan &P, const double *d_rhs, double *d_x) {
   int rc;
   // x_ord = rhs[perm]; b_ord = rhs[perm]
   k_gather<<<grid_for(n), 256, 0, P.stream>>>(n, P.d_perm, d_rhs, P.d_bo);
+  P.nlaunch++;
   NQG_CUDA(cudaMemcpyAsync(P.d_xo, P.d_bo, n * sizeof(double), cudaMemcpyDeviceToDevice, P.stream));
   if ((rc = dev_ldlt_solve_ord(P, P.d_xo))) return rc;
   int used = 0;
@@ -394,6 +425,7 @@ int dev_solve(Plan &P, const double *d_rhs, double *d_x) {
   P.tm.num_ref_iter = used;
   P.tm.last_residual = rho;
   k_scatter<<<grid_for(n), 256, 0, P.stream>>>(n, P.d_perm, P.d_xo, d_x);
+  P.nlaunch++;
   NQG_CUDA(cudaGetLastError());
   return NQG_OK;
 }

@@ -199,7 +199,10 @@ template <class T> int solve_wide_fwd(Plan &P, int s, const T *L, double *x) {
   NQG_CUDA(cudaMemsetAsync(ctl, 0, 16, P.stream));
   int G = std::max(1, P.num_sms);
   void *args[] = {(void *)&S, (void *)&nrow, (void *)&w, (void *)&rows, &x, (void *)&c0, &ctl, &status};
+  cudaEvent_t e0 = P.prof_begin();
   NQG_CUDA(cudaLaunchCooperativeKernel((void *)k_fwd_wide<T>, dim3(G), dim3(SW_THREADS), args, 0, P.stream));
+  P.nlaunch++;
+  P.prof_end(NQG_K_SOLVE, e0, 0.0, (double)nrow * w * sizeof(T));
   return NQG_OK;
 }
 
@@ -213,7 +216,10 @@ template <class T> int solve_wide_bwd(Plan &P, int s, const T *L, double *x) {
   NQG_CUDA(cudaMemsetAsync(ctl, 0, 16, P.stream));
   int G = std::max(1, P.num_sms);
   void *args[] = {(void *)&S, (void *)&nrow, (void *)&w, (void *)&rows, &x, (void *)&c0, &ctl, &status};
+  cudaEvent_t e0 = P.prof_begin();
   NQG_CUDA(cudaLaunchCooperativeKernel((void *)k_bwd_wide<T>, dim3(G), dim3(SW_THREADS), args, 0, P.stream));
+  P.nlaunch++;
+  P.prof_end(NQG_K_SOLVE, e0, 0.0, (double)nrow * w * sizeof(T));
   return NQG_OK;
 }
 

@@ -362,6 +362,7 @@ int factor_wide(Plan &P, int s, T *L, T *Dg, int nb, T *Wb, WideCtl *ctl, int nu
   const int n = P.n;
   int *perm = P.d_locperm + c0;
   k_wide_init_perm<T><<<(w + 255) / 256, 256, 0, st>>>(perm, w);
+  P.nlaunch++;
   NQG_CUDA(cudaMemsetAsync(ctl, 0, sizeof(WideCtl), st));
   int occ = 0;
   NQG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_wide_panel<T>, WP_THREADS, 0));
@@ -374,7 +375,9 @@ int factor_wide(Plan &P, int s, T *L, T *Dg, int nb, T *Wb, WideCtl *ctl, int nu
     int G = std::max(1, std::min(maxG, std::min(num_sms, (rows_left + 511) / 512)));
     int kb_want = std::min(nb, w - k0);
     void *args[] = {&S, (void *)&nrow, (void *)&w, &k0, &kb_want, &Wb, (void *)&nrow, &Dd, &De, &perm, &ctl, &status};
+    cudaEvent_t e0 = P.prof_begin();
     NQG_CUDA(cudaLaunchCooperativeKernel((void *)k_wide_panel<T>, dim3(G), dim3(WP_THREADS), args, 0, st));
+    P.nlaunch++;
     int kb = 0;
     NQG_CUDA(cudaMemcpyAsync(&kb, &ctl->kb, sizeof(int), cudaMemcpyDeviceToHost, st));
     NQG_CUDA(cudaStreamSynchronize(st));
@@ -382,7 +385,14 @@ int factor_wide(Plan &P, int s, T *L, T *Dg, int nb, T *Wb, WideCtl *ctl, int nu
     NQG_CUDA(cudaMemcpy(&abort, &ctl->abort, sizeof(int), cudaMemcpyDeviceToHost));
     if (abort || kb <= 0) return NQG_ERR_TIMEOUT;
     const int k1 = k0 + kb;
+    {
+      // panel: column GEMVs (2 * rows * j) and the L column scaling
+      double fl = 0;
+      for (int j = 0; j < kb; ++j) fl += 2.0 * (nrow - (k0 + j)) * (j + 1);
+      P.prof_end(NQG_K_WIDE_PANEL, e0, fl, 0.0);
+    }
     if (k1 < w) {
+      cudaEvent_t e1 = P.prof_begin();
       if (sizeof(T) == 4) {
         constexpr int BM = 128, BN = 128;
         int tm = (nrow - k1 + BM - 1) / BM, tn = (w - k1 + BN - 1) / BN;
@@ -392,11 +402,17 @@ int factor_wide(Plan &P, int s, T *L, T *Dg, int nb, T *Wb, WideCtl *ctl, int nu
         int tm = (nrow - k1 + BM - 1) / BM, tn = (w - k1 + BN - 1) / BN;
         k_wide_trailing<T, BM, BN, 4, 4><<<tm * tn, 256, 0, st>>>(S, nrow, w, k0, kb, Wb, nrow, tn);
       }
+      P.nlaunch++;
+      // useful multiply-adds: kb per entry of the lower trapezoid rows [k1,nrow) x cols [k1,w)
+      const double cols = w - k1;
+      const double entries = cols * (nrow - k1) - cols * (cols - 1) / 2.0;
+      P.prof_end(NQG_K_WIDE_TRAILING, e1, 2.0 * kb * entries, 0.0);
       NQG_CUDA(cudaGetLastError());
     }
     k0 = k1;
   }
   k_wide_zero_upper<T><<<std::min(w, 1024), 128, 0, st>>>(S, nrow, w);
+  P.nlaunch++;
   NQG_CUDA(cudaGetLastError());
   int piv = 0;
   NQG_CUDA(cudaMemcpyAsync(&piv, &ctl->pivoted, sizeof(int), cudaMemcpyDeviceToHost, st));
