@@ -180,6 +180,26 @@ int nqg_get_kernel_stats(nqg_plan *plan, int kernel_class, nqg_kernel_stats *sta
 /* Number of kernels this plan launched since creation. */
 int nqg_get_launch_count(const nqg_plan *plan, long long *count);
 
+/* ---- allocation-free dense factorization --------------------------------
+ * No counterpart in the reference.  For callers that must not allocate GPU
+ * memory once they are running (for example a real-time controller that
+ * reserved its memory at start-up, or a host application whose device memory
+ * is owned by another framework's allocator): Bunch-Kaufman LDL^T of one
+ * dense nrow x w panel in caller device memory -- the w x w symmetric
+ * diagonal block (lower triangle used) on top of nrow - w rows below it, the
+ * same computation the factorization applies to each wide supernode.  On
+ * return d_A holds L (unit diagonal, 2x2 sub-diagonals zeroed, the rows below
+ * solved as L21), d_D the diagonal then the 2x2 sub-diagonals (2w doubles),
+ * d_perm the pivot order (w ints, d_perm[m] = original column at position m).
+ * Requires lda == nrow and nrow <= 8192 (else NQG_ERR_SIZE).  It calls no
+ * cudaMalloc/cudaFree: its scratch is one fixed ~4.4 MB device array that
+ * every GPU loading this library holds until the process exits, shared by
+ * all calls, so calls whose GPU work overlaps (e.g. on two streams) race.
+ * The first call on each device looks up that array's address and should
+ * come before any stream capture.  Work runs on `stream` (NULL = default
+ * stream) and the call returns when it has finished. */
+int nqg_dense_ldlt_noalloc(int nrow, int w, double *d_A, int lda, double *d_D, int *d_perm, void *stream);
+
 /* ---- QP solve (dual active-set NASOQ over the GPU LBL) ------------------- */
 typedef struct nqg_qp_settings {
   int variant;          /* 0 Fixed, 1 AUTO, 2 Tuned, 3 PREDET (reference nasoq_mode) */

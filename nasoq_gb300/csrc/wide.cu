@@ -425,6 +425,60 @@ int factor_wide(Plan &P, int s, T *L, T *Dg, int nb, T *Wb, WideCtl *ctl, int nu
 
 size_t wide_ctl_bytes() { return sizeof(WideCtl); }
 
+// Same panel / trailing-update sequence as factor_wide, on caller-provided
+// buffers (values S, D, E, perm) and caller-provided scratch (Wb, ctl,
+// status); used by the allocation-free dense entry point.
+template <class T>
+int factor_wide_raw(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideCtl *ctl, int *status,
+                    cudaStream_t st, int num_sms, int nb, int *pivoted) {
+  k_wide_init_perm<T><<<(w + 255) / 256, 256, 0, st>>>(perm, w);
+  if (cudaMemsetAsync(ctl, 0, sizeof(WideCtl), st) != cudaSuccess) return NQG_ERR_CUDA;
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_wide_panel<T>, WP_THREADS, 0) != cudaSuccess)
+    return NQG_ERR_CUDA;
+  const int maxG = std::max(1, std::min(occ * num_sms, 1024));
+  int k0 = 0;
+  while (k0 < w) {
+    int rows_left = nrow - k0;
+    int G = std::max(1, std::min(maxG, std::min(num_sms, (rows_left + 511) / 512)));
+    int kb_want = std::min(nb, w - k0);
+    int ldw = nrow;
+    void *args[] = {&S, &nrow, &w, &k0, &kb_want, &Wb, &ldw, &Dd, &De, &perm, &ctl, &status};
+    if (cudaLaunchCooperativeKernel((void *)k_wide_panel<T>, dim3(G), dim3(WP_THREADS), args, 0, st) != cudaSuccess)
+      return NQG_ERR_CUDA;
+    int kb = 0, abort = 0;
+    if (cudaMemcpyAsync(&kb, &ctl->kb, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&abort, &ctl->abort, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return NQG_ERR_CUDA;
+    if (abort || kb <= 0) return NQG_ERR_TIMEOUT;
+    const int k1 = k0 + kb;
+    if (k1 < w) {
+      if (sizeof(T) == 4) {
+        constexpr int BM = 128, BN = 128;
+        int tm = (nrow - k1 + BM - 1) / BM, tn = (w - k1 + BN - 1) / BN;
+        k_wide_trailing<T, BM, BN, 8, 8><<<tm * tn, 256, 0, st>>>(S, nrow, w, k0, kb, Wb, nrow, tn);
+      } else {
+        constexpr int BM = 64, BN = 64;
+        int tm = (nrow - k1 + BM - 1) / BM, tn = (w - k1 + BN - 1) / BN;
+        k_wide_trailing<T, BM, BN, 4, 4><<<tm * tn, 256, 0, st>>>(S, nrow, w, k0, kb, Wb, nrow, tn);
+      }
+      if (cudaGetLastError() != cudaSuccess) return NQG_ERR_CUDA;
+    }
+    k0 = k1;
+  }
+  k_wide_zero_upper<T><<<std::min(w, 1024), 128, 0, st>>>(S, nrow, w);
+  int piv = 0;
+  if (cudaMemcpyAsync(&piv, &ctl->pivoted, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return NQG_ERR_CUDA;
+  if (pivoted) *pivoted = piv;
+  return NQG_OK;
+}
+
+template int factor_wide_raw<double>(double *, int, int, double *, double *, int *, double *, WideCtl *, int *,
+                                     cudaStream_t, int, int, int *);
+
 template int factor_wide<float>(Plan &, int, float *, float *, int, float *, WideCtl *, int);
 template int factor_wide<double>(Plan &, int, double *, double *, int, double *, WideCtl *, int);
 
