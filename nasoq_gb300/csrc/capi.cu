@@ -280,6 +280,49 @@ static int upload_plan(Plan &P) {
   if ((rc = dev_alloc_copy(P, &P.d_pair_d, P.pair_d.data(), P.pair_d.size()))) return rc;
   if ((rc = dev_alloc_copy(P, &P.d_pair_lb, P.pair_lb.data(), P.pair_lb.size()))) return rc;
   if ((rc = dev_alloc_copy(P, &P.d_pair_ub, P.pair_ub.data(), P.pair_ub.size()))) return rc;
+  {
+    // row renaming work: rows of every pair, and value-movement items sized so
+    // one item's rows x columns fit the shared-memory staging buffer
+    const int64_t np = (int64_t)P.pair_d.size();
+    std::vector<int64_t> roff(np + 1, 0);
+    for (int64_t q = 0; q < np; ++q) roff[q + 1] = roff[q] + std::max(0, P.pair_ub[q] - P.pair_lb[q] + 1);
+    const int64_t cap = RR_STAGE_BYTES / (int64_t)P.val_size();
+    const int64_t big_cap = RR_BIG_STAGE_BYTES / (int64_t)P.val_size();
+    std::vector<MoveItem> small, big;
+    int64_t goff = 0, big_len = 0;
+    for (int64_t q = 0; q < np; ++q) {
+      const int len = P.pair_ub[q] - P.pair_lb[q] + 1;
+      const int d = P.pair_d[q];
+      const int wd = S.super[d + 1] - S.super[d];
+      if (len <= 0 || wd <= 0) continue;
+      if (len <= cap) {
+        const int cc = (int)std::max<int64_t>(1, cap / len);
+        for (int c = 0; c < wd; c += cc) small.push_back({(int)q, c, std::min(cc, wd - c), 0, -1});
+      } else {
+        for (int c = 0; c < wd; ++c) {
+          int64_t g = -1;
+          if (len > big_cap) {
+            g = goff;
+            goff += len;
+          } else {
+            big_len = std::max<int64_t>(big_len, len);
+          }
+          big.push_back({(int)q, c, 1, 0, g});
+        }
+      }
+    }
+    P.rr_items_small = (int64_t)small.size();
+    P.rr_items_big = (int64_t)big.size();
+    P.rr_big_smem = (size_t)big_len * P.val_size();
+    small.insert(small.end(), big.begin(), big.end());
+    if ((rc = dev_alloc_copy(P, &P.d_pair_roff, roff.data(), roff.size()))) return rc;
+    if ((rc = dev_alloc_copy(P, &P.d_rr_items, small.data(), small.size()))) return rc;
+    NQG_CUDA(cudaMalloc(&P.d_rr_dest, (size_t)std::max<int64_t>(roff[np], 1) * sizeof(int)));
+    NQG_CUDA(cudaMalloc(&P.d_rr_moved, (size_t)std::max<int64_t>(np, 1)));
+    NQG_CUDA(cudaMalloc(&P.d_locinv, std::max(n, 1) * sizeof(int)));
+    if (goff > 0) NQG_CUDA(cudaMalloc(&P.d_rr_stage, (size_t)goff * P.val_size()));
+    P.rr_words = (std::max(S.max_sup_wid, 1) + 31) / 32;
+  }
   // tuning overrides: width above which the blocked multi-CTA kernels take
   // a supernode, and their panel width
   if (const char *e = std::getenv("NASOQ_GB300_WIDE_MIN")) P.wide_min = std::max(1, std::atoi(e));
@@ -334,7 +377,8 @@ static void free_plan(Plan &P) {
                   P.d_Rp, P.d_Rj, P.d_Rx, P.d_map_lo, P.d_map_hi, P.d_perm, P.d_iperm, P.d_locperm,
                   P.d_perm_tmp, P.d_L, P.d_D, P.d_tiles, P.d_tile_list, P.d_targets, P.d_pair_s, P.d_pair_d,
                   P.d_pair_lb, P.d_pair_ub, P.d_targets_lv, P.d_pivoted, P.d_visible, P.d_hidden, P.d_status,
-                  P.d_xo, P.d_bo, P.d_r, P.d_w, P.d_in, P.d_out, P.d_V, P.d_scal, P.d_wide_W, P.d_wide_ctl};
+                  P.d_xo, P.d_bo, P.d_r, P.d_w, P.d_in, P.d_out, P.d_V, P.d_scal, P.d_wide_W, P.d_wide_ctl,
+                  P.d_locinv, P.d_pair_roff, P.d_rr_dest, P.d_rr_moved, P.d_rr_items, P.d_rr_stage};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   P.prof_collect();

@@ -11,8 +11,8 @@
 //      then the panel column permutation (dlapmt), the unit triangular solve
 //      with L11^T (dtrsm) and the D^-1 scaling (blocked_2by2_solver,
 //      Sym_BLAS.cpp:492-529).
-// After all levels, k_row_reorder renames the rows of descendants that fall
-// into pivoted supernodes and re-sorts them (row_reordering,
+// After all levels, k_row_rename / k_row_move rename the rows of descendants
+// that fall into pivoted supernodes and re-sort them (row_reordering,
 // Sym_BLAS.cpp:327-490), and k_perm_compose folds the pivots into the global
 // permutation (reorder_matrix, linear_solver_wrapper.cpp:1432-1460).
 #include <cuda_runtime.h>
@@ -597,93 +597,116 @@ __global__ void __launch_bounds__(256) k_bk_global(const int *targets, int n, co
 }
 
 // ---------------------------------------------------------------------------
-// Row renaming after pivoting: for a (pivoted target s, descendant d) pair,
-// the rows of d in s's column range [lb, ub] are renamed through s's inverse
-// pivot permutation and re-sorted, moving d's value rows along.
-template <class T>
-__global__ void k_row_reorder(const int *pair_s, const int *pair_d, const int *pair_lb, const int *pair_ub, int npairs,
-                              const uint8_t *pivoted, const int *super, const int64_t *lpi, const int64_t *lpx,
-                              int *ls, const int *locperm, T *L, int *status) {
+// Row renaming after pivoting (row_reordering, Sym_BLAS.cpp:327-490): for a
+// (pivoted target s, descendant d) pair, the rows of d in s's column range
+// [lb, ub] are renamed through s's inverse pivot order and re-sorted, and
+// d's value rows move along.  Three launches, each O(rows) per pair:
+//   k_loc_inverse  locinv[c0 + locperm[c0 + m]] = m for pivoted supernodes;
+//   k_row_rename   one warp per pair: new names, their ranks (a bitmap over
+//                  s's columns + prefix popcounts) = the new positions,
+//                  sorted names written back, positions kept in dest;
+//   k_row_move     (pair, column chunk) items: the chunk's rows staged in
+//                  shared memory (global scratch for very long runs), then
+//                  stored at their new positions.
+
+__global__ void k_loc_inverse(int n, const int *col2sup, const int *super, const uint8_t *pivoted,
+                              const int *locperm, int *locinv) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int s = col2sup[i];
+    if (!pivoted[s]) continue;
+    const int c0 = super[s];
+    locinv[c0 + locperm[i]] = i - c0;
+  }
+}
+
+__global__ void k_row_rename(const int *pair_s, const int *pair_d, const int *pair_lb, const int *pair_ub,
+                             int64_t npairs, const int64_t *pair_roff, const uint8_t *pivoted, const int *super,
+                             const int64_t *lpi, int *ls, const int *locinv, int *dest_all, uint8_t *moved,
+                             int words_per_warp, int *status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int pidx = blockIdx.x;
-  if (pidx >= npairs) return;
-  const int s = pair_s[pidx];
-  if (!pivoted[s]) return;
-  const int d = pair_d[pidx], lb = pair_lb[pidx], ub = pair_ub[pidx];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int64_t p = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+  if (p >= npairs) return;
+  const int s = pair_s[p];
+  if (!pivoted[s]) {
+    if (lane == 0) moved[p] = 0;
+    return;
+  }
+  const int d = pair_d[p], lb = pair_lb[p];
+  const int len = pair_ub[p] - lb + 1;
   const int c0 = super[s], w = super[s + 1] - c0;
-  const int len = ub - lb + 1;
-  if (len <= 0) return;
-  int *dest = reinterpret_cast<int *>(smem_raw);   // len
-  int *inv = dest + len;                            // w
-  unsigned *bits = reinterpret_cast<unsigned *>(inv + w);  // (w+31)/32
-  int *wpre = reinterpret_cast<int *>(bits + (w + 31) / 32);  // (w+31)/32
-  __shared__ int s_lead_cnt;
-  const int nwords = (w + 31) / 32;
-  for (int m = threadIdx.x; m < w; m += blockDim.x) inv[locperm[c0 + m]] = m;
-  for (int q = threadIdx.x; q < nwords; q += blockDim.x) bits[q] = 0u;
-  __syncthreads();
+  const int nwords = (w + 31) >> 5;
+  unsigned *bits = reinterpret_cast<unsigned *>(smem_raw) + (size_t)warp * 2 * words_per_warp;
+  unsigned *wpre = bits + words_per_warp;
   int *rows = ls + lpi[d] + lb;
-  for (int e = threadIdx.x; e < len; e += blockDim.x) {
+  int *dest = dest_all + pair_roff[p];
+  for (int q = lane; q < nwords; q += 32) bits[q] = 0u;
+  __syncwarp();
+  for (int e = lane; e < len; e += 32) {
     int r = rows[e] - c0;
-    if (r < 0 || r >= w) {
+    int nw = (r >= 0 && r < w) ? locinv[c0 + r] : -1;
+    if (nw < 0 || nw >= w) {
       flag_status(status, ST_BOUNDS);
-      r = 0;
+      nw = 0;
     }
-    int nw = inv[r];
-    dest[e] = nw;  // temporarily the new local name
+    dest[e] = nw;
     atomicOr(&bits[nw >> 5], 1u << (nw & 31));
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int acc = 0;
-    for (int q = 0; q < nwords; ++q) {
-      wpre[q] = acc;
-      acc += __popc(bits[q]);
-    }
-    s_lead_cnt = acc;
+  __syncwarp();
+  // exclusive prefix of the word popcounts: contiguous segments per lane
+  const int seg = (nwords + 31) >> 5;
+  const int q0 = min(lane * seg, nwords), q1 = min(q0 + seg, nwords);
+  unsigned cnt = 0;
+  for (int q = q0; q < q1; ++q) cnt += __popc(bits[q]);
+  unsigned incl = cnt;
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
   }
-  __syncthreads();
-  for (int e = threadIdx.x; e < len; e += blockDim.x) {
-    int nw = dest[e];
-    int rank = wpre[nw >> 5] + __popc(bits[nw >> 5] & ((1u << (nw & 31)) - 1u));
+  unsigned acc = incl - cnt;
+  for (int q = q0; q < q1; ++q) {
+    wpre[q] = acc;
+    acc += __popc(bits[q]);
+  }
+  __syncwarp();
+  int mv = 0;
+  for (int e = lane; e < len; e += 32) {
+    const int nw = dest[e];
+    const int rank = (int)(wpre[nw >> 5] + __popc(bits[nw >> 5] & ((1u << (nw & 31)) - 1u)));
+    rows[rank] = c0 + nw;
     dest[e] = rank;
-    rows[rank] = -1 - (c0 + nw);  // staged; fixed below
+    mv |= rank != e;
   }
-  __syncthreads();
-  for (int e = threadIdx.x; e < len; e += blockDim.x) rows[e] = -1 - rows[e];
-  // cycle leaders of the position permutation (reuse inv[] as flags)
-  __syncthreads();
-  int *leader = inv;
-  for (int e = threadIdx.x; e < len; e += blockDim.x) {
-    int q = dest[e];
-    int isl = q != e;
-    int guard = 0;
-    while (isl && q != e && guard++ <= len) {
-      if (q < e) isl = 0;
-      q = dest[q];
-    }
-    leader[e] = isl;
-  }
-  __syncthreads();
-  // move value rows: element at position e goes to dest[e]; one thread per column of d
-  const int wd = super[d + 1] - super[d];
+  mv = __any_sync(0xffffffffu, mv);
+  if (lane == 0) moved[p] = (uint8_t)mv;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_row_move(const MoveItem *items, int64_t nitems, const int *pair_d,
+                                                  const int *pair_lb, const int *pair_ub, const int64_t *pair_roff,
+                                                  const uint8_t *moved, const int *super, const int64_t *lpi,
+                                                  const int64_t *lpx, const int *dest_all, T *stage_g, T *L) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int64_t it = blockIdx.x;
+  if (it >= nitems) return;
+  const MoveItem m = items[it];
+  if (!moved[m.pair]) return;
+  const int d = pair_d[m.pair], lb = pair_lb[m.pair];
+  const int len = pair_ub[m.pair] - lb + 1;
   const int nrd = (int)(lpi[d + 1] - lpi[d]);
-  T *Ld = L + lpx[d] + lb;
-  for (int c = threadIdx.x; c < wd; c += blockDim.x) {
-    T *col = Ld + (size_t)c * nrd;
-    for (int e = 0; e < len; ++e) {
-      if (!leader[e]) continue;
-      T carry = col[e];
-      int cur = dest[e];
-      int guard = 0;
-      while (guard++ <= len) {
-        T t = col[cur];
-        col[cur] = carry;
-        carry = t;
-        if (cur == e) break;
-        cur = dest[cur];
-      }
-    }
+  T *Ld = L + lpx[d] + (int64_t)m.c0 * nrd + lb;
+  const int *dest = dest_all + pair_roff[m.pair];
+  T *vb = m.goff >= 0 ? stage_g + m.goff : reinterpret_cast<T *>(smem_raw);
+  const int total = m.nc * len;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int c = t / len, e = t - c * len;
+    vb[t] = Ld[(int64_t)c * nrd + e];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int c = t / len, e = t - c * len;
+    Ld[(int64_t)c * nrd + dest[e]] = vb[t];
   }
 }
 
@@ -848,22 +871,45 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
   NQG_CUDA(cudaGetLastError());
   // row renaming in descendants of pivoted supernodes
   {
-    int64_t npairs = P.pair_d.size();
+    const int64_t npairs = (int64_t)P.pair_d.size();
     if (npairs > 0) {
-      int w = std::max(P.sym.max_sup_wid, 1);
-      size_t smem = (size_t)(w + w) * sizeof(int) + (size_t)2 * ((w + 31) / 32) * sizeof(int);
-      if (smem > 227 * 1024) return NQG_ERR_SIZE;
-      static size_t smem_set[2] = {0, 0};
-      if (smem > 48 * 1024 && smem > smem_set[ai]) {
-        NQG_CUDA(cudaFuncSetAttribute(k_row_reorder<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        smem_set[ai] = smem;
-      }
       cudaEvent_t e0 = P.prof_begin();
-      k_row_reorder<T><<<(unsigned)npairs, 128, smem, st>>>(P.d_pair_s, P.d_pair_d, P.d_pair_lb, P.d_pair_ub,
-                                                            (int)npairs, P.d_pivoted, P.d_super, P.d_lpi, P.d_lpx,
-                                                            P.d_ls, P.d_locperm, L, P.d_status);
+      const int blocks_n = std::min((n + 255) / 256, 4096);
+      k_loc_inverse<<<blocks_n, 256, 0, st>>>(n, P.d_col2sup, P.d_super, P.d_pivoted, P.d_locperm, P.d_locinv);
+      const size_t warp_bytes = (size_t)2 * P.rr_words * sizeof(unsigned);
+      int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (48 * 1024) / warp_bytes));
+      const size_t rn_smem = warp_bytes * wpb;
+      if (rn_smem > 227 * 1024) return NQG_ERR_SIZE;
+      static size_t rn_set = 0;
+      if (rn_smem > 48 * 1024 && rn_smem > rn_set) {
+        NQG_CUDA(cudaFuncSetAttribute(k_row_rename, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rn_smem));
+        rn_set = rn_smem;
+      }
+      const int64_t rn_blocks = (npairs + wpb - 1) / wpb;
+      k_row_rename<<<(unsigned)rn_blocks, 32 * wpb, rn_smem, st>>>(
+          P.d_pair_s, P.d_pair_d, P.d_pair_lb, P.d_pair_ub, npairs, P.d_pair_roff, P.d_pivoted, P.d_super, P.d_lpi,
+          P.d_ls, P.d_locinv, P.d_rr_dest, P.d_rr_moved, P.rr_words, P.d_status);
+      P.nlaunch += 2;
+      T *stage = reinterpret_cast<T *>(P.d_rr_stage);
+      if (P.rr_items_small > 0) {
+        k_row_move<T><<<(unsigned)P.rr_items_small, 256, RR_STAGE_BYTES, st>>>(
+            P.d_rr_items, P.rr_items_small, P.d_pair_d, P.d_pair_lb, P.d_pair_ub, P.d_pair_roff, P.d_rr_moved,
+            P.d_super, P.d_lpi, P.d_lpx, P.d_rr_dest, stage, L);
+        P.nlaunch++;
+      }
+      if (P.rr_items_big > 0) {
+        static size_t mv_set[2] = {0, 0};
+        const size_t big = std::max<size_t>(P.rr_big_smem, 16);
+        if (big > 48 * 1024 && big > mv_set[ai]) {
+          NQG_CUDA(cudaFuncSetAttribute(k_row_move<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)big));
+          mv_set[ai] = big;
+        }
+        k_row_move<T><<<(unsigned)P.rr_items_big, 256, big, st>>>(
+            P.d_rr_items + P.rr_items_small, P.rr_items_big, P.d_pair_d, P.d_pair_lb, P.d_pair_ub, P.d_pair_roff,
+            P.d_rr_moved, P.d_super, P.d_lpi, P.d_lpx, P.d_rr_dest, stage, L);
+        P.nlaunch++;
+      }
       P.prof_end(NQG_K_OTHER, e0, 0.0, 0.0);
-      P.nlaunch++;
     }
   }
   {

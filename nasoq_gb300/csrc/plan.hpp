@@ -28,6 +28,17 @@ struct UpdTile {
   int s, d, ri, cj, ub;
 };
 
+// One unit of row-renaming value movement: columns [c0, c0+nc) of the rows
+// of descendant pair `pair`; goff >= 0 stages through the global buffer at
+// that offset (rows too long for shared memory), else through shared memory.
+struct MoveItem {
+  int pair, c0, nc, pad;
+  int64_t goff;
+};
+
+constexpr int RR_STAGE_BYTES = 32 * 1024;       // shared staging of one movement item
+constexpr int RR_BIG_STAGE_BYTES = 200 * 1024;  // longest row run staged in shared memory
+
 constexpr int UPD_TM = 64;
 constexpr int UPD_TN = 64;
 
@@ -73,6 +84,17 @@ struct Plan {
   int *d_targets = nullptr;         // supernode ids for per-level kernels
   size_t targets_cap = 0;
   int *d_pair_s = nullptr, *d_pair_d = nullptr, *d_pair_lb = nullptr, *d_pair_ub = nullptr;
+  // row renaming after pivoting: per-pair row offsets, new positions, moved
+  // flags, value-movement items (shared-memory staged, then long rows)
+  int *d_locinv = nullptr;          // n: inverse of the in-supernode pivot order
+  int64_t *d_pair_roff = nullptr;   // npairs+1: offsets of each pair's rows
+  int *d_rr_dest = nullptr;         // new position of every pair row
+  uint8_t *d_rr_moved = nullptr;    // npairs: the pair's rows changed order
+  MoveItem *d_rr_items = nullptr;
+  int64_t rr_items_small = 0, rr_items_big = 0;
+  size_t rr_big_smem = 0;           // shared memory of the long-row launch
+  void *d_rr_stage = nullptr;       // global staging for rows beyond shared memory
+  int rr_words = 0;                 // bitmap words of the widest supernode
   int *d_targets_lv = nullptr;      // narrow supernodes grouped by level (solve kernels)
   std::vector<int> level_off;       // offsets of each level in d_targets_lv
   std::vector<int> lv_targets_host; // host copy of d_targets_lv
