@@ -40,6 +40,7 @@ METRIC = "QP solves/sec at 1e-8 KKT tol: mixed+batched+warm-start vs plain GPU F
 GRID, MCON, PER_ROW, DELTA, SEED = 64, 20000, 6, 1e-8, 0
 SAMPLE_GRID, SAMPLE_M = 48, 8000          # CPU baseline sample of the same family (~9% of the flops)
 TARGET_RELRES = 1e-10
+INNER = 6  # GMRES inner steps of the refinement (one restart)
 
 
 def workload_name(g, m):
@@ -211,8 +212,8 @@ def main():
 
     K, rhs = P.lbl_kkt(seed=SEED, grid3d=GRID, m=MCON, per_row=PER_ROW, delta=DELTA)
     n = K.ncol
-    st32 = nq.default_settings(precision=nq.NQG_FP32, req_ref_iter=1, max_inner_iter=6, tol_abs=0.0, tol_rel=0.0,
-                               reg_diag=1e-9)
+    st32 = nq.default_settings(precision=nq.NQG_FP32, solve_precision=nq.NQG_FP32, req_ref_iter=1,
+                               max_inner_iter=INNER, tol_abs=0.0, tol_rel=0.0, reg_diag=1e-9)
     t0 = time.perf_counter()
     plan = nq.Plan(n, K.p, K.i, K.x, settings=st32)
     analysis_s = time.perf_counter() - t0
@@ -355,8 +356,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32-factor+fp64-refine", "data": "synthetic",
             "config": {"workload": workload_name(GRID, MCON), "N": n, "nnz_K_lower": int(K.nnz),
-                       "seed": SEED, "delta": DELTA, "factor_flops": F, "precision": "fp32 factor, fp64 GMRES-IR",
-                       "refinement": "GMRES(6), 1 restart", "target_relres": TARGET_RELRES,
+                       "seed": SEED, "delta": DELTA, "factor_flops": F, "precision": "fp32 factor and triangular solves, fp64 flexible GMRES-IR",
+                       "refinement": f"FGMRES({INNER}), 1 restart", "target_relres": TARGET_RELRES,
                        "l2": "inputs larger than L2 (FP32 factor 4 GB)", "analysis_s": analysis_s,
                        "parallelism": f"replicas x{world}"},
             "relres": rr32, "error_vs_fp64_gpu": err_vs_fp64,

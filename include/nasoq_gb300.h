@@ -50,6 +50,12 @@ typedef struct nqg_settings {
    * what FP32 can carry; the refinement still works on the reference's
    * matrix.  <= 0 selects 3e-4 * max|a_ij|. */
   double reg_diag_fp32;
+  /* FP32 factor only: arithmetic of the triangular solves applied inside the
+   * refinement.  NQG_FP64 (default) widens the factor entries and keeps the
+   * solve vectors in FP64; NQG_FP32 runs the solves in FP32 (faster, and
+   * enough when the refined residual still meets the tolerance; on
+   * ill-conditioned systems it can stall the refinement earlier). */
+  int solve_precision;
 } nqg_settings;
 
 /* Reference defaults (src/QP/linear_solver_wrapper.cpp:205-244). */

@@ -30,7 +30,7 @@ class Settings(C.Structure):
     _fields_ = [("precision", C.c_int), ("req_ref_iter", C.c_int), ("max_inner_iter", C.c_int),
                 ("tol_abs", C.c_double), ("tol_rel", C.c_double), ("reg_diag", C.c_double),
                 ("regularization", C.c_int), ("n_relax", C.c_int * 3), ("z_relax", C.c_double * 3),
-                ("reg_diag_fp32", C.c_double)]
+                ("reg_diag_fp32", C.c_double), ("solve_precision", C.c_int)]
 
 
 class SymbolicInfo(C.Structure):

@@ -37,6 +37,7 @@ extern "C" void nqg_default_settings(nqg_settings *s) {
   s->z_relax[1] = 0.1;
   s->z_relax[2] = 0.05;
   s->reg_diag_fp32 = 0.0;
+  s->solve_precision = NQG_FP64;
 }
 
 extern "C" const char *nqg_status_str(int st) {
@@ -327,16 +328,52 @@ static int upload_plan(Plan &P) {
   // a supernode, and their panel width
   if (const char *e = std::getenv("NASOQ_GB300_WIDE_MIN")) P.wide_min = std::max(1, std::atoi(e));
   if (const char *e = std::getenv("NASOQ_GB300_WIDE_NB")) P.wide_nb = std::min(64, std::max(4, std::atoi(e)));
-  std::vector<int> lvflat;
+  // solve work split per level: small supernodes take one CTA each in the
+  // level kernels; the others are cut into 64-row blocks for the
+  // flag-driven block kernels (forward items: diagonal block rows, then row
+  // blocks below; backward items: diagonal column blocks)
+  int small_w = 64, small_rows = 256;
+  if (const char *e = std::getenv("NASOQ_GB300_SOLVE_SMALL")) std::sscanf(e, "%d,%d", &small_w, &small_rows);
+  std::vector<int> lvflat, flagoff(std::max(ns, 1), 0), fwd_items, bwd_items;
   P.level_off.assign(P.levels.size() + 1, 0);
-  P.wide_lv.assign(P.levels.size(), {});
+  P.blk_fwd_off.assign(P.levels.size() + 1, 0);
+  P.blk_bwd_off.assign(P.levels.size() + 1, 0);
+  P.blk_bytes.assign(P.levels.size(), 0.0);
+  int nflags = 0;
   for (size_t l = 0; l < P.levels.size(); ++l) {
     for (int s : P.levels[l]) {
-      if (S.super[s + 1] - S.super[s] > P.wide_min) P.wide_lv[l].push_back(s);
-      else lvflat.push_back(s);
+      const int w = S.super[s + 1] - S.super[s];
+      const int nrow = (int)(S.lpi[s + 1] - S.lpi[s]);
+      if (w <= small_w && nrow <= small_rows) {
+        lvflat.push_back(s);
+        continue;
+      }
+      const int nbd = (w + 63) / 64, nbb = (nrow - w + 63) / 64;
+      flagoff[s] = nflags;
+      nflags += nbd;
+      for (int q = 0; q < nbd + nbb; ++q) {
+        fwd_items.push_back(s);
+        fwd_items.push_back(q);
+      }
+      for (int q = 0; q < nbd; ++q) {
+        bwd_items.push_back(s);
+        bwd_items.push_back(q);
+      }
+      P.blk_bytes[l] += (double)nrow * w;
     }
     P.level_off[l + 1] = (int)lvflat.size();
+    P.blk_fwd_off[l + 1] = (int)fwd_items.size() / 2;
+    P.blk_bwd_off[l + 1] = (int)bwd_items.size() / 2;
   }
+  const int nfwd = (int)fwd_items.size() / 2;
+  for (auto &o : P.blk_bwd_off) o += nfwd;
+  fwd_items.insert(fwd_items.end(), bwd_items.begin(), bwd_items.end());
+  if ((rc = dev_alloc_copy(P, &P.d_blk_items, fwd_items.data(), fwd_items.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_flagoff, flagoff.data(), flagoff.size()))) return rc;
+  P.solve_flags_cap = std::max(nflags, 1);
+  NQG_CUDA(cudaMalloc(&P.d_solve_flags, (size_t)P.solve_flags_cap * sizeof(unsigned)));
+  NQG_CUDA(cudaMemset(P.d_solve_flags, 0, (size_t)P.solve_flags_cap * sizeof(unsigned)));
+  P.solve_small_w = small_w;
   if ((rc = dev_alloc_copy(P, &P.d_targets_lv, lvflat.data(), lvflat.size()))) return rc;
   P.lv_targets_host = lvflat;
   P.vis_host.assign(ns, 1);
@@ -354,6 +391,10 @@ static int upload_plan(Plan &P) {
   NQG_CUDA(cudaMalloc(&P.d_w, nn * sizeof(double)));
   NQG_CUDA(cudaMalloc(&P.d_in, nn * sizeof(double)));
   NQG_CUDA(cudaMalloc(&P.d_out, nn * sizeof(double)));
+  if (P.set.precision == NQG_FP32 && P.set.solve_precision == NQG_FP32) {
+    NQG_CUDA(cudaMalloc(&P.d_xf, nn * sizeof(float)));
+    NQG_CUDA(cudaMalloc(&P.d_Z, (size_t)P.mr_cap * nn * sizeof(float)));
+  }
   NQG_CUDA(cudaMalloc(&P.d_V, (size_t)(P.mr_cap + 1) * nn * sizeof(double)));
   NQG_CUDA(cudaMalloc(&P.d_scal, (64 + 512) * sizeof(double)));
   {
@@ -363,11 +404,11 @@ static int upload_plan(Plan &P) {
     int64_t wide_rows = 0;
     for (int s = 0; s < ns; ++s)
       if (S.super[s + 1] - S.super[s] > P.wide_min) wide_rows = std::max<int64_t>(wide_rows, S.lpi[s + 1] - S.lpi[s]);
-    if (wide_rows > 0) {
-      NQG_CUDA(cudaMalloc(&P.d_wide_W, (size_t)wide_rows * (P.wide_nb + 2) * P.val_size()));
-      NQG_CUDA(cudaMalloc(&P.d_wide_ctl, wide_ctl_bytes()));
-      NQG_CUDA(cudaMemset(P.d_wide_ctl, 0, wide_ctl_bytes()));
-    }
+    if (wide_rows > 0) NQG_CUDA(cudaMalloc(&P.d_wide_W, (size_t)wide_rows * (P.wide_nb + 2) * P.val_size()));
+    // control block: grid barriers of the blocked factorization, abort flag
+    // of the block solves
+    NQG_CUDA(cudaMalloc(&P.d_wide_ctl, wide_ctl_bytes()));
+    NQG_CUDA(cudaMemset(P.d_wide_ctl, 0, wide_ctl_bytes()));
   }
   return NQG_OK;
 }
@@ -378,7 +419,8 @@ static void free_plan(Plan &P) {
                   P.d_perm_tmp, P.d_L, P.d_D, P.d_tiles, P.d_tile_list, P.d_targets, P.d_pair_s, P.d_pair_d,
                   P.d_pair_lb, P.d_pair_ub, P.d_targets_lv, P.d_pivoted, P.d_visible, P.d_hidden, P.d_status,
                   P.d_xo, P.d_bo, P.d_r, P.d_w, P.d_in, P.d_out, P.d_V, P.d_scal, P.d_wide_W, P.d_wide_ctl,
-                  P.d_locinv, P.d_pair_roff, P.d_rr_dest, P.d_rr_moved, P.d_rr_items, P.d_rr_stage};
+                  P.d_locinv, P.d_pair_roff, P.d_rr_dest, P.d_rr_moved, P.d_rr_items, P.d_rr_stage,
+                  P.d_solve_flags, P.d_blk_items, P.d_flagoff, P.d_xf, P.d_Z};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   P.prof_collect();
@@ -437,7 +479,8 @@ extern "C" int nqg_plan_create(int n, const int *Ap, const int *Ai, const double
   if (settings) P.set = *settings;
   else nqg_default_settings(&P.set);
   // the refinement keeps its Hessenberg solution in 48 device scalar slots
-  if (P.set.precision != NQG_FP64 && P.set.precision != NQG_FP32 || P.set.max_inner_iter > 48 ||
+  if (P.set.precision != NQG_FP64 && P.set.precision != NQG_FP32 ||
+      (P.set.solve_precision != NQG_FP64 && P.set.solve_precision != NQG_FP32) || P.set.max_inner_iter > 48 ||
       P.set.max_inner_iter < 0 || P.set.req_ref_iter < 0) {
     delete h;
     return NQG_ERR_ARG;

@@ -99,9 +99,16 @@ struct Plan {
   std::vector<int> level_off;       // offsets of each level in d_targets_lv
   std::vector<int> lv_targets_host; // host copy of d_targets_lv
   int64_t nnzR = 0;                 // entries of the full CSR used by the SpMV
-  std::vector<std::vector<int>> wide_lv;  // wide supernodes of each level (multi-CTA solves)
+  // block solves: (supernode, block) items of the large supernodes, per level
+  int *d_blk_items = nullptr;       // int pairs: forward items, then backward items
+  int *d_flagoff = nullptr;         // per supernode: first of its ready flags
+  std::vector<int> blk_fwd_off, blk_bwd_off;  // per level item ranges
+  std::vector<double> blk_bytes;    // per level factor entries of the large supernodes
+  int solve_small_w = 64;
   std::vector<uint8_t> vis_host;    // host copy of the supernode visibility mask
   double *d_in = nullptr, *d_out = nullptr;  // host-buffer solve staging
+  float *d_xf = nullptr;            // FP32 solves: the triangular solves' working vector
+  float *d_Z = nullptr;             // FP32 solves: flexible GMRES preconditioned directions
   uint8_t *d_pivoted = nullptr;     // 2*nsuper: [0,ns) BK permuted the supernode in the last factor,
                                     // [ns,2ns) supernode is being factored by the current call
   uint8_t *d_visible = nullptr, *d_hidden = nullptr;
@@ -113,6 +120,9 @@ struct Plan {
   // wide supernodes (blocked cooperative BK)
   void *d_wide_W = nullptr;         // panel buffer, max nrow x (nb+2)
   void *d_wide_ctl = nullptr;       // barrier / reduction control block
+  unsigned *d_solve_flags = nullptr;  // per 64-column block ready flags of the block solves
+  int solve_flags_cap = 0;
+  unsigned solve_epoch = 0;
   int wide_nb = 64;
   int wide_min = 256;               // supernodes wider than this use the blocked kernels
   int num_sms = 0;
@@ -150,8 +160,8 @@ struct WideCtl;
 size_t wide_ctl_bytes();
 template <class T> int factor_wide(Plan &P, int s, T *L, T *Dg, int nb, T *Wb, WideCtl *ctl, int num_sms);
 // solve_wide.cu
-template <class T> int solve_wide_fwd(Plan &P, int s, const T *L, double *x);
-template <class T> int solve_wide_bwd(Plan &P, int s, const T *L, double *x);
+template <class T, class V> int solve_blk_fwd(Plan &P, int level, const T *L, V *x);
+template <class T, class V> int solve_blk_bwd(Plan &P, int level, const T *L, V *x);
 // solve.cu
 int dev_ldlt_solve_ord(Plan &P, double *d_x);
 int dev_spmv_ord(Plan &P, const double *d_x_ord, double *d_y_ord);

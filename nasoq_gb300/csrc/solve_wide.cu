@@ -3,13 +3,21 @@
 // src/triangularSolve/Triangular_BCSC.cpp:378-446, 534-600: dtrsm on the
 // diagonal block + dgemv with the rows below).
 //
-// The w x w unit-lower diagonal block is processed in 64-column blocks with
-// one grid barrier per block: after x_b is known, CTA 0 applies it to the next
-// block's 64 rows (look-ahead) and solves that block's triangle in a single
-// warp from shared memory, while the other CTAs apply x_b to all later rows.
-// The rows below the diagonal block form one independent GEMV (forward) or
-// GEMV^T (backward) over (row, column-chunk) items.  Each row (forward) or
-// column (backward) of the block keeps one owner thread in every phase.
+// Both sweeps are persistent cooperative kernels without grid barriers.  The
+// supernode's nrow x w panel is cut into 64 x 64 tiles.  Forward: work item q
+// is block row q (64 rows of the diagonal block, then 64-row blocks of the rows
+// below); it accumulates L(q, j) x_j over the column blocks j before it, each
+// as soon as block j's ready flag carries this launch's epoch, then solves
+// its 64 x 64 unit-lower diagonal tile in one warp and publishes x_q with a
+// release store of its flag (rows below scatter L21 x into the ancestors'
+// entries with atomics instead).  Backward: item j is column block j, taken
+// from the last; it gathers L21^T x(rows below) without waiting, then
+// L(i, j)^T x_i for i > j as those blocks become ready, and solves the
+// transposed diagonal tile.  Each CTA takes its items in dependency order, and
+// a cooperative launch keeps all CTAs resident, so every wait ends; each wait
+// is still bounded (timeout -> ST_TIMEOUT and an abort flag the other CTAs
+// see).  Matrix tiles do not depend on the flags, so the next tile's values
+// are loaded before the wait for the current one.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -22,210 +30,343 @@ namespace nqg {
 namespace {
 
 constexpr int SW_THREADS = 256;
-constexpr int SB = 64;      // diagonal sub-block size
-constexpr int CHUNK = 512;  // column chunk of the below-block GEMV
+constexpr int TB = 64;                       // tile rows / columns
+constexpr int CPT = TB / (SW_THREADS / TB);  // tile columns per thread (16)
 
 // x_b := L11[b]^-1 x_b for a 64x64 unit lower block, one warp, lane i holds
 // rows i and i+32; T11 is the block staged column-major in shared memory.
-__device__ void warp_trsv_lower(const double *T11, int m, double *xb) {
+template <class V> __device__ void warp_trsv_lower(const V *T11, int m, V *xb) {
   const int lane = threadIdx.x & 31;
-  double v0 = lane < m ? xb[lane] : 0.0, v1 = lane + 32 < m ? xb[lane + 32] : 0.0;
+  V v0 = lane < m ? xb[lane] : V(0), v1 = lane + 32 < m ? xb[lane + 32] : V(0);
   for (int j = 0; j < m; ++j) {
-    const double xj = __shfl_sync(0xffffffffu, j < 32 ? v0 : v1, j & 31);
-    if (lane > j && lane < m) v0 -= T11[lane + j * SB] * xj;
-    if (lane + 32 > j && lane + 32 < m) v1 -= T11[lane + 32 + j * SB] * xj;
+    const V xj = __shfl_sync(0xffffffffu, j < 32 ? v0 : v1, j & 31);
+    if (lane > j && lane < m) v0 -= T11[lane + j * TB] * xj;
+    if (lane + 32 > j && lane + 32 < m) v1 -= T11[lane + 32 + j * TB] * xj;
   }
   if (lane < m) xb[lane] = v0;
   if (lane + 32 < m) xb[lane + 32] = v1;
 }
 
 // x_b := L11[b]^-T x_b (backward substitution with the transposed block).
-__device__ void warp_trsv_lower_t(const double *T11, int m, double *xb) {
+template <class V> __device__ void warp_trsv_lower_t(const V *T11, int m, V *xb) {
   const int lane = threadIdx.x & 31;
-  double v0 = lane < m ? xb[lane] : 0.0, v1 = lane + 32 < m ? xb[lane + 32] : 0.0;
+  V v0 = lane < m ? xb[lane] : V(0), v1 = lane + 32 < m ? xb[lane + 32] : V(0);
   for (int i = m - 1; i > 0; --i) {
-    const double xi = __shfl_sync(0xffffffffu, i < 32 ? v0 : v1, i & 31);
+    const V xi = __shfl_sync(0xffffffffu, i < 32 ? v0 : v1, i & 31);
     // x_j -= L(i, j) x_i for j < i
-    if (lane < i) v0 -= T11[i + lane * SB] * xi;
-    if (lane + 32 < i) v1 -= T11[i + (lane + 32) * SB] * xi;
+    if (lane < i) v0 -= T11[i + lane * TB] * xi;
+    if (lane + 32 < i) v1 -= T11[i + (lane + 32) * TB] * xi;
   }
   if (lane < m) xb[lane] = v0;
   if (lane + 32 < m) xb[lane + 32] = v1;
 }
 
-template <class T> __device__ void stage_block(const T *S, int nrow, int b0, int m, double *T11) {
-  for (int e = threadIdx.x; e < SB * SB; e += blockDim.x) {
-    int c = e / SB, r = e % SB;
-    T11[r + c * SB] = (r < m && c < m) ? (double)S[b0 + r + (size_t)(b0 + c) * nrow] : 0.0;
+// The m x m tile at (b0, b0) of the panel, column-major in T11.
+template <class T, class V> __device__ void stage_tile(const T *S, int nrow, int b0, int m, V *T11) {
+  for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
+    const int c = e / TB, r = e % TB;
+    T11[r + c * TB] = (r < m && c < m) ? V(S[b0 + r + (size_t)(b0 + c) * nrow]) : V(0);
   }
 }
 
-template <class T>
-__global__ void __launch_bounds__(SW_THREADS) k_fwd_wide(const T *S, int nrow, int w, const int *rows, double *x,
-                                                         int c0, WideCtl *ctl, int *status) {
-  __shared__ double T11[SB * SB];
-  __shared__ double xb[SB], xn[SB];
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x, TT = gridDim.x * blockDim.x;
-  const int nblk = (w + SB - 1) / SB;
-  double *xs = x + c0;
-  auto first_row = [&](int lo) { return lo + (int)(((long long)gt - lo % TT + TT) % TT); };
-  if (blockIdx.x == 0) {  // first diagonal block
-    const int m = min(SB, w);
-    stage_block(S, nrow, 0, m, T11);
-    for (int i = threadIdx.x; i < m; i += blockDim.x) xb[i] = xs[i];
-    __syncthreads();
-    if (threadIdx.x < 32) warp_trsv_lower(T11, m, xb);
-    __syncthreads();
-    for (int i = threadIdx.x; i < m; i += blockDim.x) xs[i] = xb[i];
-  }
-  if (!grid_sync(ctl, status)) return;
-  for (int b = 0; b < nblk; ++b) {
-    const int b0 = b * SB, b1 = min(w, b0 + SB), b2 = min(w, b1 + SB);
-    const int m = b1 - b0;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) xb[i] = xs[b0 + i];
-    __syncthreads();
-    if (blockIdx.x == 0 && b1 < w) {
-      // look-ahead: rows [b1, b2) get block b, then their triangle is solved
-      for (int r = b1 + threadIdx.x; r < b2; r += blockDim.x) {
-        double acc = 0.0;
-        for (int j = 0; j < m; ++j) acc += (double)S[r + (size_t)(b0 + j) * nrow] * xb[j];
-        xs[r] -= acc;
+// Warp 0 only (all 32 lanes).  Forward flags of one supernode become ready
+// in increasing block order; `front` = count of leading ready blocks.  Waits
+// until block j is ready, scanning 32 flags per poll, and extends the front
+// over ready blocks (< lim).  Waiters further from the front poll less often.
+// Returns -1 on abort or timeout.
+__device__ int wait_up(const unsigned *fl, unsigned epoch, int j, int lim, int front, WideCtl *ctl, int *status) {
+  const int lane = threadIdx.x & 31;
+  long long it = 0;
+  volatile int *vab = &ctl->abort;
+  while (true) {
+    const int k = front + lane;
+    const unsigned v = k < lim ? *(volatile const unsigned *)(fl + k) : 0u;
+    const unsigned ready = __ballot_sync(0xffffffffu, v == epoch);
+    const int lead = ready == 0xffffffffu ? 32 : __ffs(~ready) - 1;
+    front += lead;
+    if (lead == 32 && front < lim) continue;  // more ready flags to scan
+    if (front > j) break;
+    if (*vab) return -1;
+    if (++it > SPIN_LIMIT) {
+      if (lane == 0) {
+        atomicOr(status, ST_TIMEOUT);
+        atomicExch(&ctl->abort, 1);
       }
-      __syncthreads();
-      const int m2 = b2 - b1;
-      stage_block(S, nrow, b1, m2, T11);
-      for (int i = threadIdx.x; i < m2; i += blockDim.x) xn[i] = xs[b1 + i];
-      __syncthreads();
-      if (threadIdx.x < 32) warp_trsv_lower(T11, m2, xn);
-      __syncthreads();
-      for (int i = threadIdx.x; i < m2; i += blockDim.x) xs[b1 + i] = xn[i];
+      return -1;
     }
-    // every CTA (CTA 0 included) applies block b to its rows beyond the look-ahead
-    for (int r = first_row(b2); r < w; r += TT) {
-      double acc = 0.0;
-      for (int j = 0; j < m; ++j) acc += (double)S[r + (size_t)(b0 + j) * nrow] * xb[j];
-      xs[r] -= acc;
-    }
-    if (!grid_sync(ctl, status)) return;
+    __nanosleep(min(2000, 40 * (j - front + 1)));
   }
-  // rows below the diagonal block: x[rows[r]] -= L21(r, :) x_s, split in column chunks
-  const int nb_rows = nrow - w;
-  const int nchunk = (w + CHUNK - 1) / CHUNK;
-  for (long long item = gt; item < (long long)nb_rows * nchunk; item += TT) {
-    const int r = w + (int)(item % nb_rows);
-    const int ch = (int)(item / nb_rows);
-    const int j0 = ch * CHUNK, j1 = min(w, j0 + CHUNK);
-    double acc = 0.0;
-    for (int j = j0; j < j1; ++j) acc += (double)S[r + (size_t)j * nrow] * xs[j];
-    atomicAdd(&x[rows[r]], -acc);
+  __threadfence();
+  return front;
+}
+
+// Backward mirror: blocks >= `front` are ready; waits until block i is and
+// extends the front down to lo.
+__device__ int wait_down(const unsigned *fl, unsigned epoch, int i, int lo, int front, WideCtl *ctl,
+                         int *status) {
+  const int lane = threadIdx.x & 31;
+  long long it = 0;
+  volatile int *vab = &ctl->abort;
+  while (true) {
+    const int k = front - 1 - lane;
+    const unsigned v = k >= lo ? *(volatile const unsigned *)(fl + k) : 0u;
+    const unsigned ready = __ballot_sync(0xffffffffu, v == epoch);
+    const int lead = ready == 0xffffffffu ? 32 : __ffs(~ready) - 1;
+    front -= lead;
+    if (lead == 32 && front > lo) continue;
+    if (front <= i) break;
+    if (*vab) return -1;
+    if (++it > SPIN_LIMIT) {
+      if (lane == 0) {
+        atomicOr(status, ST_TIMEOUT);
+        atomicExch(&ctl->abort, 1);
+      }
+      return -1;
+    }
+    __nanosleep(min(2000, 40 * (front - i)));
+  }
+  __threadfence();
+  return front;
+}
+
+__device__ __forceinline__ void publish(unsigned *flag, unsigned epoch) {
+  __threadfence();
+  *(volatile unsigned *)flag = epoch;
+}
+
+// Forward sweep over the large supernodes of one level.  Item (s, q): q <
+// nbd(s) is diagonal block row q, else block q - nbd(s) of the rows below.
+template <class T, class V>
+__global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int nitems, const int *super,
+                                                        const int64_t *lpi, const int64_t *lpx, const int *ls,
+                                                        const T *L, V *x, unsigned *flags, const int *flagoff,
+                                                        unsigned epoch, const uint8_t *visible, WideCtl *ctl,
+                                                        int *status) {
+  __shared__ V Td[TB * TB];
+  __shared__ V red[SW_THREADS];
+  __shared__ V yb[TB];
+  __shared__ int s_front;
+  const int t = threadIdx.x, r = t & (TB - 1), cg = t / TB;
+  int cur_s = -1, front = 0;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int s = items[it].x, q = items[it].y;
+    if (visible && !visible[s]) continue;
+    const int c0 = super[s], w = super[s + 1] - c0;
+    const int nrow = (int)(lpi[s + 1] - lpi[s]);
+    const T *S = L + lpx[s];
+    unsigned *fl = flags + flagoff[s];
+    V *xs = x + c0;
+    if (s != cur_s) {
+      cur_s = s;
+      front = 0;
+    }
+    const int nbd = (w + TB - 1) / TB;
+    const bool diag = q < nbd;
+    const int r0 = diag ? q * TB : w + (q - nbd) * TB;
+    const int m = min(TB, (diag ? w : nrow) - r0);
+    const int jmax = diag ? q : nbd;
+    if (diag) stage_tile(S, nrow, r0, m, Td);
+    const bool rok = r < m;
+    const T *Lr = S + r0 + r;
+    V acc = V(0);
+    T v[CPT], vn[CPT];
+#pragma unroll
+    for (int cc = 0; cc < CPT; ++cc) {
+      const int col = cg * CPT + cc;
+      v[cc] = (jmax > 0 && rok && col < w) ? Lr[(size_t)col * nrow] : T(0);
+    }
+    for (int j = 0; j < jmax; ++j) {
+      const int cbn = (j + 1) * TB + cg * CPT;
+#pragma unroll
+      for (int cc = 0; cc < CPT; ++cc)
+        vn[cc] = (j + 1 < jmax && rok && cbn + cc < w) ? Lr[(size_t)(cbn + cc) * nrow] : T(0);
+      if (j >= front) {
+        __syncthreads();
+        if (t < 32) {
+          const int f = wait_up(fl, epoch, j, nbd, front, ctl, status);
+          if (t == 0) s_front = f;
+        }
+        __syncthreads();
+        front = s_front;
+        if (front < 0) return;
+      }
+      const int cb = j * TB + cg * CPT;
+#pragma unroll
+      for (int cc = 0; cc < CPT; ++cc)
+        if (cb + cc < w) acc += V(v[cc]) * __ldcg(xs + cb + cc);
+#pragma unroll
+      for (int cc = 0; cc < CPT; ++cc) v[cc] = vn[cc];
+    }
+    red[t] = acc;
+    __syncthreads();
+    if (t < TB) yb[t] = red[t] + red[t + TB] + red[t + 2 * TB] + red[t + 3 * TB];
+    __syncthreads();
+    if (diag) {
+      if (t < m) yb[t] = __ldcg(xs + r0 + t) - yb[t];
+      __syncthreads();
+      if (t < 32) warp_trsv_lower(Td, m, yb);
+      __syncthreads();
+      if (t < m) xs[r0 + t] = yb[t];
+      __syncthreads();
+      if (t == 0) publish(fl + q, epoch);
+    } else {
+      const int *rows = ls + lpi[s];
+      if (t < m) atomicAdd(&x[rows[r0 + t]], -yb[t]);
+    }
+    __syncthreads();
   }
 }
 
-template <class T>
-__global__ void __launch_bounds__(SW_THREADS) k_bwd_wide(const T *S, int nrow, int w, const int *rows, double *x,
-                                                         int c0, WideCtl *ctl, int *status) {
-  __shared__ double T11[SB * SB];
-  __shared__ double xb[SB], xn[SB];
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x, TT = gridDim.x * blockDim.x;
-  const int nblk = (w + SB - 1) / SB;
-  double *xs = x + c0;
-  auto first_col = [&](int lo) { return lo + (int)(((long long)gt - lo % TT + TT) % TT); };
-  // x_s -= L21^T x(rows below), (column, row-chunk) items
-  const int nb_rows = nrow - w;
-  if (nb_rows > 0) {
-    const int nchunk = (nb_rows + CHUNK - 1) / CHUNK;
-    for (long long item = gt; item < (long long)w * nchunk; item += TT) {
-      const int j = (int)(item % w);
-      const int ch = (int)(item / w);
-      const int r0 = w + ch * CHUNK, r1 = min(nrow, r0 + CHUNK);
-      double acc = 0.0;
-      for (int r = r0; r < r1; ++r) acc += (double)S[r + (size_t)j * nrow] * x[rows[r]];
-      atomicAdd(&xs[j], -acc);
+// Backward sweep over the large supernodes of one level.  Item (s, q) is
+// column block j = nbd(s) - 1 - q.
+template <class T, class V>
+__global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int nitems, const int *super,
+                                                        const int64_t *lpi, const int64_t *lpx, const int *ls,
+                                                        const T *L, V *x, unsigned *flags, const int *flagoff,
+                                                        unsigned epoch, const uint8_t *visible, WideCtl *ctl,
+                                                        int *status) {
+  __shared__ V Td[TB * TB];
+  __shared__ V red[2][TB];
+  __shared__ V yb[TB];
+  __shared__ int s_front;
+  const int t = threadIdx.x, r = t & (TB - 1), cg = t / TB, lane = t & 31;
+  int cur_s = -1, front = 0;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int s = items[it].x, q = items[it].y;
+    if (visible && !visible[s]) continue;
+    const int c0 = super[s], w = super[s + 1] - c0;
+    const int nrow = (int)(lpi[s + 1] - lpi[s]);
+    const T *S = L + lpx[s];
+    const int *rows = ls + lpi[s];
+    unsigned *fl = flags + flagoff[s];
+    V *xs = x + c0;
+    const int nbd = (w + TB - 1) / TB;
+    if (s != cur_s) {
+      cur_s = s;
+      front = nbd;
     }
-  }
-  if (!grid_sync(ctl, status)) return;
-  // last diagonal block
-  const int lb0 = (nblk - 1) * SB;
-  if (blockIdx.x == 0) {
-    const int m = w - lb0;
-    stage_block(S, nrow, lb0, m, T11);
-    for (int i = threadIdx.x; i < m; i += blockDim.x) xb[i] = xs[lb0 + i];
-    __syncthreads();
-    if (threadIdx.x < 32) warp_trsv_lower_t(T11, m, xb);
-    __syncthreads();
-    for (int i = threadIdx.x; i < m; i += blockDim.x) xs[lb0 + i] = xb[i];
-  }
-  if (!grid_sync(ctl, status)) return;
-  for (int b = nblk - 1; b > 0; --b) {
-    const int b0 = b * SB, b1 = min(w, b0 + SB);
-    const int m = b1 - b0;
-    const int p0 = b0 - SB;  // previous block [p0, b0)
-    for (int i = threadIdx.x; i < m; i += blockDim.x) xb[i] = xs[b0 + i];
-    __syncthreads();
-    if (blockIdx.x == 0) {
-      // look-ahead: columns [p0, b0) get block b, then their triangle is solved
-      for (int j = p0 + threadIdx.x; j < b0; j += blockDim.x) {
-        double acc = 0.0;
-        for (int i = 0; i < m; ++i) acc += (double)S[b0 + i + (size_t)j * nrow] * xb[i];
-        xs[j] -= acc;
+    const int j = nbd - 1 - q;
+    const int b0 = j * TB, nc = min(TB, w - b0);
+    stage_tile(S, nrow, b0, nc, Td);
+    const int cb = b0 + cg * CPT;
+    const T *Lc = S + (size_t)cb * nrow;  // first of this thread's columns
+    bool cok[CPT];
+#pragma unroll
+    for (int cc = 0; cc < CPT; ++cc) cok[cc] = cb + cc < w;
+    V part[CPT];
+#pragma unroll
+    for (int cc = 0; cc < CPT; ++cc) part[cc] = V(0);
+    // rows below the diagonal block: x known from the ancestors
+    for (int row = w + r; row < nrow; row += TB) {
+      const V xv = __ldcg(x + rows[row]);
+#pragma unroll
+      for (int cc = 0; cc < CPT; ++cc)
+        if (cok[cc]) part[cc] += V(Lc[row + (size_t)cc * nrow]) * xv;
+    }
+    // diagonal-block rows of later blocks, in the order they become ready
+    T v[CPT], vn[CPT];
+    {
+      const int row = (nbd - 1) * TB + r;
+#pragma unroll
+      for (int cc = 0; cc < CPT; ++cc) v[cc] = (j < nbd - 1 && row < w && cok[cc]) ? Lc[row + (size_t)cc * nrow] : T(0);
+    }
+    for (int i = nbd - 1; i > j; --i) {
+      const int rown = (i - 1) * TB + r;
+#pragma unroll
+      for (int cc = 0; cc < CPT; ++cc)
+        vn[cc] = (i - 1 > j && rown < w && cok[cc]) ? Lc[rown + (size_t)cc * nrow] : T(0);
+      if (i < front) {
+        __syncthreads();
+        if (t < 32) {
+          const int f = wait_down(fl, epoch, i, j + 1, front, ctl, status);
+          if (t == 0) s_front = f;
+        }
+        __syncthreads();
+        front = s_front;
+        if (front < 0) return;
       }
-      __syncthreads();
-      stage_block(S, nrow, p0, SB, T11);
-      for (int i = threadIdx.x; i < SB; i += blockDim.x) xn[i] = xs[p0 + i];
-      __syncthreads();
-      if (threadIdx.x < 32) warp_trsv_lower_t(T11, SB, xn);
-      __syncthreads();
-      for (int i = threadIdx.x; i < SB; i += blockDim.x) xs[p0 + i] = xn[i];
+      const int row = i * TB + r;
+      const V xv = row < w ? __ldcg(xs + row) : V(0);
+#pragma unroll
+      for (int cc = 0; cc < CPT; ++cc) part[cc] += V(v[cc]) * xv;
+#pragma unroll
+      for (int cc = 0; cc < CPT; ++cc) v[cc] = vn[cc];
     }
-    // every CTA (CTA 0 included) applies block b to its columns before the look-ahead
-    for (int j = first_col(0); j < p0; j += TT) {
-      double acc = 0.0;
-      for (int i = 0; i < m; ++i) acc += (double)S[b0 + i + (size_t)j * nrow] * xb[i];
-      xs[j] -= acc;
+    // column sums over the 64 rows: warps 2cg and 2cg+1 hold rows 0-31, 32-63
+#pragma unroll
+    for (int cc = 0; cc < CPT; ++cc) {
+      V a = part[cc];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      if (lane == 0) red[(t >> 5) & 1][cg * CPT + cc] = a;
     }
-    if (!grid_sync(ctl, status)) return;
+    __syncthreads();
+    if (t < nc) yb[t] = __ldcg(xs + b0 + t) - (red[0][t] + red[1][t]);
+    __syncthreads();
+    if (t < 32) warp_trsv_lower_t(Td, nc, yb);
+    __syncthreads();
+    if (t < nc) xs[b0 + t] = yb[t];
+    __syncthreads();
+    if (t == 0) publish(fl + j, epoch);
+    __syncthreads();
   }
+}
+
+template <class K> static int coop_grid(Plan &P, K kern, int items) {
+  int occ = 0;
+  NQG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, SW_THREADS, 0));
+  occ = std::max(occ, 1);
+  return std::max(1, std::min(items, occ * std::max(1, P.num_sms)));
+}
+
+// Next launch epoch of the ready flags (0 never marks a ready block).
+static unsigned next_epoch(Plan &P) {
+  if (++P.solve_epoch == 0) {
+    cudaMemsetAsync(P.d_solve_flags, 0, P.solve_flags_cap * sizeof(unsigned), P.stream);
+    P.solve_epoch = 1;
+  }
+  return P.solve_epoch;
 }
 
 }  // namespace
 
-template <class T> int solve_wide_fwd(Plan &P, int s, const T *L, double *x) {
-  const int c0 = P.sym.super[s], w = P.sym.super[s + 1] - c0;
-  const int nrow = (int)(P.sym.lpi[s + 1] - P.sym.lpi[s]);
-  const T *S = L + P.sym.lpx[s];
-  const int *rows = P.d_ls + P.sym.lpi[s];
+template <class T, class V> static int launch_blk(Plan &P, bool fwd, int l, const T *L, V *x) {
+  const int off = fwd ? P.blk_fwd_off[l] : P.blk_bwd_off[l];
+  const int cnt = (fwd ? P.blk_fwd_off[l + 1] : P.blk_bwd_off[l + 1]) - off;
+  if (cnt <= 0) return NQG_OK;
+  const int2 *items = reinterpret_cast<const int2 *>(P.d_blk_items) + off;
   WideCtl *ctl = reinterpret_cast<WideCtl *>(P.d_wide_ctl);
   int *status = P.d_status;
+  unsigned *flags = P.d_solve_flags;
+  const int *flagoff = P.d_flagoff;
+  const uint8_t *vis = P.masked ? P.d_visible : nullptr;
+  const int *super = P.d_super, *ls = P.d_ls;
+  const int64_t *lpi = P.d_lpi, *lpx = P.d_lpx;
   NQG_CUDA(cudaMemsetAsync(ctl, 0, 16, P.stream));
-  int G = std::max(1, P.num_sms);
-  void *args[] = {(void *)&S, (void *)&nrow, (void *)&w, (void *)&rows, &x, (void *)&c0, &ctl, &status};
+  unsigned epoch = next_epoch(P);
+  void *kern = fwd ? (void *)k_fwd_blk<T, V> : (void *)k_bwd_blk<T, V>;
+  const int G = fwd ? coop_grid(P, k_fwd_blk<T, V>, cnt) : coop_grid(P, k_bwd_blk<T, V>, cnt);
+  void *args[] = {(void *)&items, (void *)&cnt, (void *)&super, (void *)&lpi, (void *)&lpx, (void *)&ls,
+                  (void *)&L, &x, &flags, (void *)&flagoff, &epoch, (void *)&vis, &ctl, &status};
   cudaEvent_t e0 = P.prof_begin();
-  NQG_CUDA(cudaLaunchCooperativeKernel((void *)k_fwd_wide<T>, dim3(G), dim3(SW_THREADS), args, 0, P.stream));
+  NQG_CUDA(cudaLaunchCooperativeKernel(kern, dim3(G), dim3(SW_THREADS), args, 0, P.stream));
   P.nlaunch++;
-  P.prof_end(NQG_K_SOLVE, e0, 0.0, (double)nrow * w * sizeof(T));
+  P.prof_end(NQG_K_SOLVE, e0, 0.0, P.prof ? P.blk_bytes[l] * (double)sizeof(T) : 0.0);
   return NQG_OK;
 }
 
-template <class T> int solve_wide_bwd(Plan &P, int s, const T *L, double *x) {
-  const int c0 = P.sym.super[s], w = P.sym.super[s + 1] - c0;
-  const int nrow = (int)(P.sym.lpi[s + 1] - P.sym.lpi[s]);
-  const T *S = L + P.sym.lpx[s];
-  const int *rows = P.d_ls + P.sym.lpi[s];
-  WideCtl *ctl = reinterpret_cast<WideCtl *>(P.d_wide_ctl);
-  int *status = P.d_status;
-  NQG_CUDA(cudaMemsetAsync(ctl, 0, 16, P.stream));
-  int G = std::max(1, P.num_sms);
-  void *args[] = {(void *)&S, (void *)&nrow, (void *)&w, (void *)&rows, &x, (void *)&c0, &ctl, &status};
-  cudaEvent_t e0 = P.prof_begin();
-  NQG_CUDA(cudaLaunchCooperativeKernel((void *)k_bwd_wide<T>, dim3(G), dim3(SW_THREADS), args, 0, P.stream));
-  P.nlaunch++;
-  P.prof_end(NQG_K_SOLVE, e0, 0.0, (double)nrow * w * sizeof(T));
-  return NQG_OK;
+template <class T, class V> int solve_blk_fwd(Plan &P, int l, const T *L, V *x) {
+  return launch_blk<T, V>(P, true, l, L, x);
+}
+template <class T, class V> int solve_blk_bwd(Plan &P, int l, const T *L, V *x) {
+  return launch_blk<T, V>(P, false, l, L, x);
 }
 
-template int solve_wide_fwd<float>(Plan &, int, const float *, double *);
-template int solve_wide_fwd<double>(Plan &, int, const double *, double *);
-template int solve_wide_bwd<float>(Plan &, int, const float *, double *);
-template int solve_wide_bwd<double>(Plan &, int, const double *, double *);
+template int solve_blk_fwd<float, float>(Plan &, int, const float *, float *);
+template int solve_blk_fwd<float, double>(Plan &, int, const float *, double *);
+template int solve_blk_fwd<double, double>(Plan &, int, const double *, double *);
+template int solve_blk_bwd<float, float>(Plan &, int, const float *, float *);
+template int solve_blk_bwd<float, double>(Plan &, int, const float *, double *);
+template int solve_blk_bwd<double, double>(Plan &, int, const double *, double *);
 
 }  // namespace nqg

@@ -156,15 +156,40 @@ def test_fp32_factor_gmres_ir(path):
     assert np.linalg.norm(x - xr) <= 1e-6 * np.linalg.norm(xr)
 
 
-WIDE_ENV = {"NASOQ_GB300_WIDE_MIN": "12", "NASOQ_GB300_WIDE_NB": "8"}
+@pytest.mark.gpu
+@pytest.mark.parametrize("force_blk", [False, True], ids=["level", "block"])
+@pytest.mark.parametrize("path", CASES, ids=os.path.basename)
+def test_fp32_factor_fp32_solves(path, force_blk, monkeypatch):
+    """FP32 factor with the triangular solves in FP32 (solve_precision) and
+    flexible GMRES in FP64 around them: relative residual 1e-10 whenever
+    kappa < 1e8, through the per-supernode level kernels and through the
+    flag-driven block kernels."""
+    if force_blk:
+        monkeypatch.setenv("NASOQ_GB300_SOLVE_SMALL", "0,0")
+    d = nqa.load(path)
+    n = len(d["in_rhs"])
+    if cond_of(path, d) > 1e8:
+        pytest.skip("kappa * u_fp32 >= 1: FP64 factorization territory")
+    plan = nq.Plan(n, d["in_Ap"], d["in_Ai"], d["in_Ax"],
+                   settings=_settings(d, precision=nq.NQG_FP32, solve_precision=nq.NQG_FP32, req_ref_iter=6,
+                                      max_inner_iter=6, tol_abs=1e-13, tol_rel=1e-13))
+    plan.factor()
+    x = plan.solve(d["in_rhs"])
+    assert relres(d, x) <= 1e-10
+    xr = d["out_x"]
+    assert np.linalg.norm(x - xr) <= 1e-6 * np.linalg.norm(xr)
+
+
+WIDE_ENV = {"NASOQ_GB300_WIDE_MIN": "12", "NASOQ_GB300_WIDE_NB": "8", "NASOQ_GB300_SOLVE_SMALL": "0,0"}
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("path", CASES, ids=os.path.basename)
 def test_fp64_blocked_wide_kernels(path, monkeypatch):
     """Every supernode wider than 12 columns goes through the blocked
-    multi-CTA Bunch-Kaufman (panels of 8 columns): same parity bars as the
-    single-CTA kernels."""
+    multi-CTA Bunch-Kaufman (panels of 8 columns) and every supernode through
+    the flag-driven block solves: same parity bars as the single-CTA
+    kernels."""
     for k, v in WIDE_ENV.items():
         monkeypatch.setenv(k, v)
     d = nqa.load(path)

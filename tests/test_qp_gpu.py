@@ -47,7 +47,19 @@ def rel(a, b):
 @pytest.mark.gpu
 @pytest.mark.parametrize("path", CASES, ids=os.path.basename)
 def test_qp_matches_reference(path):
-    d = nqa.load(path)
+    check_against_reference(nqa.load(path))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", CASES, ids=os.path.basename)
+def test_qp_block_solves(path, monkeypatch):
+    """Every supernode through the flag-driven block solve kernels (the
+    masked solves of the active-set loop included): same bars."""
+    monkeypatch.setenv("NASOQ_GB300_SOLVE_SMALL", "0,0")
+    check_against_reference(nqa.load(path))
+
+
+def check_against_reference(d):
     x, y, z, act, res = run(d)
     assert res.status == int(d["out_status"][0])
     assert res.num_iter == int(d["out_num_iter"][0])
