@@ -18,6 +18,9 @@ struct WideCtl {
   int cidx[2][1024];
   double rval[2][1024];
   int ridx[2][1024];
+  // FP32 panels: per column step, the packed (|value| bits, ~index) maximum
+  // of the column (row 0) and pivot-row (row 1) searches; cleared per panel
+  unsigned long long amax[2][72];
 };
 
 constexpr long long SPIN_LIMIT = 1ll << 26;  // polls before a barrier gives up
@@ -51,7 +54,7 @@ __device__ __forceinline__ bool grid_sync(WideCtl *ctl, int *status) {
           ok = 0;
           break;
         }
-        __nanosleep(64);
+        __nanosleep(32);
       }
     }
     __threadfence();

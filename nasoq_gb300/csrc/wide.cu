@@ -31,6 +31,7 @@ namespace nqg {
 namespace {
 
 constexpr int WP_THREADS = 256;
+constexpr int WP_NB = 64;  // widest panel; the row cache holds WP_NB + 2 columns
 
 template <class T> __device__ __forceinline__ T tabs_w(T v) { return v < T(0) ? -v : v; }
 
@@ -106,48 +107,95 @@ template <class T> __device__ void reduce_partials(const double *pv, const int *
   __syncthreads();
 }
 
+// Packed key of a pivot candidate for the FP32 argmax: |value| bits above
+// (monotone for non-negative floats), the complemented row index below, so
+// atomicMax keeps the largest value and, among equal values, the smallest row.
+__device__ __forceinline__ unsigned long long pack_cand(float a, int i) {
+  return ((unsigned long long)__float_as_uint(a) << 32) | (unsigned)(0x7fffffff - i);
+}
+
+// Column-step argmax over the whole grid: the CTA's candidate (valid in
+// thread 0 after cta_argmax) is combined with the other CTAs', then one grid
+// barrier; every CTA returns the same (value, index).  FP32: one atomicMax on
+// a packed key per CTA; FP64: per-CTA partials reduced redundantly by all.
+template <class T>
+__device__ bool grid_argmax(T cv, int ci, WideCtl *ctl, int phase, int step, int parity, int *status, T &v,
+                            int &idx) {
+  cta_argmax(cv, ci);
+  if constexpr (sizeof(T) == 4) {
+    if (threadIdx.x == 0 && ci >= 0) atomicMax(&ctl->amax[phase][step], pack_cand((float)cv, ci));
+    if (!grid_sync(ctl, status)) return false;
+    const unsigned long long key = *(volatile unsigned long long *)&ctl->amax[phase][step];
+    if (key == 0ull) {
+      v = T(0);
+      idx = -1;
+    } else {
+      v = (T)__uint_as_float((unsigned)(key >> 32));
+      idx = 0x7fffffff - (int)(unsigned)(key & 0xffffffffull);
+    }
+  } else {
+    double *pv = phase ? ctl->rval[parity] : ctl->cval[parity];
+    int *pi = phase ? ctl->ridx[parity] : ctl->cidx[parity];
+    if (threadIdx.x == 0) {
+      pv[blockIdx.x] = (double)cv;
+      pi[blockIdx.x] = ci;
+    }
+    if (!grid_sync(ctl, status)) return false;
+    reduce_partials(pv, pi, gridDim.x, v, idx);
+  }
+  return true;
+}
+
 // One panel: columns c = k0 .. (at most k0+nb, one more for a final 2x2).
+// Thread gt owns rows gt, gt + TT, ...; the panel entries L(gt, k0 + t) of
+// its first row are cached in shared memory (lc[t][threadIdx.x]) as they are
+// produced, so the column updates of later steps read no global memory for
+// that row.  An interchange rewrites rows kk and kp of the finished columns;
+// their owners reload the cache after the barrier that ends it.
 template <class T>
 __global__ void __launch_bounds__(WP_THREADS) k_wide_panel(T *S, int nrow, int w, int k0, int nb, T *Wb, int ldw,
                                                            T *Dd, T *De, int *perm, WideCtl *ctl, int *status) {
+  extern __shared__ __align__(16) unsigned char wp_raw[];
+  T *lc = reinterpret_cast<T *>(wp_raw);  // [WP_NB + 2][WP_THREADS]
   __shared__ T wrow[128];
   const T alpha = (T)((1.0 + sqrt(17.0)) / 8.0);
-  const int G = gridDim.x;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int TT = G * blockDim.x;
-  // Every row keeps the same owner thread in every step (r % TT == gt), so a
-  // thread reads back only the L entries it wrote itself between barriers.
+  const int TT = gridDim.x * blockDim.x;
+  const int tid = threadIdx.x;
   auto first_row = [&](int lo) { return lo + (int)(((long long)gt - lo % TT + TT) % TT); };
+  // L(r, k0 + t) for t < j: cached for the thread's first row, else global
+  auto lrow_dot = [&](int r, int j) {
+    T acc = T(0);
+    if (r == gt) {
+      for (int t = 0; t < j; ++t) acc += lc[t * WP_THREADS + tid] * wrow[t];
+    } else {
+      for (int t = 0; t < j; ++t) acc += S[r + (size_t)(k0 + t) * nrow] * wrow[t];
+    }
+    return acc;
+  };
   int j = 0;
   int parity = 0;
   while (j < nb && k0 + j < w) {
     const int c = k0 + j;
     // ---- A: updated column c into W(:, j), rows [c, nrow)
-    for (int t = threadIdx.x; t < j; t += blockDim.x) wrow[t] = Wb[(size_t)t * ldw + c];
+    for (int t = tid; t < j; t += blockDim.x) wrow[t] = Wb[(size_t)t * ldw + c];
     __syncthreads();
     T cv = T(-1);
     int ci = -1;
     for (int r = first_row(c); r < nrow; r += TT) {
-      T acc = S[r + (size_t)c * nrow];
-      for (int t = 0; t < j; ++t) acc -= S[r + (size_t)(k0 + t) * nrow] * wrow[t];
+      const T acc = S[r + (size_t)c * nrow] - lrow_dot(r, j);
       Wb[(size_t)j * ldw + r] = acc;
       if (r > c && r < w) {
-        T a = tabs_w(acc);
-        if (ci < 0 || a > cv) {
+        const T a = tabs_w(acc);
+        if (a == a && (ci < 0 || a > cv)) {
           cv = a;
           ci = r;
         }
       }
     }
-    cta_argmax(cv, ci);
-    if (threadIdx.x == 0) {
-      ctl->cval[parity][blockIdx.x] = (double)cv;
-      ctl->cidx[parity][blockIdx.x] = ci;
-    }
-    if (!grid_sync(ctl, status)) return;
     T colmax;
     int imax;
-    reduce_partials(ctl->cval[parity], ctl->cidx[parity], G, colmax, imax);
+    if (!grid_argmax(cv, ci, ctl, 0, j, parity, status, colmax, imax)) return;
     if (imax < 0) colmax = T(0);
     const T absakk = tabs_w(Wb[(size_t)j * ldw + c]);
     int kp = c, kstep = 1;
@@ -156,31 +204,25 @@ __global__ void __launch_bounds__(WP_THREADS) k_wide_panel(T *S, int nrow, int w
       zero = true;
     } else if (absakk < alpha * colmax) {
       // ---- B: updated column imax into W(:, j+1) and its off-diagonal max
-      for (int t = threadIdx.x; t < j; t += blockDim.x) wrow[t] = Wb[(size_t)t * ldw + imax];
+      for (int t = tid; t < j; t += blockDim.x) wrow[t] = Wb[(size_t)t * ldw + imax];
       __syncthreads();
       T rv = T(-1);
       int ri = -1;
       for (int r = first_row(c); r < nrow; r += TT) {
-        T acc = r < imax ? S[imax + (size_t)r * nrow] : S[r + (size_t)imax * nrow];
-        for (int t = 0; t < j; ++t) acc -= S[r + (size_t)(k0 + t) * nrow] * wrow[t];
+        const T a0 = r < imax ? S[imax + (size_t)r * nrow] : S[r + (size_t)imax * nrow];
+        const T acc = a0 - lrow_dot(r, j);
         Wb[(size_t)(j + 1) * ldw + r] = acc;
         if (r < w && r != imax) {
-          T a = tabs_w(acc);
-          if (ri < 0 || a > rv) {
+          const T a = tabs_w(acc);
+          if (a == a && (ri < 0 || a > rv)) {
             rv = a;
             ri = r;
           }
         }
       }
-      cta_argmax(rv, ri);
-      if (threadIdx.x == 0) {
-        ctl->rval[parity][blockIdx.x] = (double)rv;
-        ctl->ridx[parity][blockIdx.x] = ri;
-      }
-      if (!grid_sync(ctl, status)) return;
       T rowmax;
       int rdummy;
-      reduce_partials(ctl->rval[parity], ctl->ridx[parity], G, rowmax, rdummy);
+      if (!grid_argmax(rv, ri, ctl, 1, j, parity, status, rowmax, rdummy)) return;
       const T diag_imax = tabs_w(Wb[(size_t)(j + 1) * ldw + imax]);
       if (absakk >= alpha * colmax * (colmax / rowmax)) {
         kp = c;
@@ -216,7 +258,7 @@ __global__ void __launch_bounds__(WP_THREADS) k_wide_panel(T *S, int nrow, int w
         T t = S[kk + (size_t)kk * nrow];
         S[kk + (size_t)kk * nrow] = S[kp + (size_t)kp * nrow];
         S[kp + (size_t)kp * nrow] = t;
-        int pt = perm[kk - 0];
+        int pt = perm[kk];
         perm[kk] = perm[kp];
         perm[kp] = pt;
         if (copycol) {
@@ -238,15 +280,27 @@ __global__ void __launch_bounds__(WP_THREADS) k_wide_panel(T *S, int nrow, int w
         ctl->pivoted = 1;
       }
       if (!grid_sync(ctl, status)) return;
+      if (gt == kk || gt == kp)
+        for (int t = 0; t < j; ++t) lc[t * WP_THREADS + tid] = S[gt + (size_t)(k0 + t) * nrow];
     }
     // ---- D: L column(s) from W, D entries
     if (kstep == 1) {
       const T d = Wb[(size_t)j * ldw + c];
       if (!zero) {
         const T r1 = T(1) / d;
-        for (int r = first_row(c + 1); r < nrow; r += TT) S[r + (size_t)c * nrow] = Wb[(size_t)j * ldw + r] * r1;
-      } else if (gt == 0) {
-        atomicOr(status, ST_ZERO_PIVOT);
+        for (int r = first_row(c + 1); r < nrow; r += TT) {
+          const T l = Wb[(size_t)j * ldw + r] * r1;
+          S[r + (size_t)c * nrow] = l;
+          if (r == gt) lc[j * WP_THREADS + tid] = l;
+        }
+      } else {
+        // zero pivot column: kept unscaled (LAPACK dlasyf copies W(k:n,k))
+        for (int r = first_row(c + 1); r < nrow; r += TT) {
+          const T l = Wb[(size_t)j * ldw + r];
+          S[r + (size_t)c * nrow] = l;
+          if (r == gt) lc[j * WP_THREADS + tid] = l;
+        }
+        if (gt == 0) atomicOr(status, ST_ZERO_PIVOT);
       }
       if (gt == 0) {
         S[c + (size_t)c * nrow] = T(1);
@@ -262,8 +316,13 @@ __global__ void __launch_bounds__(WP_THREADS) k_wide_panel(T *S, int nrow, int w
       d21 = tt / d21;
       for (int r = first_row(c + 2); r < nrow; r += TT) {
         const T wk = Wb[(size_t)j * ldw + r], wk1 = Wb[(size_t)(j + 1) * ldw + r];
-        S[r + (size_t)c * nrow] = d21 * (d11 * wk - wk1);
-        S[r + (size_t)(c + 1) * nrow] = d21 * (d22 * wk1 - wk);
+        const T l0 = d21 * (d11 * wk - wk1), l1 = d21 * (d22 * wk1 - wk);
+        S[r + (size_t)c * nrow] = l0;
+        S[r + (size_t)(c + 1) * nrow] = l1;
+        if (r == gt) {
+          lc[j * WP_THREADS + tid] = l0;
+          lc[(j + 1) * WP_THREADS + tid] = l1;
+        }
       }
       if (gt == 0) {
         S[c + (size_t)c * nrow] = T(1);
@@ -352,47 +411,54 @@ template <class T> __global__ void k_wide_zero_upper(T *S, int nrow, int w) {
 
 }  // namespace
 
-// Host driver for one wide supernode s.  Scratch: Wb (nrow x (nb+2)), ctl.
+// Panel / trailing-update sequence of one wide supernode: values S (nrow x
+// w, column-major), D and E (diagonal, 2x2 sub-diagonals), in-block pivot
+// order perm; scratch Wb (nrow x (nb+2)) and ctl.  P, when given, receives the
+// launch count and the per-class timings.
 template <class T>
-int factor_wide(Plan &P, int s, T *L, T *Dg, int nb, T *Wb, WideCtl *ctl, int num_sms) {
-  cudaStream_t st = P.stream;
-  const int c0 = P.sym.super[s], w = P.sym.super[s + 1] - c0;
-  const int nrow = (int)(P.sym.lpi[s + 1] - P.sym.lpi[s]);
-  T *S = L + P.sym.lpx[s];
-  const int n = P.n;
-  int *perm = P.d_locperm + c0;
+static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideCtl *ctl, int *status,
+                    cudaStream_t st, int num_sms, int nb, int *pivoted, Plan *P) {
+  if (nb > WP_NB || nb < 1) return NQG_ERR_ARG;
   k_wide_init_perm<T><<<(w + 255) / 256, 256, 0, st>>>(perm, w);
-  P.nlaunch++;
-  NQG_CUDA(cudaMemsetAsync(ctl, 0, sizeof(WideCtl), st));
+  if (P) P->nlaunch++;
+  if (cudaMemsetAsync(ctl, 0, sizeof(WideCtl), st) != cudaSuccess) return NQG_ERR_CUDA;
+  const size_t smem = (size_t)(WP_NB + 2) * WP_THREADS * sizeof(T);
+  // per call: the attribute belongs to the current device
+  if (cudaFuncSetAttribute(k_wide_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return NQG_ERR_CUDA;
   int occ = 0;
-  NQG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_wide_panel<T>, WP_THREADS, 0));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_wide_panel<T>, WP_THREADS, smem) != cudaSuccess)
+    return NQG_ERR_CUDA;
   const int maxG = std::max(1, std::min(occ * num_sms, 1024));
-  T *Dd = Dg + c0, *De = Dg + n + c0;
-  int *status = P.d_status;
   int k0 = 0;
   while (k0 < w) {
-    int rows_left = nrow - k0;
-    int G = std::max(1, std::min(maxG, std::min(num_sms, (rows_left + 511) / 512)));
+    // one row per thread where the grid allows it
+    const int rows_left = nrow - k0;
+    const int G = std::max(1, std::min(maxG, (rows_left + WP_THREADS - 1) / WP_THREADS));
     int kb_want = std::min(nb, w - k0);
-    void *args[] = {&S, (void *)&nrow, (void *)&w, &k0, &kb_want, &Wb, (void *)&nrow, &Dd, &De, &perm, &ctl, &status};
-    cudaEvent_t e0 = P.prof_begin();
-    NQG_CUDA(cudaLaunchCooperativeKernel((void *)k_wide_panel<T>, dim3(G), dim3(WP_THREADS), args, 0, st));
-    P.nlaunch++;
-    int kb = 0;
-    NQG_CUDA(cudaMemcpyAsync(&kb, &ctl->kb, sizeof(int), cudaMemcpyDeviceToHost, st));
-    NQG_CUDA(cudaStreamSynchronize(st));
-    int abort = 0;
-    NQG_CUDA(cudaMemcpy(&abort, &ctl->abort, sizeof(int), cudaMemcpyDeviceToHost));
+    int ldw = nrow;
+    void *args[] = {&S, &nrow, &w, &k0, &kb_want, &Wb, &ldw, &Dd, &De, &perm, &ctl, &status};
+    if (cudaMemsetAsync(&ctl->amax[0][0], 0, sizeof(ctl->amax), st) != cudaSuccess) return NQG_ERR_CUDA;
+    cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
+    if (cudaLaunchCooperativeKernel((void *)k_wide_panel<T>, dim3(G), dim3(WP_THREADS), args, smem, st) !=
+        cudaSuccess)
+      return NQG_ERR_CUDA;
+    if (P) P->nlaunch++;
+    int kb = 0, abort = 0;
+    if (cudaMemcpyAsync(&kb, &ctl->kb, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&abort, &ctl->abort, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return NQG_ERR_CUDA;
     if (abort || kb <= 0) return NQG_ERR_TIMEOUT;
     const int k1 = k0 + kb;
-    {
+    if (P) {
       // panel: column GEMVs (2 * rows * j) and the L column scaling
       double fl = 0;
-      for (int j = 0; j < kb; ++j) fl += 2.0 * (nrow - (k0 + j)) * (j + 1);
-      P.prof_end(NQG_K_WIDE_PANEL, e0, fl, 0.0);
+      for (int jj = 0; jj < kb; ++jj) fl += 2.0 * (nrow - (k0 + jj)) * (jj + 1);
+      P->prof_end(NQG_K_WIDE_PANEL, e0, fl, 0.0);
     }
     if (k1 < w) {
-      cudaEvent_t e1 = P.prof_begin();
+      cudaEvent_t e1 = P ? P->prof_begin() : nullptr;
       if (sizeof(T) == 4) {
         constexpr int BM = 128, BN = 128;
         int tm = (nrow - k1 + BM - 1) / BM, tn = (w - k1 + BN - 1) / BN;
@@ -402,24 +468,44 @@ int factor_wide(Plan &P, int s, T *L, T *Dg, int nb, T *Wb, WideCtl *ctl, int nu
         int tm = (nrow - k1 + BM - 1) / BM, tn = (w - k1 + BN - 1) / BN;
         k_wide_trailing<T, BM, BN, 4, 4><<<tm * tn, 256, 0, st>>>(S, nrow, w, k0, kb, Wb, nrow, tn);
       }
-      P.nlaunch++;
-      // useful multiply-adds: kb per entry of the lower trapezoid rows [k1,nrow) x cols [k1,w)
-      const double cols = w - k1;
-      const double entries = cols * (nrow - k1) - cols * (cols - 1) / 2.0;
-      P.prof_end(NQG_K_WIDE_TRAILING, e1, 2.0 * kb * entries, 0.0);
-      NQG_CUDA(cudaGetLastError());
+      if (cudaGetLastError() != cudaSuccess) return NQG_ERR_CUDA;
+      if (P) {
+        P->nlaunch++;
+        // useful multiply-adds: kb per entry of the lower trapezoid rows [k1,nrow) x cols [k1,w)
+        const double cols = w - k1;
+        const double entries = cols * (nrow - k1) - cols * (cols - 1) / 2.0;
+        P->prof_end(NQG_K_WIDE_TRAILING, e1, 2.0 * kb * entries, 0.0);
+      }
     }
     k0 = k1;
   }
   k_wide_zero_upper<T><<<std::min(w, 1024), 128, 0, st>>>(S, nrow, w);
-  P.nlaunch++;
-  NQG_CUDA(cudaGetLastError());
+  if (P) P->nlaunch++;
+  if (cudaGetLastError() != cudaSuccess) return NQG_ERR_CUDA;
   int piv = 0;
-  NQG_CUDA(cudaMemcpyAsync(&piv, &ctl->pivoted, sizeof(int), cudaMemcpyDeviceToHost, st));
-  NQG_CUDA(cudaStreamSynchronize(st));
+  if (cudaMemcpyAsync(&piv, &ctl->pivoted, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return NQG_ERR_CUDA;
+  if (pivoted) *pivoted = piv;
+  return NQG_OK;
+}
+
+// Host driver for one wide supernode s of a plan.
+template <class T>
+int factor_wide(Plan &P, int s, T *L, T *Dg, int nb, T *Wb, WideCtl *ctl, int num_sms) {
+  const int c0 = P.sym.super[s], w = P.sym.super[s + 1] - c0;
+  const int nrow = (int)(P.sym.lpi[s + 1] - P.sym.lpi[s]);
+  int piv = 0;
+  int rc = run_wide<T>(L + P.sym.lpx[s], nrow, w, Dg + c0, Dg + P.n + c0, P.d_locperm + c0, Wb, ctl, P.d_status,
+                       P.stream, num_sms, nb, &piv, &P);
+  if (rc == NQG_ERR_CUDA) {
+    cudaError_t e = cudaGetLastError();
+    P.last_error = cudaGetErrorString(e);
+  }
+  if (rc) return rc;
   uint8_t pv = piv ? 1 : 0;
-  NQG_CUDA(cudaMemcpyAsync(P.d_pivoted + s, &pv, 1, cudaMemcpyHostToDevice, st));
-  NQG_CUDA(cudaStreamSynchronize(st));
+  NQG_CUDA(cudaMemcpyAsync(P.d_pivoted + s, &pv, 1, cudaMemcpyHostToDevice, P.stream));
+  NQG_CUDA(cudaStreamSynchronize(P.stream));
   return NQG_OK;
 }
 
@@ -431,49 +517,7 @@ size_t wide_ctl_bytes() { return sizeof(WideCtl); }
 template <class T>
 int factor_wide_raw(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideCtl *ctl, int *status,
                     cudaStream_t st, int num_sms, int nb, int *pivoted) {
-  k_wide_init_perm<T><<<(w + 255) / 256, 256, 0, st>>>(perm, w);
-  if (cudaMemsetAsync(ctl, 0, sizeof(WideCtl), st) != cudaSuccess) return NQG_ERR_CUDA;
-  int occ = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_wide_panel<T>, WP_THREADS, 0) != cudaSuccess)
-    return NQG_ERR_CUDA;
-  const int maxG = std::max(1, std::min(occ * num_sms, 1024));
-  int k0 = 0;
-  while (k0 < w) {
-    int rows_left = nrow - k0;
-    int G = std::max(1, std::min(maxG, std::min(num_sms, (rows_left + 511) / 512)));
-    int kb_want = std::min(nb, w - k0);
-    int ldw = nrow;
-    void *args[] = {&S, &nrow, &w, &k0, &kb_want, &Wb, &ldw, &Dd, &De, &perm, &ctl, &status};
-    if (cudaLaunchCooperativeKernel((void *)k_wide_panel<T>, dim3(G), dim3(WP_THREADS), args, 0, st) != cudaSuccess)
-      return NQG_ERR_CUDA;
-    int kb = 0, abort = 0;
-    if (cudaMemcpyAsync(&kb, &ctl->kb, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaMemcpyAsync(&abort, &ctl->abort, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-      return NQG_ERR_CUDA;
-    if (abort || kb <= 0) return NQG_ERR_TIMEOUT;
-    const int k1 = k0 + kb;
-    if (k1 < w) {
-      if (sizeof(T) == 4) {
-        constexpr int BM = 128, BN = 128;
-        int tm = (nrow - k1 + BM - 1) / BM, tn = (w - k1 + BN - 1) / BN;
-        k_wide_trailing<T, BM, BN, 8, 8><<<tm * tn, 256, 0, st>>>(S, nrow, w, k0, kb, Wb, nrow, tn);
-      } else {
-        constexpr int BM = 64, BN = 64;
-        int tm = (nrow - k1 + BM - 1) / BM, tn = (w - k1 + BN - 1) / BN;
-        k_wide_trailing<T, BM, BN, 4, 4><<<tm * tn, 256, 0, st>>>(S, nrow, w, k0, kb, Wb, nrow, tn);
-      }
-      if (cudaGetLastError() != cudaSuccess) return NQG_ERR_CUDA;
-    }
-    k0 = k1;
-  }
-  k_wide_zero_upper<T><<<std::min(w, 1024), 128, 0, st>>>(S, nrow, w);
-  int piv = 0;
-  if (cudaMemcpyAsync(&piv, &ctl->pivoted, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess)
-    return NQG_ERR_CUDA;
-  if (pivoted) *pivoted = piv;
-  return NQG_OK;
+  return run_wide<T>(S, nrow, w, Dd, De, perm, Wb, ctl, status, st, num_sms, nb, pivoted, nullptr);
 }
 
 template int factor_wide_raw<double>(double *, int, int, double *, double *, int *, double *, WideCtl *, int *,
