@@ -22,9 +22,12 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <string>
 
 #include "coop.cuh"
 #include "plan.hpp"
+#include "tf32x3.cuh"
 
 namespace nqg {
 
@@ -399,6 +402,85 @@ __global__ void __launch_bounds__((BM / RM) * (BN / RN)) k_wide_trailing(T *S, i
   }
 }
 
+// FP32 trailing update on tensor cores: the same A22 -= L21 W21^T as
+// k_wide_trailing, with split-TF32 mma.sync products (FP32-level accuracy).
+// CTA tile 128 x 128, eight warps of 64 x 32; K in chunks of 32 staged
+// column-major in shared memory (conflict-free fragment reads with a leading
+// dimension of 136); the result is staged through shared memory so that the
+// read-modify-write of the factor is coalesced along its columns.
+constexpr int TC_BM = 128, TC_BN = 128, TC_KC = 32, TC_LD = 136, TC_LDC = 132;
+constexpr size_t TC_SMEM = (size_t)TC_BN * TC_LDC * sizeof(float);  // >= 2 * TC_KC * TC_LD floats
+
+__global__ void __launch_bounds__(256, 2) k_wide_trailing_tc(float *S, int nrow, int w, int k0, int kb,
+                                                              const float *Wb, int ldw, int tiles_n) {
+  extern __shared__ __align__(16) float tc_smem[];
+  float *As = tc_smem;                 // [TC_KC][TC_LD]: L21 rows of the tile
+  float *Bs = tc_smem + TC_KC * TC_LD;  // [TC_KC][TC_LD]: W21 rows (= factor columns) of the tile
+  const int k1 = k0 + kb;
+  const int tn = blockIdx.x % tiles_n, tm = blockIdx.x / tiles_n;
+  const int col0 = k1 + tn * TC_BN;
+  const int row0 = k1 + tm * TC_BM;
+  if (row0 + TC_BM - 1 < col0) return;  // tile strictly above the diagonal
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = warp >> 2, wn = warp & 3, g = lane >> 2, t = lane & 3;
+  float acc[4][4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int jn = 0; jn < 4; ++jn)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[i][jn][q] = 0.f;
+  for (int kc0 = 0; kc0 < kb; kc0 += TC_KC) {
+    __syncthreads();
+    for (int e = tid; e < TC_KC * TC_BM; e += 256) {
+      const int kk = e / TC_BM, i = e % TC_BM;
+      const int kt = kc0 + kk, r = row0 + i, col = col0 + i;
+      As[kk * TC_LD + i] = (kt < kb && r < nrow) ? S[r + (size_t)(k0 + kt) * nrow] : 0.f;
+      Bs[kk * TC_LD + i] = (kt < kb && col < w) ? Wb[(size_t)kt * ldw + col] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ks = 0; ks < TC_KC; ks += 8) {
+      uint32_t ah[4][4], al[4][4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int rb = wm * 64 + i * 16 + g;
+        split_tf32(As[(ks + t) * TC_LD + rb], ah[i][0], al[i][0]);
+        split_tf32(As[(ks + t) * TC_LD + rb + 8], ah[i][1], al[i][1]);
+        split_tf32(As[(ks + t + 4) * TC_LD + rb], ah[i][2], al[i][2]);
+        split_tf32(As[(ks + t + 4) * TC_LD + rb + 8], ah[i][3], al[i][3]);
+      }
+#pragma unroll
+      for (int jn = 0; jn < 4; ++jn) {
+        const int cb = wn * 32 + jn * 8 + g;
+        uint32_t bh[2], bl[2];
+        split_tf32(Bs[(ks + t) * TC_LD + cb], bh[0], bl[0]);
+        split_tf32(Bs[(ks + t + 4) * TC_LD + cb], bh[1], bl[1]);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) mma_tf32x3(acc[i][jn], ah[i], al[i], bh, bl);
+      }
+    }
+  }
+  __syncthreads();
+  float *Cs = tc_smem;  // [TC_BN][TC_LDC], column-major tile of the product
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int jn = 0; jn < 4; ++jn) {
+      const int r = wm * 64 + i * 16 + g, c = wn * 32 + jn * 8 + 2 * t;
+      Cs[c * TC_LDC + r] = acc[i][jn][0];
+      Cs[(c + 1) * TC_LDC + r] = acc[i][jn][1];
+      Cs[c * TC_LDC + r + 8] = acc[i][jn][2];
+      Cs[(c + 1) * TC_LDC + r + 8] = acc[i][jn][3];
+    }
+  __syncthreads();
+  for (int e = tid; e < TC_BM * TC_BN; e += 256) {
+    const int c = e / TC_BM, r = e % TC_BM;
+    const int gr = row0 + r, gc = col0 + c;
+    if (gr < nrow && gc < w && gr >= gc) S[gr + (size_t)gc * nrow] -= Cs[c * TC_LDC + r];
+  }
+}
+
 template <class T> __global__ void k_wide_init_perm(int *perm, int w) {
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < w; m += gridDim.x * blockDim.x) perm[m] = m;
 }
@@ -430,6 +512,14 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_wide_panel<T>, WP_THREADS, smem) != cudaSuccess)
     return NQG_ERR_CUDA;
   const int maxG = std::max(1, std::min(occ * num_sms, 1024));
+  // FP32 trailing updates on tensor cores (split TF32) unless
+  // NASOQ_GB300_TRAILING=simt selects the CUDA-core kernel
+  const char *te = std::getenv("NASOQ_GB300_TRAILING");
+  const bool tc_trailing = !(te && std::string(te) == "simt");
+  if (sizeof(T) == 4 && tc_trailing &&
+      cudaFuncSetAttribute(k_wide_trailing_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM) !=
+          cudaSuccess)
+    return NQG_ERR_CUDA;
   int k0 = 0;
   while (k0 < w) {
     // one row per thread where the grid allows it
@@ -459,7 +549,11 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     }
     if (k1 < w) {
       cudaEvent_t e1 = P ? P->prof_begin() : nullptr;
-      if (sizeof(T) == 4) {
+      if (sizeof(T) == 4 && tc_trailing) {
+        int tm = (nrow - k1 + TC_BM - 1) / TC_BM, tn = (w - k1 + TC_BN - 1) / TC_BN;
+        k_wide_trailing_tc<<<tm * tn, 256, TC_SMEM, st>>>(reinterpret_cast<float *>(S), nrow, w, k0, kb,
+                                                          reinterpret_cast<const float *>(Wb), nrow, tn);
+      } else if (sizeof(T) == 4) {
         constexpr int BM = 128, BN = 128;
         int tm = (nrow - k1 + BM - 1) / BM, tn = (w - k1 + BN - 1) / BN;
         k_wide_trailing<T, BM, BN, 8, 8><<<tm * tn, 256, 0, st>>>(S, nrow, w, k0, kb, Wb, nrow, tn);

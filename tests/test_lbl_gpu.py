@@ -208,3 +208,27 @@ def test_fp64_blocked_wide_kernels(path, monkeypatch):
     x0 = plan.solve(d["in_rhs"])
     xr = d["out_x_noref"]
     assert np.linalg.norm(x0 - xr) <= xtol * np.linalg.norm(xr)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("trailing", ["tc", "simt"])
+@pytest.mark.parametrize("path", CASES, ids=os.path.basename)
+def test_fp32_blocked_wide_kernels(path, trailing, monkeypatch):
+    """FP32 factor with every supernode wider than 12 columns in the blocked
+    kernels, trailing updates on tensor cores (split TF32) or on CUDA cores:
+    the refined solution meets the FP32 bar of the single-CTA kernels."""
+    for k, v in WIDE_ENV.items():
+        monkeypatch.setenv(k, v)
+    monkeypatch.setenv("NASOQ_GB300_TRAILING", trailing)
+    d = nqa.load(path)
+    n = len(d["in_rhs"])
+    if cond_of(path, d) > 1e8:
+        pytest.skip("kappa * u_fp32 >= 1: FP64 factorization territory")
+    plan = nq.Plan(n, d["in_Ap"], d["in_Ai"], d["in_Ax"],
+                   settings=_settings(d, precision=nq.NQG_FP32, req_ref_iter=6, max_inner_iter=6,
+                                      tol_abs=1e-13, tol_rel=1e-13))
+    assert plan.factor() == 0
+    x = plan.solve(d["in_rhs"])
+    assert relres(d, x) <= 1e-10
+    xr = d["out_x"]
+    assert np.linalg.norm(x - xr) <= 1e-6 * np.linalg.norm(xr)
