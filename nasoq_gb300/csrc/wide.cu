@@ -27,6 +27,7 @@
 
 #include "coop.cuh"
 #include "plan.hpp"
+#include "tcgen05.cuh"
 #include "tf32x3.cuh"
 
 namespace nqg {
@@ -474,11 +475,63 @@ __global__ void __launch_bounds__(256, 2) k_wide_trailing_tc(float *S, int nrow,
       Cs[(c + 1) * TC_LDC + r + 8] = acc[i][jn][3];
     }
   __syncthreads();
-  for (int e = tid; e < TC_BM * TC_BN; e += 256) {
-    const int c = e / TC_BM, r = e % TC_BM;
-    const int gr = row0 + r, gc = col0 + c;
-    if (gr < nrow && gc < w && gr >= gc) S[gr + (size_t)gc * nrow] -= Cs[c * TC_LDC + r];
+  // read-modify-write in batches of 8 columns: the loads of a batch are issued
+  // before its stores (they cannot be reordered across stores to the factor)
+  const int r = tid & (TC_BM - 1), gr = row0 + r;
+  for (int cb = (tid >> 7) * 8; cb < TC_BN; cb += 16) {
+    float cur[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int gc = col0 + cb + q;
+      cur[q] = (gr < nrow && gc < w && gr >= gc) ? S[gr + (size_t)gc * nrow] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int gc = col0 + cb + q;
+      if (gr < nrow && gc < w && gr >= gc) S[gr + (size_t)gc * nrow] = cur[q] - Cs[(cb + q) * TC_LDC + r];
+    }
   }
+}
+
+// FP32 trailing update on the fifth-generation tensor cores: one 128 x 128
+// tile of A22 -= L21 W21^T per CTA of four warps, split-TF32 products
+// accumulated in TMEM (tile_tf32x3, one operand stage so that three CTAs share
+// an SM), and a read-modify-write epilogue in which thread r owns row r of the
+// tile (coalesced along the factor's columns).
+__global__ void __launch_bounds__(t5::THREADS) k_wide_trailing_t5(float *S, int nrow, int w, int k0, int kb,
+                                                                  const float *Wb, int ldw, int tiles_n,
+                                                                  int *status) {
+  extern __shared__ __align__(1024) unsigned char t5_smem[];
+  const int k1 = k0 + kb;
+  const int tn = blockIdx.x % tiles_n, tm = blockIdx.x / tiles_n;
+  const int col0 = k1 + tn * t5::TN;
+  const int row0 = k1 + tm * t5::TM;
+  if (row0 + t5::TM - 1 < col0) return;  // tile strictly above the diagonal
+  const float *L21 = S + (size_t)k0 * nrow;
+  auto fa = [&](int r, int k) {
+    const int gr = row0 + r;
+    return gr < nrow ? L21[gr + (size_t)k * nrow] : 0.f;
+  };
+  auto fb = [&](int n, int k) {
+    const int gc = col0 + n;
+    return gc < w ? Wb[(size_t)k * ldw + gc] : 0.f;
+  };
+  auto ep = [&](int r, int c0, const uint32_t(&v)[32]) {
+    const int gr = row0 + r;
+    if (gr >= nrow) return;
+    float cur[32];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+      const int gc = col0 + c0 + q;
+      cur[q] = (gc < w && gr >= gc) ? S[gr + (size_t)gc * nrow] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+      const int gc = col0 + c0 + q;
+      if (gc < w && gr >= gc) S[gr + (size_t)gc * nrow] = cur[q] - __uint_as_float(v[q]);
+    }
+  };
+  t5::tile_tf32x3<1>(kb, fa, fb, ep, t5_smem, status);
 }
 
 template <class T> __global__ void k_wide_init_perm(int *perm, int w) {
@@ -512,12 +565,17 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_wide_panel<T>, WP_THREADS, smem) != cudaSuccess)
     return NQG_ERR_CUDA;
   const int maxG = std::max(1, std::min(occ * num_sms, 1024));
-  // FP32 trailing updates on tensor cores (split TF32) unless
-  // NASOQ_GB300_TRAILING=simt selects the CUDA-core kernel
+  // FP32 trailing updates: tcgen05 split-TF32 tiles by default;
+  // NASOQ_GB300_TRAILING=mma selects the mma.sync split-TF32 kernel and
+  // =simt the CUDA-core kernel
   const char *te = std::getenv("NASOQ_GB300_TRAILING");
-  const bool tc_trailing = !(te && std::string(te) == "simt");
-  if (sizeof(T) == 4 && tc_trailing &&
+  const int trail = !te ? 2 : std::string(te) == "simt" ? 0 : std::string(te) == "mma" ? 1 : 2;
+  if (sizeof(T) == 4 && trail == 1 &&
       cudaFuncSetAttribute(k_wide_trailing_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM) !=
+          cudaSuccess)
+    return NQG_ERR_CUDA;
+  if (sizeof(T) == 4 && trail == 2 &&
+      cudaFuncSetAttribute(k_wide_trailing_t5, cudaFuncAttributeMaxDynamicSharedMemorySize, t5::smem_bytes(1)) !=
           cudaSuccess)
     return NQG_ERR_CUDA;
   int k0 = 0;
@@ -549,7 +607,11 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     }
     if (k1 < w) {
       cudaEvent_t e1 = P ? P->prof_begin() : nullptr;
-      if (sizeof(T) == 4 && tc_trailing) {
+      if (sizeof(T) == 4 && trail == 2) {
+        int tm = (nrow - k1 + t5::TM - 1) / t5::TM, tn = (w - k1 + t5::TN - 1) / t5::TN;
+        k_wide_trailing_t5<<<tm * tn, t5::THREADS, t5::smem_bytes(1), st>>>(
+            reinterpret_cast<float *>(S), nrow, w, k0, kb, reinterpret_cast<const float *>(Wb), nrow, tn, status);
+      } else if (sizeof(T) == 4 && trail == 1) {
         int tm = (nrow - k1 + TC_BM - 1) / TC_BM, tn = (w - k1 + TC_BN - 1) / TC_BN;
         k_wide_trailing_tc<<<tm * tn, 256, TC_SMEM, st>>>(reinterpret_cast<float *>(S), nrow, w, k0, kb,
                                                           reinterpret_cast<const float *>(Wb), nrow, tn);

@@ -211,11 +211,12 @@ def test_fp64_blocked_wide_kernels(path, monkeypatch):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("trailing", ["tc", "simt"])
+@pytest.mark.parametrize("trailing", ["tcgen05", "mma", "simt"])
 @pytest.mark.parametrize("path", CASES, ids=os.path.basename)
 def test_fp32_blocked_wide_kernels(path, trailing, monkeypatch):
     """FP32 factor with every supernode wider than 12 columns in the blocked
-    kernels, trailing updates on tensor cores (split TF32) or on CUDA cores:
+    kernels, trailing updates on the tcgen05 tensor cores or with mma.sync
+    (both split TF32) or on CUDA cores:
     the refined solution meets the FP32 bar of the single-CTA kernels."""
     for k, v in WIDE_ENV.items():
         monkeypatch.setenv(k, v)
