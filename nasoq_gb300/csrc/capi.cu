@@ -165,6 +165,15 @@ static void build_schedule(Plan &P) {
   P.pair_flops.clear();
   P.tile_ptr.assign(ns + 1, 0);
   P.tiles.clear();
+  P.tile_ptr_tc.assign(ns + 1, 0);
+  P.tiles_tc.clear();
+  // FP32 plans: pairs whose descendant has at least UPD_TC_MIN_WD columns
+  // (NASOQ_GB300_UPDATE_TC_MIN overrides) take 128 x 128 tensor-core tiles;
+  // NASOQ_GB300_UPDATE=simt keeps them all on the CUDA-core kernel
+  const char *ue = std::getenv("NASOQ_GB300_UPDATE");
+  const bool tc = P.set.precision == NQG_FP32 && !(ue && std::string(ue) == "simt");
+  int tc_min_wd = UPD_TC_MIN_WD;
+  if (const char *e = std::getenv("NASOQ_GB300_UPDATE_TC_MIN")) tc_min_wd = std::max(1, std::atoi(e));
   for (int s = 0; s < ns; ++s) {
     ereach_sn(S, P.Uord, s, S.sparent, mark, stack, lst);
     const int c1 = S.super[s], c2 = S.super[s + 1];
@@ -182,12 +191,19 @@ static void build_schedule(Plan &P) {
         const double m = nr - lb, nc = ub - lb + 1, wd = S.super[d + 1] - S.super[d];
         P.pair_flops.push_back(2.0 * wd * (nc * m - nc * (nc - 1) / 2.0));
       }
-      for (int ri = lb; ri < nr; ri += UPD_TM)
-        for (int cj = lb; cj <= ub; cj += UPD_TN)
-          if (ri + UPD_TM - 1 >= cj) P.tiles.push_back(UpdTile{s, d, ri, cj, ub});
+      if (tc && S.super[d + 1] - S.super[d] >= tc_min_wd) {
+        for (int ri = lb; ri < nr; ri += UPD_TC_T)
+          for (int cj = lb; cj <= ub; cj += UPD_TC_T)
+            if (ri + UPD_TC_T - 1 >= cj) P.tiles_tc.push_back(UpdTile{s, d, ri, cj, ub});
+      } else {
+        for (int ri = lb; ri < nr; ri += UPD_TM)
+          for (int cj = lb; cj <= ub; cj += UPD_TN)
+            if (ri + UPD_TM - 1 >= cj) P.tiles.push_back(UpdTile{s, d, ri, cj, ub});
+      }
     }
     P.pair_ptr[s + 1] = (int)P.pair_d.size();
     P.tile_ptr[s + 1] = (int64_t)P.tiles.size();
+    P.tile_ptr_tc[s + 1] = (int64_t)P.tiles_tc.size();
   }
 }
 
@@ -274,6 +290,7 @@ static int upload_plan(Plan &P) {
   NQG_CUDA(cudaMemset(P.d_L, 0, (size_t)S.xsize * P.val_size()));
   NQG_CUDA(cudaMemset(P.d_D, 0, (size_t)std::max(2 * n, 2) * P.val_size()));
   if ((rc = dev_alloc_copy(P, &P.d_tiles, P.tiles.data(), P.tiles.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_tiles_tc, P.tiles_tc.data(), P.tiles_tc.size()))) return rc;
   std::vector<int> ps(P.pair_d.size());
   for (int s = 0; s < ns; ++s)
     for (int q = P.pair_ptr[s]; q < P.pair_ptr[s + 1]; ++q) ps[q] = s;
@@ -420,7 +437,8 @@ static void free_plan(Plan &P) {
                   P.d_pair_lb, P.d_pair_ub, P.d_targets_lv, P.d_pivoted, P.d_visible, P.d_hidden, P.d_status,
                   P.d_xo, P.d_bo, P.d_r, P.d_w, P.d_in, P.d_out, P.d_V, P.d_scal, P.d_wide_W, P.d_wide_ctl,
                   P.d_locinv, P.d_pair_roff, P.d_rr_dest, P.d_rr_moved, P.d_rr_items, P.d_rr_stage,
-                  P.d_solve_flags, P.d_blk_items, P.d_flagoff, P.d_xf, P.d_Z};
+                  P.d_solve_flags, P.d_blk_items, P.d_flagoff, P.d_xf, P.d_Z, P.d_tiles_tc,
+                  P.d_tile_list_tc};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   P.prof_collect();

@@ -23,6 +23,7 @@
 #include <cstdio>
 
 #include "plan.hpp"
+#include "tcgen05.cuh"
 
 namespace nqg {
 
@@ -472,6 +473,93 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(const UpdTile *tiles, co
   }
 }
 
+// FP32 Schur update tiles of 128 x 128 on the fifth-generation tensor cores
+// (descendants of UPD_TC_MIN_WD or more columns): the same (L_d D_d)[rows] *
+// L_d[cols]^T as k_update, with the D_d product applied while the rows of the
+// A operand are loaded, split-TF32 products accumulated in TMEM, and the
+// atomic scatter into the target from the TMEM rows (thread r owns row r).
+__global__ void __launch_bounds__(t5::THREADS) k_update_t5(const UpdTile *tiles, const int *tile_ids, int n,
+                                                           const int *super, const int64_t *lpi, const int64_t *lpx,
+                                                           const int *ls, float *L, const float *Dg, int *status) {
+  extern __shared__ __align__(1024) unsigned char t5_smem[];
+  __shared__ int prow[UPD_TC_T], pcol[UPD_TC_T];
+  const int tid = threadIdx.x;
+  const UpdTile tl = tiles[tile_ids[blockIdx.x]];
+  const int s = tl.s, d = tl.d;
+  const int c0 = super[d], wd = super[d + 1] - c0;
+  const int nrd = (int)(lpi[d + 1] - lpi[d]);
+  const int *rows_d = ls + lpi[d];
+  const float *Ld = L + lpx[d];
+  const int mrows = min(UPD_TC_T, nrd - tl.ri);
+  const int ncols = min(UPD_TC_T, tl.ub + 1 - tl.cj);
+  const int cs0 = super[s], ws = super[s + 1] - cs0;
+  const int nrs = (int)(lpi[s + 1] - lpi[s]);
+  const int *rows_s = ls + lpi[s];
+  float *Lt = L + lpx[s];
+  {
+    // target positions of row tid and column tid of the tile
+    int pos = -1;
+    if (tid < mrows) {
+      const int r = rows_d[tl.ri + tid];
+      if (r < cs0 + ws) pos = r - cs0;
+      else {
+        pos = ws + lower_bound_i(rows_s + ws, nrs - ws, r);
+        if (pos >= nrs || rows_s[pos] != r) {
+          flag_status(status, ST_BOUNDS);
+          pos = -1;
+        }
+      }
+    }
+    prow[tid] = pos;
+    pos = -1;
+    if (tid < ncols) {
+      pos = rows_d[tl.cj + tid] - cs0;
+      if (pos < 0 || pos >= ws) {
+        flag_status(status, ST_BOUNDS);
+        pos = -1;
+      }
+    }
+    pcol[tid] = pos;
+  }
+  __syncthreads();
+  const float *Dd = Dg + c0, *Ed = Dg + n + c0;
+  // row r of L_d D_d: column t is d_t L(:,t) + e_t L(:,t+1) + e_{t-1} L(:,t-1)
+  auto fa = [&](int r, int k0, float(&x)[t5::TK]) {
+    const bool ok = r < mrows;
+    const float *Lr = Ld + tl.ri + r;
+    float raw[t5::TK + 2];
+#pragma unroll
+    for (int q = 0; q < t5::TK + 2; ++q) {
+      const int t = k0 - 1 + q;
+      raw[q] = (ok && t >= 0 && t < wd) ? Lr[(size_t)t * nrd] : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < t5::TK; ++k) {
+      const int t = k0 + k;
+      const float dk = t < wd ? Dd[t] : 0.f, ek = t < wd ? Ed[t] : 0.f;
+      const float em = (t >= 1 && t - 1 < wd) ? Ed[t - 1] : 0.f;
+      x[k] = dk * raw[k + 1] + ek * raw[k + 2] + em * raw[k];
+    }
+  };
+  auto fb = [&](int c, int k0, float(&x)[t5::TK]) {
+    const bool ok = c < ncols;
+    const float *Lc = Ld + tl.cj + c;
+#pragma unroll
+    for (int k = 0; k < t5::TK; ++k) x[k] = (ok && k0 + k < wd) ? Lc[(size_t)(k0 + k) * nrd] : 0.f;
+  };
+  auto ep = [&](int r, int cb, const uint32_t(&v)[32]) {
+    if (r >= mrows || prow[r] < 0) return;
+    float *dst = Lt + prow[r];
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+      const int c = cb + q;
+      if (c < ncols && pcol[c] >= 0 && tl.ri + r >= tl.cj + c)
+        atomicAdd(dst + (size_t)pcol[c] * nrs, -__uint_as_float(v[q]));
+    }
+  };
+  t5::tile_tf32x3<1>(wd, fa, fb, ep, t5_smem, status);
+}
+
 // ---------------------------------------------------------------------------
 // Diagonal block BK + panel, one CTA per supernode.  SMALL: the block and a
 // row chunk of the panel are staged in shared memory.
@@ -747,8 +835,8 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
     }
   std::vector<int> order;      // targets grouped by level
   std::vector<int> lv_small_off, lv_small_cnt, lv_glob_off, lv_glob_cnt;
-  std::vector<int> tile_ids;
-  std::vector<int64_t> lv_tile_off, lv_tile_cnt;
+  std::vector<int> tile_ids, tile_ids_tc;
+  std::vector<int64_t> lv_tile_off, lv_tile_cnt, lv_tc_off, lv_tc_cnt;
   const int nlev = (int)P.levels.size();
   for (int l = 0; l < nlev; ++l) {
     int so = (int)order.size();
@@ -771,6 +859,12 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
         for (int64_t t = P.tile_ptr[s]; t < P.tile_ptr[s + 1]; ++t) tile_ids.push_back((int)t);
     lv_tile_off.push_back(to);
     lv_tile_cnt.push_back((int64_t)tile_ids.size() - to);
+    const int64_t tco = (int64_t)tile_ids_tc.size();
+    for (int s : P.levels[l])
+      if (mark[s])
+        for (int64_t t = P.tile_ptr_tc[s]; t < P.tile_ptr_tc[s + 1]; ++t) tile_ids_tc.push_back((int)t);
+    lv_tc_off.push_back(tco);
+    lv_tc_cnt.push_back((int64_t)tile_ids_tc.size() - tco);
   }
   bool any = false;
   for (int s = 0; s < ns && !any; ++s) any = mark[s] != 0;
@@ -790,6 +884,16 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
   if (!tile_ids.empty())
     NQG_CUDA(cudaMemcpyAsync(P.d_tile_list, tile_ids.data(), tile_ids.size() * sizeof(int), cudaMemcpyHostToDevice,
                              st));
+  if (tile_ids_tc.size() > P.tile_list_tc_cap) {
+    if (P.d_tile_list_tc) cudaFree(P.d_tile_list_tc);
+    P.tile_list_tc_cap = std::max<size_t>(tile_ids_tc.size(), 64);
+    NQG_CUDA(cudaMalloc(&P.d_tile_list_tc, P.tile_list_tc_cap * sizeof(int)));
+  }
+  if (!tile_ids_tc.empty())
+    NQG_CUDA(cudaMemcpyAsync(P.d_tile_list_tc, tile_ids_tc.data(), tile_ids_tc.size() * sizeof(int),
+                             cudaMemcpyHostToDevice, st));
+  if (!tile_ids_tc.empty())
+    NQG_CUDA(cudaFuncSetAttribute(k_update_t5, cudaFuncAttributeMaxDynamicSharedMemorySize, t5::smem_bytes(1)));
   uint8_t *d_mark = P.d_pivoted + ns;  // second half of the pivoted buffer holds the marks
   NQG_CUDA(cudaMemcpyAsync(d_mark, mark.data(), ns, cudaMemcpyHostToDevice, st));
   NQG_CUDA(cudaMemsetAsync(P.d_pivoted, 0, ns, st));
@@ -830,18 +934,28 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
     return w * r * r - r * w * (w - 1) + (w - 1) * w * (2 * w - 1) / 6.0;
   };
   for (int l = 0; l < nlev; ++l) {
-    if (lv_tile_cnt[l] > 0) {
+    if (lv_tile_cnt[l] + lv_tc_cnt[l] > 0) {
       double fl = 0;
       if (P.prof)
         for (int s : P.levels[l])
           if (mark[s])
             for (int q = P.pair_ptr[s]; q < P.pair_ptr[s + 1]; ++q) fl += P.pair_flops[q];
       cudaEvent_t e0 = P.prof_begin();
-      k_update<T><<<(unsigned)lv_tile_cnt[l], UPD_THREADS, 0, st>>>(P.d_tiles, P.d_tile_list + lv_tile_off[l],
-                                                                    (int)lv_tile_cnt[l], n, P.d_super, P.d_lpi,
-                                                                    P.d_lpx, P.d_ls, L, D, P.d_status);
+      if (lv_tile_cnt[l] > 0) {
+        k_update<T><<<(unsigned)lv_tile_cnt[l], UPD_THREADS, 0, st>>>(P.d_tiles, P.d_tile_list + lv_tile_off[l],
+                                                                      (int)lv_tile_cnt[l], n, P.d_super, P.d_lpi,
+                                                                      P.d_lpx, P.d_ls, L, D, P.d_status);
+        P.nlaunch++;
+      }
+      if constexpr (sizeof(T) == 4) {
+        if (lv_tc_cnt[l] > 0) {
+          k_update_t5<<<(unsigned)lv_tc_cnt[l], t5::THREADS, t5::smem_bytes(1), st>>>(
+              P.d_tiles_tc, P.d_tile_list_tc + lv_tc_off[l], n, P.d_super, P.d_lpi, P.d_lpx, P.d_ls, L, D,
+              P.d_status);
+          P.nlaunch++;
+        }
+      }
       P.prof_end(NQG_K_UPDATE, e0, fl, 0.0);
-      P.nlaunch++;
     }
     if (lv_small_cnt[l] + lv_glob_cnt[l] > 0) {
       double fl = 0;

@@ -41,6 +41,8 @@ constexpr int RR_BIG_STAGE_BYTES = 200 * 1024;  // longest row run staged in sha
 
 constexpr int UPD_TM = 64;
 constexpr int UPD_TN = 64;
+constexpr int UPD_TC_T = 128;       // tensor-core update tiles (FP32 plans)
+constexpr int UPD_TC_MIN_WD = 32;   // narrowest descendant whose pairs use them
 
 template <class T> struct DevBuf {
   T *p = nullptr;
@@ -63,6 +65,8 @@ struct Plan {
   std::vector<int> pair_d, pair_lb, pair_ub;
   std::vector<int64_t> tile_ptr;    // per supernode s: range of its update tiles
   std::vector<UpdTile> tiles;
+  std::vector<int64_t> tile_ptr_tc;  // per supernode s: range of its tensor-core update tiles
+  std::vector<UpdTile> tiles_tc;
   std::vector<int> wide;            // supernodes factored by the blocked kernel
   int64_t ssize = 0;
 
@@ -79,6 +83,9 @@ struct Plan {
   void *d_L = nullptr;              // factor values (double or float)
   void *d_D = nullptr;              // 2n: diagonal then 2x2 sub-diagonal
   UpdTile *d_tiles = nullptr;
+  UpdTile *d_tiles_tc = nullptr;
+  int *d_tile_list_tc = nullptr;    // tensor-core tile ids of the current factorization
+  size_t tile_list_tc_cap = 0;
   int *d_tile_list = nullptr;       // tile ids for a partial refactor
   size_t tile_list_cap = 0;
   int *d_targets = nullptr;         // supernode ids for per-level kernels

@@ -137,8 +137,9 @@ __device__ __forceinline__ void store_row_split(unsigned char *hi_tile, unsigned
 }
 
 // acc(128 x 128) = A(128 x kdim) * B(128 x kdim)^T with split-TF32 products,
-// by a CTA of THREADS threads.  fa(r, k) / fb(n, k) return the FP32 operand
-// entries (0 outside the operands), called with r, n = threadIdx.x.  The
+// by a CTA of THREADS threads.  Row loaders fa(r, k0, x) / fb(n, k0, x) fill
+// x[0..TK) with entries k0 .. k0+TK-1 of operand row r / n (0 outside the
+// operands), called with r, n = threadIdx.x.  The
 // epilogue ep(r, c0, v) receives, for row r = threadIdx.x, the 32 product
 // values of columns [c0, c0 + 32).  smem_raw: smem_bytes(NSTAGE) of dynamic
 // shared memory (NSTAGE operand stages of 64 KB: with one stage three CTAs fit
@@ -181,11 +182,8 @@ __device__ bool tile_tf32x3(int kdim, FA fa, FB fb, EP ep, unsigned char *smem_r
     }
     const int k0 = ch * TK;
     float xa[TK], xb[TK];
-#pragma unroll
-    for (int k = 0; k < TK; ++k) {
-      xa[k] = (k0 + k < kdim) ? fa(tid, k0 + k) : 0.f;
-      xb[k] = (k0 + k < kdim) ? fb(tid, k0 + k) : 0.f;
-    }
+    fa(tid, k0, xa);
+    fb(tid, k0, xb);
     store_row_split(stg, stg + OPND_BYTES, tid, xa);
     store_row_split(stg + 2 * OPND_BYTES, stg + 3 * OPND_BYTES, tid, xb);
     fence_proxy_async();

@@ -508,13 +508,16 @@ __global__ void __launch_bounds__(t5::THREADS) k_wide_trailing_t5(float *S, int 
   const int row0 = k1 + tm * t5::TM;
   if (row0 + t5::TM - 1 < col0) return;  // tile strictly above the diagonal
   const float *L21 = S + (size_t)k0 * nrow;
-  auto fa = [&](int r, int k) {
+  auto fa = [&](int r, int k0c, float(&x)[t5::TK]) {
     const int gr = row0 + r;
-    return gr < nrow ? L21[gr + (size_t)k * nrow] : 0.f;
+#pragma unroll
+    for (int k = 0; k < t5::TK; ++k)
+      x[k] = (gr < nrow && k0c + k < kb) ? L21[gr + (size_t)(k0c + k) * nrow] : 0.f;
   };
-  auto fb = [&](int n, int k) {
+  auto fb = [&](int n, int k0c, float(&x)[t5::TK]) {
     const int gc = col0 + n;
-    return gc < w ? Wb[(size_t)k * ldw + gc] : 0.f;
+#pragma unroll
+    for (int k = 0; k < t5::TK; ++k) x[k] = (gc < w && k0c + k < kb) ? Wb[(size_t)(k0c + k) * ldw + gc] : 0.f;
   };
   auto ep = [&](int r, int c0, const uint32_t(&v)[32]) {
     const int gr = row0 + r;

@@ -233,3 +233,28 @@ def test_fp32_blocked_wide_kernels(path, trailing, monkeypatch):
     assert relres(d, x) <= 1e-10
     xr = d["out_x"]
     assert np.linalg.norm(x - xr) <= 1e-6 * np.linalg.norm(xr)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("update", ["tcgen05", "simt"])
+@pytest.mark.parametrize("path", CASES, ids=os.path.basename)
+def test_fp32_update_kernels(path, update, monkeypatch):
+    """FP32 factor with every Schur update between supernodes on the tcgen05
+    tiles (any descendant width) or every one on the CUDA-core tiles: the
+    refined solution meets the FP32 bar."""
+    if update == "tcgen05":
+        monkeypatch.setenv("NASOQ_GB300_UPDATE_TC_MIN", "1")
+    else:
+        monkeypatch.setenv("NASOQ_GB300_UPDATE", "simt")
+    d = nqa.load(path)
+    n = len(d["in_rhs"])
+    if cond_of(path, d) > 1e8:
+        pytest.skip("kappa * u_fp32 >= 1: FP64 factorization territory")
+    plan = nq.Plan(n, d["in_Ap"], d["in_Ai"], d["in_Ax"],
+                   settings=_settings(d, precision=nq.NQG_FP32, req_ref_iter=6, max_inner_iter=6,
+                                      tol_abs=1e-13, tol_rel=1e-13))
+    assert plan.factor() == 0
+    x = plan.solve(d["in_rhs"])
+    assert relres(d, x) <= 1e-10
+    xr = d["out_x"]
+    assert np.linalg.norm(x - xr) <= 1e-6 * np.linalg.norm(xr)
