@@ -345,6 +345,10 @@ static int upload_plan(Plan &P) {
   // a supernode, and their panel width
   if (const char *e = std::getenv("NASOQ_GB300_WIDE_MIN")) P.wide_min = std::max(1, std::atoi(e));
   if (const char *e = std::getenv("NASOQ_GB300_WIDE_NB")) P.wide_nb = std::min(64, std::max(4, std::atoi(e)));
+  // supernodes of at most this width take the shared-memory BK kernel (<= 64)
+  if (const char *e = std::getenv("NASOQ_GB300_BK_SMALL")) P.bk_small = std::min(64, std::max(1, std::atoi(e)));
+  // =serial: the rows below the k_bk_global blocks are solved in that kernel
+  if (const char *e = std::getenv("NASOQ_GB300_PANEL_ROWS")) P.panel_rows_serial = std::string(e) == "serial";
   // solve work split per level: small supernodes take one CTA each in the
   // level kernels; the others are cut into 64-row blocks for the
   // flag-driven block kernels (forward items: diagonal block rows, then row
@@ -438,7 +442,7 @@ static void free_plan(Plan &P) {
                   P.d_xo, P.d_bo, P.d_r, P.d_w, P.d_in, P.d_out, P.d_V, P.d_scal, P.d_wide_W, P.d_wide_ctl,
                   P.d_locinv, P.d_pair_roff, P.d_rr_dest, P.d_rr_moved, P.d_rr_items, P.d_rr_stage,
                   P.d_solve_flags, P.d_blk_items, P.d_flagoff, P.d_xf, P.d_Z, P.d_tiles_tc,
-                  P.d_tile_list_tc};
+                  P.d_tile_list_tc, P.d_row_items};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   P.prof_collect();

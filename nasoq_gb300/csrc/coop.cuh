@@ -18,9 +18,9 @@ struct WideCtl {
   int cidx[2][1024];
   double rval[2][1024];
   int ridx[2][1024];
-  // FP32 panels: per column step, the packed (|value| bits, ~index) maximum
-  // of the column (row 0) and pivot-row (row 1) searches; cleared per panel
-  unsigned long long amax[2][72];
+  // panel exchanges: per CTA and parity, (candidate << 8) | epoch; cleared
+  // before every panel launch
+  unsigned long long pslot[2][1024];
 };
 
 constexpr long long SPIN_LIMIT = 1ll << 26;  // polls before a barrier gives up

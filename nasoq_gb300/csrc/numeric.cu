@@ -605,7 +605,7 @@ __global__ void __launch_bounds__(BK_THREADS) k_bk_small(const int *targets, int
 template <class T>
 __global__ void __launch_bounds__(256) k_bk_global(const int *targets, int n, const int *super, const int64_t *lpi,
                                                    const int64_t *lpx, T *L, T *Dg, int *locperm, uint8_t *pivoted,
-                                                   int *cycle_buf, int *status) {
+                                                   int *cycle_buf, int do_rows, int *status) {
   const int s = targets[blockIdx.x];
   const int c0 = super[s], w = super[s + 1] - c0;
   const int nrow = (int)(lpi[s + 1] - lpi[s]);
@@ -623,7 +623,7 @@ __global__ void __launch_bounds__(256) k_bk_global(const int *targets, int n, co
   const T *D = Dg + c0, *E = Dg + n + c0;
   // cycle leaders of the column permutation new[j] = old[perm[j]]
   int *lead = cycle_buf + c0;  // n-sized scratch, this supernode's slice
-  if (piv) {
+  if (piv && do_rows) {
     for (int j = threadIdx.x; j < w; j += blockDim.x) {
       // j leads its cycle if it is the smallest index on it
       int q = perm[j], isl = 1;
@@ -639,7 +639,7 @@ __global__ void __launch_bounds__(256) k_bk_global(const int *targets, int n, co
     }
   }
   __syncthreads();
-  for (int r = w + threadIdx.x; r < nrow; r += blockDim.x) {
+  for (int r = w + threadIdx.x; do_rows && r < nrow; r += blockDim.x) {
     T *row = Ls + r;  // element j at row[j*nrow]
     if (piv) {
       for (int j = 0; j < w; ++j) {
@@ -682,6 +682,106 @@ __global__ void __launch_bounds__(256) k_bk_global(const int *targets, int n, co
   for (int m = threadIdx.x; m < w; m += blockDim.x)
     if (!isfinite((double)D[m])) bad = true;
   if (block_any(bad) && threadIdx.x == 0) flag_status(status, ST_NONFINITE);
+}
+
+// ---------------------------------------------------------------------------
+// Rows below the diagonal block of a supernode factored by k_bk_global:
+// L21 = (A21 P^T) L11^-T D^-1 (dlapmt + dtrsm + blocked_2by2_solver,
+// src/ldl/Serial_blocked_ldl_02_2.cpp:137-161), spread over (supernode,
+// 64-row block) items.  The CTA stages its rows with the pivot column order
+// applied, then works through L11 in panels of PR_KB columns staged in shared
+// memory: each panel's triangle is solved one row per thread, and its
+// contribution is subtracted from the later columns.  Every entry receives
+// the terms x_t L(j, t) in increasing t, as in the per-row substitution.
+constexpr int PR_ROWS = 64, PR_KB = 32, PR_CG = 4;  // rows per item, panel width, columns per thread
+
+__host__ __device__ constexpr size_t panel_rows_smem(int wmax, int vsize) {
+  return ((size_t)PR_ROWS * (wmax + 1) + (size_t)wmax * (PR_KB + 1)) * vsize;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_panel_rows(const int2 *items, int n, const int *super, const int64_t *lpi,
+                                                    const int64_t *lpx, T *L, const T *Dg, const int *locperm,
+                                                    const uint8_t *pivoted) {
+  extern __shared__ __align__(16) unsigned char pr_raw[];
+  const int s = items[blockIdx.x].x, rb = items[blockIdx.x].y;
+  const int c0 = super[s], w = super[s + 1] - c0;
+  const int nrow = (int)(lpi[s + 1] - lpi[s]);
+  T *Ls = L + lpx[s];
+  const int *perm = locperm + c0;
+  const bool piv = pivoted[s] != 0;
+  const int r0 = w + rb * PR_ROWS, m = min(PR_ROWS, nrow - r0);
+  if (m <= 0) return;
+  const int ldx = w + 1;
+  T *X = reinterpret_cast<T *>(pr_raw);  // [PR_ROWS][ldx]
+  T *Lp = X + (size_t)PR_ROWS * ldx;     // [w][PR_KB + 1]: columns jb .. jb+kb of L11, rows jb .. w
+  const int tid = threadIdx.x;
+  for (int e = tid; e < m * w; e += blockDim.x) {
+    const int r = e % m, j = e / m;
+    X[r * ldx + j] = Ls[(r0 + r) + (size_t)(piv ? perm[j] : j) * nrow];
+  }
+  for (int jb = 0; jb < w; jb += PR_KB) {
+    const int kb = min(PR_KB, w - jb);
+    __syncthreads();
+    for (int e = tid; e < (w - jb) * kb; e += blockDim.x) {
+      const int i = e % (w - jb), jj = e / (w - jb);
+      Lp[i * (PR_KB + 1) + jj] = Ls[(jb + i) + (size_t)(jb + jj) * nrow];
+    }
+    __syncthreads();
+    // triangle of the panel: row r, columns jb .. jb+kb
+    if (tid < m) {
+      T *xr = X + tid * ldx;
+      for (int j = 0; j < kb; ++j) {
+        T x = xr[jb + j];
+        for (int t = 0; t < j; ++t) x -= xr[jb + t] * Lp[j * (PR_KB + 1) + t];
+        xr[jb + j] = x;
+      }
+    }
+    __syncthreads();
+    // later columns c >= jb+kb: x(r, c) -= sum_t x(r, jb+t) L(c, jb+t), t increasing
+    const int c_lo = jb + kb, ncg = (w - c_lo + PR_CG - 1) / PR_CG;
+    for (int e = tid; e < m * ncg; e += blockDim.x) {
+      const int r = e % m, cg0 = c_lo + (e / m) * PR_CG;
+      T *xr = X + r * ldx;
+      T acc[PR_CG];
+#pragma unroll
+      for (int q = 0; q < PR_CG; ++q) acc[q] = cg0 + q < w ? xr[cg0 + q] : T(0);
+      for (int t = 0; t < kb; ++t) {
+        const T xt = xr[jb + t];
+#pragma unroll
+        for (int q = 0; q < PR_CG; ++q)
+          if (cg0 + q < w) acc[q] -= xt * Lp[(cg0 + q - jb) * (PR_KB + 1) + t];
+      }
+#pragma unroll
+      for (int q = 0; q < PR_CG; ++q)
+        if (cg0 + q < w) xr[cg0 + q] = acc[q];
+    }
+  }
+  __syncthreads();
+  // D^-1 (1x1 and 2x2 blocks, Cramer's rule) and write back
+  const T *D = Dg + c0, *E = Dg + n + c0;
+  if (tid < m) {
+    T *xr = X + tid * ldx;
+    for (int j = 0; j < w; ++j) {
+      if (E[j] == T(0)) {
+        T inv = T(1) / D[j];
+        xr[j] *= inv;
+      } else {
+        T sd = E[j];
+        T det = D[j] * D[j + 1] - sd * sd;
+        T inv = T(1) / det;
+        T x1 = xr[j], x2 = xr[j + 1];
+        xr[j] = (x1 * D[j + 1] - x2 * sd) * inv;
+        xr[j + 1] = (x2 * D[j] - x1 * sd) * inv;
+        ++j;
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < m * w; e += blockDim.x) {
+    const int r = e % m, j = e / m;
+    Ls[(r0 + r) + (size_t)j * nrow] = X[r * ldx + j];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -835,6 +935,7 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
     }
   std::vector<int> order;      // targets grouped by level
   std::vector<int> lv_small_off, lv_small_cnt, lv_glob_off, lv_glob_cnt;
+  std::vector<int> row_items, lv_row_off, lv_row_cnt;  // (supernode, row block) items of k_panel_rows
   std::vector<int> tile_ids, tile_ids_tc;
   std::vector<int64_t> lv_tile_off, lv_tile_cnt, lv_tc_off, lv_tc_cnt;
   const int nlev = (int)P.levels.size();
@@ -842,17 +943,28 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
     int so = (int)order.size();
     for (int s : P.levels[l]) {
       const int w = P.sym.super[s + 1] - P.sym.super[s];
-      if (mark[s] && w <= BK_SMALL && w <= P.wide_min) order.push_back(s);
+      if (mark[s] && w <= P.bk_small && w <= P.wide_min) order.push_back(s);
     }
     int go = (int)order.size();
     for (int s : P.levels[l]) {
       const int w = P.sym.super[s + 1] - P.sym.super[s];
-      if (mark[s] && w > BK_SMALL && w <= P.wide_min) order.push_back(s);
+      if (mark[s] && w > P.bk_small && w <= P.wide_min) order.push_back(s);
     }
     lv_small_off.push_back(so);
     lv_small_cnt.push_back(go - so);
     lv_glob_off.push_back(go);
     lv_glob_cnt.push_back((int)order.size() - go);
+    lv_row_off.push_back((int)row_items.size() / 2);
+    for (int q = go; q < (int)order.size(); ++q) {
+      const int s = order[q];
+      const int w = P.sym.super[s + 1] - P.sym.super[s];
+      const int nb_rows = (int)(P.sym.lpi[s + 1] - P.sym.lpi[s]) - w;
+      for (int rb = 0; rb * PR_ROWS < nb_rows; ++rb) {
+        row_items.push_back(s);
+        row_items.push_back(rb);
+      }
+    }
+    lv_row_cnt.push_back((int)row_items.size() / 2 - lv_row_off.back());
     int64_t to = (int64_t)tile_ids.size();
     for (int s : P.levels[l])
       if (mark[s])
@@ -878,6 +990,24 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
     if (P.d_tile_list) cudaFree(P.d_tile_list);
     P.tile_list_cap = std::max<size_t>(tile_ids.size(), 64);
     NQG_CUDA(cudaMalloc(&P.d_tile_list, P.tile_list_cap * sizeof(int)));
+  }
+  // rows below the diagonal blocks of the k_bk_global supernodes: multi-CTA
+  // kernel when its shared-memory staging fits, else inside k_bk_global
+  int wmax_glob = 0;
+  for (int q = 0; q < (int)lv_glob_off.size(); ++q)
+    for (int k = lv_glob_off[q]; k < lv_glob_off[q] + lv_glob_cnt[q]; ++k)
+      wmax_glob = std::max(wmax_glob, P.sym.super[order[k] + 1] - P.sym.super[order[k]]);
+  const size_t pr_smem = panel_rows_smem(std::max(wmax_glob, 1), (int)sizeof(T));
+  const bool rows_split = pr_smem <= 227 * 1024 && !P.panel_rows_serial;
+  if (rows_split && !row_items.empty()) {
+    if (row_items.size() > P.row_items_cap) {
+      if (P.d_row_items) cudaFree(P.d_row_items);
+      P.row_items_cap = std::max<size_t>(row_items.size(), 128);
+      NQG_CUDA(cudaMalloc(&P.d_row_items, P.row_items_cap * sizeof(int)));
+    }
+    NQG_CUDA(cudaMemcpyAsync(P.d_row_items, row_items.data(), row_items.size() * sizeof(int), cudaMemcpyHostToDevice,
+                             st));
+    NQG_CUDA(cudaFuncSetAttribute(k_panel_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pr_smem));
   }
   if (!order.empty())
     NQG_CUDA(cudaMemcpyAsync(P.d_targets, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -970,8 +1100,15 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
       }
       if (lv_glob_cnt[l] > 0) {
         k_bk_global<T><<<lv_glob_cnt[l], 256, 0, st>>>(P.d_targets + lv_glob_off[l], n, P.d_super, P.d_lpi, P.d_lpx,
-                                                        L, D, P.d_locperm, P.d_pivoted, P.d_perm_tmp, P.d_status);
+                                                        L, D, P.d_locperm, P.d_pivoted, P.d_perm_tmp,
+                                                        rows_split ? 0 : 1, P.d_status);
         P.nlaunch++;
+        if (rows_split && lv_row_cnt[l] > 0) {
+          k_panel_rows<T><<<lv_row_cnt[l], 256, pr_smem, st>>>(
+              reinterpret_cast<const int2 *>(P.d_row_items) + lv_row_off[l], n, P.d_super, P.d_lpi, P.d_lpx, L, D,
+              P.d_locperm, P.d_pivoted);
+          P.nlaunch++;
+        }
       }
       P.prof_end(NQG_K_BK, e0, fl, 0.0);
     }

@@ -90,6 +90,8 @@ struct Plan {
   size_t tile_list_cap = 0;
   int *d_targets = nullptr;         // supernode ids for per-level kernels
   size_t targets_cap = 0;
+  int *d_row_items = nullptr;       // (supernode, row block) pairs of the panel row solves
+  size_t row_items_cap = 0;
   int *d_pair_s = nullptr, *d_pair_d = nullptr, *d_pair_lb = nullptr, *d_pair_ub = nullptr;
   // row renaming after pivoting: per-pair row offsets, new positions, moved
   // flags, value-movement items (shared-memory staged, then long rows)
@@ -132,6 +134,8 @@ struct Plan {
   unsigned solve_epoch = 0;
   int wide_nb = 64;
   int wide_min = 256;               // supernodes wider than this use the blocked kernels
+  int bk_small = 64;                // supernodes up to this width: shared-memory BK kernel
+  bool panel_rows_serial = false;   // rows below k_bk_global blocks solved inside that kernel
   int num_sms = 0;
 
   // measurement: launch counter and per-class event timing

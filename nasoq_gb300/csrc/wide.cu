@@ -84,8 +84,8 @@ template <class T> __device__ void reduce_partials(const double *pv, const int *
     double bv = -1.0;
     int bi = -1;
     for (int g = threadIdx.x; g < G; g += 32) {
-      double x = pv[g];
-      int xi = pi[g];
+      double x = __ldcg(pv + g);
+      int xi = __ldcg(pi + g);
       if (xi >= 0 && (bi < 0 || x > bv || (x == bv && xi < bi))) {
         bv = x;
         bi = xi;
@@ -111,40 +111,98 @@ template <class T> __device__ void reduce_partials(const double *pv, const int *
   __syncthreads();
 }
 
-// Packed key of a pivot candidate for the FP32 argmax: |value| bits above
-// (monotone for non-negative floats), the complemented row index below, so
-// atomicMax keeps the largest value and, among equal values, the smallest row.
-__device__ __forceinline__ unsigned long long pack_cand(float a, int i) {
-  return ((unsigned long long)__float_as_uint(a) << 32) | (unsigned)(0x7fffffff - i);
+// Panel exchange: every CTA publishes one 64-bit word per synchronisation,
+// (candidate << 8) | epoch, into its own slot of the current parity; one warp
+// of every CTA then polls all slots until each carries this epoch and takes
+// their maximum.  This is the grid barrier and the pivot search in one step,
+// without atomics.  The slot is written after __syncthreads + __threadfence
+// (the CTA's earlier writes are ordered before it) and read back before a
+// __threadfence (later reads see the other CTAs' writes); data written by
+// other CTAs is read with ld.cg.  Two parities let a fast CTA publish the
+// next exchange while a slow one still reads this one.  The wait is bounded.
+__device__ bool grid_exchange(WideCtl *ctl, unsigned &epoch, unsigned long long cand, int *status,
+                              unsigned long long &best) {
+  __shared__ unsigned long long s_best;
+  __shared__ int s_ok;
+  ++epoch;
+  const unsigned e = epoch & 0xFFu;  // at most 255 exchanges per panel launch: never 0
+  const int par = epoch & 1;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    *(volatile unsigned long long *)&ctl->pslot[par][blockIdx.x] = (cand << 8) | e;
+  }
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    long long it = 0;
+    int ok = 1;
+    unsigned long long m = 0;
+    while (true) {
+      bool all = true;
+      m = 0;
+      for (int g = lane; g < (int)gridDim.x; g += 32) {
+        const unsigned long long v = *(volatile unsigned long long *)&ctl->pslot[par][g];
+        if ((unsigned)(v & 0xFFu) != e) all = false;
+        else m = max(m, v >> 8);
+      }
+      if (__all_sync(0xffffffffu, all)) break;
+      int ab = lane == 0 ? *(volatile int *)&ctl->abort : 0;
+      ab = __shfl_sync(0xffffffffu, ab, 0);
+      if (ab) {
+        ok = 0;
+        break;
+      }
+      if (++it > SPIN_LIMIT) {
+        if (lane == 0) {
+          atomicOr(status, ST_TIMEOUT);
+          atomicExch(&ctl->abort, 1);
+        }
+        ok = 0;
+        break;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __threadfence();
+    if (lane == 0) {
+      s_best = m;
+      s_ok = ok;
+    }
+  }
+  __syncthreads();
+  best = s_best;
+  return s_ok != 0;
 }
 
-// Column-step argmax over the whole grid: the CTA's candidate (valid in
-// thread 0 after cta_argmax) is combined with the other CTAs', then one grid
-// barrier; every CTA returns the same (value, index).  FP32: one atomicMax on
-// a packed key per CTA; FP64: per-CTA partials reduced redundantly by all.
+// Column-step argmax over the whole grid (valid on return in every thread,
+// the same in every CTA).  FP32: the candidate rides in the exchange word as
+// (|value| bits << 24) | (0xFFFFFF - row), 0 for none, so the maximum keeps
+// the largest value and, among equal values, the smallest row (rows < 2^24).
+// FP64: per-CTA partials beside the exchange, reduced redundantly by all.
 template <class T>
-__device__ bool grid_argmax(T cv, int ci, WideCtl *ctl, int phase, int step, int parity, int *status, T &v,
-                            int &idx) {
+__device__ bool grid_argmax(T cv, int ci, WideCtl *ctl, int phase, unsigned &epoch, int *status, T &v, int &idx) {
   cta_argmax(cv, ci);
+  unsigned long long best = 0;
   if constexpr (sizeof(T) == 4) {
-    if (threadIdx.x == 0 && ci >= 0) atomicMax(&ctl->amax[phase][step], pack_cand((float)cv, ci));
-    if (!grid_sync(ctl, status)) return false;
-    const unsigned long long key = *(volatile unsigned long long *)&ctl->amax[phase][step];
-    if (key == 0ull) {
+    unsigned long long cand = 0;
+    if (ci >= 0) cand = ((unsigned long long)__float_as_uint((float)cv) << 24) | (0xFFFFFFull - (unsigned)ci);
+    if (!grid_exchange(ctl, epoch, cand, status, best)) return false;
+    if (best == 0ull) {
       v = T(0);
       idx = -1;
     } else {
-      v = (T)__uint_as_float((unsigned)(key >> 32));
-      idx = 0x7fffffff - (int)(unsigned)(key & 0xffffffffull);
+      v = (T)__uint_as_float((unsigned)(best >> 24));
+      idx = 0xFFFFFF - (int)(best & 0xFFFFFFull);
     }
   } else {
-    double *pv = phase ? ctl->rval[parity] : ctl->cval[parity];
-    int *pi = phase ? ctl->ridx[parity] : ctl->cidx[parity];
+    const int par = (epoch + 1) & 1;  // parity of the coming exchange
+    double *pv = phase ? ctl->rval[par] : ctl->cval[par];
+    int *pi = phase ? ctl->ridx[par] : ctl->cidx[par];
     if (threadIdx.x == 0) {
       pv[blockIdx.x] = (double)cv;
       pi[blockIdx.x] = ci;
     }
-    if (!grid_sync(ctl, status)) return false;
+    if (!grid_exchange(ctl, epoch, 0ull, status, best)) return false;
     reduce_partials(pv, pi, gridDim.x, v, idx);
   }
   return true;
@@ -153,41 +211,43 @@ __device__ bool grid_argmax(T cv, int ci, WideCtl *ctl, int phase, int step, int
 // One panel: columns c = k0 .. (at most k0+nb, one more for a final 2x2).
 // Thread gt owns rows gt, gt + TT, ...; the panel entries L(gt, k0 + t) of
 // its first row are cached in shared memory (lc[t][threadIdx.x]) as they are
-// produced, so the column updates of later steps read no global memory for
-// that row.  An interchange rewrites rows kk and kp of the finished columns;
-// their owners reload the cache after the barrier that ends it.
+// produced, and its W entries stay in registers, so the column updates read
+// no global memory for that row.  After each column's exchange one round of
+// loads brings the pivot W(c, j), the next column's own entry S(gt, c+1) and
+// the row W(c+1, 0..j) of the next update; a pivot search or an interchange
+// (rare once the pivot order has settled) reloads what it changed.
 template <class T>
 __global__ void __launch_bounds__(WP_THREADS) k_wide_panel(T *S, int nrow, int w, int k0, int nb, T *Wb, int ldw,
                                                            T *Dd, T *De, int *perm, WideCtl *ctl, int *status) {
   extern __shared__ __align__(16) unsigned char wp_raw[];
   T *lc = reinterpret_cast<T *>(wp_raw);  // [WP_NB + 2][WP_THREADS]
-  __shared__ T wrow[128];
+  __shared__ T wbuf[2][WP_NB + 2];        // W(c, 0..j-1) of the current column, and of the next
+  __shared__ T wrB[WP_NB + 2];            // W(imax, 0..j-1) of a pivot-row update
   const T alpha = (T)((1.0 + sqrt(17.0)) / 8.0);
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int TT = gridDim.x * blockDim.x;
   const int tid = threadIdx.x;
   auto first_row = [&](int lo) { return lo + (int)(((long long)gt - lo % TT + TT) % TT); };
-  // L(r, k0 + t) for t < j: cached for the thread's first row, else global
-  auto lrow_dot = [&](int r, int j) {
-    T acc = T(0);
-    if (r == gt) {
-      for (int t = 0; t < j; ++t) acc += lc[t * WP_THREADS + tid] * wrow[t];
-    } else {
-      for (int t = 0; t < j; ++t) acc += S[r + (size_t)(k0 + t) * nrow] * wrow[t];
-    }
-    return acc;
-  };
+  unsigned epoch = 0;
+  int cur = 0;  // wbuf[cur] holds W(c, 0..j-1)
+  T s_own = (gt >= k0 && gt < nrow && k0 < w) ? __ldcg(S + gt + (size_t)k0 * nrow) : T(0);
   int j = 0;
-  int parity = 0;
   while (j < nb && k0 + j < w) {
     const int c = k0 + j;
+    const T *wrow = wbuf[cur];
     // ---- A: updated column c into W(:, j), rows [c, nrow)
-    for (int t = tid; t < j; t += blockDim.x) wrow[t] = Wb[(size_t)t * ldw + c];
-    __syncthreads();
-    T cv = T(-1);
+    T cv = T(-1), w_own = T(0);
     int ci = -1;
     for (int r = first_row(c); r < nrow; r += TT) {
-      const T acc = S[r + (size_t)c * nrow] - lrow_dot(r, j);
+      T acc;
+      if (r == gt) {
+        acc = s_own;
+        for (int t = 0; t < j; ++t) acc -= lc[t * WP_THREADS + tid] * wrow[t];
+        w_own = acc;
+      } else {
+        acc = __ldcg(S + r + (size_t)c * nrow);
+        for (int t = 0; t < j; ++t) acc -= __ldcg(S + r + (size_t)(k0 + t) * nrow) * wrow[t];
+      }
       Wb[(size_t)j * ldw + r] = acc;
       if (r > c && r < w) {
         const T a = tabs_w(acc);
@@ -199,22 +259,34 @@ __global__ void __launch_bounds__(WP_THREADS) k_wide_panel(T *S, int nrow, int w
     }
     T colmax;
     int imax;
-    if (!grid_argmax(cv, ci, ctl, 0, j, parity, status, colmax, imax)) return;
+    if (!grid_argmax(cv, ci, ctl, 0, epoch, status, colmax, imax)) return;
     if (imax < 0) colmax = T(0);
-    const T absakk = tabs_w(Wb[(size_t)j * ldw + c]);
+    // one round of loads: pivot, and the next column's inputs on the fast path
+    const T wcc = __ldcg(Wb + (size_t)j * ldw + c);
+    T *wnext = wbuf[cur ^ 1];
+    if (tid <= j && c + 1 < nrow) wnext[tid] = __ldcg(Wb + (size_t)tid * ldw + c + 1);
+    const T s_next = (gt >= c + 1 && gt < nrow && c + 1 < w) ? __ldcg(S + gt + (size_t)(c + 1) * nrow) : T(0);
+    const T absakk = tabs_w(wcc);
     int kp = c, kstep = 1;
-    bool zero = false;
+    bool zero = false, slow = false;
+    T w_own1 = T(0);
     if ((absakk >= colmax ? absakk : colmax) == T(0) || absakk != absakk) {
       zero = true;
     } else if (absakk < alpha * colmax) {
+      slow = true;
       // ---- B: updated column imax into W(:, j+1) and its off-diagonal max
-      for (int t = tid; t < j; t += blockDim.x) wrow[t] = Wb[(size_t)t * ldw + imax];
+      for (int t = tid; t < j; t += blockDim.x) wrB[t] = __ldcg(Wb + (size_t)t * ldw + imax);
       __syncthreads();
       T rv = T(-1);
       int ri = -1;
       for (int r = first_row(c); r < nrow; r += TT) {
-        const T a0 = r < imax ? S[imax + (size_t)r * nrow] : S[r + (size_t)imax * nrow];
-        const T acc = a0 - lrow_dot(r, j);
+        T acc = r < imax ? __ldcg(S + imax + (size_t)r * nrow) : __ldcg(S + r + (size_t)imax * nrow);
+        if (r == gt) {
+          for (int t = 0; t < j; ++t) acc -= lc[t * WP_THREADS + tid] * wrB[t];
+          w_own1 = acc;
+        } else {
+          for (int t = 0; t < j; ++t) acc -= __ldcg(S + r + (size_t)(k0 + t) * nrow) * wrB[t];
+        }
         Wb[(size_t)(j + 1) * ldw + r] = acc;
         if (r < w && r != imax) {
           const T a = tabs_w(acc);
@@ -226,8 +298,8 @@ __global__ void __launch_bounds__(WP_THREADS) k_wide_panel(T *S, int nrow, int w
       }
       T rowmax;
       int rdummy;
-      if (!grid_argmax(rv, ri, ctl, 1, j, parity, status, rowmax, rdummy)) return;
-      const T diag_imax = tabs_w(Wb[(size_t)(j + 1) * ldw + imax]);
+      if (!grid_argmax(rv, ri, ctl, 1, epoch, status, rowmax, rdummy)) return;
+      const T diag_imax = tabs_w(__ldcg(Wb + (size_t)(j + 1) * ldw + imax));
       if (absakk >= alpha * colmax * (colmax / rowmax)) {
         kp = c;
       } else if (diag_imax >= alpha * rowmax) {
@@ -242,84 +314,87 @@ __global__ void __launch_bounds__(WP_THREADS) k_wide_panel(T *S, int nrow, int w
     if (kp != kk) {
       const bool copycol = (kstep == 1);  // working column becomes the updated column kp
       for (int r = first_row(c); r < nrow; r += TT) {
-        if (copycol && r != kk && r != kp) Wb[(size_t)j * ldw + r] = Wb[(size_t)(j + 1) * ldw + r];
+        if (copycol && r != kk && r != kp) {
+          const T v1 = __ldcg(Wb + (size_t)(j + 1) * ldw + r);
+          Wb[(size_t)j * ldw + r] = v1;
+        }
         if (r > kp) {
-          T t = S[r + (size_t)kk * nrow];
-          S[r + (size_t)kk * nrow] = S[r + (size_t)kp * nrow];
+          T t = __ldcg(S + r + (size_t)kk * nrow);
+          S[r + (size_t)kk * nrow] = __ldcg(S + r + (size_t)kp * nrow);
           S[r + (size_t)kp * nrow] = t;
         } else if (r > kk && r < kp) {
-          T t = S[r + (size_t)kk * nrow];
-          S[r + (size_t)kk * nrow] = S[kp + (size_t)r * nrow];
+          T t = __ldcg(S + r + (size_t)kk * nrow);
+          S[r + (size_t)kk * nrow] = __ldcg(S + kp + (size_t)r * nrow);
           S[kp + (size_t)r * nrow] = t;
         }
       }
       for (int col = gt; col < kk; col += TT) {  // rows kk, kp of all finished columns
-        T t = S[kk + (size_t)col * nrow];
-        S[kk + (size_t)col * nrow] = S[kp + (size_t)col * nrow];
+        T t = __ldcg(S + kk + (size_t)col * nrow);
+        S[kk + (size_t)col * nrow] = __ldcg(S + kp + (size_t)col * nrow);
         S[kp + (size_t)col * nrow] = t;
       }
       if (gt == 0) {
-        T t = S[kk + (size_t)kk * nrow];
-        S[kk + (size_t)kk * nrow] = S[kp + (size_t)kp * nrow];
+        T t = __ldcg(S + kk + (size_t)kk * nrow);
+        S[kk + (size_t)kk * nrow] = __ldcg(S + kp + (size_t)kp * nrow);
         S[kp + (size_t)kp * nrow] = t;
         int pt = perm[kk];
         perm[kk] = perm[kp];
         perm[kp] = pt;
         if (copycol) {
-          T a1 = Wb[(size_t)(j + 1) * ldw + kp], a2 = Wb[(size_t)(j + 1) * ldw + kk];
+          T a1 = __ldcg(Wb + (size_t)(j + 1) * ldw + kp), a2 = __ldcg(Wb + (size_t)(j + 1) * ldw + kk);
           Wb[(size_t)j * ldw + kk] = a1;
           Wb[(size_t)j * ldw + kp] = a2;
           for (int t2 = 0; t2 < j; ++t2) {
-            T x = Wb[(size_t)t2 * ldw + kk];
-            Wb[(size_t)t2 * ldw + kk] = Wb[(size_t)t2 * ldw + kp];
+            T x = __ldcg(Wb + (size_t)t2 * ldw + kk);
+            Wb[(size_t)t2 * ldw + kk] = __ldcg(Wb + (size_t)t2 * ldw + kp);
             Wb[(size_t)t2 * ldw + kp] = x;
           }
         } else {
           for (int t2 = 0; t2 <= j + 1; ++t2) {
-            T x = Wb[(size_t)t2 * ldw + kk];
-            Wb[(size_t)t2 * ldw + kk] = Wb[(size_t)t2 * ldw + kp];
+            T x = __ldcg(Wb + (size_t)t2 * ldw + kk);
+            Wb[(size_t)t2 * ldw + kk] = __ldcg(Wb + (size_t)t2 * ldw + kp);
             Wb[(size_t)t2 * ldw + kp] = x;
           }
         }
         ctl->pivoted = 1;
       }
-      if (!grid_sync(ctl, status)) return;
+      unsigned long long dummy;
+      if (!grid_exchange(ctl, epoch, 0ull, status, dummy)) return;
       if (gt == kk || gt == kp)
-        for (int t = 0; t < j; ++t) lc[t * WP_THREADS + tid] = S[gt + (size_t)(k0 + t) * nrow];
+        for (int t = 0; t < j; ++t) lc[t * WP_THREADS + tid] = __ldcg(S + gt + (size_t)(k0 + t) * nrow);
+    }
+    if (slow && gt < nrow) {
+      // W entries of the thread's own row after the pivot search / interchange
+      w_own = __ldcg(Wb + (size_t)j * ldw + gt);
+      w_own1 = __ldcg(Wb + (size_t)(j + 1) * ldw + gt);
     }
     // ---- D: L column(s) from W, D entries
     if (kstep == 1) {
-      const T d = Wb[(size_t)j * ldw + c];
-      if (!zero) {
-        const T r1 = T(1) / d;
-        for (int r = first_row(c + 1); r < nrow; r += TT) {
-          const T l = Wb[(size_t)j * ldw + r] * r1;
-          S[r + (size_t)c * nrow] = l;
-          if (r == gt) lc[j * WP_THREADS + tid] = l;
-        }
-      } else {
+      const T d = slow ? __ldcg(Wb + (size_t)j * ldw + c) : wcc;
+      const T r1 = zero ? T(1) : T(1) / d;
+      for (int r = first_row(c + 1); r < nrow; r += TT) {
+        const T wv = r == gt ? w_own : __ldcg(Wb + (size_t)j * ldw + r);
         // zero pivot column: kept unscaled (LAPACK dlasyf copies W(k:n,k))
-        for (int r = first_row(c + 1); r < nrow; r += TT) {
-          const T l = Wb[(size_t)j * ldw + r];
-          S[r + (size_t)c * nrow] = l;
-          if (r == gt) lc[j * WP_THREADS + tid] = l;
-        }
-        if (gt == 0) atomicOr(status, ST_ZERO_PIVOT);
+        const T l = zero ? wv : wv * r1;
+        S[r + (size_t)c * nrow] = l;
+        if (r == gt) lc[j * WP_THREADS + tid] = l;
       }
       if (gt == 0) {
+        if (zero) atomicOr(status, ST_ZERO_PIVOT);
         S[c + (size_t)c * nrow] = T(1);
         Dd[c] = d;
         De[c] = T(0);
       }
     } else {
-      const T D11 = Wb[(size_t)j * ldw + c], D21 = Wb[(size_t)j * ldw + c + 1];
-      const T D22 = Wb[(size_t)(j + 1) * ldw + c + 1];
+      const T D11 = __ldcg(Wb + (size_t)j * ldw + c), D21 = __ldcg(Wb + (size_t)j * ldw + c + 1);
+      const T D22 = __ldcg(Wb + (size_t)(j + 1) * ldw + c + 1);
       T d21 = D21;
       const T d11 = D22 / d21, d22 = D11 / d21;
       const T tt = T(1) / (d11 * d22 - T(1));
       d21 = tt / d21;
       for (int r = first_row(c + 2); r < nrow; r += TT) {
-        const T wk = Wb[(size_t)j * ldw + r], wk1 = Wb[(size_t)(j + 1) * ldw + r];
+        const T wk = r == gt ? w_own : __ldcg(Wb + (size_t)j * ldw + r);
+        const T wk1 = r == gt ? w_own1 : __ldcg(Wb + (size_t)(j + 1) * ldw + r);
         const T l0 = d21 * (d11 * wk - wk1), l1 = d21 * (d22 * wk1 - wk);
         S[r + (size_t)c * nrow] = l0;
         S[r + (size_t)(c + 1) * nrow] = l1;
@@ -339,7 +414,19 @@ __global__ void __launch_bounds__(WP_THREADS) k_wide_panel(T *S, int nrow, int w
       }
     }
     j += kstep;
-    parity ^= 1;
+    const int cn = k0 + j;
+    if (!slow) {
+      // fast path: no interchange, next column is c + 1
+      s_own = s_next;
+      cur ^= 1;
+      __syncthreads();
+    } else if (j < nb && cn < w) {
+      // reload the next column's inputs after the pivot search / interchange
+      __syncthreads();
+      if (tid < j) wbuf[cur][tid] = __ldcg(Wb + (size_t)tid * ldw + cn);
+      s_own = (gt >= cn && gt < nrow) ? __ldcg(S + gt + (size_t)cn * nrow) : T(0);
+      __syncthreads();
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) ctl->kb = j;
 }
@@ -589,7 +676,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     int kb_want = std::min(nb, w - k0);
     int ldw = nrow;
     void *args[] = {&S, &nrow, &w, &k0, &kb_want, &Wb, &ldw, &Dd, &De, &perm, &ctl, &status};
-    if (cudaMemsetAsync(&ctl->amax[0][0], 0, sizeof(ctl->amax), st) != cudaSuccess) return NQG_ERR_CUDA;
+    if (cudaMemsetAsync(&ctl->pslot[0][0], 0, sizeof(ctl->pslot), st) != cudaSuccess) return NQG_ERR_CUDA;
     cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
     if (cudaLaunchCooperativeKernel((void *)k_wide_panel<T>, dim3(G), dim3(WP_THREADS), args, smem, st) !=
         cudaSuccess)

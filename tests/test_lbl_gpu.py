@@ -258,3 +258,27 @@ def test_fp32_update_kernels(path, update, monkeypatch):
     assert relres(d, x) <= 1e-10
     xr = d["out_x"]
     assert np.linalg.norm(x - xr) <= 1e-6 * np.linalg.norm(xr)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", CASES, ids=os.path.basename)
+def test_panel_rows_kernels(path, monkeypatch):
+    """Supernodes wider than 4 columns through k_bk_global, the rows below
+    each diagonal block solved by the multi-CTA kernel or by the per-row
+    substitution inside k_bk_global: both FP64 factors pass the backward
+    error bar.  (Two factorizations are not compared bit for bit: the Schur
+    updates scatter with atomics, so summation order varies run to run.)"""
+    monkeypatch.setenv("NASOQ_GB300_BK_SMALL", "4")
+    d = nqa.load(path)
+    n = len(d["in_rhs"])
+    for mode in ("split", "serial"):
+        monkeypatch.setenv("NASOQ_GB300_PANEL_ROWS", mode)
+        plan = nq.Plan(n, d["in_Ap"], d["in_Ai"], d["in_Ax"], settings=_settings(d, req_ref_iter=0))
+        assert plan.factor() == 0
+        vals, dv, perm, ls = plan.factor_arrays()
+        Kp = dense_sym(n, d["in_Ap"], d["in_Ai"], d["out_Ax_perturbed"])[np.ix_(perm, perm)]
+        Ld, Dd = dense_factor(plan.symbolic, vals, dv, ls)
+        R = Kp - Ld @ Dd @ Ld.T
+        mag = np.abs(Ld) @ np.abs(Dd) @ np.abs(Ld).T
+        assert np.abs(R).max() <= 1e-13 * mag.max(), mode
+        plan.close()
