@@ -40,6 +40,10 @@ METRIC = "QP solves/sec at 1e-8 KKT tol: mixed+batched+warm-start vs plain GPU F
 GRID, MCON, PER_ROW, DELTA, SEED = 64, 20000, 6, 1e-8, 0
 SAMPLE_GRID, SAMPLE_M = 48, 8000          # CPU baseline sample of the same family (~9% of the flops)
 TARGET_RELRES = 1e-10
+# DRAM bytes (read + write) per launch of the dominant kernel classes, scaled
+# from one ncu capture of the 48^3 / m=8000 case of this workload family (see
+# profiles/); None where no capture exists yet
+NCU_TRAFFIC = {}
 INNER = 6  # GMRES inner steps of the refinement (one restart)
 
 
@@ -154,7 +158,7 @@ def run_reference(args, world, rank):
     from nasoq_gb300 import Symbolic
     from nasoq_gb300 import problems as P
 
-    Kc, _ = P.lbl_kkt(seed=SEED, grid3d=GRID, m=MCON, per_row=PER_ROW, delta=DELTA)
+    Kc, _ = P.lbl_kkt(seed=SEED, grid3d=args.grid, m=args.mcon, per_row=PER_ROW, delta=DELTA)
     F_full = factor_flops(Symbolic(Kc.ncol, Kc.p, Kc.i))
     for _ in range(args.warmup):
         cpu_sample()
@@ -171,7 +175,7 @@ def run_reference(args, world, rank):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / max(args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(GRID, MCON), "N": Kc.ncol},
+        "config": {"workload": workload_name(args.grid, args.mcon), "N": Kc.ncol},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": samples[0]["threads"], "kind": "port",
                          "sample": f"each step: full factor + refined solve of the same KKT family at "
                                    f"{SAMPLE_GRID}^3 grid, m={SAMPLE_M} (N={samples[0]['N']}, "
@@ -192,6 +196,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison step")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--grid", type=int, default=GRID, help="Laplacian grid edge (smaller cases for profiler captures)")
+    ap.add_argument("--mcon", type=int, default=MCON, help="constraint rows")
     ap.add_argument("--profile-once", action="store_true",
                     help="analysis + exactly one timed step and nothing else (for profiler launch lists)")
     args = ap.parse_args()
@@ -210,7 +216,7 @@ def main():
         dist.init_process_group("nccl")
     stream = torch.cuda.current_stream()
 
-    K, rhs = P.lbl_kkt(seed=SEED, grid3d=GRID, m=MCON, per_row=PER_ROW, delta=DELTA)
+    K, rhs = P.lbl_kkt(seed=SEED, grid3d=args.grid, m=args.mcon, per_row=PER_ROW, delta=DELTA)
     n = K.ncol
     st32 = nq.default_settings(precision=nq.NQG_FP32, solve_precision=nq.NQG_FP32, req_ref_iter=1,
                                max_inner_iter=INNER, tol_abs=0.0, tol_rel=0.0, reg_diag=1e-9)
@@ -333,7 +339,25 @@ def main():
         roof = {"bound": "tensor", "achieved": ach, "peak": bf16_peak, "unit": "TFLOP/s", "frac": ach / bf16_peak,
                 "fp32_cuda_core_nominal_tflops": 80.5, "frac_of_fp32_nominal": ach / 80.5}
     roof.update({"kernel": dom, "launches_per_step": ds["launches"] / 2, "avg_launch_ms": avg_ms,
-                 "traffic": None, "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"})
+                 "traffic": NCU_TRAFFIC.get(dom), "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"})
+    # every class: factor classes against the measured tensor peak (the tcgen05
+    # classes do 3 split-TF32 MMAs per useful multiply-add), solves and SpMV
+    # against the measured copy bandwidth
+    by_class = {}
+    for k, v in stats.items():
+        sec = v["total_ms"] / 1000.0
+        if sec <= 0:
+            continue
+        if k in ("solve", "spmv"):
+            a = v["alg_bytes"] / sec / 1e9
+            by_class[k] = {"bound": "hbm", "achieved": a, "unit": "GB/s", "frac": a / hbm_peak}
+        else:
+            a = v["alg_flops"] / sec / 1e12
+            e = {"bound": "tensor", "achieved": a, "unit": "TFLOP/s", "frac": a / bf16_peak}
+            if k in ("update", "wide_trailing"):
+                e["mma_tflops"] = 3 * a
+            by_class[k] = e
+    roof["by_class"] = by_class
     kinfo = {k: {"ms_per_step": v["total_ms"] / 2, "launches_per_step": v["launches"] / 2} for k, v in stats.items()}
 
     cpu = None
@@ -355,7 +379,7 @@ def main():
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32-factor+fp64-refine", "data": "synthetic",
-            "config": {"workload": workload_name(GRID, MCON), "N": n, "nnz_K_lower": int(K.nnz),
+            "config": {"workload": workload_name(args.grid, args.mcon), "N": n, "nnz_K_lower": int(K.nnz),
                        "seed": SEED, "delta": DELTA, "factor_flops": F, "precision": "fp32 factor and triangular solves, fp64 flexible GMRES-IR",
                        "refinement": f"FGMRES({INNER}), 1 restart", "target_relres": TARGET_RELRES,
                        "l2": "inputs larger than L2 (FP32 factor 4 GB)", "analysis_s": analysis_s,

@@ -707,9 +707,38 @@ extern "C" int nqg_spmv_device(nqg_plan *h, const double *d_x, double *d_y) {
   return dev_spmv_orig(h->P, d_x, d_y);
 }
 
+// 2x2 pivot blocks (nonzero sub-diagonal entries of D) and supernodes that
+// Bunch-Kaufman permuted in the last factorization; counts[0..1] on device.
+template <class T>
+__global__ void k_pivot_counts(int n, const T *Dg, int ns, const uint8_t *pivoted, int *counts) {
+  int a = 0, b = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a += Dg[n + i] != T(0);
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) b += pivoted[s] != 0;
+  if (a) atomicAdd(&counts[0], a);
+  if (b) atomicAdd(&counts[1], b);
+}
+
 extern "C" int nqg_get_timings(const nqg_plan *h, nqg_timings *t) {
   if (!h || !t) return NQG_ERR_ARG;
-  *t = h->P.tm;
+  Plan &P = const_cast<nqg_plan *>(h)->P;
+  if (P.factored) {
+    // pivot statistics of the last factorization, counted on demand
+    int *cnt = reinterpret_cast<int *>(P.d_scal + 60);  // spare slots of the scalar area
+    NQG_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(int), P.stream));
+    const int blocks = std::max(1, std::min((P.n + 255) / 256, 1024));
+    if (P.set.precision == NQG_FP32)
+      k_pivot_counts<float><<<blocks, 256, 0, P.stream>>>(P.n, reinterpret_cast<const float *>(P.d_D),
+                                                          P.sym.nsuper, P.d_pivoted, cnt);
+    else
+      k_pivot_counts<double><<<blocks, 256, 0, P.stream>>>(P.n, reinterpret_cast<const double *>(P.d_D),
+                                                           P.sym.nsuper, P.d_pivoted, cnt);
+    int hc[2] = {0, 0};
+    NQG_CUDA(cudaMemcpyAsync(hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, P.stream));
+    NQG_CUDA(cudaStreamSynchronize(P.stream));
+    P.tm.num_2x2 = hc[0];
+    P.tm.num_pivot_supernodes = hc[1];
+  }
+  *t = P.tm;
   return NQG_OK;
 }
 

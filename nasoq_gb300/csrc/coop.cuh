@@ -13,7 +13,8 @@ struct WideCtl {
   int abort;
   int kb;          // columns completed by the last panel launch
   int pivoted;     // any interchange in this supernode
-  int pad[3];
+  int stop;        // the fast panel stopped where a pivot search is needed
+  int pad[2];
   double cval[2][1024];
   int cidx[2][1024];
   double rval[2][1024];

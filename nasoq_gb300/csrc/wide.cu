@@ -208,6 +208,211 @@ __device__ bool grid_argmax(T cv, int ci, WideCtl *ctl, int phase, unsigned &epo
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// FP32 fast panel: the columns of a panel for which Bunch-Kaufman keeps the
+// diagonal pivot (|a_cc| >= alpha * colmax, no interchange) -- every column
+// once the pivot order has settled.  Every CTA keeps its own copy of the
+// panel's diagonal-block rows R = [k0, k0 + nbR): their original entries Sr,
+// their W entries Wr and their L entries Lr, computed redundantly with the
+// same arithmetic in every CTA.  The pivot W(c, j) and the next update row
+// W(c+1, 0..j) are then local, the only value that crosses CTAs is the
+// column-max candidate, and the exchange needs no memory fences.  The other
+// rows are owned one per thread (512 threads per CTA, L entries cached in
+// shared memory).  At the first column that needs a pivot search (or has a
+// zero or NaN pivot) every CTA stops with the same decision; kb = columns
+// done and ctl->stop tell the host to close this partial panel and hand the
+// column to the general kernel.
+constexpr int FP_THREADS = 512;
+
+// CTA argmax of packed FP32 candidates (hi = |value| bits, lo = 0xFFFFFF -
+// row; 0/0 for none) with redux.sync; result valid in every thread.
+__device__ __forceinline__ unsigned long long cta_max_key(unsigned hi, unsigned lo) {
+  __shared__ unsigned s_hi[FP_THREADS / 32], s_lo[FP_THREADS / 32];
+  __shared__ unsigned long long s_key;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  unsigned mh = __reduce_max_sync(0xffffffffu, hi);
+  unsigned ml = __reduce_max_sync(0xffffffffu, hi == mh ? lo : 0u);
+  if (lane == 0) {
+    s_hi[wid] = mh;
+    s_lo[wid] = ml;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const unsigned h = lane < nw ? s_hi[lane] : 0u, l = lane < nw ? s_lo[lane] : 0u;
+    mh = __reduce_max_sync(0xffffffffu, h);
+    ml = __reduce_max_sync(0xffffffffu, h == mh ? l : 0u);
+    if (lane == 0) s_key = ((unsigned long long)mh << 24) | ml;
+  }
+  __syncthreads();
+  return s_key;
+}
+
+// Barrier + maximum over the CTAs' candidate words, without fences (nothing
+// else is exchanged).  Same slots, epochs and parities as grid_exchange.
+__device__ bool grid_max_nofence(WideCtl *ctl, unsigned &epoch, unsigned long long cand, int *status,
+                                 unsigned long long &best) {
+  __shared__ unsigned long long s_best;
+  __shared__ int s_ok;
+  ++epoch;
+  const unsigned e = epoch & 0xFFu;
+  const int par = epoch & 1;
+  if (threadIdx.x == 0) *(volatile unsigned long long *)&ctl->pslot[par][blockIdx.x] = (cand << 8) | e;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    long long it = 0;
+    int ok = 1;
+    unsigned long long m = 0;
+    while (true) {
+      bool all = true;
+      m = 0;
+      for (int g = lane; g < (int)gridDim.x; g += 32) {
+        const unsigned long long v = *(volatile unsigned long long *)&ctl->pslot[par][g];
+        if ((unsigned)(v & 0xFFu) != e) all = false;
+        else m = max(m, v >> 8);
+      }
+      if (__all_sync(0xffffffffu, all)) break;
+      int ab = lane == 0 ? *(volatile int *)&ctl->abort : 0;
+      ab = __shfl_sync(0xffffffffu, ab, 0);
+      if (ab) {
+        ok = 0;
+        break;
+      }
+      if (++it > SPIN_LIMIT) {
+        if (lane == 0) {
+          atomicOr(status, ST_TIMEOUT);
+          atomicExch(&ctl->abort, 1);
+        }
+        ok = 0;
+        break;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) {
+      s_best = m;
+      s_ok = ok;
+    }
+  }
+  __syncthreads();
+  best = s_best;
+  return s_ok != 0;
+}
+
+__host__ __device__ constexpr size_t fast_panel_smem(int nb) {
+  return ((size_t)nb * FP_THREADS + 3 * (size_t)nb * (nb + 1)) * sizeof(float);
+}
+
+__global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nrow, int w, int k0, int nb,
+                                                                float *Wb, int ldw, float *Dd, float *De,
+                                                                WideCtl *ctl, int *status) {
+  extern __shared__ __align__(16) unsigned char fp_raw[];
+  const int nbR = min(nb, w - k0);  // panel columns = rows of R
+  const int ldr = nbR + 1;
+  float *lc = reinterpret_cast<float *>(fp_raw);  // [nb][FP_THREADS]: L of the thread's first row
+  float *Sr = lc + (size_t)nb * FP_THREADS;       // [nbR][ldr]: Sr[i * ldr + j] = S(k0 + i, k0 + j)
+  float *Wr = Sr + (size_t)nbR * ldr;             // W(k0 + i, j)
+  float *Lr = Wr + (size_t)nbR * ldr;             // L(k0 + i, k0 + j)
+  const float alpha = (float)((1.0 + sqrt(17.0)) / 8.0);
+  const int tid = threadIdx.x;
+  const int gt = blockIdx.x * blockDim.x + tid, TT = gridDim.x * blockDim.x;
+  const int rbeg = k0 + nbR;  // first row outside R
+  for (int e = tid; e < nbR * nbR; e += blockDim.x) {
+    const int i = e % nbR, jj = e / nbR;
+    Sr[i * ldr + jj] = i >= jj ? __ldcg(S + (k0 + i) + (size_t)(k0 + jj) * nrow) : 0.f;
+  }
+  const int r_own = rbeg + gt;  // the thread's first (cached) row
+  float s_own = r_own < nrow ? __ldcg(S + r_own + (size_t)k0 * nrow) : 0.f;
+  unsigned epoch = 0;
+  int j = 0;
+  bool stop = false;
+  __syncthreads();
+  while (j < nbR) {
+    const int c = k0 + j;
+    const float *wrow = Wr + (size_t)j * ldr;  // W(c, 0..j-1)
+    // ---- R rows c .. k0+nbR-1 (redundant in every CTA)
+    unsigned hi = 0u, lo = 0u;
+    if (tid < nbR - j) {
+      const int i = j + tid;
+      float acc = Sr[i * ldr + j];
+      for (int t = 0; t < j; ++t) acc -= Lr[i * ldr + t] * wrow[t];
+      Wr[i * ldr + j] = acc;
+      const int r = k0 + i;
+      if (r > c && r < w) {
+        const float a = fabsf(acc);
+        if (a == a) {
+          hi = __float_as_uint(a);
+          lo = 0xFFFFFFu - (unsigned)r;
+        }
+      }
+    }
+    // ---- owned rows
+    float w_own = 0.f;
+    float s_next = 0.f;
+    for (int r = r_own; r < nrow; r += TT) {
+      float acc;
+      if (r == r_own) {
+        acc = s_own;
+        for (int t = 0; t < j; ++t) acc -= lc[t * FP_THREADS + tid] * wrow[t];
+        w_own = acc;
+        if (j + 1 < nbR) s_next = __ldcg(S + r + (size_t)(c + 1) * nrow);
+      } else {
+        acc = __ldcg(S + r + (size_t)c * nrow);
+        for (int t = 0; t < j; ++t) acc -= __ldcg(S + r + (size_t)(k0 + t) * nrow) * wrow[t];
+      }
+      Wb[(size_t)j * ldw + r] = acc;
+      if (r < w) {
+        const float a = fabsf(acc);
+        const unsigned h = __float_as_uint(a), l = 0xFFFFFFu - (unsigned)r;
+        if (a == a && (h > hi || (h == hi && l > lo))) {
+          hi = h;
+          lo = l;
+        }
+      }
+    }
+    const unsigned long long cand = cta_max_key(hi, lo);  // includes a __syncthreads: Wr visible
+    unsigned long long best;
+    if (!grid_max_nofence(ctl, epoch, cand, status, best)) return;
+    const float colmax = (float)__uint_as_float((unsigned)(best >> 24));
+    const float d = Wr[j * ldr + j];
+    const float absakk = fabsf(d);
+    if (!(absakk >= alpha * colmax) || absakk == 0.f) {
+      stop = true;  // pivot search, zero or NaN pivot: the general kernel takes column c
+      break;
+    }
+    // ---- L column c
+    const float r1 = 1.f / d;
+    for (int r = r_own; r < nrow; r += TT) {
+      const float wv = r == r_own ? w_own : __ldcg(Wb + (size_t)j * ldw + r);
+      const float l = wv * r1;
+      S[r + (size_t)c * nrow] = l;
+      if (r == r_own) lc[j * FP_THREADS + tid] = l;
+    }
+    if (tid < nbR - j - 1) {
+      const int i = j + 1 + tid;
+      Lr[i * ldr + j] = Wr[i * ldr + j] * r1;
+    }
+    if (blockIdx.x == 0) {
+      // R rows of W and L to global for the trailing update and the factor
+      for (int i = j + tid; i < nbR; i += blockDim.x) {
+        Wb[(size_t)j * ldw + k0 + i] = Wr[i * ldr + j];
+        if (i > j) S[(k0 + i) + (size_t)c * nrow] = Wr[i * ldr + j] * r1;
+      }
+      if (tid == 0) {
+        S[c + (size_t)c * nrow] = 1.f;
+        Dd[c] = d;
+        De[c] = 0.f;
+      }
+    }
+    s_own = s_next;
+    ++j;
+    __syncthreads();
+  }
+  if (blockIdx.x == 0 && tid == 0) {
+    ctl->kb = j;
+    ctl->stop = stop ? 1 : 0;
+  }
+}
+
 // One panel: columns c = k0 .. (at most k0+nb, one more for a final 2x2).
 // Thread gt owns rows gt, gt + TT, ...; the panel entries L(gt, k0 + t) of
 // its first row are cached in shared memory (lc[t][threadIdx.x]) as they are
@@ -668,26 +873,67 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       cudaFuncSetAttribute(k_wide_trailing_t5, cudaFuncAttributeMaxDynamicSharedMemorySize, t5::smem_bytes(1)) !=
           cudaSuccess)
     return NQG_ERR_CUDA;
-  int k0 = 0;
-  while (k0 < w) {
-    // one row per thread where the grid allows it
-    const int rows_left = nrow - k0;
-    const int G = std::max(1, std::min(maxG, (rows_left + WP_THREADS - 1) / WP_THREADS));
-    int kb_want = std::min(nb, w - k0);
-    int ldw = nrow;
-    void *args[] = {&S, &nrow, &w, &k0, &kb_want, &Wb, &ldw, &Dd, &De, &perm, &ctl, &status};
-    if (cudaMemsetAsync(&ctl->pslot[0][0], 0, sizeof(ctl->pslot), st) != cudaSuccess) return NQG_ERR_CUDA;
-    cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
-    if (cudaLaunchCooperativeKernel((void *)k_wide_panel<T>, dim3(G), dim3(WP_THREADS), args, smem, st) !=
+  // FP32: fast panels (no pivot search) until a column needs one; the
+  // general kernel then factors one panel from that column.
+  // NASOQ_GB300_PANEL=general keeps every panel on the general kernel.
+  const char *pe = std::getenv("NASOQ_GB300_PANEL");
+  const bool fast_enabled = sizeof(T) == 4 && !(pe && std::string(pe) == "general");
+  const size_t fsmem = fast_panel_smem(nb);
+  int maxG_fast = 0;
+  if (fast_enabled) {
+    if (cudaFuncSetAttribute(k_wide_panel_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem) !=
         cudaSuccess)
       return NQG_ERR_CUDA;
+    int occf = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occf, k_wide_panel_fast, FP_THREADS, fsmem) != cudaSuccess)
+      return NQG_ERR_CUDA;
+    maxG_fast = std::min(std::max(occf, 0) * num_sms, 1024);
+  }
+  bool use_general = false;  // the next panel starts at a column that needs a pivot search
+  int k0 = 0;
+  while (k0 < w) {
+    int kb = 0, abort = 0, stop = 0;
+    int ldw = nrow;
+    int kb_want = std::min(nb, w - k0);
+    const bool fast = fast_enabled && maxG_fast > 0 && !use_general;
+    if (cudaMemsetAsync(&ctl->pslot[0][0], 0, sizeof(ctl->pslot), st) != cudaSuccess) return NQG_ERR_CUDA;
+    cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
+    if (fast) {
+      const int rows_out = nrow - k0 - kb_want;
+      const int G = std::max(1, std::min(maxG_fast, (rows_out + FP_THREADS - 1) / FP_THREADS));
+      float *Sf = reinterpret_cast<float *>(S), *Wf = reinterpret_cast<float *>(Wb);
+      float *Df = reinterpret_cast<float *>(Dd), *Ef = reinterpret_cast<float *>(De);
+      void *args[] = {&Sf, &nrow, &w, &k0, &kb_want, &Wf, &ldw, &Df, &Ef, &ctl, &status};
+      if (cudaLaunchCooperativeKernel((void *)k_wide_panel_fast, dim3(G), dim3(FP_THREADS), args, fsmem, st) !=
+          cudaSuccess)
+        return NQG_ERR_CUDA;
+    } else {
+      // one row per thread where the grid allows it
+      const int rows_left = nrow - k0;
+      const int G = std::max(1, std::min(maxG, (rows_left + WP_THREADS - 1) / WP_THREADS));
+      void *args[] = {&S, &nrow, &w, &k0, &kb_want, &Wb, &ldw, &Dd, &De, &perm, &ctl, &status};
+      if (cudaLaunchCooperativeKernel((void *)k_wide_panel<T>, dim3(G), dim3(WP_THREADS), args, smem, st) !=
+          cudaSuccess)
+        return NQG_ERR_CUDA;
+    }
     if (P) P->nlaunch++;
-    int kb = 0, abort = 0;
     if (cudaMemcpyAsync(&kb, &ctl->kb, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaMemcpyAsync(&abort, &ctl->abort, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&stop, &ctl->stop, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
       return NQG_ERR_CUDA;
-    if (abort || kb <= 0) return NQG_ERR_TIMEOUT;
+    if (abort) return NQG_ERR_TIMEOUT;
+    if (fast) {
+      use_general = stop != 0;
+      if (kb <= 0) {
+        if (!use_general) return NQG_ERR_TIMEOUT;
+        if (P) P->prof_end(NQG_K_WIDE_PANEL, e0, 0.0, 0.0);
+        continue;  // the first column already needs the general kernel
+      }
+    } else {
+      use_general = false;
+      if (kb <= 0) return NQG_ERR_TIMEOUT;
+    }
     const int k1 = k0 + kb;
     if (P) {
       // panel: column GEMVs (2 * rows * j) and the L column scaling
