@@ -299,103 +299,80 @@ __device__ bool grid_max_nofence(WideCtl *ctl, unsigned &epoch, unsigned long lo
 }
 
 __host__ __device__ constexpr size_t fast_panel_smem(int nb) {
-  return ((size_t)nb * FP_THREADS + 3 * (size_t)nb * (nb + 1)) * sizeof(float);
+  return ((size_t)nb * FP_THREADS + (size_t)nb * (nb + 1)) * sizeof(float);
 }
 
+// Right-looking: after column j, the thread's row and the replicated rows R
+// get the rank-1 term L(r, j) W(k0 + j', j) subtracted from every later panel
+// column j' at once (independent FMAs), so the next column's W values and
+// pivot candidates are ready without a dot product.  Each entry receives the
+// same FMAs in the same order as the general kernel's left-looking update.
+// Requires at most one owned row per thread (nrow - k0 - nbR <= threads).
 __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nrow, int w, int k0, int nb,
                                                                 float *Wb, int ldw, float *Dd, float *De,
                                                                 WideCtl *ctl, int *status) {
   extern __shared__ __align__(16) unsigned char fp_raw[];
   const int nbR = min(nb, w - k0);  // panel columns = rows of R
   const int ldr = nbR + 1;
-  float *lc = reinterpret_cast<float *>(fp_raw);  // [nb][FP_THREADS]: L of the thread's first row
-  float *Sr = lc + (size_t)nb * FP_THREADS;       // [nbR][ldr]: Sr[i * ldr + j] = S(k0 + i, k0 + j)
-  float *Wr = Sr + (size_t)nbR * ldr;             // W(k0 + i, j)
-  float *Lr = Wr + (size_t)nbR * ldr;             // L(k0 + i, k0 + j)
+  float *sr = reinterpret_cast<float *>(fp_raw);  // [nbR][FP_THREADS]: the thread's row, panel columns
+  float *Sr = sr + (size_t)nb * FP_THREADS;       // [nbR][ldr]: rows of R, W values once final
   const float alpha = (float)((1.0 + sqrt(17.0)) / 8.0);
   const int tid = threadIdx.x;
-  const int gt = blockIdx.x * blockDim.x + tid, TT = gridDim.x * blockDim.x;
-  const int rbeg = k0 + nbR;  // first row outside R
+  const int gt = blockIdx.x * blockDim.x + tid;
+  const int r_own = k0 + nbR + gt;  // the thread's row (if < nrow)
+  const bool own = r_own < nrow;
   for (int e = tid; e < nbR * nbR; e += blockDim.x) {
     const int i = e % nbR, jj = e / nbR;
     Sr[i * ldr + jj] = i >= jj ? __ldcg(S + (k0 + i) + (size_t)(k0 + jj) * nrow) : 0.f;
   }
-  const int r_own = rbeg + gt;  // the thread's first (cached) row
-  float s_own = r_own < nrow ? __ldcg(S + r_own + (size_t)k0 * nrow) : 0.f;
+  if (own)
+    for (int jj = 0; jj < nbR; ++jj) sr[jj * FP_THREADS + tid] = __ldcg(S + r_own + (size_t)(k0 + jj) * nrow);
+  __syncthreads();
+  // candidates of column 0
+  unsigned hi = 0u, lo = 0u;
+  auto consider = [&](float v, int r) {
+    const float a = fabsf(v);
+    const unsigned h = __float_as_uint(a), l = 0xFFFFFFu - (unsigned)r;
+    if (a == a && (h > hi || (h == hi && l > lo))) {
+      hi = h;
+      lo = l;
+    }
+  };
+  if (own && r_own < w) consider(sr[tid], r_own);
+  if (tid >= 1 && tid < nbR && k0 + tid < w) consider(Sr[tid * ldr], k0 + tid);
   unsigned epoch = 0;
   int j = 0;
   bool stop = false;
-  __syncthreads();
   while (j < nbR) {
     const int c = k0 + j;
-    const float *wrow = Wr + (size_t)j * ldr;  // W(c, 0..j-1)
-    // ---- R rows c .. k0+nbR-1 (redundant in every CTA)
-    unsigned hi = 0u, lo = 0u;
-    if (tid < nbR - j) {
-      const int i = j + tid;
-      float acc = Sr[i * ldr + j];
-      for (int t = 0; t < j; ++t) acc -= Lr[i * ldr + t] * wrow[t];
-      Wr[i * ldr + j] = acc;
-      const int r = k0 + i;
-      if (r > c && r < w) {
-        const float a = fabsf(acc);
-        if (a == a) {
-          hi = __float_as_uint(a);
-          lo = 0xFFFFFFu - (unsigned)r;
-        }
-      }
-    }
-    // ---- owned rows
-    float w_own = 0.f;
-    float s_next = 0.f;
-    for (int r = r_own; r < nrow; r += TT) {
-      float acc;
-      if (r == r_own) {
-        acc = s_own;
-        for (int t = 0; t < j; ++t) acc -= lc[t * FP_THREADS + tid] * wrow[t];
-        w_own = acc;
-        if (j + 1 < nbR) s_next = __ldcg(S + r + (size_t)(c + 1) * nrow);
-      } else {
-        acc = __ldcg(S + r + (size_t)c * nrow);
-        for (int t = 0; t < j; ++t) acc -= __ldcg(S + r + (size_t)(k0 + t) * nrow) * wrow[t];
-      }
-      Wb[(size_t)j * ldw + r] = acc;
-      if (r < w) {
-        const float a = fabsf(acc);
-        const unsigned h = __float_as_uint(a), l = 0xFFFFFFu - (unsigned)r;
-        if (a == a && (h > hi || (h == hi && l > lo))) {
-          hi = h;
-          lo = l;
-        }
-      }
-    }
-    const unsigned long long cand = cta_max_key(hi, lo);  // includes a __syncthreads: Wr visible
+    const unsigned long long cand = cta_max_key(hi, lo);
     unsigned long long best;
     if (!grid_max_nofence(ctl, epoch, cand, status, best)) return;
     const float colmax = (float)__uint_as_float((unsigned)(best >> 24));
-    const float d = Wr[j * ldr + j];
+    const float d = Sr[j * ldr + j];
     const float absakk = fabsf(d);
     if (!(absakk >= alpha * colmax) || absakk == 0.f) {
       stop = true;  // pivot search, zero or NaN pivot: the general kernel takes column c
       break;
     }
-    // ---- L column c
     const float r1 = 1.f / d;
-    for (int r = r_own; r < nrow; r += TT) {
-      const float wv = r == r_own ? w_own : __ldcg(Wb + (size_t)j * ldw + r);
+    hi = 0u;
+    lo = 0u;
+    // the thread's row: L(r, c), then the rank-1 term on the later columns
+    if (own) {
+      const float wv = sr[j * FP_THREADS + tid];
       const float l = wv * r1;
-      S[r + (size_t)c * nrow] = l;
-      if (r == r_own) lc[j * FP_THREADS + tid] = l;
+      Wb[(size_t)j * ldw + r_own] = wv;
+      S[r_own + (size_t)c * nrow] = l;
+      for (int jj = j + 1; jj < nbR; ++jj)
+        sr[jj * FP_THREADS + tid] = fmaf(-l, Sr[jj * ldr + j], sr[jj * FP_THREADS + tid]);
+      if (j + 1 < nbR && r_own < w) consider(sr[(j + 1) * FP_THREADS + tid], r_own);
     }
-    if (tid < nbR - j - 1) {
-      const int i = j + 1 + tid;
-      Lr[i * ldr + j] = Wr[i * ldr + j] * r1;
-    }
+    // rows of R: global copies (CTA 0), then the rank-1 term on the trailing block
     if (blockIdx.x == 0) {
-      // R rows of W and L to global for the trailing update and the factor
       for (int i = j + tid; i < nbR; i += blockDim.x) {
-        Wb[(size_t)j * ldw + k0 + i] = Wr[i * ldr + j];
-        if (i > j) S[(k0 + i) + (size_t)c * nrow] = Wr[i * ldr + j] * r1;
+        Wb[(size_t)j * ldw + k0 + i] = Sr[i * ldr + j];
+        if (i > j) S[(k0 + i) + (size_t)c * nrow] = Sr[i * ldr + j] * r1;
       }
       if (tid == 0) {
         S[c + (size_t)c * nrow] = 1.f;
@@ -403,9 +380,15 @@ __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nr
         De[c] = 0.f;
       }
     }
-    s_own = s_next;
-    ++j;
+    const int m = nbR - j - 1;
+    for (int e = tid; e < m * m; e += blockDim.x) {
+      const int i = j + 1 + e % m, jj = j + 1 + e / m;
+      if (jj <= i) Sr[i * ldr + jj] = fmaf(-(Sr[i * ldr + j] * r1), Sr[jj * ldr + j], Sr[i * ldr + jj]);
+    }
     __syncthreads();
+    // candidates of column j+1 among the rows of R
+    if (tid >= j + 2 && tid < nbR && k0 + tid < w) consider(Sr[tid * ldr + j + 1], k0 + tid);
+    ++j;
   }
   if (blockIdx.x == 0 && tid == 0) {
     ctl->kb = j;
@@ -895,7 +878,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     int kb = 0, abort = 0, stop = 0;
     int ldw = nrow;
     int kb_want = std::min(nb, w - k0);
-    const bool fast = fast_enabled && maxG_fast > 0 && !use_general;
+    const bool fast = fast_enabled && !use_general && nrow - k0 - kb_want <= maxG_fast * FP_THREADS;
     if (cudaMemsetAsync(&ctl->pslot[0][0], 0, sizeof(ctl->pslot), st) != cudaSuccess) return NQG_ERR_CUDA;
     cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
     if (fast) {
