@@ -347,6 +347,8 @@ static int upload_plan(Plan &P) {
   if (const char *e = std::getenv("NASOQ_GB300_WIDE_NB")) P.wide_nb = std::min(64, std::max(4, std::atoi(e)));
   // supernodes of at most this width take the shared-memory BK kernel (<= 64)
   if (const char *e = std::getenv("NASOQ_GB300_BK_SMALL")) P.bk_small = std::min(64, std::max(1, std::atoi(e)));
+  // panels per delayed trailing update of the FP32 wide supernodes (1..4)
+  if (const char *e = std::getenv("NASOQ_GB300_WIDE_DEPTH")) P.wide_depth = std::min(4, std::max(1, std::atoi(e)));
   // =serial: the rows below the k_bk_global blocks are solved in that kernel
   if (const char *e = std::getenv("NASOQ_GB300_PANEL_ROWS")) P.panel_rows_serial = std::string(e) == "serial";
   // solve work split per level: small supernodes take one CTA each in the
@@ -425,7 +427,11 @@ static int upload_plan(Plan &P) {
     int64_t wide_rows = 0;
     for (int s = 0; s < ns; ++s)
       if (S.super[s + 1] - S.super[s] > P.wide_min) wide_rows = std::max<int64_t>(wide_rows, S.lpi[s + 1] - S.lpi[s]);
-    if (wide_rows > 0) NQG_CUDA(cudaMalloc(&P.d_wide_W, (size_t)wide_rows * (P.wide_nb + 2) * P.val_size()));
+    // W of up to wide_depth pending panels (each at most nb + 1 columns) plus
+    // the two working columns of the panel kernel
+    if (wide_rows > 0)
+      NQG_CUDA(cudaMalloc(&P.d_wide_W,
+                          (size_t)wide_rows * (P.wide_depth * (P.wide_nb + 1) + 2) * P.val_size()));
     // control block: grid barriers of the blocked factorization, abort flag
     // of the block solves
     NQG_CUDA(cudaMalloc(&P.d_wide_ctl, wide_ctl_bytes()));

@@ -143,8 +143,8 @@ __device__ __forceinline__ void store_row_split(unsigned char *hi_tile, unsigned
 // epilogue ep(r, c0, v) receives, for row r = threadIdx.x, the 32 product
 // values of columns [c0, c0 + 32).  smem_raw: smem_bytes(NSTAGE) of dynamic
 // shared memory (NSTAGE operand stages of 64 KB: with one stage three CTAs fit
-// on an SM, with two the next K chunk is staged while the MMAs run).  Called at most once per CTA (the TMEM allocation permit is
-// relinquished).  Returns false on a timeout (ST_TIMEOUT set in *status).
+// on an SM; the next K chunk is loaded into registers while the MMAs run).
+// Called at most once per CTA (the TMEM allocation permit is relinquished).  Returns false on a timeout (ST_TIMEOUT set in *status).
 template <int NSTAGE, class FA, class FB, class EP>
 __device__ bool tile_tf32x3(int kdim, FA fa, FB fb, EP ep, unsigned char *smem_raw, int *status) {
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -168,6 +168,13 @@ __device__ bool tile_tf32x3(int kdim, FA fa, FB fb, EP ep, unsigned char *smem_r
   const int nchunk = (kdim + TK - 1) / TK;
   int last_stage = -1;
   bool ok = true;
+  // operand rows of the next chunk are loaded into registers while the
+  // tensor cores work on the current one
+  float xa[TK], xb[TK];
+  if (nchunk > 0) {
+    fa(tid, 0, xa);
+    fb(tid, 0, xb);
+  }
   for (int ch = 0; ch < nchunk && ok; ++ch) {
     const int s = ch % NSTAGE;
     unsigned char *stg = base + s * STAGE_BYTES;
@@ -180,10 +187,6 @@ __device__ bool tile_tf32x3(int kdim, FA fa, FB fb, EP ep, unsigned char *smem_r
         break;
       }
     }
-    const int k0 = ch * TK;
-    float xa[TK], xb[TK];
-    fa(tid, k0, xa);
-    fb(tid, k0, xb);
     store_row_split(stg, stg + OPND_BYTES, tid, xa);
     store_row_split(stg + 2 * OPND_BYTES, stg + 3 * OPND_BYTES, tid, xb);
     fence_proxy_async();
@@ -204,6 +207,10 @@ __device__ bool tile_tf32x3(int kdim, FA fa, FB fb, EP ep, unsigned char *smem_r
     }
     ++uses[s];
     last_stage = s;
+    if (ch + 1 < nchunk) {
+      fa(tid, (ch + 1) * TK, xa);
+      fb(tid, (ch + 1) * TK, xb);
+    }
   }
   // wait for every issued MMA (bounded), then read the accumulator
   if (tid == 0) {

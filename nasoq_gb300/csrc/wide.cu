@@ -773,16 +773,17 @@ __global__ void __launch_bounds__(256, 2) k_wide_trailing_tc(float *S, int nrow,
 // accumulated in TMEM (tile_tf32x3, one operand stage so that three CTAs share
 // an SM), and a read-modify-write epilogue in which thread r owns row r of the
 // tile (coalesced along the factor's columns).
-__global__ void __launch_bounds__(t5::THREADS) k_wide_trailing_t5(float *S, int nrow, int w, int k0, int kb,
-                                                                  const float *Wb, int ldw, int tiles_n,
+// Columns [cbeg, w) (rows from cbeg, lower part) receive the update of the
+// kb factor columns starting at kL, whose W = L D columns are Wb[0..kb).
+__global__ void __launch_bounds__(t5::THREADS) k_wide_trailing_t5(float *S, int nrow, int kL, int kb, int cbeg,
+                                                                  int w, const float *Wb, int ldw, int tiles_n,
                                                                   int *status) {
   extern __shared__ __align__(1024) unsigned char t5_smem[];
-  const int k1 = k0 + kb;
   const int tn = blockIdx.x % tiles_n, tm = blockIdx.x / tiles_n;
-  const int col0 = k1 + tn * t5::TN;
-  const int row0 = k1 + tm * t5::TM;
+  const int col0 = cbeg + tn * t5::TN;
+  const int row0 = cbeg + tm * t5::TM;
   if (row0 + t5::TM - 1 < col0) return;  // tile strictly above the diagonal
-  const float *L21 = S + (size_t)k0 * nrow;
+  const float *L21 = S + (size_t)kL * nrow;
   auto fa = [&](int r, int k0c, float(&x)[t5::TK]) {
     const int gr = row0 + r;
 #pragma unroll
@@ -830,7 +831,7 @@ template <class T> __global__ void k_wide_zero_upper(T *S, int nrow, int w) {
 // launch count and the per-class timings.
 template <class T>
 static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideCtl *ctl, int *status,
-                    cudaStream_t st, int num_sms, int nb, int *pivoted, Plan *P) {
+                    cudaStream_t st, int num_sms, int nb, int *pivoted, Plan *P, int depth) {
   if (nb > WP_NB || nb < 1) return NQG_ERR_ARG;
   k_wide_init_perm<T><<<(w + 255) / 256, 256, 0, st>>>(perm, w);
   if (P) P->nlaunch++;
@@ -873,18 +874,62 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     maxG_fast = std::min(std::max(occf, 0) * num_sms, 1024);
   }
   bool use_general = false;  // the next panel starts at a column that needs a pivot search
+  // Delayed trailing updates (FP32 tcgen05 path): up to `depth` consecutive
+  // panels are pending, their W columns side by side in Wb, and one update of
+  // K = their total width flushes them to the columns beyond the frontier F.
+  // Invariant: columns < F carry the update of every pending panel, columns
+  // >= F of none.  Before a panel, the band [F, k0 + nb + 1) (every column the
+  // panel can factor, a final 2x2 included) is brought up to date; after it,
+  // the panel's own update covers [k1, F).  A panel on the general kernel may
+  // interchange rows and columns anywhere in the trailing block, so every
+  // pending update is flushed before it.
+  const bool delayed = sizeof(T) == 4 && trail == 2 && depth > 1;
+  int F = 0, pend_k0 = 0, pend_K = 0, npend = 0;
+  auto apply = [&](int kL, int K, int woff, int cb, int ce) -> int {
+    if (ce <= cb || K <= 0) return NQG_OK;
+    cudaEvent_t e1 = P ? P->prof_begin() : nullptr;
+    const int tm = (nrow - cb + t5::TM - 1) / t5::TM, tn = (ce - cb + t5::TN - 1) / t5::TN;
+    k_wide_trailing_t5<<<tm * tn, t5::THREADS, t5::smem_bytes(1), st>>>(
+        reinterpret_cast<float *>(S), nrow, kL, K, cb, ce, reinterpret_cast<const float *>(Wb) + (size_t)woff * nrow,
+        nrow, tn, status);
+    if (cudaGetLastError() != cudaSuccess) return NQG_ERR_CUDA;
+    if (P) {
+      P->nlaunch++;
+      const double cols = ce - cb;
+      const double entries = cols * (nrow - cb) - cols * (cols - 1) / 2.0;
+      P->prof_end(NQG_K_WIDE_TRAILING, e1, 2.0 * K * entries, 0.0);
+    }
+    return NQG_OK;
+  };
   int k0 = 0;
   while (k0 < w) {
     int kb = 0, abort = 0, stop = 0;
     int ldw = nrow;
     int kb_want = std::min(nb, w - k0);
     const bool fast = fast_enabled && !use_general && nrow - k0 - kb_want <= maxG_fast * FP_THREADS;
+    if (delayed) {
+      if (!fast && npend > 0) {
+        int rc = apply(pend_k0, pend_K, 0, F, w);
+        if (rc) return rc;
+        npend = 0;
+        pend_K = 0;
+        F = k0;
+      }
+      const int bend = std::min(w, k0 + nb + 1);
+      if (npend > 0 && F < bend) {
+        int rc = apply(pend_k0, pend_K, 0, F, bend);
+        if (rc) return rc;
+      }
+      F = std::max(F, bend);
+    }
+    const int woff = delayed ? pend_K : 0;  // this panel's W columns
+    T *Wp = Wb + (size_t)woff * nrow;
     if (cudaMemsetAsync(&ctl->pslot[0][0], 0, sizeof(ctl->pslot), st) != cudaSuccess) return NQG_ERR_CUDA;
     cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
     if (fast) {
       const int rows_out = nrow - k0 - kb_want;
       const int G = std::max(1, std::min(maxG_fast, (rows_out + FP_THREADS - 1) / FP_THREADS));
-      float *Sf = reinterpret_cast<float *>(S), *Wf = reinterpret_cast<float *>(Wb);
+      float *Sf = reinterpret_cast<float *>(S), *Wf = reinterpret_cast<float *>(Wp);
       float *Df = reinterpret_cast<float *>(Dd), *Ef = reinterpret_cast<float *>(De);
       void *args[] = {&Sf, &nrow, &w, &k0, &kb_want, &Wf, &ldw, &Df, &Ef, &ctl, &status};
       if (cudaLaunchCooperativeKernel((void *)k_wide_panel_fast, dim3(G), dim3(FP_THREADS), args, fsmem, st) !=
@@ -894,7 +939,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       // one row per thread where the grid allows it
       const int rows_left = nrow - k0;
       const int G = std::max(1, std::min(maxG, (rows_left + WP_THREADS - 1) / WP_THREADS));
-      void *args[] = {&S, &nrow, &w, &k0, &kb_want, &Wb, &ldw, &Dd, &De, &perm, &ctl, &status};
+      void *args[] = {&S, &nrow, &w, &k0, &kb_want, &Wp, &ldw, &Dd, &De, &perm, &ctl, &status};
       if (cudaLaunchCooperativeKernel((void *)k_wide_panel<T>, dim3(G), dim3(WP_THREADS), args, smem, st) !=
           cudaSuccess)
         return NQG_ERR_CUDA;
@@ -924,12 +969,25 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       for (int jj = 0; jj < kb; ++jj) fl += 2.0 * (nrow - (k0 + jj)) * (jj + 1);
       P->prof_end(NQG_K_WIDE_PANEL, e0, fl, 0.0);
     }
-    if (k1 < w) {
+    if (delayed) {
+      int rc = k1 < F ? apply(k0, kb, woff, k1, F) : NQG_OK;
+      if (rc) return rc;
+      if (npend == 0) pend_k0 = k0;
+      pend_K += kb;
+      ++npend;
+      if (npend == depth || k1 >= w) {
+        if ((rc = apply(pend_k0, pend_K, 0, F, w))) return rc;
+        npend = 0;
+        pend_K = 0;
+        F = k1;
+      }
+    } else if (k1 < w) {
       cudaEvent_t e1 = P ? P->prof_begin() : nullptr;
       if (sizeof(T) == 4 && trail == 2) {
         int tm = (nrow - k1 + t5::TM - 1) / t5::TM, tn = (w - k1 + t5::TN - 1) / t5::TN;
         k_wide_trailing_t5<<<tm * tn, t5::THREADS, t5::smem_bytes(1), st>>>(
-            reinterpret_cast<float *>(S), nrow, w, k0, kb, reinterpret_cast<const float *>(Wb), nrow, tn, status);
+            reinterpret_cast<float *>(S), nrow, k0, kb, k1, w, reinterpret_cast<const float *>(Wb), nrow, tn,
+            status);
       } else if (sizeof(T) == 4 && trail == 1) {
         int tm = (nrow - k1 + TC_BM - 1) / TC_BM, tn = (w - k1 + TC_BN - 1) / TC_BN;
         k_wide_trailing_tc<<<tm * tn, 256, TC_SMEM, st>>>(reinterpret_cast<float *>(S), nrow, w, k0, kb,
@@ -972,7 +1030,7 @@ int factor_wide(Plan &P, int s, T *L, T *Dg, int nb, T *Wb, WideCtl *ctl, int nu
   const int nrow = (int)(P.sym.lpi[s + 1] - P.sym.lpi[s]);
   int piv = 0;
   int rc = run_wide<T>(L + P.sym.lpx[s], nrow, w, Dg + c0, Dg + P.n + c0, P.d_locperm + c0, Wb, ctl, P.d_status,
-                       P.stream, num_sms, nb, &piv, &P);
+                       P.stream, num_sms, nb, &piv, &P, P.wide_depth);
   if (rc == NQG_ERR_CUDA) {
     cudaError_t e = cudaGetLastError();
     P.last_error = cudaGetErrorString(e);
@@ -992,7 +1050,7 @@ size_t wide_ctl_bytes() { return sizeof(WideCtl); }
 template <class T>
 int factor_wide_raw(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideCtl *ctl, int *status,
                     cudaStream_t st, int num_sms, int nb, int *pivoted) {
-  return run_wide<T>(S, nrow, w, Dd, De, perm, Wb, ctl, status, st, num_sms, nb, pivoted, nullptr);
+  return run_wide<T>(S, nrow, w, Dd, De, perm, Wb, ctl, status, st, num_sms, nb, pivoted, nullptr, 1);
 }
 
 template int factor_wide_raw<double>(double *, int, int, double *, double *, int *, double *, WideCtl *, int *,

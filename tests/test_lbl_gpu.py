@@ -211,18 +211,22 @@ def test_fp64_blocked_wide_kernels(path, monkeypatch):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("trailing", ["tcgen05", "mma", "simt", "general-panels"])
+@pytest.mark.parametrize("trailing", ["tcgen05", "tcgen05-depth1", "tcgen05-depth4", "mma", "simt",
+                                      "general-panels"])
 @pytest.mark.parametrize("path", CASES, ids=os.path.basename)
 def test_fp32_blocked_wide_kernels(path, trailing, monkeypatch):
     """FP32 factor with every supernode wider than 12 columns in the blocked
     kernels (fast panels where no pivot search is needed, or every panel on
-    the general kernel), trailing updates on the tcgen05 tensor cores or with
-    mma.sync (both split TF32) or on CUDA cores:
+    the general kernel), trailing updates on the tcgen05 tensor cores (one,
+    two or four panels per delayed update) or with mma.sync (both split TF32)
+    or on CUDA cores:
     the refined solution meets the FP32 bar of the single-CTA kernels."""
     for k, v in WIDE_ENV.items():
         monkeypatch.setenv(k, v)
     if trailing == "general-panels":
         monkeypatch.setenv("NASOQ_GB300_PANEL", "general")
+    elif trailing.startswith("tcgen05-depth"):
+        monkeypatch.setenv("NASOQ_GB300_WIDE_DEPTH", trailing[-1])
     else:
         monkeypatch.setenv("NASOQ_GB300_TRAILING", trailing)
     d = nqa.load(path)
