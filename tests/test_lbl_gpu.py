@@ -211,7 +211,7 @@ def test_fp64_blocked_wide_kernels(path, monkeypatch):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("trailing", ["tcgen05", "tcgen05-depth1", "tcgen05-depth4", "mma", "simt",
+@pytest.mark.parametrize("trailing", ["tcgen05", "tcgen05-depth1", "tcgen05-depth2", "mma", "simt",
                                       "general-panels"])
 @pytest.mark.parametrize("path", CASES, ids=os.path.basename)
 def test_fp32_blocked_wide_kernels(path, trailing, monkeypatch):
