@@ -14,7 +14,9 @@ struct WideCtl {
   int kb;          // columns completed by the last panel launch
   int pivoted;     // any interchange in this supernode
   int stop;        // the fast panel stopped where a pivot search is needed
-  int pad[2];
+  int halt;        // a speculative fast panel stopped early: later queued kernels skip
+  int pad;
+  int kb_log[16];  // columns done by each fast panel of a speculative batch
   double cval[2][1024];
   int cidx[2][1024];
   double rval[2][1024];

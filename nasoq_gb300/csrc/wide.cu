@@ -308,10 +308,14 @@ __host__ __device__ constexpr size_t fast_panel_smem(int nb) {
 // pivot candidates are ready without a dot product.  Each entry receives the
 // same FMAs in the same order as the general kernel's left-looking update.
 // Requires at most one owned row per thread (nrow - k0 - nbR <= threads).
+// slot >= 0: one panel of a speculative batch -- kb goes to ctl->kb_log[slot]
+// and an early stop sets ctl->halt, which makes every kernel queued after it
+// return without work (the host replays from this panel).
 __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nrow, int w, int k0, int nb,
                                                                 float *Wb, int ldw, float *Dd, float *De,
-                                                                WideCtl *ctl, int *status) {
+                                                                WideCtl *ctl, int slot, int *status) {
   extern __shared__ __align__(16) unsigned char fp_raw[];
+  if (*(volatile int *)&ctl->halt) return;  // queued behind a fast panel that stopped early
   const int nbR = min(nb, w - k0);  // panel columns = rows of R
   const int ldr = nbR + 1;
   float *sr = reinterpret_cast<float *>(fp_raw);  // [nbR][FP_THREADS]: the thread's row, panel columns
@@ -393,6 +397,10 @@ __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nr
   if (blockIdx.x == 0 && tid == 0) {
     ctl->kb = j;
     ctl->stop = stop ? 1 : 0;
+    if (slot >= 0) {
+      ctl->kb_log[slot] = j;
+      if (stop) ctl->halt = 1;
+    }
   }
 }
 
@@ -777,8 +785,9 @@ __global__ void __launch_bounds__(256, 2) k_wide_trailing_tc(float *S, int nrow,
 // kb factor columns starting at kL, whose W = L D columns are Wb[0..kb).
 __global__ void __launch_bounds__(t5::THREADS) k_wide_trailing_t5(float *S, int nrow, int kL, int kb, int cbeg,
                                                                   int w, const float *Wb, int ldw, int tiles_n,
-                                                                  int *status) {
+                                                                  const int *halt, int *status) {
   extern __shared__ __align__(1024) unsigned char t5_smem[];
+  if (*(volatile const int *)halt) return;  // queued behind a fast panel that stopped early
   const int tn = blockIdx.x % tiles_n, tm = blockIdx.x / tiles_n;
   const int col0 = cbeg + tn * t5::TN;
   const int row0 = cbeg + tm * t5::TM;
@@ -883,15 +892,34 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   // the panel's own update covers [k1, F).  A panel on the general kernel may
   // interchange rows and columns anywhere in the trailing block, so every
   // pending update is flushed before it.
+  //
+  // Speculation (FP32 tcgen05 path): fast panels are queued assuming they
+  // factor all their columns, up to SPEC_MAX per host synchronisation, with
+  // the updates that follow from that assumption.  A fast panel that stops
+  // early sets ctl->halt and every kernel queued after it returns untouched;
+  // at the next synchronisation the host restores the state it saved before
+  // that panel's updates and replays them with the real column count.
   const bool delayed = sizeof(T) == 4 && trail == 2 && depth > 1;
-  int F = 0, pend_k0 = 0, pend_K = 0, npend = 0;
+  const bool spec_ok = fast_enabled && trail == 2;
+  constexpr int SPEC_MAX = 16;
+  struct State {
+    int k0, F, pend_k0, pend_K, npend;
+  };
+  struct Spec {
+    State st;  // state after the panel's band update, before the panel
+    int kb, woff;
+  };
+  State cs{0, 0, 0, 0, 0};
+  std::vector<Spec> specs;
+  int spec_limit = SPEC_MAX;  // batch size: 1 after a rewind, doubling after each clean batch
+  const int *halt = &ctl->halt;
   auto apply = [&](int kL, int K, int woff, int cb, int ce) -> int {
     if (ce <= cb || K <= 0) return NQG_OK;
     cudaEvent_t e1 = P ? P->prof_begin() : nullptr;
     const int tm = (nrow - cb + t5::TM - 1) / t5::TM, tn = (ce - cb + t5::TN - 1) / t5::TN;
     k_wide_trailing_t5<<<tm * tn, t5::THREADS, t5::smem_bytes(1), st>>>(
         reinterpret_cast<float *>(S), nrow, kL, K, cb, ce, reinterpret_cast<const float *>(Wb) + (size_t)woff * nrow,
-        nrow, tn, status);
+        nrow, tn, halt, status);
     if (cudaGetLastError() != cudaSuccess) return NQG_ERR_CUDA;
     if (P) {
       P->nlaunch++;
@@ -901,92 +929,42 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     }
     return NQG_OK;
   };
-  int k0 = 0;
-  while (k0 < w) {
-    int kb = 0, abort = 0, stop = 0;
-    int ldw = nrow;
-    int kb_want = std::min(nb, w - k0);
-    const bool fast = fast_enabled && !use_general && nrow - k0 - kb_want <= maxG_fast * FP_THREADS;
+  // band update before a panel at s.k0 (flushing everything before a general one)
+  auto pre = [&](State &s, bool general) -> int {
+    if (!delayed) return NQG_OK;
+    int rc;
+    if (general && s.npend > 0) {
+      if ((rc = apply(s.pend_k0, s.pend_K, 0, s.F, w))) return rc;
+      s.npend = 0;
+      s.pend_K = 0;
+      s.F = s.k0;
+    }
+    const int bend = std::min(w, s.k0 + nb + 1);
+    if (s.npend > 0 && s.F < bend && (rc = apply(s.pend_k0, s.pend_K, 0, s.F, bend))) return rc;
+    s.F = std::max(s.F, bend);
+    return NQG_OK;
+  };
+  // updates after a panel of kb columns at s.k0 whose W starts at column woff
+  auto post = [&](State &s, int kb, int woff) -> int {
+    const int k0 = s.k0, k1 = k0 + kb;
+    int rc;
     if (delayed) {
-      if (!fast && npend > 0) {
-        int rc = apply(pend_k0, pend_K, 0, F, w);
-        if (rc) return rc;
-        npend = 0;
-        pend_K = 0;
-        F = k0;
-      }
-      const int bend = std::min(w, k0 + nb + 1);
-      if (npend > 0 && F < bend) {
-        int rc = apply(pend_k0, pend_K, 0, F, bend);
-        if (rc) return rc;
-      }
-      F = std::max(F, bend);
-    }
-    const int woff = delayed ? pend_K : 0;  // this panel's W columns
-    T *Wp = Wb + (size_t)woff * nrow;
-    if (cudaMemsetAsync(&ctl->pslot[0][0], 0, sizeof(ctl->pslot), st) != cudaSuccess) return NQG_ERR_CUDA;
-    cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
-    if (fast) {
-      const int rows_out = nrow - k0 - kb_want;
-      const int G = std::max(1, std::min(maxG_fast, (rows_out + FP_THREADS - 1) / FP_THREADS));
-      float *Sf = reinterpret_cast<float *>(S), *Wf = reinterpret_cast<float *>(Wp);
-      float *Df = reinterpret_cast<float *>(Dd), *Ef = reinterpret_cast<float *>(De);
-      void *args[] = {&Sf, &nrow, &w, &k0, &kb_want, &Wf, &ldw, &Df, &Ef, &ctl, &status};
-      if (cudaLaunchCooperativeKernel((void *)k_wide_panel_fast, dim3(G), dim3(FP_THREADS), args, fsmem, st) !=
-          cudaSuccess)
-        return NQG_ERR_CUDA;
-    } else {
-      // one row per thread where the grid allows it
-      const int rows_left = nrow - k0;
-      const int G = std::max(1, std::min(maxG, (rows_left + WP_THREADS - 1) / WP_THREADS));
-      void *args[] = {&S, &nrow, &w, &k0, &kb_want, &Wp, &ldw, &Dd, &De, &perm, &ctl, &status};
-      if (cudaLaunchCooperativeKernel((void *)k_wide_panel<T>, dim3(G), dim3(WP_THREADS), args, smem, st) !=
-          cudaSuccess)
-        return NQG_ERR_CUDA;
-    }
-    if (P) P->nlaunch++;
-    if (cudaMemcpyAsync(&kb, &ctl->kb, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaMemcpyAsync(&abort, &ctl->abort, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaMemcpyAsync(&stop, &ctl->stop, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-      return NQG_ERR_CUDA;
-    if (abort) return NQG_ERR_TIMEOUT;
-    if (fast) {
-      use_general = stop != 0;
-      if (kb <= 0) {
-        if (!use_general) return NQG_ERR_TIMEOUT;
-        if (P) P->prof_end(NQG_K_WIDE_PANEL, e0, 0.0, 0.0);
-        continue;  // the first column already needs the general kernel
-      }
-    } else {
-      use_general = false;
-      if (kb <= 0) return NQG_ERR_TIMEOUT;
-    }
-    const int k1 = k0 + kb;
-    if (P) {
-      // panel: column GEMVs (2 * rows * j) and the L column scaling
-      double fl = 0;
-      for (int jj = 0; jj < kb; ++jj) fl += 2.0 * (nrow - (k0 + jj)) * (jj + 1);
-      P->prof_end(NQG_K_WIDE_PANEL, e0, fl, 0.0);
-    }
-    if (delayed) {
-      int rc = k1 < F ? apply(k0, kb, woff, k1, F) : NQG_OK;
-      if (rc) return rc;
-      if (npend == 0) pend_k0 = k0;
-      pend_K += kb;
-      ++npend;
-      if (npend == depth || k1 >= w) {
-        if ((rc = apply(pend_k0, pend_K, 0, F, w))) return rc;
-        npend = 0;
-        pend_K = 0;
-        F = k1;
+      if (k1 < s.F && (rc = apply(k0, kb, woff, k1, s.F))) return rc;
+      if (s.npend == 0) s.pend_k0 = k0;
+      s.pend_K += kb;
+      ++s.npend;
+      if (s.npend == depth || k1 >= w) {
+        if ((rc = apply(s.pend_k0, s.pend_K, 0, s.F, w))) return rc;
+        s.npend = 0;
+        s.pend_K = 0;
+        s.F = k1;
       }
     } else if (k1 < w) {
       cudaEvent_t e1 = P ? P->prof_begin() : nullptr;
       if (sizeof(T) == 4 && trail == 2) {
         int tm = (nrow - k1 + t5::TM - 1) / t5::TM, tn = (w - k1 + t5::TN - 1) / t5::TN;
         k_wide_trailing_t5<<<tm * tn, t5::THREADS, t5::smem_bytes(1), st>>>(
-            reinterpret_cast<float *>(S), nrow, k0, kb, k1, w, reinterpret_cast<const float *>(Wb), nrow, tn,
+            reinterpret_cast<float *>(S), nrow, k0, kb, k1, w, reinterpret_cast<const float *>(Wb), nrow, tn, halt,
             status);
       } else if (sizeof(T) == 4 && trail == 1) {
         int tm = (nrow - k1 + TC_BM - 1) / TC_BM, tn = (w - k1 + TC_BN - 1) / TC_BN;
@@ -1010,7 +988,116 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
         P->prof_end(NQG_K_WIDE_TRAILING, e1, 2.0 * kb * entries, 0.0);
       }
     }
-    k0 = k1;
+    s.k0 = k1;
+    return NQG_OK;
+  };
+  auto panel_flops = [&](int k0, int kb) {
+    double fl = 0;  // column GEMVs (2 * rows * j) and the L column scaling
+    for (int jj = 0; jj < kb; ++jj) fl += 2.0 * (nrow - (k0 + jj)) * (jj + 1);
+    return fl;
+  };
+  auto launch_fast = [&](int k0, int kb_want, T *Wp, int slot) -> int {
+    const int rows_out = nrow - k0 - kb_want;
+    const int G = std::max(1, std::min(maxG_fast, (rows_out + FP_THREADS - 1) / FP_THREADS));
+    int ldw = nrow;
+    float *Sf = reinterpret_cast<float *>(S), *Wf = reinterpret_cast<float *>(Wp);
+    float *Df = reinterpret_cast<float *>(Dd), *Ef = reinterpret_cast<float *>(De);
+    void *args[] = {&Sf, &nrow, &w, &k0, &kb_want, &Wf, &ldw, &Df, &Ef, &ctl, &slot, &status};
+    if (cudaMemsetAsync(&ctl->pslot[0][0], 0, sizeof(ctl->pslot), st) != cudaSuccess) return NQG_ERR_CUDA;
+    cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
+    if (cudaLaunchCooperativeKernel((void *)k_wide_panel_fast, dim3(G), dim3(FP_THREADS), args, fsmem, st) !=
+        cudaSuccess)
+      return NQG_ERR_CUDA;
+    if (P) {
+      P->nlaunch++;
+      P->prof_end(NQG_K_WIDE_PANEL, e0, panel_flops(k0, kb_want), 0.0);
+    }
+    return NQG_OK;
+  };
+  // synchronise with a speculative batch; replay from its first short panel
+  auto resolve = [&]() -> int {
+    if (specs.empty()) return NQG_OK;
+    const int n = (int)specs.size();
+    int kbs[SPEC_MAX] = {}, abort = 0;
+    if (cudaMemcpyAsync(kbs, ctl->kb_log, n * sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&abort, &ctl->abort, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return NQG_ERR_CUDA;
+    if (abort) return NQG_ERR_TIMEOUT;
+    int i = 0;
+    while (i < n && kbs[i] == specs[i].kb) ++i;
+    if (i < n) {
+      if (cudaMemsetAsync(&ctl->halt, 0, sizeof(int), st) != cudaSuccess) return NQG_ERR_CUDA;
+      cs = specs[i].st;
+      if (kbs[i] > 0) {
+        int rc = post(cs, kbs[i], specs[i].woff);
+        if (rc) return rc;
+      }
+      use_general = true;  // the column after the short panel needs a pivot search
+      spec_limit = 1;
+    } else {
+      spec_limit = std::min(SPEC_MAX, 2 * spec_limit);
+    }
+    specs.clear();
+    return NQG_OK;
+  };
+  while (cs.k0 < w) {
+    const int kb_want = std::min(nb, w - cs.k0);
+    const bool fast = fast_enabled && !use_general && nrow - cs.k0 - kb_want <= maxG_fast * FP_THREADS;
+    if (fast && spec_ok) {
+      int rc = pre(cs, false);
+      if (rc) return rc;
+      const int woff = delayed ? cs.pend_K : 0;
+      specs.push_back(Spec{cs, kb_want, woff});
+      if ((rc = launch_fast(cs.k0, kb_want, Wb + (size_t)woff * nrow, (int)specs.size() - 1))) return rc;
+      if ((rc = post(cs, kb_want, woff))) return rc;
+      if (((int)specs.size() >= spec_limit || cs.k0 >= w) && (rc = resolve())) return rc;
+      continue;
+    }
+    if (!specs.empty()) {
+      int rc = resolve();
+      if (rc) return rc;
+      continue;  // the state may have been rewound
+    }
+    int rc = pre(cs, !fast);
+    if (rc) return rc;
+    const int woff = delayed ? cs.pend_K : 0;  // this panel's W columns
+    T *Wp = Wb + (size_t)woff * nrow;
+    int kb = 0, abort = 0, stop = 0, ldw = nrow, kbw = kb_want, k0 = cs.k0;
+    if (fast) {
+      if ((rc = launch_fast(k0, kb_want, Wp, -1))) return rc;
+    } else {
+      if (cudaMemsetAsync(&ctl->pslot[0][0], 0, sizeof(ctl->pslot), st) != cudaSuccess) return NQG_ERR_CUDA;
+      cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
+      // one row per thread where the grid allows it
+      const int rows_left = nrow - k0;
+      const int G = std::max(1, std::min(maxG, (rows_left + WP_THREADS - 1) / WP_THREADS));
+      void *args[] = {&S, &nrow, &w, &k0, &kbw, &Wp, &ldw, &Dd, &De, &perm, &ctl, &status};
+      if (cudaLaunchCooperativeKernel((void *)k_wide_panel<T>, dim3(G), dim3(WP_THREADS), args, smem, st) !=
+          cudaSuccess)
+        return NQG_ERR_CUDA;
+      if (P) {
+        P->nlaunch++;
+        P->prof_end(NQG_K_WIDE_PANEL, e0, panel_flops(k0, kb_want), 0.0);
+      }
+    }
+    if (cudaMemcpyAsync(&kb, &ctl->kb, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&abort, &ctl->abort, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&stop, &ctl->stop, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return NQG_ERR_CUDA;
+    if (abort) return NQG_ERR_TIMEOUT;
+    if (fast) {
+      use_general = stop != 0;
+      if (kb <= 0) {
+        if (!use_general) return NQG_ERR_TIMEOUT;
+        continue;  // the first column already needs the general kernel
+      }
+    } else {
+      use_general = false;
+      if (kb <= 0) return NQG_ERR_TIMEOUT;
+    }
+    if ((rc = post(cs, kb, woff))) return rc;
   }
   k_wide_zero_upper<T><<<std::min(w, 1024), 128, 0, st>>>(S, nrow, w);
   if (P) P->nlaunch++;
