@@ -227,6 +227,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
                                                         int *status) {
   __shared__ V Td[TB * TB];
   __shared__ V red[2][TB];
+  __shared__ V redS[sizeof(V) == 4 ? TB * (TB + 1) : 1];  // FP32: column sums through a transpose
   __shared__ V yb[TB];
   __shared__ int s_front;
   const int t = threadIdx.x, r = t & (TB - 1), cg = t / TB, lane = t & 31;
@@ -256,8 +257,23 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
     V part[CPT];
 #pragma unroll
     for (int cc = 0; cc < CPT; ++cc) part[cc] = V(0);
-    // rows below the diagonal block: x known from the ancestors
-    for (int row = w + r; row < nrow; row += TB) {
+    // rows below the diagonal block: x known from the ancestors; four rows
+    // per step so that their index and value loads are in flight together
+    int row = w + r;
+    for (; row + 3 * TB < nrow; row += 4 * TB) {
+      const int i0 = rows[row], i1 = rows[row + TB], i2 = rows[row + 2 * TB], i3 = rows[row + 3 * TB];
+      const V x0 = __ldcg(x + i0), x1 = __ldcg(x + i1), x2 = __ldcg(x + i2), x3 = __ldcg(x + i3);
+#pragma unroll
+      for (int cc = 0; cc < CPT; ++cc)
+        if (cok[cc]) {
+          const T *lp = Lc + row + (size_t)cc * nrow;
+          part[cc] += V(lp[0]) * x0;
+          part[cc] += V(lp[TB]) * x1;
+          part[cc] += V(lp[2 * TB]) * x2;
+          part[cc] += V(lp[3 * TB]) * x3;
+        }
+    }
+    for (; row < nrow; row += TB) {
       const V xv = __ldcg(x + rows[row]);
 #pragma unroll
       for (int cc = 0; cc < CPT; ++cc)
@@ -292,16 +308,36 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
 #pragma unroll
       for (int cc = 0; cc < CPT; ++cc) v[cc] = vn[cc];
     }
-    // column sums over the 64 rows: warps 2cg and 2cg+1 hold rows 0-31, 32-63
+    // column sums over the 64 rows
+    if constexpr (sizeof(V) == 4) {
+      // transpose through shared memory, then one thread per column
 #pragma unroll
-    for (int cc = 0; cc < CPT; ++cc) {
-      V a = part[cc];
+      for (int cc = 0; cc < CPT; ++cc) redS[(cg * CPT + cc) * (TB + 1) + r] = part[cc];
+      __syncthreads();
+      if (t < nc) {
+        const V *col = redS + t * (TB + 1);
+        V a0 = V(0), a1 = V(0), a2 = V(0), a3 = V(0);
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-      if (lane == 0) red[(t >> 5) & 1][cg * CPT + cc] = a;
+        for (int k = 0; k < TB; k += 4) {
+          a0 += col[k];
+          a1 += col[k + 1];
+          a2 += col[k + 2];
+          a3 += col[k + 3];
+        }
+        yb[t] = __ldcg(xs + b0 + t) - ((a0 + a1) + (a2 + a3));
+      }
+    } else {
+      // warps 2cg and 2cg+1 hold rows 0-31, 32-63
+#pragma unroll
+      for (int cc = 0; cc < CPT; ++cc) {
+        V a = part[cc];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) red[(t >> 5) & 1][cg * CPT + cc] = a;
+      }
+      __syncthreads();
+      if (t < nc) yb[t] = __ldcg(xs + b0 + t) - (red[0][t] + red[1][t]);
     }
-    __syncthreads();
-    if (t < nc) yb[t] = __ldcg(xs + b0 + t) - (red[0][t] + red[1][t]);
     __syncthreads();
     if (t < 32) warp_trsv_lower_t(Td, nc, yb);
     __syncthreads();
