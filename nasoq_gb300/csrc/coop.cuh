@@ -24,6 +24,8 @@ struct WideCtl {
   // panel exchanges: per CTA and parity, (candidate << 8) | epoch; cleared
   // before every panel launch
   unsigned long long pslot[2][1024];
+  // fast panels: up to four candidate words per CTA and exchange
+  unsigned long long mslot[2][4][1024];
 };
 
 constexpr long long SPIN_LIMIT = 1ll << 26;  // polls before a barrier gives up

@@ -298,6 +298,65 @@ __device__ bool grid_max_nofence(WideCtl *ctl, unsigned &epoch, unsigned long lo
   return s_ok != 0;
 }
 
+// Exchange of g <= FP_COLS candidate words per CTA at once (columns j ..
+// j+g-1 of a fast panel); best[q] = maximum over the CTAs of word q.
+constexpr int FP_COLS = 4;
+__device__ bool grid_max_multi(WideCtl *ctl, unsigned &epoch, const unsigned long long (&cand)[FP_COLS], int g,
+                               int *status, unsigned long long (&best)[FP_COLS]) {
+  __shared__ unsigned long long s_best[FP_COLS];
+  __shared__ int s_ok;
+  ++epoch;
+  const unsigned e = epoch & 0xFFu;
+  const int par = epoch & 1;
+  const int G = (int)gridDim.x;
+  if (threadIdx.x < g) *(volatile unsigned long long *)&ctl->mslot[par][threadIdx.x][blockIdx.x] = (cand[threadIdx.x] << 8) | e;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    long long it = 0;
+    int ok = 1;
+    unsigned long long m[FP_COLS];
+    while (true) {
+      bool all = true;
+#pragma unroll
+      for (int q = 0; q < FP_COLS; ++q) {
+        m[q] = 0;
+        if (q < g)
+          for (int b = lane; b < G; b += 32) {
+            const unsigned long long v = *(volatile unsigned long long *)&ctl->mslot[par][q][b];
+            if ((unsigned)(v & 0xFFu) != e) all = false;
+            else m[q] = max(m[q], v >> 8);
+          }
+      }
+      if (__all_sync(0xffffffffu, all)) break;
+      int ab = lane == 0 ? *(volatile int *)&ctl->abort : 0;
+      ab = __shfl_sync(0xffffffffu, ab, 0);
+      if (ab) {
+        ok = 0;
+        break;
+      }
+      if (++it > SPIN_LIMIT) {
+        if (lane == 0) {
+          atomicOr(status, ST_TIMEOUT);
+          atomicExch(&ctl->abort, 1);
+        }
+        ok = 0;
+        break;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < FP_COLS; ++q) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) m[q] = max(m[q], __shfl_xor_sync(0xffffffffu, m[q], o));
+      if (lane == 0) s_best[q] = m[q];
+    }
+    if (lane == 0) s_ok = ok;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < FP_COLS; ++q) best[q] = s_best[q];
+  return s_ok != 0;
+}
+
 __host__ __device__ constexpr size_t fast_panel_smem(int nb) {
   return ((size_t)nb * FP_THREADS + (size_t)nb * (nb + 1)) * sizeof(float);
 }
@@ -308,6 +367,13 @@ __host__ __device__ constexpr size_t fast_panel_smem(int nb) {
 // pivot candidates are ready without a dot product.  Each entry receives the
 // same FMAs in the same order as the general kernel's left-looking update.
 // Requires at most one owned row per thread (nrow - k0 - nbR <= threads).
+// Columns go FP_COLS at a time through one exchange: the pivot W(c, c) is
+// local, so every CTA can run the next columns' updates and candidate
+// searches on the assumption that the earlier ones keep their diagonal
+// pivots, and the exchange then returns all their column maxima.  The
+// longest prefix that passes the test is kept; the global writes of a column
+// (L, W, D) happen only once it is kept, so a stop leaves the later columns
+// untouched for the general kernel.
 // slot >= 0: one panel of a speculative batch -- kb goes to ctl->kb_log[slot]
 // and an early stop sets ctl->halt, which makes every kernel queued after it
 // return without work (the host replays from this panel).
@@ -344,39 +410,41 @@ __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nr
   };
   if (own && r_own < w) consider(sr[tid], r_own);
   if (tid >= 1 && tid < nbR && k0 + tid < w) consider(Sr[tid * ldr], k0 + tid);
-  unsigned epoch = 0;
-  int j = 0;
-  bool stop = false;
-  while (j < nbR) {
-    const int c = k0 + j;
-    const unsigned long long cand = cta_max_key(hi, lo);
-    unsigned long long best;
-    if (!grid_max_nofence(ctl, epoch, cand, status, best)) return;
-    const float colmax = (float)__uint_as_float((unsigned)(best >> 24));
-    const float d = Sr[j * ldr + j];
-    const float absakk = fabsf(d);
-    if (!(absakk >= alpha * colmax) || absakk == 0.f) {
-      stop = true;  // pivot search, zero or NaN pivot: the general kernel takes column c
-      break;
-    }
-    const float r1 = 1.f / d;
+  // right-looking update of local column jc (shared memory only), then the
+  // candidates of column jc + 1
+  auto step = [&](int jc) {
+    const float r1 = 1.f / Sr[jc * ldr + jc];
     hi = 0u;
     lo = 0u;
-    // the thread's row: L(r, c), then the rank-1 term on the later columns
     if (own) {
-      const float wv = sr[j * FP_THREADS + tid];
-      const float l = wv * r1;
-      Wb[(size_t)j * ldw + r_own] = wv;
-      S[r_own + (size_t)c * nrow] = l;
-      for (int jj = j + 1; jj < nbR; ++jj)
-        sr[jj * FP_THREADS + tid] = fmaf(-l, Sr[jj * ldr + j], sr[jj * FP_THREADS + tid]);
-      if (j + 1 < nbR && r_own < w) consider(sr[(j + 1) * FP_THREADS + tid], r_own);
+      const float l = sr[jc * FP_THREADS + tid] * r1;
+      for (int jj = jc + 1; jj < nbR; ++jj)
+        sr[jj * FP_THREADS + tid] = fmaf(-l, Sr[jj * ldr + jc], sr[jj * FP_THREADS + tid]);
+      if (jc + 1 < nbR && r_own < w) consider(sr[(jc + 1) * FP_THREADS + tid], r_own);
     }
-    // rows of R: global copies (CTA 0), then the rank-1 term on the trailing block
+    const int m = nbR - jc - 1;
+    for (int e = tid; e < m * m; e += blockDim.x) {
+      const int i = jc + 1 + e % m, jj = jc + 1 + e / m;
+      if (jj <= i) Sr[i * ldr + jj] = fmaf(-(Sr[i * ldr + jc] * r1), Sr[jj * ldr + jc], Sr[i * ldr + jj]);
+    }
+    __syncthreads();
+    if (tid >= jc + 2 && tid < nbR && k0 + tid < w) consider(Sr[tid * ldr + jc + 1], k0 + tid);
+  };
+  // global writes of kept column jc: L and W of the thread's row, and (CTA 0)
+  // of the rows of R, the unit diagonal and D
+  auto commit = [&](int jc) {
+    const int c = k0 + jc;
+    const float d = Sr[jc * ldr + jc];
+    const float r1 = 1.f / d;
+    if (own) {
+      const float wv = sr[jc * FP_THREADS + tid];
+      Wb[(size_t)jc * ldw + r_own] = wv;
+      S[r_own + (size_t)c * nrow] = wv * r1;
+    }
     if (blockIdx.x == 0) {
-      for (int i = j + tid; i < nbR; i += blockDim.x) {
-        Wb[(size_t)j * ldw + k0 + i] = Sr[i * ldr + j];
-        if (i > j) S[(k0 + i) + (size_t)c * nrow] = Sr[i * ldr + j] * r1;
+      for (int i = jc + tid; i < nbR; i += blockDim.x) {
+        Wb[(size_t)jc * ldw + k0 + i] = Sr[i * ldr + jc];
+        if (i > jc) S[(k0 + i) + (size_t)c * nrow] = Sr[i * ldr + jc] * r1;
       }
       if (tid == 0) {
         S[c + (size_t)c * nrow] = 1.f;
@@ -384,15 +452,34 @@ __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nr
         De[c] = 0.f;
       }
     }
-    const int m = nbR - j - 1;
-    for (int e = tid; e < m * m; e += blockDim.x) {
-      const int i = j + 1 + e % m, jj = j + 1 + e / m;
-      if (jj <= i) Sr[i * ldr + jj] = fmaf(-(Sr[i * ldr + j] * r1), Sr[jj * ldr + j], Sr[i * ldr + jj]);
+  };
+  unsigned epoch = 0;
+  int j = 0;
+  bool stop = false;
+  while (j < nbR) {
+    const int g = min(FP_COLS, nbR - j);
+    unsigned long long keys[FP_COLS] = {};
+    keys[0] = cta_max_key(hi, lo);
+    for (int q = 1; q < g; ++q) {
+      step(j + q - 1);
+      keys[q] = cta_max_key(hi, lo);
     }
-    __syncthreads();
-    // candidates of column j+1 among the rows of R
-    if (tid >= j + 2 && tid < nbR && k0 + tid < w) consider(Sr[tid * ldr + j + 1], k0 + tid);
-    ++j;
+    unsigned long long best[FP_COLS];
+    if (!grid_max_multi(ctl, epoch, keys, g, status, best)) return;
+    int kept = 0;
+    for (; kept < g; ++kept) {
+      const float colmax = (float)__uint_as_float((unsigned)(best[kept] >> 24));
+      const float absakk = fabsf(Sr[(j + kept) * ldr + j + kept]);
+      if (!(absakk >= alpha * colmax) || absakk == 0.f) break;  // pivot search, zero or NaN pivot
+    }
+    for (int q = 0; q < kept; ++q) commit(j + q);
+    if (kept < g) {
+      j += kept;
+      stop = true;  // the general kernel takes column k0 + j
+      break;
+    }
+    j += g;
+    if (j < nbR) step(j - 1);
   }
   if (blockIdx.x == 0 && tid == 0) {
     ctl->kb = j;
@@ -1003,7 +1090,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     float *Sf = reinterpret_cast<float *>(S), *Wf = reinterpret_cast<float *>(Wp);
     float *Df = reinterpret_cast<float *>(Dd), *Ef = reinterpret_cast<float *>(De);
     void *args[] = {&Sf, &nrow, &w, &k0, &kb_want, &Wf, &ldw, &Df, &Ef, &ctl, &slot, &status};
-    if (cudaMemsetAsync(&ctl->pslot[0][0], 0, sizeof(ctl->pslot), st) != cudaSuccess) return NQG_ERR_CUDA;
+    if (cudaMemsetAsync(&ctl->mslot[0][0][0], 0, sizeof(ctl->mslot), st) != cudaSuccess) return NQG_ERR_CUDA;
     cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
     if (cudaLaunchCooperativeKernel((void *)k_wide_panel_fast, dim3(G), dim3(FP_THREADS), args, fsmem, st) !=
         cudaSuccess)
