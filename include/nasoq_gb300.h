@@ -48,7 +48,7 @@ typedef struct nqg_settings {
    * replaced by +-reg_diag_fp32 (sign kept, 0 -> +) in the matrix that is
    * factored, bounding the element growth of block-restricted pivoting to
    * what FP32 can carry; the refinement still works on the reference's
-   * matrix.  <= 0 selects 3e-4 * max|a_ij|. */
+   * matrix.  <= 0 selects 3e-5 * max|a_ij|. */
   double reg_diag_fp32;
   /* FP32 factor only: arithmetic of the triangular solves applied inside the
    * refinement.  NQG_FP64 (default) widens the factor entries and keeps the

@@ -485,7 +485,7 @@ static void apply_perturbation(Plan &P) {
     if (tau <= 0) {
       double amax = 0;
       for (double v : P.Kx_spmv) amax = std::max(amax, std::abs(v));
-      tau = 3e-4 * (amax > 0 ? amax : 1.0);
+      tau = 3e-5 * (amax > 0 ? amax : 1.0);
     }
     P.reg32 = tau;
     for (int j = 0; j < P.n; ++j) {
