@@ -422,10 +422,15 @@ __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nr
         sr[jj * FP_THREADS + tid] = fmaf(-l, Sr[jj * ldr + jc], sr[jj * FP_THREADS + tid]);
       if (jc + 1 < nbR && r_own < w) consider(sr[(jc + 1) * FP_THREADS + tid], r_own);
     }
-    const int m = nbR - jc - 1;
-    for (int e = tid; e < m * m; e += blockDim.x) {
-      const int i = jc + 1 + e % m, jj = jc + 1 + e / m;
-      if (jj <= i) Sr[i * ldr + jj] = fmaf(-(Sr[i * ldr + jc] * r1), Sr[jj * ldr + jc], Sr[i * ldr + jj]);
+    // lower triangle of the trailing block of R: thread = (row, column lane)
+    const int m = nbR - jc - 1, io = tid & 63, jl = tid >> 6;
+    if (io < m) {
+      const int i = jc + 1 + io;
+      const float li = Sr[i * ldr + jc] * r1;
+      for (int jo = jl; jo <= io; jo += FP_THREADS / 64) {
+        const int jj = jc + 1 + jo;
+        Sr[i * ldr + jj] = fmaf(-li, Sr[jj * ldr + jc], Sr[i * ldr + jj]);
+      }
     }
     __syncthreads();
     if (tid >= jc + 2 && tid < nbR && k0 + tid < w) consider(Sr[tid * ldr + jc + 1], k0 + tid);
