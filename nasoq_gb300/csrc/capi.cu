@@ -347,8 +347,8 @@ static int upload_plan(Plan &P) {
   if (const char *e = std::getenv("NASOQ_GB300_WIDE_NB")) P.wide_nb = std::min(64, std::max(4, std::atoi(e)));
   // supernodes of at most this width take the shared-memory BK kernel (<= 64)
   if (const char *e = std::getenv("NASOQ_GB300_BK_SMALL")) P.bk_small = std::min(64, std::max(1, std::atoi(e)));
-  // panels per delayed trailing update of the FP32 wide supernodes (1..4)
-  if (const char *e = std::getenv("NASOQ_GB300_WIDE_DEPTH")) P.wide_depth = std::min(4, std::max(1, std::atoi(e)));
+  // panels per delayed trailing update of the FP32 wide supernodes (1..8)
+  if (const char *e = std::getenv("NASOQ_GB300_WIDE_DEPTH")) P.wide_depth = std::min(8, std::max(1, std::atoi(e)));
   // =serial: the rows below the k_bk_global blocks are solved in that kernel
   if (const char *e = std::getenv("NASOQ_GB300_PANEL_ROWS")) P.panel_rows_serial = std::string(e) == "serial";
   // solve work split per level: small supernodes take one CTA each in the
