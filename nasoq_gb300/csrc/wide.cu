@@ -381,6 +381,7 @@ __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nr
                                                                 float *Wb, int ldw, float *Dd, float *De,
                                                                 WideCtl *ctl, int slot, int *status) {
   extern __shared__ __align__(16) unsigned char fp_raw[];
+  __shared__ __align__(16) float wgrp[WP_NB * FP_COLS];  // W of a group's columns, rows of R
   if (*(volatile int *)&ctl->halt) return;  // queued behind a fast panel that stopped early
   const int nbR = min(nb, w - k0);  // panel columns = rows of R
   const int ldr = nbR + 1;
@@ -410,19 +411,10 @@ __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nr
   };
   if (own && r_own < w) consider(sr[tid], r_own);
   if (tid >= 1 && tid < nbR && k0 + tid < w) consider(Sr[tid * ldr], k0 + tid);
-  // right-looking update of local column jc (shared memory only), then the
-  // candidates of column jc + 1
-  auto step = [&](int jc) {
+  // rows of R: rank-1 term of local column jc on the lower triangle of the
+  // trailing block (thread = row, column lane)
+  auto rtri = [&](int jc) {
     const float r1 = 1.f / Sr[jc * ldr + jc];
-    hi = 0u;
-    lo = 0u;
-    if (own) {
-      const float l = sr[jc * FP_THREADS + tid] * r1;
-      for (int jj = jc + 1; jj < nbR; ++jj)
-        sr[jj * FP_THREADS + tid] = fmaf(-l, Sr[jj * ldr + jc], sr[jj * FP_THREADS + tid]);
-      if (jc + 1 < nbR && r_own < w) consider(sr[(jc + 1) * FP_THREADS + tid], r_own);
-    }
-    // lower triangle of the trailing block of R: thread = (row, column lane)
     const int m = nbR - jc - 1, io = tid & 63, jl = tid >> 6;
     if (io < m) {
       const int i = jc + 1 + io;
@@ -432,17 +424,14 @@ __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nr
         Sr[i * ldr + jj] = fmaf(-li, Sr[jj * ldr + jc], Sr[i * ldr + jj]);
       }
     }
-    __syncthreads();
-    if (tid >= jc + 2 && tid < nbR && k0 + tid < w) consider(Sr[tid * ldr + jc + 1], k0 + tid);
   };
-  // global writes of kept column jc: L and W of the thread's row, and (CTA 0)
-  // of the rows of R, the unit diagonal and D
-  auto commit = [&](int jc) {
+  // global writes of kept column jc (the thread's W value wv): L and W of the
+  // thread's row, and (CTA 0) of the rows of R, the unit diagonal and D
+  auto commit = [&](int jc, float wv) {
     const int c = k0 + jc;
     const float d = Sr[jc * ldr + jc];
     const float r1 = 1.f / d;
     if (own) {
-      const float wv = sr[jc * FP_THREADS + tid];
       Wb[(size_t)jc * ldw + r_own] = wv;
       S[r_own + (size_t)c * nrow] = wv * r1;
     }
@@ -458,15 +447,34 @@ __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nr
       }
     }
   };
+  // Columns go in groups of FP_COLS.  At a group's start the thread's row sr
+  // carries the update of every earlier group; inside the group each column's
+  // own entry gets the group's earlier columns as a short correction, and at
+  // its end one rank-FP_COLS update (W of the group's columns as one float4 per
+  // row of R) brings the rest of the row up to date.  Every entry receives
+  // the same FMAs in the same order as a column-by-column update.
   unsigned epoch = 0;
   int j = 0;
   bool stop = false;
   while (j < nbR) {
     const int g = min(FP_COLS, nbR - j);
+    float wq[FP_COLS] = {}, lq[FP_COLS] = {};  // the thread's W and L in the group's columns
+    if (own) wq[0] = sr[j * FP_THREADS + tid];
     unsigned long long keys[FP_COLS] = {};
     keys[0] = cta_max_key(hi, lo);
     for (int q = 1; q < g; ++q) {
-      step(j + q - 1);
+      lq[q - 1] = wq[q - 1] * (1.f / Sr[(j + q - 1) * ldr + j + q - 1]);
+      hi = 0u;
+      lo = 0u;
+      if (own) {
+        float v = sr[(j + q) * FP_THREADS + tid];
+        for (int t = 0; t < q; ++t) v = fmaf(-lq[t], Sr[(j + q) * ldr + j + t], v);
+        wq[q] = v;
+        if (r_own < w) consider(v, r_own);
+      }
+      rtri(j + q - 1);
+      __syncthreads();
+      if (tid >= j + q + 1 && tid < nbR && k0 + tid < w) consider(Sr[tid * ldr + j + q], k0 + tid);
       keys[q] = cta_max_key(hi, lo);
     }
     unsigned long long best[FP_COLS];
@@ -477,14 +485,40 @@ __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nr
       const float absakk = fabsf(Sr[(j + kept) * ldr + j + kept]);
       if (!(absakk >= alpha * colmax) || absakk == 0.f) break;  // pivot search, zero or NaN pivot
     }
-    for (int q = 0; q < kept; ++q) commit(j + q);
+    for (int q = 0; q < kept; ++q) commit(j + q, wq[q]);
     if (kept < g) {
       j += kept;
       stop = true;  // the general kernel takes column k0 + j
       break;
     }
-    j += g;
-    if (j < nbR) step(j - 1);
+    const int jn = j + g;
+    if (jn < nbR) {
+      lq[g - 1] = wq[g - 1] * (1.f / Sr[(jn - 1) * ldr + jn - 1]);
+      rtri(jn - 1);
+      // W of the group's columns, rows jn .. nbR-1 of R (final: their last
+      // term came from column jn - 2)
+      for (int e = tid; e < (nbR - jn) * FP_COLS; e += blockDim.x) {
+        const int i = jn + e / FP_COLS, q = e % FP_COLS;
+        wgrp[i * FP_COLS + q] = q < g ? Sr[i * ldr + j + q] : 0.f;
+      }
+      __syncthreads();
+      hi = 0u;
+      lo = 0u;
+      if (own) {
+        for (int jj = jn; jj < nbR; ++jj) {
+          const float4 wv = *reinterpret_cast<const float4 *>(wgrp + jj * FP_COLS);
+          float v = sr[jj * FP_THREADS + tid];
+          v = fmaf(-lq[0], wv.x, v);
+          if (g > 1) v = fmaf(-lq[1], wv.y, v);
+          if (g > 2) v = fmaf(-lq[2], wv.z, v);
+          if (g > 3) v = fmaf(-lq[3], wv.w, v);
+          sr[jj * FP_THREADS + tid] = v;
+        }
+        if (r_own < w) consider(sr[jn * FP_THREADS + tid], r_own);
+      }
+      if (tid >= jn + 1 && tid < nbR && k0 + tid < w) consider(Sr[tid * ldr + jn], k0 + tid);
+    }
+    j = jn;
   }
   if (blockIdx.x == 0 && tid == 0) {
     ctl->kb = j;
