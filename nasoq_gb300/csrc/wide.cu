@@ -1013,8 +1013,9 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   // panels are pending, their W columns side by side in Wb, and one update of
   // K = their total width flushes them to the columns beyond the frontier F.
   // Invariant: columns < F carry the update of every pending panel, columns
-  // >= F of none.  Before a panel, the band [F, k0 + nb + 1) (every column the
-  // panel can factor, a final 2x2 included) is brought up to date; after it,
+  // >= F of none.  Before a panel, the band from F to its last possible
+  // column (k0 + nb, or k0 + nb + 1 for a final 2x2 of the general kernel) is
+  // brought up to date; after it,
   // the panel's own update covers [k1, F).  A panel on the general kernel may
   // interchange rows and columns anywhere in the trailing block, so every
   // pending update is flushed before it.
@@ -1065,7 +1066,10 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       s.pend_K = 0;
       s.F = s.k0;
     }
-    const int bend = std::min(w, s.k0 + nb + 1);
+    // a general panel may end with a 2x2 pivot one column past nb; a fast
+    // panel never goes past nb, so its band stops at k0 + nb and a complete
+    // fast panel leaves no remainder of its own update to apply
+    const int bend = std::min(w, s.k0 + nb + (general ? 1 : 0));
     if (s.npend > 0 && s.F < bend && (rc = apply(s.pend_k0, s.pend_K, 0, s.F, bend))) return rc;
     s.F = std::max(s.F, bend);
     return NQG_OK;
