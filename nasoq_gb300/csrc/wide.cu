@@ -530,6 +530,249 @@ __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nr
   }
 }
 
+// Block-first fast panel (no pivot search).  The nbR x nbR diagonal block R
+// is factored first, replicated in every CTA with diagonal pivots assumed,
+// eight columns at a time (one warp factors the 8 x 8 diagonal block with
+// shuffles, the rows below it are solved against that block, then a rank-8
+// update brings the rest of R up to date); then every owned row is solved
+// against R in registers, and ONE grid exchange returns the maxima of all
+// panel columns.  The longest prefix of columns whose diagonal passes the
+// Bunch-Kaufman test is kept and written; the later columns stay untouched
+// for the general kernel, as in k_wide_panel_fast.  Every entry receives the
+// same FMAs in the same order as a column-by-column update, so both fast
+// kernels give the same factor bit for bit.
+// Exchange words: CTA b writes (maximum |W| bits of column j) << 32 | seq to
+// word j * FB_MAXG + b of ctl->mslot; seq is unique per launch between two
+// clearings of the control block, so the words need no clearing per launch.
+constexpr int FB_THREADS = 256;  // one row below the panel per thread
+constexpr int FB_MAXG = 128;     // CTAs per launch (WP_NB x FB_MAXG words fit in ctl->mslot)
+constexpr int FB_LD = WP_NB;     // leading dimension of R, stored by columns
+static_assert(WP_NB * FB_MAXG <= (int)(sizeof(WideCtl::mslot) / sizeof(unsigned long long)),
+              "exchange words of the block-first panel");
+static_assert(FB_THREADS % WP_NB == 0, "column parts of the exchange");
+
+__host__ __device__ constexpr size_t fast_blk_smem() {
+  return ((size_t)WP_NB * FB_THREADS + (size_t)WP_NB * FB_LD + 8 * FB_LD) * sizeof(float);
+}
+
+__global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nrow, int w, int k0, int nb, float *Wb,
+                                                               int ldw, float *Dd, float *De, WideCtl *ctl,
+                                                               int slot, unsigned seq, int *status) {
+  extern __shared__ __align__(16) unsigned char fb_raw[];
+  __shared__ float rinv[WP_NB];
+  __shared__ unsigned cpart[FB_THREADS / WP_NB][WP_NB];
+  __shared__ int s_kept;
+  if (*(volatile int *)&ctl->halt) return;  // queued behind a fast panel that stopped early
+  const int nbR = min(nb, w - k0);           // panel columns = rows of R
+  float *wsm = reinterpret_cast<float *>(fb_raw);  // [WP_NB][FB_THREADS]: W of the thread's row
+  float *Rc = wsm + (size_t)WP_NB * FB_THREADS;    // [WP_NB][FB_LD]: R by columns, W values once final
+  float *Lb = Rc + (size_t)WP_NB * FB_LD;          // [8][FB_LD]: L of the current column block
+  const float alpha = (float)((1.0 + sqrt(17.0)) / 8.0);
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int r_own = k0 + nbR + blockIdx.x * FB_THREADS + tid;  // the thread's row (if < nrow)
+  const bool own = r_own < nrow;
+  for (int e = tid; e < WP_NB * FB_LD; e += FB_THREADS) {
+    const int t = e / FB_LD, i = e % FB_LD;
+    Rc[e] = (t < nbR && i < nbR && i >= t) ? __ldcg(S + (k0 + i) + (size_t)(k0 + t) * nrow) : 0.f;
+  }
+  if (tid < WP_NB) rinv[tid] = 0.f;
+  __syncthreads();
+  // --- R = L_R D_R L_R^T, eight columns at a time -------------------------
+  for (int b = 0; b < nbR; b += 8) {
+    const int nc = min(8, nbR - b);
+    if (wid == 0) {
+      // the 8 x 8 diagonal block: lane q holds row b + q
+      const int q = lane;
+      float v[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) v[c] = (q < nc && c <= q) ? Rc[(b + c) * FB_LD + b + q] : 0.f;
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        if (t < nc) {
+          const float r1 = 1.f / __shfl_sync(0xffffffffu, v[t], t);
+          const float l = v[t] * r1;
+#pragma unroll
+          for (int c = t + 1; c < 8; ++c) {
+            const float wct = __shfl_sync(0xffffffffu, v[t], c);  // W(b + c, b + t), final
+            if (q < nc && q >= c) v[c] = fmaf(-l, wct, v[c]);
+          }
+          if (q == 0) rinv[b + t] = r1;
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (q < nc && c <= q) Rc[(b + c) * FB_LD + b + q] = v[c];
+    }
+    __syncthreads();
+    const int mb = nbR - b - 8;  // rows of R below the block (the block is full when > 0)
+    if (mb <= 0) break;
+    if (tid < mb) {
+      const int i = b + 8 + tid;
+      float v[8], lv[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) v[c] = Rc[(b + c) * FB_LD + i];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+#pragma unroll
+        for (int t = 0; t < c; ++t) v[c] = fmaf(-lv[t], Rc[(b + t) * FB_LD + b + c], v[c]);
+        lv[c] = v[c] * rinv[b + c];
+      }
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        Rc[(b + c) * FB_LD + i] = v[c];
+        Lb[c * FB_LD + i] = lv[c];
+      }
+    }
+    __syncthreads();
+    for (int e = tid; e < mb * mb; e += FB_THREADS) {
+      const int io = e % mb, jo = e / mb;
+      if (io < jo) continue;
+      const int i = b + 8 + io, jj = b + 8 + jo;
+      float x = Rc[jj * FB_LD + i];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) x = fmaf(-Lb[t * FB_LD + i], Rc[(b + t) * FB_LD + jj], x);
+      Rc[jj * FB_LD + i] = x;
+    }
+    __syncthreads();
+  }
+  // --- the thread's row: forward substitution against R, 8 columns at a time
+  if (own) {
+    for (int jb = 0; jb < nbR; jb += 8) {
+      const int nc = min(8, nbR - jb);
+      float v[8], lv[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) v[q] = q < nc ? __ldcg(S + r_own + (size_t)(k0 + jb + q) * nrow) : 0.f;
+      for (int t = 0; t < jb; ++t) {
+        const float l = wsm[t * FB_THREADS + tid] * rinv[t];
+        const float4 x0 = *reinterpret_cast<const float4 *>(Rc + t * FB_LD + jb);
+        const float4 x1 = *reinterpret_cast<const float4 *>(Rc + t * FB_LD + jb + 4);
+        v[0] = fmaf(-l, x0.x, v[0]);
+        v[1] = fmaf(-l, x0.y, v[1]);
+        v[2] = fmaf(-l, x0.z, v[2]);
+        v[3] = fmaf(-l, x0.w, v[3]);
+        v[4] = fmaf(-l, x1.x, v[4]);
+        v[5] = fmaf(-l, x1.y, v[5]);
+        v[6] = fmaf(-l, x1.z, v[6]);
+        v[7] = fmaf(-l, x1.w, v[7]);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+#pragma unroll
+        for (int t = 0; t < q; ++t) v[q] = fmaf(-lv[t], Rc[(jb + t) * FB_LD + jb + q], v[q]);
+        lv[q] = v[q] * rinv[jb + q];
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < nc) wsm[(jb + q) * FB_THREADS + tid] = v[q];
+    }
+  }
+  __syncthreads();
+  // --- column maxima: own rows inside the diagonal block and rows of R below
+  // the diagonal, per CTA, then over the grid
+  unsigned long long *slots = &ctl->mslot[0][0][0];
+  const int nvalid = max(0, min(FB_THREADS, min(nrow, w) - (k0 + nbR + (int)blockIdx.x * FB_THREADS)));
+  for (int j = wid; j < nbR; j += FB_THREADS / 32) {
+    unsigned m = 0u;
+    for (int t = lane; t < nvalid; t += 32) {
+      const float a = fabsf(wsm[j * FB_THREADS + t]);
+      if (a == a) m = max(m, __float_as_uint(a));
+    }
+    for (int i = j + 1 + lane; i < nbR; i += 32) {
+      const float a = fabsf(Rc[j * FB_LD + i]);
+      if (a == a) m = max(m, __float_as_uint(a));
+    }
+    m = __reduce_max_sync(0xffffffffu, m);
+    if (lane == 0)
+      *(volatile unsigned long long *)&slots[j * FB_MAXG + blockIdx.x] = ((unsigned long long)m << 32) | seq;
+  }
+  {
+    const int G = (int)gridDim.x;
+    const int q = tid % WP_NB, p = tid / WP_NB;
+    long long it = 0;
+    bool fail = false;
+    // first every CTA's word of column 0, then every word (each re-checked)
+    for (int phase = 0; phase < 2 && !fail; ++phase) {
+      unsigned m = 0u;
+      while (true) {
+        bool all = true;
+        m = 0u;
+        if (phase == 0) {
+          for (int bb = tid; bb < G; bb += FB_THREADS)
+            if ((unsigned)*(volatile unsigned long long *)&slots[bb] != seq) all = false;
+        } else if (q < nbR) {
+          for (int bb = p; bb < G; bb += FB_THREADS / WP_NB) {
+            const unsigned long long v = *(volatile unsigned long long *)&slots[q * FB_MAXG + bb];
+            if ((unsigned)v != seq) all = false;
+            else m = max(m, (unsigned)(v >> 32));
+          }
+        }
+        if (__syncthreads_and(all)) break;
+        const int ab = tid == 0 ? *(volatile int *)&ctl->abort : 0;
+        if (__syncthreads_or(ab)) {
+          fail = true;
+          break;
+        }
+        if (++it > SPIN_LIMIT) {
+          if (tid == 0) {
+            atomicOr(status, ST_TIMEOUT);
+            atomicExch(&ctl->abort, 1);
+          }
+          fail = true;
+          break;
+        }
+      }
+      if (phase == 1) cpart[p][q] = m;
+    }
+    if (fail) return;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    int k = 0;
+    for (; k < nbR; ++k) {
+      unsigned mb = 0u;
+#pragma unroll
+      for (int p = 0; p < FB_THREADS / WP_NB; ++p) mb = max(mb, cpart[p][k]);
+      const float colmax = __uint_as_float(mb);
+      const float absakk = fabsf(Rc[k * FB_LD + k]);
+      if (!(absakk >= alpha * colmax) || absakk == 0.f) break;  // pivot search, zero or NaN pivot
+    }
+    s_kept = k;
+  }
+  __syncthreads();
+  // --- global writes of the kept columns
+  const int kept = s_kept;
+  if (own)
+    for (int j = 0; j < kept; ++j) {
+      const float wv = wsm[j * FB_THREADS + tid];
+      Wb[(size_t)j * ldw + r_own] = wv;
+      S[r_own + (size_t)(k0 + j) * nrow] = wv * rinv[j];
+    }
+  if (blockIdx.x == 0) {
+    for (int e = tid; e < kept * nbR; e += FB_THREADS) {
+      const int j = e / nbR, i = e % nbR;
+      if (i < j) continue;
+      const float v = Rc[j * FB_LD + i];
+      const int c = k0 + j;
+      Wb[(size_t)j * ldw + k0 + i] = v;
+      if (i > j) {
+        S[(k0 + i) + (size_t)c * nrow] = v * rinv[j];
+      } else {
+        S[c + (size_t)c * nrow] = 1.f;
+        Dd[c] = v;
+        De[c] = 0.f;
+      }
+    }
+    if (tid == 0) {
+      ctl->kb = kept;
+      ctl->stop = kept < nbR ? 1 : 0;
+      if (slot >= 0) {
+        ctl->kb_log[slot] = kept;
+        if (kept < nbR) ctl->halt = 1;
+      }
+    }
+  }
+}
+
 // One panel: columns c = k0 .. (at most k0+nb, one more for a final 2x2).
 // Thread gt owns rows gt, gt + TT, ...; the panel entries L(gt, k0 + t) of
 // its first row are cached in shared memory (lc[t][threadIdx.x]) as they are
@@ -995,10 +1238,14 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   // FP32: fast panels (no pivot search) until a column needs one; the
   // general kernel then factors one panel from that column.
   // NASOQ_GB300_PANEL=general keeps every panel on the general kernel.
+  // NASOQ_GB300_PANEL=general keeps every panel on the general kernel;
+  // =group keeps fast panels on the grouped kernel (four columns per
+  // exchange) instead of the block-first one (one exchange per panel).
   const char *pe = std::getenv("NASOQ_GB300_PANEL");
   const bool fast_enabled = sizeof(T) == 4 && !(pe && std::string(pe) == "general");
+  const bool blk_enabled = fast_enabled && !(pe && std::string(pe) == "group");
   const size_t fsmem = fast_panel_smem(nb);
-  int maxG_fast = 0;
+  int maxG_fast = 0, maxG_blk = 0;
   if (fast_enabled) {
     if (cudaFuncSetAttribute(k_wide_panel_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem) !=
         cudaSuccess)
@@ -1008,6 +1255,21 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       return NQG_ERR_CUDA;
     maxG_fast = std::min(std::max(occf, 0) * num_sms, 1024);
   }
+  if (blk_enabled) {
+    if (cudaFuncSetAttribute(k_wide_panel_blk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)fast_blk_smem()) != cudaSuccess)
+      return NQG_ERR_CUDA;
+    int occb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occb, k_wide_panel_blk, FB_THREADS, fast_blk_smem()) !=
+        cudaSuccess)
+      return NQG_ERR_CUDA;
+    maxG_blk = std::min(std::max(occb, 0) * num_sms, FB_MAXG);
+  }
+  // exchange words of the block-first kernel: seq per launch; the grouped
+  // kernel leaves words of its own format behind (cleared before the next
+  // block-first launch)
+  unsigned blk_seq = 0;
+  bool mslot_dirty = false;
   bool use_general = false;  // the next panel starts at a column that needs a pivot search
   // Delayed trailing updates (FP32 tcgen05 path): up to `depth` consecutive
   // panels are pending, their W columns side by side in Wb, and one update of
@@ -1128,12 +1390,32 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   };
   auto launch_fast = [&](int k0, int kb_want, T *Wp, int slot) -> int {
     const int rows_out = nrow - k0 - kb_want;
-    const int G = std::max(1, std::min(maxG_fast, (rows_out + FP_THREADS - 1) / FP_THREADS));
     int ldw = nrow;
     float *Sf = reinterpret_cast<float *>(S), *Wf = reinterpret_cast<float *>(Wp);
     float *Df = reinterpret_cast<float *>(Dd), *Ef = reinterpret_cast<float *>(De);
+    const int Gb = std::max(1, (rows_out + FB_THREADS - 1) / FB_THREADS);
+    if (blk_enabled && Gb <= maxG_blk) {
+      if (mslot_dirty) {
+        if (cudaMemsetAsync(&ctl->mslot[0][0][0], 0, sizeof(ctl->mslot), st) != cudaSuccess) return NQG_ERR_CUDA;
+        mslot_dirty = false;
+      }
+      if (++blk_seq == 0) blk_seq = 1;
+      unsigned seq = blk_seq;
+      void *args[] = {&Sf, &nrow, &w, &k0, &kb_want, &Wf, &ldw, &Df, &Ef, &ctl, &slot, &seq, &status};
+      cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
+      if (cudaLaunchCooperativeKernel((void *)k_wide_panel_blk, dim3(Gb), dim3(FB_THREADS), args, fast_blk_smem(),
+                                      st) != cudaSuccess)
+        return NQG_ERR_CUDA;
+      if (P) {
+        P->nlaunch++;
+        P->prof_end(NQG_K_WIDE_PANEL, e0, panel_flops(k0, kb_want), 0.0);
+      }
+      return NQG_OK;
+    }
+    const int G = std::max(1, std::min(maxG_fast, (rows_out + FP_THREADS - 1) / FP_THREADS));
     void *args[] = {&Sf, &nrow, &w, &k0, &kb_want, &Wf, &ldw, &Df, &Ef, &ctl, &slot, &status};
     if (cudaMemsetAsync(&ctl->mslot[0][0][0], 0, sizeof(ctl->mslot), st) != cudaSuccess) return NQG_ERR_CUDA;
+    mslot_dirty = true;
     cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
     if (cudaLaunchCooperativeKernel((void *)k_wide_panel_fast, dim3(G), dim3(FP_THREADS), args, fsmem, st) !=
         cudaSuccess)

@@ -290,3 +290,54 @@ def test_panel_rows_kernels(path, monkeypatch):
         mag = np.abs(Ld) @ np.abs(Dd) @ np.abs(Ld).T
         assert np.abs(R).max() <= 1e-13 * mag.max(), mode
         plan.close()
+
+
+def _dense_lower_csc(M):
+    n = M.shape[0]
+    Ap = np.zeros(n + 1, np.int32)
+    Ap[1:] = np.cumsum(np.arange(n, 0, -1))
+    Ai = np.concatenate([np.arange(j, n, dtype=np.int32) for j in range(n)])
+    Ax = np.concatenate([M[j:, j] for j in range(n)])
+    return Ap, Ai, Ax
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,pivots", [(900, False), (900, True), (1201, True)])
+def test_fast_panel_kernels_agree(n, pivots, monkeypatch):
+    """One dense FP32 supernode through the wide kernels (no atomics, so the
+    factor is deterministic): the block-first fast panel (one exchange per
+    panel) and the grouped one (four columns per exchange) apply the same
+    FMAs in the same order and stop at the same columns, so the factors are
+    identical bit for bit (compared from the same settled pivot order); with
+    small diagonals scattered through the matrix the general kernel takes
+    over after every stop.  The refined solution
+    meets the FP32 bar."""
+    rng = np.random.default_rng(n + pivots)
+    M = rng.standard_normal((n, n))
+    M = (M + M.T) / 2
+    dg = rng.uniform(0.5 * n, n, n) * rng.choice([-1.0, 1.0], n)
+    if pivots:
+        dg[rng.choice(n, n // 40, replace=False)] = 1e-3
+    M[np.diag_indices(n)] = dg
+    Ap, Ai, Ax = _dense_lower_csc(M)
+    st = nq.default_settings(precision=nq.NQG_FP32, req_ref_iter=6, max_inner_iter=6, tol_abs=1e-13,
+                             tol_rel=1e-13, reg_diag=0.0)
+    plan = nq.Plan(n, Ap, Ai, Ax, settings=st)
+    assert plan.symbolic.info.nsuper == 1
+    # the first factorization settles the pivot order that later ones start from
+    monkeypatch.setenv("NASOQ_GB300_PANEL", "group")
+    assert plan.factor() == 0
+    out = {}
+    for mode in ("group", "block"):
+        if mode == "group":
+            monkeypatch.setenv("NASOQ_GB300_PANEL", "group")
+        else:
+            monkeypatch.delenv("NASOQ_GB300_PANEL", raising=False)
+        assert plan.factor() == 0
+        out[mode] = plan.factor_arrays()
+    for a, b in zip(out["group"], out["block"]):
+        assert np.array_equal(a, b)
+    rhs = rng.standard_normal(n)
+    x = plan.solve(rhs)
+    assert np.linalg.norm(rhs - M @ x) <= 1e-10 * np.linalg.norm(rhs)
+    plan.close()
