@@ -432,6 +432,18 @@ static int upload_plan(Plan &P) {
     if (wide_rows > 0)
       NQG_CUDA(cudaMalloc(&P.d_wide_W,
                           (size_t)wide_rows * (P.wide_depth * (P.wide_nb + 1) + 2) * P.val_size()));
+    // FP32: packed operands of the persistent trailing update -- row blocks
+    // of 128 (L rows, then W rows) x wide_depth panels of chunks of 32
+    // columns, hi + lo TF32 halves of 16 KB each
+    if (wide_rows > 0 && P.set.precision == NQG_FP32) {
+      int64_t blocks = 0;
+      for (int s = 0; s < ns; ++s)
+        if (S.super[s + 1] - S.super[s] > P.wide_min)
+          blocks = std::max<int64_t>(blocks, (S.lpi[s + 1] - S.lpi[s] + 127) / 128 +
+                                                 (S.super[s + 1] - S.super[s] + 127) / 128);
+      const int64_t nkc = (int64_t)std::max(P.wide_depth, 1) * ((P.wide_nb + 1 + 31) / 32);
+      NQG_CUDA(cudaMalloc(&P.d_wide_pack, (size_t)(blocks * nkc) * 32768));
+    }
     // control block: grid barriers of the blocked factorization, abort flag
     // of the block solves
     NQG_CUDA(cudaMalloc(&P.d_wide_ctl, wide_ctl_bytes()));
@@ -446,7 +458,7 @@ static void free_plan(Plan &P) {
                   P.d_perm_tmp, P.d_L, P.d_D, P.d_tiles, P.d_tile_list, P.d_targets, P.d_pair_s, P.d_pair_d,
                   P.d_pair_lb, P.d_pair_ub, P.d_targets_lv, P.d_pivoted, P.d_visible, P.d_hidden, P.d_status,
                   P.d_xo, P.d_bo, P.d_r, P.d_w, P.d_in, P.d_out, P.d_V, P.d_scal, P.d_wide_W, P.d_wide_ctl,
-                  P.d_locinv, P.d_pair_roff, P.d_rr_dest, P.d_rr_moved, P.d_rr_items, P.d_rr_stage,
+                  P.d_wide_pack, P.d_locinv, P.d_pair_roff, P.d_rr_dest, P.d_rr_moved, P.d_rr_items, P.d_rr_stage,
                   P.d_solve_flags, P.d_blk_items, P.d_flagoff, P.d_xf, P.d_Z, P.d_tiles_tc,
                   P.d_tile_list_tc, P.d_row_items};
   for (void *p : ptrs)

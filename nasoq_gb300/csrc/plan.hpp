@@ -129,6 +129,7 @@ struct Plan {
   // wide supernodes (blocked cooperative BK)
   void *d_wide_W = nullptr;         // panel buffer, max nrow x (nb+2)
   void *d_wide_ctl = nullptr;       // barrier / reduction control block
+  unsigned char *d_wide_pack = nullptr;  // FP32: split-TF32 operand blocks of the trailing updates
   unsigned *d_solve_flags = nullptr;  // per 64-column block ready flags of the block solves
   int solve_flags_cap = 0;
   unsigned solve_epoch = 0;

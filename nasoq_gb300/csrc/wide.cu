@@ -1191,6 +1191,233 @@ __global__ void __launch_bounds__(t5::THREADS) k_wide_trailing_t5(float *S, int 
   t5::tile_tf32x3<1>(kb, fa, fb, ep, t5_smem, status);
 }
 
+// ---------------------------------------------------------------------------
+// Persistent trailing update on the tcgen05 tensor cores.
+//
+// Operands are packed once per panel: k_pack_split writes the panel's L rows
+// (A) and W rows (B) as split-TF32 blocks of 128 rows x 32 columns of K (hi
+// then lo, 16 KB each, in the swizzled K-major layout of
+// t5::store_row_split), block (rb, kc) at rb * nkc_stride + kc, row blocks at
+// absolute 128-row positions of the supernode, every panel starting on a new
+// chunk (zeros pad a partial chunk).  k_wide_trailing_pers then runs one CTA
+// per SM over the lower-triangular set of 128 x 128 tiles: warp 0 streams
+// both operand blocks of each K chunk into a three-stage shared-memory ring
+// with bulk copies, warp 1 issues the split-TF32 MMAs (the same three
+// products per K step as t5::tile_tf32x3) into one of two TMEM accumulators,
+// and warps 2-5 subtract the finished accumulator from S while the next tile
+// accumulates in the other one.
+constexpr int PK_BLOCK = 2 * t5::OPND_BYTES;  // hi + lo of one 128 x 32 block
+constexpr int TP_STAGES = 3;
+constexpr int TP_THREADS = 192;
+
+__host__ __device__ constexpr size_t tp_smem_bytes() { return (size_t)TP_STAGES * t5::STAGE_BYTES + 1024; }
+
+// Blocks of rows [rb_first * 128, row_hi) x columns [0, kb) of src (element
+// (r, k) at src[r + k * ld]) into chunks kc0 .. of the pack buffer.
+__global__ void __launch_bounds__(256) k_pack_split(const float *src, int ld, int row_hi, int kb, unsigned char *dst,
+                                                    int nkc_stride, int kc0, int rb_first, const int *halt) {
+  __shared__ float tk[t5::TK][t5::TM + 1];
+  if (*(volatile const int *)halt) return;  // queued behind a fast panel that stopped early
+  const int rb = rb_first + blockIdx.x, kcl = blockIdx.y;
+  const int r0 = rb * t5::TM, k0 = kcl * t5::TK;
+  for (int e = threadIdx.x; e < t5::TK * t5::TM; e += blockDim.x) {
+    const int k = e / t5::TM, r = e % t5::TM, gr = r0 + r;
+    tk[k][r] = (gr < row_hi && k0 + k < kb) ? __ldcg(src + gr + (size_t)(k0 + k) * ld) : 0.f;
+  }
+  __syncthreads();
+  unsigned char *hi = dst + ((size_t)rb * nkc_stride + kc0 + kcl) * PK_BLOCK, *lo = hi + t5::OPND_BYTES;
+  const int r = threadIdx.x >> 1;
+#pragma unroll
+  for (int cc = 0; cc < 4; ++cc) {
+    const int c = (threadIdx.x & 1) * 4 + cc;
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float x = tk[4 * c + q][r];
+      h[q] = t5::tf32_rna(x);
+      l[q] = t5::tf32_rna(x - __uint_as_float(h[q]));
+    }
+    const int off = r * 128 + ((c ^ (r & 7)) << 4);
+    *reinterpret_cast<uint4 *>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+  }
+}
+
+// Tile t of the lower-triangular tile set: column block c holds row blocks
+// c .. nrb-1 (both relative to the first block).
+__device__ __forceinline__ void tp_tile(int t, int nrb, int ncb, int &rbl, int &cbl) {
+  int lo = 0, hi = ncb - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    const long long o = (long long)mid * nrb - (long long)mid * (mid - 1) / 2;
+    if (o <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  cbl = lo;
+  rbl = lo + (int)(t - ((long long)lo * nrb - (long long)lo * (lo - 1) / 2));
+}
+
+// Bounded mbarrier wait that also gives up once another role has given up.
+__device__ __forceinline__ bool tp_wait(uint32_t mbar, uint32_t parity, volatile int *abort, int *status) {
+  for (long long it = 0; it < t5::WAIT_LIMIT; ++it) {
+    if (t5::mbar_test(mbar, parity)) return true;
+    if (*abort) return false;
+  }
+  *abort = 1;
+  atomicOr(status, ST_TIMEOUT);
+  return false;
+}
+
+// S[gr, gc] -= sum over chunks kc0 .. kc1-1 of A(gr, :) B(gc, :)^T for
+// gc in [cb, ce), gr >= gc, gr < nrow; tiles of blocks blk0 + (rbl, cbl).
+__global__ void __launch_bounds__(TP_THREADS, 1) k_wide_trailing_pers(float *S, int nrow, int cb, int ce,
+                                                                      const unsigned char *pack_a,
+                                                                      const unsigned char *pack_b, int nkc_stride,
+                                                                      int kc0, int kc1, int blk0, int nrb, int ncb,
+                                                                      int ntile, const int *halt, int *status) {
+  extern __shared__ __align__(1024) unsigned char tp_raw[];
+  __shared__ __align__(8) uint64_t bar[2 * TP_STAGES + 4];
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_abort;
+  if (*(volatile const int *)halt) return;  // queued behind a fast panel that stopped early
+  unsigned char *base =
+      reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(tp_raw) + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  uint64_t *full = bar, *empty = bar + TP_STAGES, *accf = bar + 2 * TP_STAGES, *acce = accf + 2;
+  if (warp == 1) t5::tmem_alloc(t5::smem_u32(&s_tmem), 2 * t5::TN);
+  if (tid == 0) {
+    s_abort = 0;
+    for (int s = 0; s < TP_STAGES; ++s) {
+      t5::mbar_init(t5::smem_u32(&full[s]), 1);
+      t5::mbar_init(t5::smem_u32(&empty[s]), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      t5::mbar_init(t5::smem_u32(&accf[b]), 1);
+      t5::mbar_init(t5::smem_u32(&acce[b]), 4);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  t5::fence_before();
+  __syncthreads();
+  t5::fence_after();
+  const uint32_t tmem = s_tmem;
+  volatile int *abort = &s_abort;
+  const int G = (int)gridDim.x;
+  if (warp == 0) {
+    if (lane == 0) {
+      // producer: both operand blocks of every K chunk, in tile order
+      uint32_t it = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntile && ok; t += G) {
+        int rbl, cbl;
+        tp_tile(t, nrb, ncb, rbl, cbl);
+        const unsigned char *a = pack_a + (size_t)(blk0 + rbl) * nkc_stride * PK_BLOCK;
+        const unsigned char *b = pack_b + (size_t)(blk0 + cbl) * nkc_stride * PK_BLOCK;
+        for (int kc = kc0; kc < kc1; ++kc, ++it) {
+          const int s = (int)(it % TP_STAGES);
+          const uint32_t use = it / TP_STAGES;
+          if (use > 0 && !tp_wait(t5::smem_u32(&empty[s]), (use - 1) & 1, abort, status)) {
+            ok = false;
+            break;
+          }
+          const uint32_t dst = t5::smem_u32(base + (size_t)s * t5::STAGE_BYTES);
+          const uint32_t fb = t5::smem_u32(&full[s]);
+          t5::mbar_arrive_expect_tx(fb, 2 * PK_BLOCK);
+          t5::bulk_g2s(dst, a + (size_t)kc * PK_BLOCK, PK_BLOCK, fb);
+          t5::bulk_g2s(dst + PK_BLOCK, b + (size_t)kc * PK_BLOCK, PK_BLOCK, fb);
+        }
+      }
+      // copies still in flight land before the CTA leaves
+      for (int s = 0; s < TP_STAGES; ++s)
+        if (it > (uint32_t)s) t5::mbar_wait(t5::smem_u32(&full[s]), ((it - 1 - s) / TP_STAGES) & 1);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issue: 3 split-TF32 products per K step of 8
+      constexpr uint32_t IDESC = t5::idesc_tf32(t5::TM, t5::TN);
+      uint32_t it = 0, last_bar = 0, last_par = 0;
+      bool ok = true, any = false;
+      int i = 0;
+      for (int t = blockIdx.x; t < ntile && ok; t += G, ++i) {
+        const int buf = i & 1;
+        const uint32_t u = (uint32_t)i >> 1;
+        if (u > 0 && !tp_wait(t5::smem_u32(&acce[buf]), (u - 1) & 1, abort, status)) break;
+        t5::fence_after();
+        const uint32_t d = tmem + (uint32_t)(buf * t5::TN);
+        for (int kc = kc0; kc < kc1; ++kc, ++it) {
+          const int s = (int)(it % TP_STAGES);
+          const uint32_t use = it / TP_STAGES;
+          if (!tp_wait(t5::smem_u32(&full[s]), use & 1, abort, status)) {
+            ok = false;
+            break;
+          }
+          t5::fence_after();
+          const uint32_t a_hi = t5::smem_u32(base + (size_t)s * t5::STAGE_BYTES), a_lo = a_hi + t5::OPND_BYTES;
+          const uint32_t b_hi = a_hi + 2 * t5::OPND_BYTES, b_lo = a_hi + 3 * t5::OPND_BYTES;
+#pragma unroll
+          for (int ks = 0; ks < t5::TK / 8; ++ks) {
+            const uint32_t off = ks * 32;
+            const uint32_t acc0 = (kc > kc0 || ks > 0) ? 1u : 0u;
+            t5::mma_tf32(d, t5::desc_sw128(a_lo + off), t5::desc_sw128(b_hi + off), IDESC, acc0);
+            t5::mma_tf32(d, t5::desc_sw128(a_hi + off), t5::desc_sw128(b_lo + off), IDESC, 1u);
+            t5::mma_tf32(d, t5::desc_sw128(a_hi + off), t5::desc_sw128(b_hi + off), IDESC, 1u);
+          }
+          t5::mma_commit(t5::smem_u32(&empty[s]));
+          last_bar = t5::smem_u32(&empty[s]);
+          last_par = use & 1;
+          any = true;
+        }
+        if (ok) t5::mma_commit(t5::smem_u32(&accf[buf]));
+      }
+      // MMAs still running finish before the TMEM is released
+      if (any) t5::mbar_wait(last_bar, last_par);
+    }
+  } else {
+    // epilogue: thread = TMEM lane = tile row
+    const int q = warp & 3, r = q * 32 + lane;
+    int i = 0;
+    for (int t = blockIdx.x; t < ntile; t += G, ++i) {
+      const int buf = i & 1;
+      const uint32_t u = (uint32_t)i >> 1;
+      int rbl, cbl;
+      tp_tile(t, nrb, ncb, rbl, cbl);
+      const int gr = (blk0 + rbl) * t5::TM + r, gc0 = (blk0 + cbl) * t5::TN;
+      // one lane waits, so that the whole warp leaves or goes on together
+      int okw = 0;
+      if (lane == 0) okw = tp_wait(t5::smem_u32(&accf[buf]), u & 1, abort, status) ? 1 : 0;
+      if (!__shfl_sync(0xffffffffu, okw, 0)) break;
+      t5::fence_after();
+#pragma unroll 1
+      for (int cc = 0; cc < t5::TN; cc += 32) {
+        uint32_t v[32];
+        t5::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * t5::TN + cc), v);
+        if (gr < nrow) {
+          float cur[32];
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int gc = gc0 + cc + j;
+            cur[j] = (gc >= cb && gc < ce && gr >= gc) ? S[gr + (size_t)gc * nrow] : 0.f;
+          }
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int gc = gc0 + cc + j;
+            if (gc >= cb && gc < ce && gr >= gc) S[gr + (size_t)gc * nrow] = cur[j] - __uint_as_float(v[j]);
+          }
+        }
+      }
+      t5::fence_before();
+      __syncwarp();
+      if (lane == 0) t5::mbar_arrive(t5::smem_u32(&acce[buf]));
+    }
+  }
+  t5::fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    t5::fence_after();
+    t5::tmem_dealloc(tmem, 2 * t5::TN);
+  }
+}
+
 template <class T> __global__ void k_wide_init_perm(int *perm, int w) {
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < w; m += gridDim.x * blockDim.x) perm[m] = m;
 }
@@ -1225,8 +1452,22 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   // FP32 trailing updates: tcgen05 split-TF32 tiles by default;
   // NASOQ_GB300_TRAILING=mma selects the mma.sync split-TF32 kernel and
   // =simt the CUDA-core kernel
+  // NASOQ_GB300_TRAILING=tile keeps the tcgen05 updates on one CTA per tile
+  // with operands split while they are loaded, instead of the persistent
+  // kernel on packed operands
   const char *te = std::getenv("NASOQ_GB300_TRAILING");
   const int trail = !te ? 2 : std::string(te) == "simt" ? 0 : std::string(te) == "mma" ? 1 : 2;
+  const bool tile_only = te && std::string(te) == "tile";
+  // packed split-TF32 operands: row blocks of A (L rows) then of B (W rows),
+  // nkc_stride chunks each (every pending panel starts on a new chunk)
+  unsigned char *pack_a = (sizeof(T) == 4 && trail == 2 && !tile_only && P) ? P->d_wide_pack : nullptr;
+  const int nch_panel = (nb + 1 + t5::TK - 1) / t5::TK;
+  const int nkc_stride = std::max(depth, 1) * nch_panel;
+  const int nrb_all = (nrow + t5::TM - 1) / t5::TM, ncb_all = (w + t5::TN - 1) / t5::TN;
+  unsigned char *pack_b = pack_a ? pack_a + (size_t)nrb_all * nkc_stride * PK_BLOCK : nullptr;
+  if (pack_a && cudaFuncSetAttribute(k_wide_trailing_pers, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tp_smem_bytes()) != cudaSuccess)
+    return NQG_ERR_CUDA;
   if (sizeof(T) == 4 && trail == 1 &&
       cudaFuncSetAttribute(k_wide_trailing_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM) !=
           cudaSuccess)
@@ -1292,23 +1533,62 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   const bool spec_ok = fast_enabled && trail == 2;
   constexpr int SPEC_MAX = 16;
   struct State {
-    int k0, F, pend_k0, pend_K, npend;
+    int k0, F, pend_k0, pend_K, npend, pend_C;  // pend_C: packed chunks of the pending panels
   };
   struct Spec {
     State st;  // state after the panel's band update, before the panel
     int kb, woff;
   };
-  State cs{0, 0, 0, 0, 0};
+  State cs{0, 0, 0, 0, 0, 0};
   std::vector<Spec> specs;
   int spec_limit = SPEC_MAX;  // batch size: 1 after a rewind, doubling after each clean batch
   const int *halt = &ctl->halt;
-  auto apply = [&](int kL, int K, int woff, int cb, int ce) -> int {
+  // chunks of a panel of kb columns in the pack buffer
+  auto nch = [&](int kb) { return (kb + t5::TK - 1) / t5::TK; };
+  // split-TF32 blocks of a finished panel (columns k0 .. k0+kb-1, W at
+  // column woff of Wb) into chunks kcs .. of the pack buffer, rows from the
+  // block holding k0 + kb on (the rows every later update of it touches)
+  auto pack_panel = [&](int k0, int kb, int woff, int kcs) -> int {
+    const int k1 = k0 + kb;
+    if (!pack_a || k1 >= w || kb <= 0) return NQG_OK;
+    cudaEvent_t e1 = P ? P->prof_begin() : nullptr;
+    const int rb_first = k1 / t5::TM;
+    int ld = nrow;
+    k_pack_split<<<dim3(nrb_all - rb_first, nch(kb)), 256, 0, st>>>(reinterpret_cast<const float *>(S) +
+                                                                         (size_t)k0 * nrow,
+                                                                     ld, nrow, kb, pack_a, nkc_stride, kcs,
+                                                                     rb_first, halt);
+    k_pack_split<<<dim3(ncb_all - rb_first, nch(kb)), 256, 0, st>>>(reinterpret_cast<const float *>(Wb) +
+                                                                         (size_t)woff * nrow,
+                                                                     ld, w, kb, pack_b, nkc_stride, kcs, rb_first,
+                                                                     halt);
+    if (cudaGetLastError() != cudaSuccess) return NQG_ERR_CUDA;
+    if (P) {
+      P->nlaunch += 2;
+      const double bytes = (double)kb * ((nrow - rb_first * t5::TM) + (w - rb_first * t5::TM)) * 12.0;
+      P->prof_end(NQG_K_WIDE_TRAILING, e1, 0.0, bytes);
+    }
+    return NQG_OK;
+  };
+  // S[cb.., cb..ce) -= L(:, kL .. kL+K) W(:, woff ..)^T (lower part); with
+  // packed operands the same product from chunks kca .. kcb-1
+  auto apply = [&](int kL, int K, int woff, int kca, int kcb, int cb, int ce) -> int {
     if (ce <= cb || K <= 0) return NQG_OK;
     cudaEvent_t e1 = P ? P->prof_begin() : nullptr;
-    const int tm = (nrow - cb + t5::TM - 1) / t5::TM, tn = (ce - cb + t5::TN - 1) / t5::TN;
-    k_wide_trailing_t5<<<tm * tn, t5::THREADS, t5::smem_bytes(1), st>>>(
-        reinterpret_cast<float *>(S), nrow, kL, K, cb, ce, reinterpret_cast<const float *>(Wb) + (size_t)woff * nrow,
-        nrow, tn, halt, status);
+    if (pack_a) {
+      const int blk0 = cb / t5::TM;
+      const int nrb = nrb_all - blk0, ncb = (ce + t5::TN - 1) / t5::TN - blk0;
+      const int ntile = ncb * nrb - ncb * (ncb - 1) / 2;
+      const int G = std::max(1, std::min(ntile, num_sms));
+      float *Sf = reinterpret_cast<float *>(S);
+      k_wide_trailing_pers<<<G, TP_THREADS, tp_smem_bytes(), st>>>(Sf, nrow, cb, ce, pack_a, pack_b, nkc_stride,
+                                                                   kca, kcb, blk0, nrb, ncb, ntile, halt, status);
+    } else {
+      const int tm = (nrow - cb + t5::TM - 1) / t5::TM, tn = (ce - cb + t5::TN - 1) / t5::TN;
+      k_wide_trailing_t5<<<tm * tn, t5::THREADS, t5::smem_bytes(1), st>>>(
+          reinterpret_cast<float *>(S), nrow, kL, K, cb, ce,
+          reinterpret_cast<const float *>(Wb) + (size_t)woff * nrow, nrow, tn, halt, status);
+    }
     if (cudaGetLastError() != cudaSuccess) return NQG_ERR_CUDA;
     if (P) {
       P->nlaunch++;
@@ -1323,16 +1603,17 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     if (!delayed) return NQG_OK;
     int rc;
     if (general && s.npend > 0) {
-      if ((rc = apply(s.pend_k0, s.pend_K, 0, s.F, w))) return rc;
+      if ((rc = apply(s.pend_k0, s.pend_K, 0, 0, s.pend_C, s.F, w))) return rc;
       s.npend = 0;
       s.pend_K = 0;
+      s.pend_C = 0;
       s.F = s.k0;
     }
     // a general panel may end with a 2x2 pivot one column past nb; a fast
     // panel never goes past nb, so its band stops at k0 + nb and a complete
     // fast panel leaves no remainder of its own update to apply
     const int bend = std::min(w, s.k0 + nb + (general ? 1 : 0));
-    if (s.npend > 0 && s.F < bend && (rc = apply(s.pend_k0, s.pend_K, 0, s.F, bend))) return rc;
+    if (s.npend > 0 && s.F < bend && (rc = apply(s.pend_k0, s.pend_K, 0, 0, s.pend_C, s.F, bend))) return rc;
     s.F = std::max(s.F, bend);
     return NQG_OK;
   };
@@ -1341,16 +1622,21 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     const int k0 = s.k0, k1 = k0 + kb;
     int rc;
     if (delayed) {
-      if (k1 < s.F && (rc = apply(k0, kb, woff, k1, s.F))) return rc;
+      if ((rc = pack_panel(k0, kb, woff, s.pend_C))) return rc;
+      if (k1 < s.F && (rc = apply(k0, kb, woff, s.pend_C, s.pend_C + nch(kb), k1, s.F))) return rc;
       if (s.npend == 0) s.pend_k0 = k0;
       s.pend_K += kb;
+      s.pend_C += nch(kb);
       ++s.npend;
       if (s.npend == depth || k1 >= w) {
-        if ((rc = apply(s.pend_k0, s.pend_K, 0, s.F, w))) return rc;
+        if ((rc = apply(s.pend_k0, s.pend_K, 0, 0, s.pend_C, s.F, w))) return rc;
         s.npend = 0;
         s.pend_K = 0;
+        s.pend_C = 0;
         s.F = k1;
       }
+    } else if (k1 < w && pack_a) {
+      if ((rc = pack_panel(k0, kb, 0, 0)) || (rc = apply(k0, kb, 0, 0, nch(kb), k1, w))) return rc;
     } else if (k1 < w) {
       cudaEvent_t e1 = P ? P->prof_begin() : nullptr;
       if (sizeof(T) == 4 && trail == 2) {

@@ -211,15 +211,16 @@ def test_fp64_blocked_wide_kernels(path, monkeypatch):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("trailing", ["tcgen05", "tcgen05-depth1", "tcgen05-depth2", "mma", "simt",
+@pytest.mark.parametrize("trailing", ["tcgen05", "tcgen05-depth1", "tcgen05-depth2", "tcgen05-tile", "mma", "simt",
                                       "general-panels"])
 @pytest.mark.parametrize("path", CASES, ids=os.path.basename)
 def test_fp32_blocked_wide_kernels(path, trailing, monkeypatch):
     """FP32 factor with every supernode wider than 12 columns in the blocked
     kernels (fast panels where no pivot search is needed, or every panel on
     the general kernel), trailing updates on the tcgen05 tensor cores (one,
-    two or four panels per delayed update) or with mma.sync (both split TF32)
-    or on CUDA cores:
+    two or four panels per delayed update; the persistent kernel on packed
+    operands or one CTA per tile) or with mma.sync (both split TF32) or on
+    CUDA cores:
     the refined solution meets the FP32 bar of the single-CTA kernels."""
     for k, v in WIDE_ENV.items():
         monkeypatch.setenv(k, v)
@@ -227,6 +228,8 @@ def test_fp32_blocked_wide_kernels(path, trailing, monkeypatch):
         monkeypatch.setenv("NASOQ_GB300_PANEL", "general")
     elif trailing.startswith("tcgen05-depth"):
         monkeypatch.setenv("NASOQ_GB300_WIDE_DEPTH", trailing[-1])
+    elif trailing == "tcgen05-tile":
+        monkeypatch.setenv("NASOQ_GB300_TRAILING", "tile")
     else:
         monkeypatch.setenv("NASOQ_GB300_TRAILING", trailing)
     d = nqa.load(path)
@@ -337,6 +340,52 @@ def test_fast_panel_kernels_agree(n, pivots, monkeypatch):
         out[mode] = plan.factor_arrays()
     for a, b in zip(out["group"], out["block"]):
         assert np.array_equal(a, b)
+    rhs = rng.standard_normal(n)
+    x = plan.solve(rhs)
+    assert np.linalg.norm(rhs - M @ x) <= 1e-10 * np.linalg.norm(rhs)
+    plan.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,pivots", [(1024, False), (1100, True)])
+def test_trailing_kernels_agree(n, pivots, monkeypatch):
+    """One dense FP32 supernode: the persistent tcgen05 trailing update on
+    packed split-TF32 operands against the one-CTA-per-tile kernel that
+    splits its operands while loading them.  With full 64-column panels both
+    sum the same products in the same chunks of 32, so the factors agree bit
+    for bit; with pivot searches (panels of any width, padded chunks) both
+    factors reach a backward error of 1e-4 max(|L||D||L|^T) (no diagonal
+    floor) and the refined solution the FP32 bar."""
+    rng = np.random.default_rng(7 * n + pivots)
+    M = rng.standard_normal((n, n))
+    M = (M + M.T) / 2
+    dg = rng.uniform(0.5 * n, n, n) * rng.choice([-1.0, 1.0], n)
+    if pivots:
+        dg[rng.choice(n, n // 40, replace=False)] = 1e-3
+    M[np.diag_indices(n)] = dg
+    Ap, Ai, Ax = _dense_lower_csc(M)
+    st = nq.default_settings(precision=nq.NQG_FP32, req_ref_iter=6, max_inner_iter=6, tol_abs=1e-13,
+                             tol_rel=1e-13, reg_diag=0.0, reg_diag_fp32=1e-30)
+    plan = nq.Plan(n, Ap, Ai, Ax, settings=st)
+    assert plan.symbolic.info.nsuper == 1
+    monkeypatch.setenv("NASOQ_GB300_TRAILING", "tile")
+    assert plan.factor() == 0
+    out = {}
+    for mode in ("tile", "persistent"):
+        if mode == "tile":
+            monkeypatch.setenv("NASOQ_GB300_TRAILING", "tile")
+        else:
+            monkeypatch.delenv("NASOQ_GB300_TRAILING", raising=False)
+        assert plan.factor() == 0
+        out[mode] = plan.factor_arrays()
+        vals, dv, perm, ls = out[mode]
+        Ld, Dd = dense_factor(plan.symbolic, vals, dv, ls)
+        R = M[np.ix_(perm, perm)] - Ld @ Dd @ Ld.T
+        mag = np.abs(Ld) @ np.abs(Dd) @ np.abs(Ld).T
+        assert np.abs(R).max() <= 1e-4 * mag.max(), mode
+    if not pivots:
+        for a, b in zip(out["tile"], out["persistent"]):
+            assert np.array_equal(a, b)
     rhs = rng.standard_normal(n)
     x = plan.solve(rhs)
     assert np.linalg.norm(rhs - M @ x) <= 1e-10 * np.linalg.norm(rhs)
