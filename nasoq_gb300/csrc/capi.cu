@@ -163,10 +163,14 @@ static void build_schedule(Plan &P) {
   P.pair_lb.clear();
   P.pair_ub.clear();
   P.pair_flops.clear();
+  P.pair_pers.clear();
   P.tile_ptr.assign(ns + 1, 0);
   P.tiles.clear();
   P.tile_ptr_tc.assign(ns + 1, 0);
   P.tiles_tc.clear();
+  P.pers_ptr.assign(ns + 1, 0);
+  P.pers_pair.clear();
+  P.pers_map_ints = 0;
   // FP32 plans: pairs whose descendant has at least UPD_TC_MIN_WD columns
   // (NASOQ_GB300_UPDATE_TC_MIN overrides) take 128 x 128 tensor-core tiles;
   // NASOQ_GB300_UPDATE=simt keeps them all on the CUDA-core kernel
@@ -174,6 +178,10 @@ static void build_schedule(Plan &P) {
   const bool tc = P.set.precision == NQG_FP32 && !(ue && std::string(ue) == "simt");
   int tc_min_wd = UPD_TC_MIN_WD;
   if (const char *e = std::getenv("NASOQ_GB300_UPDATE_TC_MIN")) tc_min_wd = std::max(1, std::atoi(e));
+  // pairs of at least this many useful flops go to the persistent kernel
+  // (NASOQ_GB300_UPDATE_PERSIST_MIN; a negative value keeps every pair on tiles)
+  double pers_min = 1e10;
+  if (const char *e = std::getenv("NASOQ_GB300_UPDATE_PERSIST_MIN")) pers_min = std::atof(e);
   for (int s = 0; s < ns; ++s) {
     ereach_sn(S, P.Uord, s, S.sparent, mark, stack, lst);
     const int c1 = S.super[s], c2 = S.super[s + 1];
@@ -190,8 +198,13 @@ static void build_schedule(Plan &P) {
         // useful multiply-adds: lower trapezoid of the (nr-lb) x (ub-lb+1) block, depth = width of d
         const double m = nr - lb, nc = ub - lb + 1, wd = S.super[d + 1] - S.super[d];
         P.pair_flops.push_back(2.0 * wd * (nc * m - nc * (nc - 1) / 2.0));
+        P.pair_pers.push_back(0);
       }
-      if (tc && S.super[d + 1] - S.super[d] >= tc_min_wd) {
+      if (tc && S.super[d + 1] - S.super[d] >= tc_min_wd && pers_min >= 0 && P.pair_flops.back() >= pers_min) {
+        P.pers_pair.push_back((int)P.pair_d.size() - 1);
+        P.pair_pers.back() = 1;
+        P.pers_map_ints = std::max<int64_t>(P.pers_map_ints, (int64_t)(nr - lb) + (ub - lb + 1));
+      } else if (tc && S.super[d + 1] - S.super[d] >= tc_min_wd) {
         for (int ri = lb; ri < nr; ri += UPD_TC_T)
           for (int cj = lb; cj <= ub; cj += UPD_TC_T)
             if (ri + UPD_TC_T - 1 >= cj) P.tiles_tc.push_back(UpdTile{s, d, ri, cj, ub});
@@ -204,6 +217,7 @@ static void build_schedule(Plan &P) {
     P.pair_ptr[s + 1] = (int)P.pair_d.size();
     P.tile_ptr[s + 1] = (int64_t)P.tiles.size();
     P.tile_ptr_tc[s + 1] = (int64_t)P.tiles_tc.size();
+    P.pers_ptr[s + 1] = (int)P.pers_pair.size();
   }
 }
 
@@ -432,17 +446,30 @@ static int upload_plan(Plan &P) {
     if (wide_rows > 0)
       NQG_CUDA(cudaMalloc(&P.d_wide_W,
                           (size_t)wide_rows * (P.wide_depth * (P.wide_nb + 1) + 2) * P.val_size()));
-    // FP32: packed operands of the persistent trailing update -- row blocks
-    // of 128 (L rows, then W rows) x wide_depth panels of chunks of 32
-    // columns, hi + lo TF32 halves of 16 KB each
-    if (wide_rows > 0 && P.set.precision == NQG_FP32) {
-      int64_t blocks = 0;
-      for (int s = 0; s < ns; ++s)
-        if (S.super[s + 1] - S.super[s] > P.wide_min)
-          blocks = std::max<int64_t>(blocks, (S.lpi[s + 1] - S.lpi[s] + 127) / 128 +
-                                                 (S.super[s + 1] - S.super[s] + 127) / 128);
-      const int64_t nkc = (int64_t)std::max(P.wide_depth, 1) * ((P.wide_nb + 1 + 31) / 32);
-      NQG_CUDA(cudaMalloc(&P.d_wide_pack, (size_t)(blocks * nkc) * 32768));
+    // FP32: packed split-TF32 operands of the persistent tcgen05 updates,
+    // blocks of 128 rows x 32 columns (hi + lo TF32 halves of 16 KB each).
+    // Trailing updates of a wide supernode: row blocks of L then of W, each
+    // wide_depth panels of chunks; a persistent descendant pair: row blocks
+    // of L D then of L, the descendant's width in chunks.  One buffer serves
+    // both (they never run at the same time).
+    if (P.set.precision == NQG_FP32) {
+      int64_t chunks = 0;
+      if (wide_rows > 0) {
+        int64_t blocks = 0;
+        for (int s = 0; s < ns; ++s)
+          if (S.super[s + 1] - S.super[s] > P.wide_min)
+            blocks = std::max<int64_t>(blocks, (S.lpi[s + 1] - S.lpi[s] + 127) / 128 +
+                                                   (S.super[s + 1] - S.super[s] + 127) / 128);
+        chunks = blocks * (int64_t)std::max(P.wide_depth, 1) * ((P.wide_nb + 1 + 31) / 32);
+      }
+      for (int q : P.pers_pair) {
+        const int d = P.pair_d[q];
+        const int64_t m = (S.lpi[d + 1] - S.lpi[d]) - P.pair_lb[q], nc = P.pair_ub[q] - P.pair_lb[q] + 1;
+        const int64_t wd = S.super[d + 1] - S.super[d];
+        chunks = std::max<int64_t>(chunks, ((m + 127) / 128 + (nc + 127) / 128) * ((wd + 31) / 32));
+      }
+      if (chunks > 0) NQG_CUDA(cudaMalloc(&P.d_wide_pack, (size_t)chunks * 32768));
+      if (P.pers_map_ints > 0) NQG_CUDA(cudaMalloc(&P.d_pers_map, (size_t)P.pers_map_ints * sizeof(int)));
     }
     // control block: grid barriers of the blocked factorization, abort flag
     // of the block solves
@@ -458,7 +485,7 @@ static void free_plan(Plan &P) {
                   P.d_perm_tmp, P.d_L, P.d_D, P.d_tiles, P.d_tile_list, P.d_targets, P.d_pair_s, P.d_pair_d,
                   P.d_pair_lb, P.d_pair_ub, P.d_targets_lv, P.d_pivoted, P.d_visible, P.d_hidden, P.d_status,
                   P.d_xo, P.d_bo, P.d_r, P.d_w, P.d_in, P.d_out, P.d_V, P.d_scal, P.d_wide_W, P.d_wide_ctl,
-                  P.d_wide_pack, P.d_locinv, P.d_pair_roff, P.d_rr_dest, P.d_rr_moved, P.d_rr_items, P.d_rr_stage,
+                  P.d_wide_pack, P.d_pers_map, P.d_locinv, P.d_pair_roff, P.d_rr_dest, P.d_rr_moved, P.d_rr_items, P.d_rr_stage,
                   P.d_solve_flags, P.d_blk_items, P.d_flagoff, P.d_xf, P.d_Z, P.d_tiles_tc,
                   P.d_tile_list_tc, P.d_row_items};
   for (void *p : ptrs)

@@ -1069,7 +1069,8 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
       if (P.prof)
         for (int s : P.levels[l])
           if (mark[s])
-            for (int q = P.pair_ptr[s]; q < P.pair_ptr[s + 1]; ++q) fl += P.pair_flops[q];
+            for (int q = P.pair_ptr[s]; q < P.pair_ptr[s + 1]; ++q)
+              if (!P.pair_pers[q]) fl += P.pair_flops[q];
       cudaEvent_t e0 = P.prof_begin();
       if (lv_tile_cnt[l] > 0) {
         k_update<T><<<(unsigned)lv_tile_cnt[l], UPD_THREADS, 0, st>>>(P.d_tiles, P.d_tile_list + lv_tile_off[l],
@@ -1086,6 +1087,15 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
         }
       }
       P.prof_end(NQG_K_UPDATE, e0, fl, 0.0);
+    }
+    if constexpr (sizeof(T) == 4) {
+      // the largest pairs of this level, one persistent launch each
+      for (int s : P.levels[l])
+        if (mark[s])
+          for (int k = P.pers_ptr[s]; k < P.pers_ptr[s + 1]; ++k) {
+            int rc = update_pair_persistent(P, s, P.pers_pair[k], L, D);
+            if (rc) return rc;
+          }
     }
     if (lv_small_cnt[l] + lv_glob_cnt[l] > 0) {
       double fl = 0;

@@ -67,6 +67,12 @@ struct Plan {
   std::vector<UpdTile> tiles;
   std::vector<int64_t> tile_ptr_tc;  // per supernode s: range of its tensor-core update tiles
   std::vector<UpdTile> tiles_tc;
+  // FP32: descendant pairs with at least pers_min_flops useful flops run as
+  // one persistent tcgen05 launch each on packed operands instead of tiles
+  std::vector<int> pers_ptr;        // per supernode s: range in pers_pair
+  std::vector<int> pers_pair;       // pair indices
+  std::vector<uint8_t> pair_pers;   // per pair: 1 if it is one of them
+  int64_t pers_map_ints = 0;        // largest rows + columns of such a pair
   std::vector<int> wide;            // supernodes factored by the blocked kernel
   int64_t ssize = 0;
 
@@ -129,7 +135,8 @@ struct Plan {
   // wide supernodes (blocked cooperative BK)
   void *d_wide_W = nullptr;         // panel buffer, max nrow x (nb+2)
   void *d_wide_ctl = nullptr;       // barrier / reduction control block
-  unsigned char *d_wide_pack = nullptr;  // FP32: split-TF32 operand blocks of the trailing updates
+  unsigned char *d_wide_pack = nullptr;  // FP32: split-TF32 operand blocks of the tcgen05 updates
+  int *d_pers_map = nullptr;              // target positions of a persistent pair's rows and columns
   unsigned *d_solve_flags = nullptr;  // per 64-column block ready flags of the block solves
   int solve_flags_cap = 0;
   unsigned solve_epoch = 0;
@@ -172,6 +179,9 @@ int dev_factor(Plan &P, const std::vector<int> *subset);
 struct WideCtl;
 size_t wide_ctl_bytes();
 template <class T> int factor_wide(Plan &P, int s, T *L, T *Dg, int nb, T *Wb, WideCtl *ctl, int num_sms);
+// Schur update of target s by descendant pair q on the persistent tcgen05
+// kernel (FP32 plans).
+int update_pair_persistent(Plan &P, int s, int q, float *L, const float *Dg);
 // solve_wide.cu
 template <class T, class V> int solve_blk_fwd(Plan &P, int level, const T *L, V *x);
 template <class T, class V> int solve_blk_bwd(Plan &P, int level, const T *L, V *x);

@@ -1199,16 +1199,17 @@ __global__ void __launch_bounds__(t5::THREADS) k_wide_trailing_t5(float *S, int 
 // then lo, 16 KB each, in the swizzled K-major layout of
 // t5::store_row_split), block (rb, kc) at rb * nkc_stride + kc, row blocks at
 // absolute 128-row positions of the supernode, every panel starting on a new
-// chunk (zeros pad a partial chunk).  k_wide_trailing_pers then runs one CTA
+// chunk (zeros pad a partial chunk).  k_tc_persistent then runs one CTA
 // per SM over the lower-triangular set of 128 x 128 tiles: warp 0 streams
 // both operand blocks of each K chunk into a three-stage shared-memory ring
 // with bulk copies, warp 1 issues the split-TF32 MMAs (the same three
 // products per K step as t5::tile_tf32x3) into one of two TMEM accumulators,
-// and warps 2-5 subtract the finished accumulator from S while the next tile
-// accumulates in the other one.
+// and warps 2-9 (two per TMEM lane quarter, 64 columns each) subtract the
+// finished accumulator from S while the next tile accumulates in the other
+// one; they load their S values before the accumulator is ready.
 constexpr int PK_BLOCK = 2 * t5::OPND_BYTES;  // hi + lo of one 128 x 32 block
 constexpr int TP_STAGES = 3;
-constexpr int TP_THREADS = 192;
+constexpr int TP_THREADS = 320;  // producer warp, MMA warp, 8 epilogue warps
 
 __host__ __device__ constexpr size_t tp_smem_bytes() { return (size_t)TP_STAGES * t5::STAGE_BYTES + 1024; }
 
@@ -1217,7 +1218,7 @@ __host__ __device__ constexpr size_t tp_smem_bytes() { return (size_t)TP_STAGES 
 __global__ void __launch_bounds__(256) k_pack_split(const float *src, int ld, int row_hi, int kb, unsigned char *dst,
                                                     int nkc_stride, int kc0, int rb_first, const int *halt) {
   __shared__ float tk[t5::TK][t5::TM + 1];
-  if (*(volatile const int *)halt) return;  // queued behind a fast panel that stopped early
+  if (halt && *(volatile const int *)halt) return;  // queued behind a fast panel that stopped early
   const int rb = rb_first + blockIdx.x, kcl = blockIdx.y;
   const int r0 = rb * t5::TM, k0 = kcl * t5::TK;
   for (int e = threadIdx.x; e < t5::TK * t5::TM; e += blockDim.x) {
@@ -1240,6 +1241,71 @@ __global__ void __launch_bounds__(256) k_pack_split(const float *src, int ld, in
     const int off = r * 128 + ((c ^ (r & 7)) << 4);
     *reinterpret_cast<uint4 *>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
     *reinterpret_cast<uint4 *>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+  }
+}
+
+// Split-TF32 blocks of (L D)(i, k) = d_k L(i, k) + e_k L(i, k+1) + e_{k-1}
+// L(i, k-1) for rows [0, row_hi) and columns [0, kb) of src (element (i, t)
+// at src[i + t * ld]; d, e the descendant's diagonal and 2 x 2 sub-diagonal),
+// in the layout of k_pack_split, chunk kc of row block rb at rb * nkc + kc.
+__global__ void __launch_bounds__(256) k_pack_ld(const float *src, int ld, int row_hi, int kb, const float *Dd,
+                                                 const float *Ed, unsigned char *dst, int nkc) {
+  __shared__ float tk[t5::TK + 2][t5::TM + 1];
+  const int rb = blockIdx.x, kc = blockIdx.y;
+  const int r0 = rb * t5::TM, k0 = kc * t5::TK;
+  for (int e = threadIdx.x; e < (t5::TK + 2) * t5::TM; e += blockDim.x) {
+    const int q = e / t5::TM, r = e % t5::TM, t = k0 - 1 + q, gr = r0 + r;
+    tk[q][r] = (gr < row_hi && t >= 0 && t < kb) ? __ldcg(src + gr + (size_t)t * ld) : 0.f;
+  }
+  __syncthreads();
+  unsigned char *hi = dst + ((size_t)rb * nkc + kc) * PK_BLOCK, *lo = hi + t5::OPND_BYTES;
+  const int r = threadIdx.x >> 1;
+#pragma unroll
+  for (int cc = 0; cc < 4; ++cc) {
+    const int c = (threadIdx.x & 1) * 4 + cc;
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int k = 4 * c + q, t = k0 + k;
+      const float dk = t < kb ? Dd[t] : 0.f, ek = t < kb ? Ed[t] : 0.f;
+      const float em = (t >= 1 && t - 1 < kb) ? Ed[t - 1] : 0.f;
+      const float x = dk * tk[k + 1][r] + ek * tk[k + 2][r] + em * tk[k][r];
+      h[q] = t5::tf32_rna(x);
+      l[q] = t5::tf32_rna(x - __uint_as_float(h[q]));
+    }
+    const int off = r * 128 + ((c ^ (r & 7)) << 4);
+    *reinterpret_cast<uint4 *>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+  }
+}
+
+// Target positions of a descendant pair: row i (< m) of the pair's rows goes
+// to row prow[i] of the target supernode (cs0, ws columns, nrs rows listed in
+// rows_s), column j (< nc) to column pcol[j]; -1 and ST_BOUNDS when absent.
+__global__ void k_pair_map(const int *rows, int m, int nc, const int *rows_s, int nrs, int cs0, int ws, int *prow,
+                           int *pcol, int *status) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const int r = rows[i];
+    int pos;
+    if (r < cs0 + ws) {
+      pos = r - cs0;
+    } else {
+      int lo = ws, hi = nrs;  // first listed row >= r
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (rows_s[mid] < r) lo = mid + 1;
+        else hi = mid;
+      }
+      pos = (lo < nrs && rows_s[lo] == r) ? lo : -1;
+    }
+    if (pos < 0) atomicOr(status, ST_BOUNDS);
+    prow[i] = pos;
+    if (i < nc) {
+      const int c = r - cs0;
+      const bool ok = c >= 0 && c < ws;
+      if (!ok) atomicOr(status, ST_BOUNDS);
+      pcol[i] = ok ? c : -1;
+    }
   }
 }
 
@@ -1268,18 +1334,24 @@ __device__ __forceinline__ bool tp_wait(uint32_t mbar, uint32_t parity, volatile
   return false;
 }
 
-// S[gr, gc] -= sum over chunks kc0 .. kc1-1 of A(gr, :) B(gc, :)^T for
-// gc in [cb, ce), gr >= gc, gr < nrow; tiles of blocks blk0 + (rbl, cbl).
-__global__ void __launch_bounds__(TP_THREADS, 1) k_wide_trailing_pers(float *S, int nrow, int cb, int ce,
-                                                                      const unsigned char *pack_a,
-                                                                      const unsigned char *pack_b, int nkc_stride,
-                                                                      int kc0, int kc1, int blk0, int nrb, int ncb,
-                                                                      int ntile, const int *halt, int *status) {
+// Sum over chunks kc0 .. kc1-1 of A(i, :) B(j, :)^T for the tiles of blocks
+// blk0 + (rbl, cbl), subtracted from S:
+//   MAPPED = false (trailing update, S column-major with leading dimension
+//     nrow): at S[i, j] for j in [cb, ce), i >= j, i < nrow;
+//   MAPPED = true (descendant pair, i, j relative to its first row): at
+//     S[prow[i] + pcol[j] * nrow] for i < mrows, j < ncols, j <= i.
+template <bool MAPPED>
+__global__ void __launch_bounds__(TP_THREADS, 1) k_tc_persistent(float *S, int nrow, int cb, int ce,
+                                                                 const unsigned char *pack_a,
+                                                                 const unsigned char *pack_b, int nkc_stride, int kc0,
+                                                                 int kc1, int blk0, int nrb, int ncb, int ntile,
+                                                                 const int *halt, int *status, const int *prow,
+                                                                 const int *pcol, int mrows, int ncols) {
   extern __shared__ __align__(1024) unsigned char tp_raw[];
   __shared__ __align__(8) uint64_t bar[2 * TP_STAGES + 4];
   __shared__ uint32_t s_tmem;
   __shared__ int s_abort;
-  if (*(volatile const int *)halt) return;  // queued behind a fast panel that stopped early
+  if (halt && *(volatile const int *)halt) return;  // queued behind a fast panel that stopped early
   unsigned char *base =
       reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(tp_raw) + 1023) & ~(uintptr_t)1023);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -1293,7 +1365,7 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_wide_trailing_pers(float *S, 
     }
     for (int b = 0; b < 2; ++b) {
       t5::mbar_init(t5::smem_u32(&accf[b]), 1);
-      t5::mbar_init(t5::smem_u32(&acce[b]), 4);
+      t5::mbar_init(t5::smem_u32(&acce[b]), (TP_THREADS - 64) / 32);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -1373,41 +1445,91 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_wide_trailing_pers(float *S, 
       if (any) t5::mbar_wait(last_bar, last_par);
     }
   } else {
-    // epilogue: thread = TMEM lane = tile row
-    const int q = warp & 3, r = q * 32 + lane;
-    int i = 0;
-    for (int t = blockIdx.x; t < ntile; t += G, ++i) {
-      const int buf = i & 1;
-      const uint32_t u = (uint32_t)i >> 1;
-      int rbl, cbl;
-      tp_tile(t, nrb, ncb, rbl, cbl);
-      const int gr = (blk0 + rbl) * t5::TM + r, gc0 = (blk0 + cbl) * t5::TN;
-      // one lane waits, so that the whole warp leaves or goes on together
-      int okw = 0;
-      if (lane == 0) okw = tp_wait(t5::smem_u32(&accf[buf]), u & 1, abort, status) ? 1 : 0;
-      if (!__shfl_sync(0xffffffffu, okw, 0)) break;
-      t5::fence_after();
+    if constexpr (MAPPED) {
+      // epilogue: thread = TMEM lane = tile row, 64 of the tile's columns
+      const int q = warp & 3, r = q * 32 + lane, cofs = ((warp - 2) >> 2) * 64;
+      int i = 0;
+      for (int t = blockIdx.x; t < ntile; t += G, ++i) {
+        const int buf = i & 1;
+        const uint32_t u = (uint32_t)i >> 1;
+        int rbl, cbl;
+        tp_tile(t, nrb, ncb, rbl, cbl);
+        const int gi = (blk0 + rbl) * t5::TM + r, gj0 = (blk0 + cbl) * t5::TN + cofs;
+        const int pr = gi < mrows ? prow[gi] : -1;
+        const int jhi = pr >= 0 ? min(64, min(ncols - gj0, gi - gj0 + 1)) : 0;  // columns gj0 + [0, jhi)
+        int okw = 0;
+        if (lane == 0) okw = tp_wait(t5::smem_u32(&accf[buf]), u & 1, abort, status) ? 1 : 0;
+        if (!__shfl_sync(0xffffffffu, okw, 0)) break;
+        t5::fence_after();
 #pragma unroll 1
-      for (int cc = 0; cc < t5::TN; cc += 32) {
-        uint32_t v[32];
-        t5::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * t5::TN + cc), v);
-        if (gr < nrow) {
+        for (int g = 0; g < 2; ++g) {
+          uint32_t v[32];
+          t5::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * t5::TN + cofs + g * 32), v);
           float cur[32];
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
-            const int gc = gc0 + cc + j;
-            cur[j] = (gc >= cb && gc < ce && gr >= gc) ? S[gr + (size_t)gc * nrow] : 0.f;
+            const int jj = g * 32 + j;
+            const int pc = jj < jhi ? __ldg(pcol + gj0 + jj) : -1;
+            cur[j] = pc >= 0 ? S[(size_t)pc * nrow + pr] : 0.f;
           }
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
-            const int gc = gc0 + cc + j;
-            if (gc >= cb && gc < ce && gr >= gc) S[gr + (size_t)gc * nrow] = cur[j] - __uint_as_float(v[j]);
+            const int jj = g * 32 + j;
+            const int pc = jj < jhi ? __ldg(pcol + gj0 + jj) : -1;
+            if (pc >= 0) S[(size_t)pc * nrow + pr] = cur[j] - __uint_as_float(v[j]);
           }
         }
+        t5::fence_before();
+        __syncwarp();
+        if (lane == 0) t5::mbar_arrive(t5::smem_u32(&acce[buf]));
       }
-      t5::fence_before();
-      __syncwarp();
-      if (lane == 0) t5::mbar_arrive(t5::smem_u32(&acce[buf]));
+    } else {
+      // epilogue: thread = TMEM lane = tile row, 64 of the tile's columns
+      const int q = warp & 3, r = q * 32 + lane, cofs = ((warp - 2) >> 2) * 64;
+      int i = 0;
+      for (int t = blockIdx.x; t < ntile; t += G, ++i) {
+        const int buf = i & 1;
+        const uint32_t u = (uint32_t)i >> 1;
+        int rbl, cbl;
+        tp_tile(t, nrb, ncb, rbl, cbl);
+        const int gr = (blk0 + rbl) * t5::TM + r, gc0 = (blk0 + cbl) * t5::TN + cofs;
+        // columns gc0 + [jlo, jhi) of row gr are in the update (gc >= cb,
+        // gc < ce, gc <= gr); their current values are loaded first, so that
+        // the latency overlaps the tile's MMAs
+        const int jlo = max(0, cb - gc0);
+        const int jhi = gr < nrow ? min(64, min(ce - gc0, gr - gc0 + 1)) : 0;
+        float *row = S + gr + (size_t)gc0 * nrow;
+        const size_t ld = (size_t)nrow;
+        float cur[64];
+        {
+          const float *pp = row;
+#pragma unroll
+          for (int j = 0; j < 64; ++j) {
+            cur[j] = (j >= jlo && j < jhi) ? __ldcs(pp) : 0.f;
+            pp += ld;
+          }
+        }
+        // one lane waits, so that the whole warp leaves or goes on together
+        int okw = 0;
+        if (lane == 0) okw = tp_wait(t5::smem_u32(&accf[buf]), u & 1, abort, status) ? 1 : 0;
+        if (!__shfl_sync(0xffffffffu, okw, 0)) break;
+        t5::fence_after();
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+          uint32_t v[32];
+          t5::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * t5::TN + cofs + g * 32), v);
+          float *pp = row + (size_t)(g * 32) * ld;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int jj = g * 32 + j;
+            if (jj >= jlo && jj < jhi) *pp = cur[jj] - __uint_as_float(v[j]);
+            pp += ld;
+          }
+        }
+        t5::fence_before();
+        __syncwarp();
+        if (lane == 0) t5::mbar_arrive(t5::smem_u32(&acce[buf]));
+      }
     }
   }
   t5::fence_before();
@@ -1465,7 +1587,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   const int nkc_stride = std::max(depth, 1) * nch_panel;
   const int nrb_all = (nrow + t5::TM - 1) / t5::TM, ncb_all = (w + t5::TN - 1) / t5::TN;
   unsigned char *pack_b = pack_a ? pack_a + (size_t)nrb_all * nkc_stride * PK_BLOCK : nullptr;
-  if (pack_a && cudaFuncSetAttribute(k_wide_trailing_pers, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (pack_a && cudaFuncSetAttribute(k_tc_persistent<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)tp_smem_bytes()) != cudaSuccess)
     return NQG_ERR_CUDA;
   if (sizeof(T) == 4 && trail == 1 &&
@@ -1581,8 +1703,9 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       const int ntile = ncb * nrb - ncb * (ncb - 1) / 2;
       const int G = std::max(1, std::min(ntile, num_sms));
       float *Sf = reinterpret_cast<float *>(S);
-      k_wide_trailing_pers<<<G, TP_THREADS, tp_smem_bytes(), st>>>(Sf, nrow, cb, ce, pack_a, pack_b, nkc_stride,
-                                                                   kca, kcb, blk0, nrb, ncb, ntile, halt, status);
+      k_tc_persistent<false><<<G, TP_THREADS, tp_smem_bytes(), st>>>(Sf, nrow, cb, ce, pack_a, pack_b, nkc_stride,
+                                                                     kca, kcb, blk0, nrb, ncb, ntile, halt, status,
+                                                                     nullptr, nullptr, 0, 0);
     } else {
       const int tm = (nrow - cb + t5::TM - 1) / t5::TM, tn = (ce - cb + t5::TN - 1) / t5::TN;
       k_wide_trailing_t5<<<tm * tn, t5::THREADS, t5::smem_bytes(1), st>>>(
@@ -1824,6 +1947,44 @@ int factor_wide(Plan &P, int s, T *L, T *Dg, int nb, T *Wb, WideCtl *ctl, int nu
   uint8_t pv = piv ? 1 : 0;
   NQG_CUDA(cudaMemcpyAsync(P.d_pivoted + s, &pv, 1, cudaMemcpyHostToDevice, P.stream));
   NQG_CUDA(cudaStreamSynchronize(P.stream));
+  return NQG_OK;
+}
+
+// Schur update of target s by descendant pair q as one persistent launch:
+// target positions, packed (L D) rows and L rows of the pair, then the
+// tcgen05 product subtracted in place (the pair's tiles are disjoint, and no
+// other update of the target runs at the same time).
+int update_pair_persistent(Plan &P, int s, int q, float *L, const float *Dg) {
+  const int d = P.pair_d[q], lb = P.pair_lb[q], ub = P.pair_ub[q];
+  const int c0 = P.sym.super[d], wd = P.sym.super[d + 1] - c0;
+  const int nrd = (int)(P.sym.lpi[d + 1] - P.sym.lpi[d]);
+  const int cs0 = P.sym.super[s], ws = P.sym.super[s + 1] - cs0;
+  const int nrs = (int)(P.sym.lpi[s + 1] - P.sym.lpi[s]);
+  const int m = nrd - lb, nc = ub - lb + 1;
+  if (m <= 0 || nc <= 0 || wd <= 0) return NQG_OK;
+  const int nkc = (wd + t5::TK - 1) / t5::TK, nrb = (m + t5::TM - 1) / t5::TM, ncb = (nc + t5::TN - 1) / t5::TN;
+  unsigned char *pa = P.d_wide_pack, *pb = pa + (size_t)nrb * nkc * PK_BLOCK;
+  int *prow = P.d_pers_map, *pcol = prow + m;
+  if (!pa || !prow) return NQG_ERR_ARG;
+  cudaStream_t st = P.stream;
+  if (cudaFuncSetAttribute(k_tc_persistent<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)tp_smem_bytes()) != cudaSuccess)
+    return NQG_ERR_CUDA;
+  cudaEvent_t e0 = P.prof_begin();
+  k_pair_map<<<std::min((m + 255) / 256, 1024), 256, 0, st>>>(P.d_ls + P.sym.lpi[d] + lb, m, nc,
+                                                              P.d_ls + P.sym.lpi[s], nrs, cs0, ws, prow, pcol,
+                                                              P.d_status);
+  const float *Ld = L + P.sym.lpx[d] + lb;
+  k_pack_ld<<<dim3(nrb, nkc), 256, 0, st>>>(Ld, nrd, m, wd, Dg + c0, Dg + P.n + c0, pa, nkc);
+  k_pack_split<<<dim3(ncb, nkc), 256, 0, st>>>(Ld, nrd, nc, wd, pb, nkc, 0, 0, nullptr);
+  const int ntile = ncb * nrb - ncb * (ncb - 1) / 2;
+  const int G = std::max(1, std::min(ntile, P.num_sms));
+  k_tc_persistent<true><<<G, TP_THREADS, tp_smem_bytes(), st>>>(L + P.sym.lpx[s], nrs, 0, 0, pa, pb, nkc, 0, nkc, 0,
+                                                                nrb, ncb, ntile, nullptr, P.d_status, prow, pcol, m,
+                                                                nc);
+  if (cudaGetLastError() != cudaSuccess) return NQG_ERR_CUDA;
+  P.nlaunch += 4;
+  P.prof_end(NQG_K_UPDATE, e0, P.pair_flops[q], 0.0);
   return NQG_OK;
 }
 

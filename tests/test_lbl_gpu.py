@@ -247,14 +247,19 @@ def test_fp32_blocked_wide_kernels(path, trailing, monkeypatch):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("update", ["tcgen05", "simt"])
+@pytest.mark.parametrize("update", ["tcgen05", "tcgen05-persistent", "simt"])
 @pytest.mark.parametrize("path", CASES, ids=os.path.basename)
 def test_fp32_update_kernels(path, update, monkeypatch):
     """FP32 factor with every Schur update between supernodes on the tcgen05
-    tiles (any descendant width) or every one on the CUDA-core tiles: the
-    refined solution meets the FP32 bar."""
+    tiles (any descendant width), every one as a persistent tcgen05 launch
+    on packed operands, or every one on the CUDA-core tiles: the refined
+    solution meets the FP32 bar."""
     if update == "tcgen05":
         monkeypatch.setenv("NASOQ_GB300_UPDATE_TC_MIN", "1")
+        monkeypatch.setenv("NASOQ_GB300_UPDATE_PERSIST_MIN", "-1")
+    elif update == "tcgen05-persistent":
+        monkeypatch.setenv("NASOQ_GB300_UPDATE_TC_MIN", "1")
+        monkeypatch.setenv("NASOQ_GB300_UPDATE_PERSIST_MIN", "0")
     else:
         monkeypatch.setenv("NASOQ_GB300_UPDATE", "simt")
     d = nqa.load(path)
