@@ -335,7 +335,7 @@ def main():
     dom = max(stats, key=lambda k: stats[k]["total_ms"])
     ds = stats[dom]
     avg_ms = ds["total_ms"] / max(ds["launches"], 1)
-    if dom in ("solve", "spmv"):
+    if dom in ("solve", "spmv", "pack"):
         ach = ds["alg_bytes"] / (ds["total_ms"] / 1000.0) / 1e9
         roof = {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak}
     else:
@@ -353,7 +353,7 @@ def main():
         sec = v["total_ms"] / 1000.0
         if sec <= 0:
             continue
-        if k in ("solve", "spmv"):
+        if k in ("solve", "spmv", "pack"):
             a = v["alg_bytes"] / sec / 1e9
             by_class[k] = {"bound": "hbm", "achieved": a, "unit": "GB/s", "frac": a / hbm_peak}
         else:

@@ -167,13 +167,15 @@ int nqg_get_device_status(const nqg_plan *plan, int *status_bits);
  * is on; alg_flops / alg_bytes are the algorithmic work of the launches
  * (useful multiply-adds x 2, and bytes of factor values that must be read). */
 #define NQG_K_UPDATE 0          /* Schur updates between supernodes */
-#define NQG_K_WIDE_PANEL 1      /* wide supernode: BK panel */
+#define NQG_K_WIDE_PANEL 1      /* wide supernode: BK panel without pivot search */
 #define NQG_K_WIDE_TRAILING 2   /* wide supernode: trailing update */
 #define NQG_K_BK 3              /* narrow supernodes: BK + panel */
 #define NQG_K_SOLVE 4           /* forward / backward supernodal solves */
 #define NQG_K_SPMV 5            /* refinement residual SpMV */
 #define NQG_K_OTHER 6           /* assembly, row renaming, vector kernels */
-#define NQG_K_CLASSES 7
+#define NQG_K_WIDE_PIVOT 7      /* wide supernode: BK panel with pivot search */
+#define NQG_K_PACK 8            /* split-TF32 operand packing of the tcgen05 updates */
+#define NQG_K_CLASSES 9
 typedef struct nqg_kernel_stats {
   long long launches;
   double total_ms;

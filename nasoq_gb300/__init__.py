@@ -50,7 +50,8 @@ class KernelStats(C.Structure):
                 ("alg_bytes", C.c_double)]
 
 
-KERNEL_CLASSES = {"update": 0, "wide_panel": 1, "wide_trailing": 2, "bk": 3, "solve": 4, "spmv": 5, "other": 6}
+KERNEL_CLASSES = {"update": 0, "wide_panel": 1, "wide_trailing": 2, "bk": 3, "solve": 4, "spmv": 5, "other": 6,
+                  "wide_pivot": 7, "pack": 8}
 
 
 class QPSettings(C.Structure):

@@ -557,7 +557,9 @@ __host__ __device__ constexpr size_t fast_blk_smem() {
 
 __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nrow, int w, int k0, int nb, float *Wb,
                                                                int ldw, float *Dd, float *De, WideCtl *ctl,
-                                                               int slot, unsigned seq, int *status) {
+                                                               int slot, unsigned seq, int *status,
+                                                               unsigned char *pack_a, unsigned char *pack_b,
+                                                               int nkc_stride, int kcs) {
   extern __shared__ __align__(16) unsigned char fb_raw[];
   __shared__ float rinv[WP_NB];
   __shared__ unsigned cpart[FB_THREADS / WP_NB][WP_NB];
@@ -747,6 +749,39 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
       Wb[(size_t)j * ldw + r_own] = wv;
       S[r_own + (size_t)(k0 + j) * nrow] = wv * rinv[j];
     }
+  // operands of the trailing updates (pack_a non-null): the thread's row of
+  // L (A) and, inside the diagonal block, of W (B) as split-TF32 blocks in the
+  // layout of k_pack_split, chunks kcs .. of row block r_own / 128, columns
+  // from kept on zero.  Rows of the panel itself are never read by a later
+  // update (they lie above every updated column) and are not written.
+  if (pack_a && own) {
+    const int rb = r_own / t5::TM, rr = r_own % t5::TM;
+    for (int c = 0; c * t5::TK < nbR; ++c) {
+      const size_t blk = ((size_t)rb * nkc_stride + kcs + c) * (2 * t5::OPND_BYTES);
+      unsigned char *ah = pack_a + blk, *bh = r_own < w ? pack_b + blk : nullptr;
+#pragma unroll 2
+      for (int cc = 0; cc < t5::TK / 4; ++cc) {
+        uint32_t lh[4], ll[4], wh[4], wl[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int j = c * t5::TK + cc * 4 + q;
+          const float wv = j < kept ? wsm[j * FB_THREADS + tid] : 0.f;
+          const float lv = j < kept ? wv * rinv[j] : 0.f;
+          lh[q] = t5::tf32_rna(lv);
+          ll[q] = t5::tf32_rna(lv - __uint_as_float(lh[q]));
+          wh[q] = t5::tf32_rna(wv);
+          wl[q] = t5::tf32_rna(wv - __uint_as_float(wh[q]));
+        }
+        const int off = rr * 128 + ((cc ^ (rr & 7)) << 4);
+        *reinterpret_cast<uint4 *>(ah + off) = make_uint4(lh[0], lh[1], lh[2], lh[3]);
+        *reinterpret_cast<uint4 *>(ah + t5::OPND_BYTES + off) = make_uint4(ll[0], ll[1], ll[2], ll[3]);
+        if (bh) {
+          *reinterpret_cast<uint4 *>(bh + off) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+          *reinterpret_cast<uint4 *>(bh + t5::OPND_BYTES + off) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
+        }
+      }
+    }
+  }
   if (blockIdx.x == 0) {
     for (int e = tid; e < kept * nbR; e += FB_THREADS) {
       const int j = e / nbR, i = e % nbR;
@@ -1323,6 +1358,27 @@ __device__ __forceinline__ void tp_tile(int t, int nrb, int ncb, int &rbl, int &
   rbl = lo + (int)(t - ((long long)lo * nrb - (long long)lo * (lo - 1) / 2));
 }
 
+// Tiles in groups of TP_GB x TP_GB blocks (lower-triangular set of groups,
+// by columns; tiles inside a group by columns): the CTAs of one wave work on
+// about TP_GB row blocks and TP_GB column blocks, so that each operand block
+// comes from DRAM once per group and from L2 for the other tiles of the
+// group.  Flat index t covers every position of every group; positions
+// outside the tile set return false.
+constexpr int TP_GB = 12;
+__host__ __device__ constexpr long long tp_flat_count(int nrb, int ncb) {
+  return (((long long)(ncb + TP_GB - 1) / TP_GB) * ((nrb + TP_GB - 1) / TP_GB) -
+          ((long long)(ncb + TP_GB - 1) / TP_GB) * ((ncb + TP_GB - 1) / TP_GB - 1) / 2) *
+         TP_GB * TP_GB;
+}
+__device__ __forceinline__ bool tp_tile_grouped(int t, int nrb, int ncb, int &rbl, int &cbl) {
+  const int gidx = t / (TP_GB * TP_GB), l = t % (TP_GB * TP_GB);
+  int gi, gj;
+  tp_tile(gidx, (nrb + TP_GB - 1) / TP_GB, (ncb + TP_GB - 1) / TP_GB, gi, gj);
+  rbl = gi * TP_GB + l % TP_GB;
+  cbl = gj * TP_GB + l / TP_GB;
+  return rbl < nrb && cbl < ncb && rbl >= cbl;
+}
+
 // Bounded mbarrier wait that also gives up once another role has given up.
 __device__ __forceinline__ bool tp_wait(uint32_t mbar, uint32_t parity, volatile int *abort, int *status) {
   for (long long it = 0; it < t5::WAIT_LIMIT; ++it) {
@@ -1335,7 +1391,8 @@ __device__ __forceinline__ bool tp_wait(uint32_t mbar, uint32_t parity, volatile
 }
 
 // Sum over chunks kc0 .. kc1-1 of A(i, :) B(j, :)^T for the tiles of blocks
-// blk0 + (rbl, cbl), subtracted from S:
+// blk0 + (rbl, cbl) (ntile: tiles, or tp_flat_count positions when MAPPED),
+// subtracted from S:
 //   MAPPED = false (trailing update, S column-major with leading dimension
 //     nrow): at S[i, j] for j in [cb, ce), i >= j, i < nrow;
 //   MAPPED = true (descendant pair, i, j relative to its first row): at
@@ -1349,6 +1406,16 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_tc_persistent(float *S, int n
                                                                  const int *pcol, int mrows, int ncols) {
   extern __shared__ __align__(1024) unsigned char tp_raw[];
   __shared__ __align__(8) uint64_t bar[2 * TP_STAGES + 4];
+  // long-K pair products read each operand block many times: grouped order;
+  // short-K trailing updates: every position a tile, by columns
+  auto tp_next = [](int t, int nrb_, int ncb_, int &rbl, int &cbl) {
+    if constexpr (MAPPED) {
+      return tp_tile_grouped(t, nrb_, ncb_, rbl, cbl);
+    } else {
+      tp_tile(t, nrb_, ncb_, rbl, cbl);
+      return true;
+    }
+  };
   __shared__ uint32_t s_tmem;
   __shared__ int s_abort;
   if (halt && *(volatile const int *)halt) return;  // queued behind a fast panel that stopped early
@@ -1382,7 +1449,7 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_tc_persistent(float *S, int n
       bool ok = true;
       for (int t = blockIdx.x; t < ntile && ok; t += G) {
         int rbl, cbl;
-        tp_tile(t, nrb, ncb, rbl, cbl);
+        if (!tp_next(t, nrb, ncb, rbl, cbl)) continue;
         const unsigned char *a = pack_a + (size_t)(blk0 + rbl) * nkc_stride * PK_BLOCK;
         const unsigned char *b = pack_b + (size_t)(blk0 + cbl) * nkc_stride * PK_BLOCK;
         for (int kc = kc0; kc < kc1; ++kc, ++it) {
@@ -1410,7 +1477,9 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_tc_persistent(float *S, int n
       uint32_t it = 0, last_bar = 0, last_par = 0;
       bool ok = true, any = false;
       int i = 0;
-      for (int t = blockIdx.x; t < ntile && ok; t += G, ++i) {
+      for (int t = blockIdx.x; t < ntile && ok; t += G) {
+        int rbl, cbl;
+        if (!tp_next(t, nrb, ncb, rbl, cbl)) continue;
         const int buf = i & 1;
         const uint32_t u = (uint32_t)i >> 1;
         if (u > 0 && !tp_wait(t5::smem_u32(&acce[buf]), (u - 1) & 1, abort, status)) break;
@@ -1440,6 +1509,7 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_tc_persistent(float *S, int n
           any = true;
         }
         if (ok) t5::mma_commit(t5::smem_u32(&accf[buf]));
+        ++i;
       }
       // MMAs still running finish before the TMEM is released
       if (any) t5::mbar_wait(last_bar, last_par);
@@ -1449,11 +1519,11 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_tc_persistent(float *S, int n
       // epilogue: thread = TMEM lane = tile row, 64 of the tile's columns
       const int q = warp & 3, r = q * 32 + lane, cofs = ((warp - 2) >> 2) * 64;
       int i = 0;
-      for (int t = blockIdx.x; t < ntile; t += G, ++i) {
+      for (int t = blockIdx.x; t < ntile; t += G) {
+        int rbl, cbl;
+        if (!tp_next(t, nrb, ncb, rbl, cbl)) continue;
         const int buf = i & 1;
         const uint32_t u = (uint32_t)i >> 1;
-        int rbl, cbl;
-        tp_tile(t, nrb, ncb, rbl, cbl);
         const int gi = (blk0 + rbl) * t5::TM + r, gj0 = (blk0 + cbl) * t5::TN + cofs;
         const int pr = gi < mrows ? prow[gi] : -1;
         const int jhi = pr >= 0 ? min(64, min(ncols - gj0, gi - gj0 + 1)) : 0;  // columns gj0 + [0, jhi)
@@ -1482,16 +1552,17 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_tc_persistent(float *S, int n
         t5::fence_before();
         __syncwarp();
         if (lane == 0) t5::mbar_arrive(t5::smem_u32(&acce[buf]));
+        ++i;
       }
     } else {
       // epilogue: thread = TMEM lane = tile row, 64 of the tile's columns
       const int q = warp & 3, r = q * 32 + lane, cofs = ((warp - 2) >> 2) * 64;
       int i = 0;
-      for (int t = blockIdx.x; t < ntile; t += G, ++i) {
+      for (int t = blockIdx.x; t < ntile; t += G) {
+        int rbl, cbl;
+        if (!tp_next(t, nrb, ncb, rbl, cbl)) continue;
         const int buf = i & 1;
         const uint32_t u = (uint32_t)i >> 1;
-        int rbl, cbl;
-        tp_tile(t, nrb, ncb, rbl, cbl);
         const int gr = (blk0 + rbl) * t5::TM + r, gc0 = (blk0 + cbl) * t5::TN + cofs;
         // columns gc0 + [jlo, jhi) of row gr are in the update (gc >= cb,
         // gc < ce, gc <= gr); their current values are loaded first, so that
@@ -1529,6 +1600,7 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_tc_persistent(float *S, int n
         t5::fence_before();
         __syncwarp();
         if (lane == 0) t5::mbar_arrive(t5::smem_u32(&acce[buf]));
+        ++i;
       }
     }
   }
@@ -1688,7 +1760,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     if (P) {
       P->nlaunch += 2;
       const double bytes = (double)kb * ((nrow - rb_first * t5::TM) + (w - rb_first * t5::TM)) * 12.0;
-      P->prof_end(NQG_K_WIDE_TRAILING, e1, 0.0, bytes);
+      P->prof_end(NQG_K_PACK, e1, 0.0, bytes);
     }
     return NQG_OK;
   };
@@ -1741,11 +1813,11 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     return NQG_OK;
   };
   // updates after a panel of kb columns at s.k0 whose W starts at column woff
-  auto post = [&](State &s, int kb, int woff) -> int {
+  auto post = [&](State &s, int kb, int woff, bool packed) -> int {
     const int k0 = s.k0, k1 = k0 + kb;
     int rc;
     if (delayed) {
-      if ((rc = pack_panel(k0, kb, woff, s.pend_C))) return rc;
+      if (!packed && (rc = pack_panel(k0, kb, woff, s.pend_C))) return rc;
       if (k1 < s.F && (rc = apply(k0, kb, woff, s.pend_C, s.pend_C + nch(kb), k1, s.F))) return rc;
       if (s.npend == 0) s.pend_k0 = k0;
       s.pend_K += kb;
@@ -1759,7 +1831,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
         s.F = k1;
       }
     } else if (k1 < w && pack_a) {
-      if ((rc = pack_panel(k0, kb, 0, 0)) || (rc = apply(k0, kb, 0, 0, nch(kb), k1, w))) return rc;
+      if ((!packed && (rc = pack_panel(k0, kb, 0, 0))) || (rc = apply(k0, kb, 0, 0, nch(kb), k1, w))) return rc;
     } else if (k1 < w) {
       cudaEvent_t e1 = P ? P->prof_begin() : nullptr;
       if (sizeof(T) == 4 && trail == 2) {
@@ -1797,7 +1869,10 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     for (int jj = 0; jj < kb; ++jj) fl += 2.0 * (nrow - (k0 + jj)) * (jj + 1);
     return fl;
   };
-  auto launch_fast = [&](int k0, int kb_want, T *Wp, int slot) -> int {
+  // packed: set when the block-first kernel packs the panel's operands itself
+  // (chunks from kcs on)
+  auto launch_fast = [&](int k0, int kb_want, T *Wp, int slot, int kcs, bool &packed) -> int {
+    packed = false;
     const int rows_out = nrow - k0 - kb_want;
     int ldw = nrow;
     float *Sf = reinterpret_cast<float *>(S), *Wf = reinterpret_cast<float *>(Wp);
@@ -1810,7 +1885,10 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       }
       if (++blk_seq == 0) blk_seq = 1;
       unsigned seq = blk_seq;
-      void *args[] = {&Sf, &nrow, &w, &k0, &kb_want, &Wf, &ldw, &Df, &Ef, &ctl, &slot, &seq, &status};
+      unsigned char *pa = k0 + kb_want < w ? pack_a : nullptr, *pb = pack_b;
+      int nkcs = nkc_stride;
+      void *args[] = {&Sf, &nrow, &w, &k0, &kb_want, &Wf, &ldw, &Df, &Ef, &ctl, &slot, &seq, &status, &pa, &pb,
+                      &nkcs, &kcs};
       cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
       if (cudaLaunchCooperativeKernel((void *)k_wide_panel_blk, dim3(Gb), dim3(FB_THREADS), args, fast_blk_smem(),
                                       st) != cudaSuccess)
@@ -1819,6 +1897,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
         P->nlaunch++;
         P->prof_end(NQG_K_WIDE_PANEL, e0, panel_flops(k0, kb_want), 0.0);
       }
+      packed = pa != nullptr;
       return NQG_OK;
     }
     const int G = std::max(1, std::min(maxG_fast, (rows_out + FP_THREADS - 1) / FP_THREADS));
@@ -1851,7 +1930,9 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       if (cudaMemsetAsync(&ctl->halt, 0, sizeof(int), st) != cudaSuccess) return NQG_ERR_CUDA;
       cs = specs[i].st;
       if (kbs[i] > 0) {
-        int rc = post(cs, kbs[i], specs[i].woff);
+        // a short panel did not pack the rows of its diagonal block below its
+        // last column: pack_panel does it all again
+        int rc = post(cs, kbs[i], specs[i].woff, false);
         if (rc) return rc;
       }
       use_general = true;  // the column after the short panel needs a pivot search
@@ -1869,9 +1950,12 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       int rc = pre(cs, false);
       if (rc) return rc;
       const int woff = delayed ? cs.pend_K : 0;
+      bool packed = false;
+      if ((rc = launch_fast(cs.k0, kb_want, Wb + (size_t)woff * nrow, (int)specs.size(), delayed ? cs.pend_C : 0,
+                            packed)))
+        return rc;
       specs.push_back(Spec{cs, kb_want, woff});
-      if ((rc = launch_fast(cs.k0, kb_want, Wb + (size_t)woff * nrow, (int)specs.size() - 1))) return rc;
-      if ((rc = post(cs, kb_want, woff))) return rc;
+      if ((rc = post(cs, kb_want, woff, packed))) return rc;
       if (((int)specs.size() >= spec_limit || cs.k0 >= w) && (rc = resolve())) return rc;
       continue;
     }
@@ -1885,8 +1969,9 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     const int woff = delayed ? cs.pend_K : 0;  // this panel's W columns
     T *Wp = Wb + (size_t)woff * nrow;
     int kb = 0, abort = 0, stop = 0, ldw = nrow, kbw = kb_want, k0 = cs.k0;
+    bool packed = false;
     if (fast) {
-      if ((rc = launch_fast(k0, kb_want, Wp, -1))) return rc;
+      if ((rc = launch_fast(k0, kb_want, Wp, -1, delayed ? cs.pend_C : 0, packed))) return rc;
     } else {
       if (cudaMemsetAsync(&ctl->pslot[0][0], 0, sizeof(ctl->pslot), st) != cudaSuccess) return NQG_ERR_CUDA;
       cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
@@ -1899,7 +1984,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
         return NQG_ERR_CUDA;
       if (P) {
         P->nlaunch++;
-        P->prof_end(NQG_K_WIDE_PANEL, e0, panel_flops(k0, kb_want), 0.0);
+        P->prof_end(NQG_K_WIDE_PIVOT, e0, panel_flops(k0, kb_want), 0.0);
       }
     }
     if (cudaMemcpyAsync(&kb, &ctl->kb, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
@@ -1918,7 +2003,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       use_general = false;
       if (kb <= 0) return NQG_ERR_TIMEOUT;
     }
-    if ((rc = post(cs, kb, woff))) return rc;
+    if ((rc = post(cs, kb, woff, packed && kb == kb_want))) return rc;
   }
   k_wide_zero_upper<T><<<std::min(w, 1024), 128, 0, st>>>(S, nrow, w);
   if (P) P->nlaunch++;
@@ -1970,17 +2055,20 @@ int update_pair_persistent(Plan &P, int s, int q, float *L, const float *Dg) {
   if (cudaFuncSetAttribute(k_tc_persistent<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)tp_smem_bytes()) != cudaSuccess)
     return NQG_ERR_CUDA;
-  cudaEvent_t e0 = P.prof_begin();
+  cudaEvent_t ep = P.prof_begin();
   k_pair_map<<<std::min((m + 255) / 256, 1024), 256, 0, st>>>(P.d_ls + P.sym.lpi[d] + lb, m, nc,
                                                               P.d_ls + P.sym.lpi[s], nrs, cs0, ws, prow, pcol,
                                                               P.d_status);
   const float *Ld = L + P.sym.lpx[d] + lb;
   k_pack_ld<<<dim3(nrb, nkc), 256, 0, st>>>(Ld, nrd, m, wd, Dg + c0, Dg + P.n + c0, pa, nkc);
   k_pack_split<<<dim3(ncb, nkc), 256, 0, st>>>(Ld, nrd, nc, wd, pb, nkc, 0, 0, nullptr);
+  P.prof_end(NQG_K_PACK, ep, 0.0, (double)(m + nc) * wd * 12.0);
+  cudaEvent_t e0 = P.prof_begin();
   const int ntile = ncb * nrb - ncb * (ncb - 1) / 2;
   const int G = std::max(1, std::min(ntile, P.num_sms));
+  const int nflat = (int)tp_flat_count(nrb, ncb);
   k_tc_persistent<true><<<G, TP_THREADS, tp_smem_bytes(), st>>>(L + P.sym.lpx[s], nrs, 0, 0, pa, pb, nkc, 0, nkc, 0,
-                                                                nrb, ncb, ntile, nullptr, P.d_status, prow, pcol, m,
+                                                                nrb, ncb, nflat, nullptr, P.d_status, prow, pcol, m,
                                                                 nc);
   if (cudaGetLastError() != cudaSuccess) return NQG_ERR_CUDA;
   P.nlaunch += 4;
