@@ -573,11 +573,30 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int r_own = k0 + nbR + blockIdx.x * FB_THREADS + tid;  // the thread's row (if < nrow)
   const bool own = r_own < nrow;
+  // R's lower triangle (zeros elsewhere), copied asynchronously
   for (int e = tid; e < WP_NB * FB_LD; e += FB_THREADS) {
     const int t = e / FB_LD, i = e % FB_LD;
-    Rc[e] = (t < nbR && i < nbR && i >= t) ? __ldcg(S + (k0 + i) + (size_t)(k0 + t) * nrow) : 0.f;
+    const bool in = t < nbR && i < nbR && i >= t;
+    const float *src = in ? S + (k0 + i) + (size_t)(k0 + t) * nrow : S;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"((uint32_t)__cvta_generic_to_shared(Rc + e)),
+                 "l"(src), "r"(in ? 4 : 0)
+                 : "memory");
   }
+  asm volatile("cp.async.commit_group;" ::: "memory");
   if (tid < WP_NB) rinv[tid] = 0.f;
+  // the thread's row, copied asynchronously so that the latency overlaps
+  // the factorization of R (wsm[j][tid] is the thread's own column)
+  if (own) {
+    for (int j = 0; j < nbR; ++j)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                       (uint32_t)__cvta_generic_to_shared(wsm + j * FB_THREADS + tid)),
+                   "l"(S + r_own + (size_t)(k0 + j) * nrow)
+                   : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  }
+  // R landed (the row copies may still be in flight)
+  if (own) asm volatile("cp.async.wait_group 1;" ::: "memory");
+  else asm volatile("cp.async.wait_group 0;" ::: "memory");
   __syncthreads();
   // --- R = L_R D_R L_R^T, eight columns at a time -------------------------
   for (int b = 0; b < nbR; b += 8) {
@@ -639,11 +658,12 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
   }
   // --- the thread's row: forward substitution against R, 8 columns at a time
   if (own) {
+    asm volatile("cp.async.wait_all;" ::: "memory");
     for (int jb = 0; jb < nbR; jb += 8) {
       const int nc = min(8, nbR - jb);
       float v[8], lv[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) v[q] = q < nc ? __ldcg(S + r_own + (size_t)(k0 + jb + q) * nrow) : 0.f;
+      for (int q = 0; q < 8; ++q) v[q] = q < nc ? wsm[(jb + q) * FB_THREADS + tid] : 0.f;
       for (int t = 0; t < jb; ++t) {
         const float l = wsm[t * FB_THREADS + tid] * rinv[t];
         const float4 x0 = *reinterpret_cast<const float4 *>(Rc + t * FB_LD + jb);
