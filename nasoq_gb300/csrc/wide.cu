@@ -532,9 +532,9 @@ __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nr
 
 // Block-first fast panel (no pivot search).  The nbR x nbR diagonal block R
 // is factored first, replicated in every CTA with diagonal pivots assumed,
-// eight columns at a time (one warp factors the 8 x 8 diagonal block with
-// shuffles, the rows below it are solved against that block, then a rank-8
-// update brings the rest of R up to date); then every owned row is solved
+// FB_RB columns at a time (one warp factors the diagonal block of the step
+// with shuffles, the rows below it are solved against that block, then a
+// rank-FB_RB update brings the rest of R up to date); then every owned row is solved
 // against R in registers, and ONE grid exchange returns the maxima of all
 // panel columns.  The longest prefix of columns whose diagonal passes the
 // Bunch-Kaufman test is kept and written; the later columns stay untouched
@@ -547,12 +547,13 @@ __global__ void __launch_bounds__(FP_THREADS) k_wide_panel_fast(float *S, int nr
 constexpr int FB_THREADS = 256;  // one row below the panel per thread
 constexpr int FB_MAXG = 128;     // CTAs per launch (WP_NB x FB_MAXG words fit in ctl->mslot)
 constexpr int FB_LD = WP_NB;     // leading dimension of R, stored by columns
+constexpr int FB_RB = 16;        // columns of R per blocked step
 static_assert(WP_NB * FB_MAXG <= (int)(sizeof(WideCtl::mslot) / sizeof(unsigned long long)),
               "exchange words of the block-first panel");
 static_assert(FB_THREADS % WP_NB == 0, "column parts of the exchange");
 
 __host__ __device__ constexpr size_t fast_blk_smem() {
-  return ((size_t)WP_NB * FB_THREADS + (size_t)WP_NB * FB_LD + 8 * FB_LD) * sizeof(float);
+  return ((size_t)WP_NB * FB_THREADS + (size_t)WP_NB * FB_LD + FB_RB * FB_LD) * sizeof(float);
 }
 
 __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nrow, int w, int k0, int nb, float *Wb,
@@ -568,7 +569,7 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
   const int nbR = min(nb, w - k0);           // panel columns = rows of R
   float *wsm = reinterpret_cast<float *>(fb_raw);  // [WP_NB][FB_THREADS]: W of the thread's row
   float *Rc = wsm + (size_t)WP_NB * FB_THREADS;    // [WP_NB][FB_LD]: R by columns, W values once final
-  float *Lb = Rc + (size_t)WP_NB * FB_LD;          // [8][FB_LD]: L of the current column block
+  float *Lb = Rc + (size_t)WP_NB * FB_LD;          // [FB_RB][FB_LD]: L of the current column block
   const float alpha = (float)((1.0 + sqrt(17.0)) / 8.0);
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int r_own = k0 + nbR + blockIdx.x * FB_THREADS + tid;  // the thread's row (if < nrow)
@@ -598,48 +599,49 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
   if (own) asm volatile("cp.async.wait_group 1;" ::: "memory");
   else asm volatile("cp.async.wait_group 0;" ::: "memory");
   __syncthreads();
-  // --- R = L_R D_R L_R^T, eight columns at a time -------------------------
-  for (int b = 0; b < nbR; b += 8) {
-    const int nc = min(8, nbR - b);
+  // --- R = L_R D_R L_R^T, FB_RB columns at a time -------------------------
+  for (int b = 0; b < nbR; b += FB_RB) {
+    const int nc = min(FB_RB, nbR - b);
     if (wid == 0) {
-      // the 8 x 8 diagonal block: lane q holds row b + q
+      // the FB_RB x FB_RB diagonal block: lane q holds row b + q
       const int q = lane;
-      float v[8];
+      float v[FB_RB];
 #pragma unroll
-      for (int c = 0; c < 8; ++c) v[c] = (q < nc && c <= q) ? Rc[(b + c) * FB_LD + b + q] : 0.f;
+      for (int c = 0; c < FB_RB; ++c) v[c] = (q < nc && c <= q) ? Rc[(b + c) * FB_LD + b + q] : 0.f;
+      // Every lane updates all its entries right of column t; those of its
+      // strict upper part (c > q) and of lanes q >= nc are never read as
+      // factor values nor stored, so no predicate is needed.
 #pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        if (t < nc) {
-          const float r1 = 1.f / __shfl_sync(0xffffffffu, v[t], t);
-          const float l = v[t] * r1;
+      for (int t = 0; t < FB_RB; ++t) {
+        const float r1 = 1.f / __shfl_sync(0xffffffffu, v[t], t);
+        const float l = v[t] * r1;
 #pragma unroll
-          for (int c = t + 1; c < 8; ++c) {
-            const float wct = __shfl_sync(0xffffffffu, v[t], c);  // W(b + c, b + t), final
-            if (q < nc && q >= c) v[c] = fmaf(-l, wct, v[c]);
-          }
-          if (q == 0) rinv[b + t] = r1;
+        for (int c = t + 1; c < FB_RB; ++c) {
+          const float wct = __shfl_sync(0xffffffffu, v[t], c);  // W(b + c, b + t), final
+          v[c] = fmaf(-l, wct, v[c]);
         }
+        if (q == 0 && t < nc) rinv[b + t] = r1;
       }
 #pragma unroll
-      for (int c = 0; c < 8; ++c)
+      for (int c = 0; c < FB_RB; ++c)
         if (q < nc && c <= q) Rc[(b + c) * FB_LD + b + q] = v[c];
     }
     __syncthreads();
-    const int mb = nbR - b - 8;  // rows of R below the block (the block is full when > 0)
+    const int mb = nbR - b - FB_RB;  // rows of R below the block (the block is full when > 0)
     if (mb <= 0) break;
     if (tid < mb) {
-      const int i = b + 8 + tid;
-      float v[8], lv[8];
+      const int i = b + FB_RB + tid;
+      float v[FB_RB], lv[FB_RB];
 #pragma unroll
-      for (int c = 0; c < 8; ++c) v[c] = Rc[(b + c) * FB_LD + i];
+      for (int c = 0; c < FB_RB; ++c) v[c] = Rc[(b + c) * FB_LD + i];
 #pragma unroll
-      for (int c = 0; c < 8; ++c) {
+      for (int c = 0; c < FB_RB; ++c) {
 #pragma unroll
         for (int t = 0; t < c; ++t) v[c] = fmaf(-lv[t], Rc[(b + t) * FB_LD + b + c], v[c]);
         lv[c] = v[c] * rinv[b + c];
       }
 #pragma unroll
-      for (int c = 0; c < 8; ++c) {
+      for (int c = 0; c < FB_RB; ++c) {
         Rc[(b + c) * FB_LD + i] = v[c];
         Lb[c * FB_LD + i] = lv[c];
       }
@@ -648,10 +650,10 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
     for (int e = tid; e < mb * mb; e += FB_THREADS) {
       const int io = e % mb, jo = e / mb;
       if (io < jo) continue;
-      const int i = b + 8 + io, jj = b + 8 + jo;
+      const int i = b + FB_RB + io, jj = b + FB_RB + jo;
       float x = Rc[jj * FB_LD + i];
 #pragma unroll
-      for (int t = 0; t < 8; ++t) x = fmaf(-Lb[t * FB_LD + i], Rc[(b + t) * FB_LD + jj], x);
+      for (int t = 0; t < FB_RB; ++t) x = fmaf(-Lb[t * FB_LD + i], Rc[(b + t) * FB_LD + jj], x);
       Rc[jj * FB_LD + i] = x;
     }
     __syncthreads();
@@ -763,10 +765,13 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
   __syncthreads();
   // --- global writes of the kept columns
   const int kept = s_kept;
+  // W goes to Wb only where a later kernel reads it there: without packed
+  // operands, or for a short panel (its operands are packed again from Wb)
+  const bool wb_out = !pack_a || kept < nbR;
   if (own)
     for (int j = 0; j < kept; ++j) {
       const float wv = wsm[j * FB_THREADS + tid];
-      Wb[(size_t)j * ldw + r_own] = wv;
+      if (wb_out) Wb[(size_t)j * ldw + r_own] = wv;
       S[r_own + (size_t)(k0 + j) * nrow] = wv * rinv[j];
     }
   // operands of the trailing updates (pack_a non-null): the thread's row of
@@ -808,7 +813,7 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
       if (i < j) continue;
       const float v = Rc[j * FB_LD + i];
       const int c = k0 + j;
-      Wb[(size_t)j * ldw + k0 + i] = v;
+      if (wb_out) Wb[(size_t)j * ldw + k0 + i] = v;
       if (i > j) {
         S[(k0 + i) + (size_t)c * nrow] = v * rinv[j];
       } else {
