@@ -138,6 +138,7 @@ struct Plan {
   unsigned char *d_wide_pack = nullptr;  // FP32: split-TF32 operand blocks of the tcgen05 updates
   int *d_pers_map = nullptr;              // target positions of a persistent pair's rows and columns
   unsigned *d_solve_flags = nullptr;  // per 64-column block ready flags of the block solves
+  unsigned long long *d_xw = nullptr;  // FP32 block solves: (epoch << 32) | x bits per column
   int solve_flags_cap = 0;
   unsigned solve_epoch = 0;
   int wide_nb = 64;

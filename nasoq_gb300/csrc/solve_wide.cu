@@ -74,13 +74,20 @@ template <class T, class V> __device__ void stage_tile(const T *S, int nrow, int
 // until block j is ready, scanning 32 flags per poll, and extends the front
 // over ready blocks (< lim).  Waiters further from the front poll less often.
 // Returns -1 on abort or timeout.
-__device__ int wait_up(const unsigned *fl, unsigned epoch, int j, int lim, int front, WideCtl *ctl, int *status) {
+// With xws (the x words of the supernode's w columns; FP32 sweeps) the flag
+// of block k is the epoch of the block's last word instead of fl[k], and no
+// fence follows: the consumer reads the values as words and checks them.
+__device__ int wait_up(const unsigned *fl, unsigned epoch, int j, int lim, int front, WideCtl *ctl, int *status,
+                       const unsigned long long *xws = nullptr, int w = 0) {
   const int lane = threadIdx.x & 31;
   long long it = 0;
   volatile int *vab = &ctl->abort;
   while (true) {
     const int k = front + lane;
-    const unsigned v = k < lim ? *(volatile const unsigned *)(fl + k) : 0u;
+    unsigned v = 0u;
+    if (k < lim)
+      v = xws ? (unsigned)(*(volatile const unsigned long long *)(xws + min(w, (k + 1) * TB) - 1) >> 32)
+              : *(volatile const unsigned *)(fl + k);
     const unsigned ready = __ballot_sync(0xffffffffu, v == epoch);
     const int lead = ready == 0xffffffffu ? 32 : __ffs(~ready) - 1;
     front += lead;
@@ -96,20 +103,23 @@ __device__ int wait_up(const unsigned *fl, unsigned epoch, int j, int lim, int f
     }
     __nanosleep(min(2000, 40 * (j - front + 1)));
   }
-  __threadfence();
+  if (!xws) __threadfence();
   return front;
 }
 
 // Backward mirror: blocks >= `front` are ready; waits until block i is and
 // extends the front down to lo.
-__device__ int wait_down(const unsigned *fl, unsigned epoch, int i, int lo, int front, WideCtl *ctl,
-                         int *status) {
+__device__ int wait_down(const unsigned *fl, unsigned epoch, int i, int lo, int front, WideCtl *ctl, int *status,
+                         const unsigned long long *xws = nullptr, int w = 0) {
   const int lane = threadIdx.x & 31;
   long long it = 0;
   volatile int *vab = &ctl->abort;
   while (true) {
     const int k = front - 1 - lane;
-    const unsigned v = k >= lo ? *(volatile const unsigned *)(fl + k) : 0u;
+    unsigned v = 0u;
+    if (k >= lo)
+      v = xws ? (unsigned)(*(volatile const unsigned long long *)(xws + min(w, (k + 1) * TB) - 1) >> 32)
+              : *(volatile const unsigned *)(fl + k);
     const unsigned ready = __ballot_sync(0xffffffffu, v == epoch);
     const int lead = ready == 0xffffffffu ? 32 : __ffs(~ready) - 1;
     front -= lead;
@@ -125,13 +135,49 @@ __device__ int wait_down(const unsigned *fl, unsigned epoch, int i, int lo, int 
     }
     __nanosleep(min(2000, 40 * (front - i)));
   }
-  __threadfence();
+  if (!xws) __threadfence();
   return front;
 }
 
 __device__ __forceinline__ void publish(unsigned *flag, unsigned epoch) {
   __threadfence();
   *(volatile unsigned *)flag = epoch;
+}
+
+// FP32 sweeps publish each solved x value as one 64-bit word (epoch << 32 |
+// value bits): a consumer sees value and readiness in the same load, so
+// neither side needs a fence or a flag.  Reads the n (<= CPT) words at wp
+// into xv (0 beyond n), the whole warp polling until all of its lanes'
+// words carry this epoch; false on abort or timeout.
+template <int N>
+__device__ __forceinline__ bool wait_words(const unsigned long long *wp, int n, unsigned epoch, float (&xv)[N],
+                                           WideCtl *ctl, int *status) {
+  long long it = 0;
+  while (true) {
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      xv[k] = 0.f;
+      if (k < n) {
+        const unsigned long long v = *(volatile const unsigned long long *)(wp + k);
+        if ((unsigned)(v >> 32) != epoch) ok = false;
+        xv[k] = __uint_as_float((unsigned)v);
+      }
+    }
+    if (__all_sync(0xffffffffu, ok)) return true;
+    if (*(volatile int *)&ctl->abort) return false;
+    if (++it > SPIN_LIMIT) {
+      if ((threadIdx.x & 31) == 0) {
+        atomicOr(status, ST_TIMEOUT);
+        atomicExch(&ctl->abort, 1);
+      }
+      return false;
+    }
+    __nanosleep(64);
+  }
+}
+__device__ __forceinline__ void put_word(unsigned long long *wp, unsigned epoch, float v) {
+  *(volatile unsigned long long *)wp = ((unsigned long long)epoch << 32) | __float_as_uint(v);
 }
 
 // Forward sweep over the large supernodes of one level.  Item (s, q): q <
@@ -141,7 +187,8 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
                                                         const int64_t *lpi, const int64_t *lpx, const int *ls,
                                                         const T *L, V *x, unsigned *flags, const int *flagoff,
                                                         unsigned epoch, const uint8_t *visible, WideCtl *ctl,
-                                                        int *status) {
+                                                        int *status, unsigned long long *xw) {
+  constexpr bool WORDS = sizeof(V) == 4;  // x of the diagonal blocks through words
   __shared__ V Td[TB * TB];
   __shared__ V red[SW_THREADS];
   __shared__ V yb[TB];
@@ -166,6 +213,8 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
     const int m = min(TB, (diag ? w : nrow) - r0);
     const int jmax = diag ? q : nbd;
     if (diag) stage_tile(S, nrow, r0, m, Td);
+    // right-hand side of the block, final before this launch
+    const V bq = (diag && t < m) ? __ldcg(xs + r0 + t) : V(0);
     const bool rok = r < m;
     const T *Lr = S + r0 + r;
     V acc = V(0);
@@ -180,20 +229,37 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
 #pragma unroll
       for (int cc = 0; cc < CPT; ++cc)
         vn[cc] = (j + 1 < jmax && rok && cbn + cc < w) ? Lr[(size_t)(cbn + cc) * nrow] : T(0);
-      if (j >= front) {
-        __syncthreads();
-        if (t < 32) {
-          const int f = wait_up(fl, epoch, j, nbd, front, ctl, status);
-          if (t == 0) s_front = f;
-        }
-        __syncthreads();
-        front = s_front;
-        if (front < 0) return;
-      }
       const int cb = j * TB + cg * CPT;
+      if constexpr (WORDS) {
+        if (j >= front) {
+          __syncthreads();
+          if (t < 32) {
+            const int f = wait_up(fl, epoch, j, nbd, front, ctl, status, xw + c0, w);
+            if (t == 0) s_front = f;
+          }
+          __syncthreads();
+          front = s_front;
+          if (front < 0) return;
+        }
+        float xv[CPT];
+        if (!wait_words(xw + c0 + cb, min(CPT, w - cb), epoch, xv, ctl, status)) return;
 #pragma unroll
-      for (int cc = 0; cc < CPT; ++cc)
-        if (cb + cc < w) acc += V(v[cc]) * __ldcg(xs + cb + cc);
+        for (int cc = 0; cc < CPT; ++cc) acc += V(v[cc]) * xv[cc];
+      } else {
+        if (j >= front) {
+          __syncthreads();
+          if (t < 32) {
+            const int f = wait_up(fl, epoch, j, nbd, front, ctl, status);
+            if (t == 0) s_front = f;
+          }
+          __syncthreads();
+          front = s_front;
+          if (front < 0) return;
+        }
+#pragma unroll
+        for (int cc = 0; cc < CPT; ++cc)
+          if (cb + cc < w) acc += V(v[cc]) * __ldcg(xs + cb + cc);
+      }
 #pragma unroll
       for (int cc = 0; cc < CPT; ++cc) v[cc] = vn[cc];
     }
@@ -202,13 +268,18 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
     if (t < TB) yb[t] = red[t] + red[t + TB] + red[t + 2 * TB] + red[t + 3 * TB];
     __syncthreads();
     if (diag) {
-      if (t < m) yb[t] = __ldcg(xs + r0 + t) - yb[t];
+      if (t < m) yb[t] = bq - yb[t];
       __syncthreads();
       if (t < 32) warp_trsv_lower(Td, m, yb);
       __syncthreads();
-      if (t < m) xs[r0 + t] = yb[t];
-      __syncthreads();
-      if (t == 0) publish(fl + q, epoch);
+      if (t < m) {
+        xs[r0 + t] = yb[t];
+        if constexpr (WORDS) put_word(xw + c0 + r0 + t, epoch, float(yb[t]));
+      }
+      if constexpr (!WORDS) {
+        __syncthreads();
+        if (t == 0) publish(fl + q, epoch);
+      }
     } else {
       const int *rows = ls + lpi[s];
       if (t < m) atomicAdd(&x[rows[r0 + t]], -yb[t]);
@@ -224,7 +295,8 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
                                                         const int64_t *lpi, const int64_t *lpx, const int *ls,
                                                         const T *L, V *x, unsigned *flags, const int *flagoff,
                                                         unsigned epoch, const uint8_t *visible, WideCtl *ctl,
-                                                        int *status) {
+                                                        int *status, unsigned long long *xw) {
+  constexpr bool WORDS = sizeof(V) == 4;  // x of the diagonal blocks through words
   __shared__ V Td[TB * TB];
   __shared__ V red[2][TB];
   __shared__ V redS[sizeof(V) == 4 ? TB * (TB + 1) : 1];  // FP32: column sums through a transpose
@@ -291,18 +363,35 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
 #pragma unroll
       for (int cc = 0; cc < CPT; ++cc)
         vn[cc] = (i - 1 > j && rown < w && cok[cc]) ? Lc[rown + (size_t)cc * nrow] : T(0);
-      if (i < front) {
-        __syncthreads();
-        if (t < 32) {
-          const int f = wait_down(fl, epoch, i, j + 1, front, ctl, status);
-          if (t == 0) s_front = f;
-        }
-        __syncthreads();
-        front = s_front;
-        if (front < 0) return;
-      }
       const int row = i * TB + r;
-      const V xv = row < w ? __ldcg(xs + row) : V(0);
+      V xv;
+      if constexpr (WORDS) {
+        if (i < front) {
+          __syncthreads();
+          if (t < 32) {
+            const int f = wait_down(fl, epoch, i, j + 1, front, ctl, status, xw + c0, w);
+            if (t == 0) s_front = f;
+          }
+          __syncthreads();
+          front = s_front;
+          if (front < 0) return;
+        }
+        float xw1[1];
+        if (!wait_words(xw + c0 + row, row < w ? 1 : 0, epoch, xw1, ctl, status)) return;
+        xv = xw1[0];
+      } else {
+        if (i < front) {
+          __syncthreads();
+          if (t < 32) {
+            const int f = wait_down(fl, epoch, i, j + 1, front, ctl, status);
+            if (t == 0) s_front = f;
+          }
+          __syncthreads();
+          front = s_front;
+          if (front < 0) return;
+        }
+        xv = row < w ? __ldcg(xs + row) : V(0);
+      }
 #pragma unroll
       for (int cc = 0; cc < CPT; ++cc) part[cc] += V(v[cc]) * xv;
 #pragma unroll
@@ -341,9 +430,14 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
     __syncthreads();
     if (t < 32) warp_trsv_lower_t(Td, nc, yb);
     __syncthreads();
-    if (t < nc) xs[b0 + t] = yb[t];
-    __syncthreads();
-    if (t == 0) publish(fl + j, epoch);
+    if (t < nc) {
+      xs[b0 + t] = yb[t];
+      if constexpr (WORDS) put_word(xw + c0 + b0 + t, epoch, float(yb[t]));
+    }
+    if constexpr (!WORDS) {
+      __syncthreads();
+      if (t == 0) publish(fl + j, epoch);
+    }
     __syncthreads();
   }
 }
@@ -359,6 +453,7 @@ template <class K> static int coop_grid(Plan &P, K kern, int items) {
 static unsigned next_epoch(Plan &P) {
   if (++P.solve_epoch == 0) {
     cudaMemsetAsync(P.d_solve_flags, 0, P.solve_flags_cap * sizeof(unsigned), P.stream);
+    cudaMemsetAsync(P.d_xw, 0, (size_t)std::max(P.n, 1) * sizeof(unsigned long long), P.stream);
     P.solve_epoch = 1;
   }
   return P.solve_epoch;
@@ -382,8 +477,9 @@ template <class T, class V> static int launch_blk(Plan &P, bool fwd, int l, cons
   unsigned epoch = next_epoch(P);
   void *kern = fwd ? (void *)k_fwd_blk<T, V> : (void *)k_bwd_blk<T, V>;
   const int G = fwd ? coop_grid(P, k_fwd_blk<T, V>, cnt) : coop_grid(P, k_bwd_blk<T, V>, cnt);
+  unsigned long long *xw = P.d_xw;
   void *args[] = {(void *)&items, (void *)&cnt, (void *)&super, (void *)&lpi, (void *)&lpx, (void *)&ls,
-                  (void *)&L, &x, &flags, (void *)&flagoff, &epoch, (void *)&vis, &ctl, &status};
+                  (void *)&L, &x, &flags, (void *)&flagoff, &epoch, (void *)&vis, &ctl, &status, &xw};
   cudaEvent_t e0 = P.prof_begin();
   NQG_CUDA(cudaLaunchCooperativeKernel(kern, dim3(G), dim3(SW_THREADS), args, 0, P.stream));
   P.nlaunch++;
