@@ -412,6 +412,10 @@ static int upload_plan(Plan &P) {
   NQG_CUDA(cudaMemset(P.d_solve_flags, 0, (size_t)P.solve_flags_cap * sizeof(unsigned)));
   NQG_CUDA(cudaMalloc(&P.d_xw, (size_t)std::max(n, 1) * sizeof(unsigned long long)));
   NQG_CUDA(cudaMemset(P.d_xw, 0, (size_t)std::max(n, 1) * sizeof(unsigned long long)));
+  // FP32 factor with FP32 block solves: inverses of the diagonal tiles
+  // (64 x 65 floats each, one per ready flag)
+  if (P.set.precision == NQG_FP32 && P.set.solve_precision == NQG_FP32)
+    NQG_CUDA(cudaMalloc(&P.d_tinv, (size_t)std::max(nflags, 1) * 64 * 65 * sizeof(float)));
   P.solve_small_w = small_w;
   if ((rc = dev_alloc_copy(P, &P.d_targets_lv, lvflat.data(), lvflat.size()))) return rc;
   P.lv_targets_host = lvflat;
@@ -488,7 +492,7 @@ static void free_plan(Plan &P) {
                   P.d_pair_lb, P.d_pair_ub, P.d_targets_lv, P.d_pivoted, P.d_visible, P.d_hidden, P.d_status,
                   P.d_xo, P.d_bo, P.d_r, P.d_w, P.d_in, P.d_out, P.d_V, P.d_scal, P.d_wide_W, P.d_wide_ctl,
                   P.d_wide_pack, P.d_pers_map, P.d_locinv, P.d_pair_roff, P.d_rr_dest, P.d_rr_moved, P.d_rr_items, P.d_rr_stage,
-                  P.d_solve_flags, P.d_xw, P.d_blk_items, P.d_flagoff, P.d_xf, P.d_Z, P.d_tiles_tc,
+                  P.d_solve_flags, P.d_xw, P.d_tinv, P.d_blk_items, P.d_flagoff, P.d_xf, P.d_Z, P.d_tiles_tc,
                   P.d_tile_list_tc, P.d_row_items};
   for (void *p : ptrs)
     if (p) cudaFree(p);

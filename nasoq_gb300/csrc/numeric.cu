@@ -1186,6 +1186,7 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
 }
 
 int dev_factor(Plan &P, const std::vector<int> *subset) {
+  P.tinv_valid = false;  // the block solves form their tile inverses again
   if (P.set.precision == NQG_FP32) return factor_impl<float>(P, subset);
   return factor_impl<double>(P, subset);
 }

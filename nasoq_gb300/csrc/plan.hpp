@@ -139,6 +139,8 @@ struct Plan {
   int *d_pers_map = nullptr;              // target positions of a persistent pair's rows and columns
   unsigned *d_solve_flags = nullptr;  // per 64-column block ready flags of the block solves
   unsigned long long *d_xw = nullptr;  // FP32 block solves: (epoch << 32) | x bits per column
+  float *d_tinv = nullptr;             // FP32 block solves: inverses of the diagonal 64 x 64 tiles
+  bool tinv_valid = false;             // formed for the current factor
   int solve_flags_cap = 0;
   unsigned solve_epoch = 0;
   int wide_nb = 64;

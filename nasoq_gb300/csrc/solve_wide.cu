@@ -61,6 +61,54 @@ template <class V> __device__ void warp_trsv_lower_t(const V *T11, int m, V *xb)
   if (lane + 32 < m) xb[lane + 32] = v1;
 }
 
+// FP32 sweeps solve a diagonal tile by a product with its inverse.  The
+// inverses of all diagonal 64 x 64 tiles of the block-solved supernodes are
+// formed once per factorization: tile (s, j) at tinv + (flagoff[s] + j) * TI,
+// entry (k, c) at [c * (TB + 1) + k], zero outside the tile's m x m block.
+constexpr int TI = TB * (TB + 1);
+
+// One CTA of TB threads per diagonal tile (items: the backward items, (s, q)
+// for column block nbd(s) - 1 - q).  Thread c forms column c by forward
+// substitution in registers; its entries above row c start at 0 and stay 0,
+// so the unrolled recurrences need no predicate.
+__global__ void __launch_bounds__(TB) k_tile_inverse(const int2 *items, const int *super, const int64_t *lpi,
+                                                     const int64_t *lpx, const float *L, const int *flagoff,
+                                                     float *tinv) {
+  __shared__ float T11[TB * TB];
+  const int s = items[blockIdx.x].x, q = items[blockIdx.x].y;
+  const int c0 = super[s], w = super[s + 1] - c0;
+  const int nrow = (int)(lpi[s + 1] - lpi[s]);
+  const int nbd = (w + TB - 1) / TB, j = nbd - 1 - q;
+  const int b0 = j * TB, m = min(TB, w - b0);
+  const float *S = L + lpx[s];
+  for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
+    const int cc = e / TB, r = e % TB;
+    T11[r + cc * TB] = (r < m && cc < m) ? S[b0 + r + (size_t)(b0 + cc) * nrow] : 0.f;
+  }
+  __syncthreads();
+  const int c = threadIdx.x;
+  float x[TB];
+#pragma unroll
+  for (int k = 0; k < TB; ++k) x[k] = k == c ? 1.f : 0.f;
+#pragma unroll
+  for (int i = 1; i < TB; ++i) {
+    float acc = 0.f;
+#pragma unroll
+    for (int k = 0; k < i; ++k) acc = fmaf(T11[i + k * TB], x[k], acc);
+    if (i > c) x[i] = -acc;
+  }
+  float *out = tinv + (size_t)(flagoff[s] + j) * TI + (size_t)c * (TB + 1);
+#pragma unroll
+  for (int k = 0; k < TB; ++k) out[k] = (c < m && k < m) ? x[k] : 0.f;
+  out[TB] = 0.f;
+}
+
+// Inverse of diagonal tile (s, j) into shared memory (FP32 sweeps).
+__device__ __forceinline__ void stage_inverse(const float *tinv, const int *flagoff, int s, int j, float *Ti) {
+  const float4 *src = reinterpret_cast<const float4 *>(tinv + (size_t)(flagoff[s] + j) * TI);
+  for (int e = threadIdx.x; e < TI / 4; e += blockDim.x) reinterpret_cast<float4 *>(Ti)[e] = __ldcg(src + e);
+}
+
 // The m x m tile at (b0, b0) of the panel, column-major in T11.
 template <class T, class V> __device__ void stage_tile(const T *S, int nrow, int b0, int m, V *T11) {
   for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
@@ -187,9 +235,9 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
                                                         const int64_t *lpi, const int64_t *lpx, const int *ls,
                                                         const T *L, V *x, unsigned *flags, const int *flagoff,
                                                         unsigned epoch, const uint8_t *visible, WideCtl *ctl,
-                                                        int *status, unsigned long long *xw) {
+                                                        int *status, unsigned long long *xw, const float *tinv) {
   constexpr bool WORDS = sizeof(V) == 4;  // x of the diagonal blocks through words
-  __shared__ V Td[TB * TB];
+  __shared__ __align__(16) V Td[TB * (TB + 1)];  // diagonal tile (FP32: its inverse)
   __shared__ V red[SW_THREADS];
   __shared__ V yb[TB];
   __shared__ int s_front;
@@ -212,7 +260,11 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
     const int r0 = diag ? q * TB : w + (q - nbd) * TB;
     const int m = min(TB, (diag ? w : nrow) - r0);
     const int jmax = diag ? q : nbd;
-    if (diag) stage_tile(S, nrow, r0, m, Td);
+    if constexpr (WORDS) {
+      if (diag) stage_inverse(tinv, flagoff, s, q, Td);
+    } else {
+      if (diag) stage_tile(S, nrow, r0, m, Td);
+    }
     // right-hand side of the block, final before this launch
     const V bq = (diag && t < m) ? __ldcg(xs + r0 + t) : V(0);
     const bool rok = r < m;
@@ -231,7 +283,9 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
         vn[cc] = (j + 1 < jmax && rok && cbn + cc < w) ? Lr[(size_t)(cbn + cc) * nrow] : T(0);
       const int cb = j * TB + cg * CPT;
       if constexpr (WORDS) {
-        if (j >= front) {
+        // the block just before a diagonal item's own is the last link of
+        // the chain: its words are polled directly by every warp
+        if (j >= front && !(diag && j == q - 1)) {
           __syncthreads();
           if (t < 32) {
             const int f = wait_up(fl, epoch, j, nbd, front, ctl, status, xw + c0, w);
@@ -270,13 +324,23 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
     if (diag) {
       if (t < m) yb[t] = bq - yb[t];
       __syncthreads();
-      if (t < 32) warp_trsv_lower(Td, m, yb);
-      __syncthreads();
-      if (t < m) {
-        xs[r0 + t] = yb[t];
-        if constexpr (WORDS) put_word(xw + c0 + r0 + t, epoch, float(yb[t]));
-      }
-      if constexpr (!WORDS) {
+      if constexpr (WORDS) {
+        // x_q = L_qq^-1 y_q
+        V a = V(0);
+#pragma unroll
+        for (int cc = 0; cc < CPT; ++cc)
+          if (cg * CPT + cc < m) a += Td[(cg * CPT + cc) * (TB + 1) + r] * yb[cg * CPT + cc];
+        red[t] = a;
+        __syncthreads();
+        if (t < m) {
+          const V xq = red[t] + red[t + TB] + red[t + 2 * TB] + red[t + 3 * TB];
+          xs[r0 + t] = xq;
+          put_word(xw + c0 + r0 + t, epoch, float(xq));
+        }
+      } else {
+        if (t < 32) warp_trsv_lower(Td, m, yb);
+        __syncthreads();
+        if (t < m) xs[r0 + t] = yb[t];
         __syncthreads();
         if (t == 0) publish(fl + q, epoch);
       }
@@ -295,9 +359,9 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
                                                         const int64_t *lpi, const int64_t *lpx, const int *ls,
                                                         const T *L, V *x, unsigned *flags, const int *flagoff,
                                                         unsigned epoch, const uint8_t *visible, WideCtl *ctl,
-                                                        int *status, unsigned long long *xw) {
+                                                        int *status, unsigned long long *xw, const float *tinv) {
   constexpr bool WORDS = sizeof(V) == 4;  // x of the diagonal blocks through words
-  __shared__ V Td[TB * TB];
+  __shared__ __align__(16) V Td[TB * (TB + 1)];  // diagonal tile (FP32: its inverse)
   __shared__ V red[2][TB];
   __shared__ V redS[sizeof(V) == 4 ? TB * (TB + 1) : 1];  // FP32: column sums through a transpose
   __shared__ V yb[TB];
@@ -320,7 +384,8 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
     }
     const int j = nbd - 1 - q;
     const int b0 = j * TB, nc = min(TB, w - b0);
-    stage_tile(S, nrow, b0, nc, Td);
+    if constexpr (WORDS) stage_inverse(tinv, flagoff, s, j, Td);
+    else stage_tile(S, nrow, b0, nc, Td);
     const int cb = b0 + cg * CPT;
     const T *Lc = S + (size_t)cb * nrow;  // first of this thread's columns
     bool cok[CPT];
@@ -366,7 +431,8 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
       const int row = i * TB + r;
       V xv;
       if constexpr (WORDS) {
-        if (i < front) {
+        // block j + 1 is the last link of the chain: polled directly
+        if (i < front && i != j + 1) {
           __syncthreads();
           if (t < 32) {
             const int f = wait_down(fl, epoch, i, j + 1, front, ctl, status, xw + c0, w);
@@ -428,13 +494,23 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
       if (t < nc) yb[t] = __ldcg(xs + b0 + t) - (red[0][t] + red[1][t]);
     }
     __syncthreads();
-    if (t < 32) warp_trsv_lower_t(Td, nc, yb);
-    __syncthreads();
-    if (t < nc) {
-      xs[b0 + t] = yb[t];
-      if constexpr (WORDS) put_word(xw + c0 + b0 + t, epoch, float(yb[t]));
-    }
-    if constexpr (!WORDS) {
+    if constexpr (WORDS) {
+      // x_j = L_jj^-T y_j
+      V a = V(0);
+#pragma unroll
+      for (int cc = 0; cc < CPT; ++cc)
+        if (cg * CPT + cc < nc) a += Td[r * (TB + 1) + cg * CPT + cc] * yb[cg * CPT + cc];
+      redS[t] = a;
+      __syncthreads();
+      if (t < nc) {
+        const V xj = redS[t] + redS[t + TB] + redS[t + 2 * TB] + redS[t + 3 * TB];
+        xs[b0 + t] = xj;
+        put_word(xw + c0 + b0 + t, epoch, float(xj));
+      }
+    } else {
+      if (t < 32) warp_trsv_lower_t(Td, nc, yb);
+      __syncthreads();
+      if (t < nc) xs[b0 + t] = yb[t];
       __syncthreads();
       if (t == 0) publish(fl + j, epoch);
     }
@@ -478,8 +554,27 @@ template <class T, class V> static int launch_blk(Plan &P, bool fwd, int l, cons
   void *kern = fwd ? (void *)k_fwd_blk<T, V> : (void *)k_bwd_blk<T, V>;
   const int G = fwd ? coop_grid(P, k_fwd_blk<T, V>, cnt) : coop_grid(P, k_bwd_blk<T, V>, cnt);
   unsigned long long *xw = P.d_xw;
+  const float *tinv = reinterpret_cast<const float *>(P.d_tinv);
+  if constexpr (sizeof(V) == 4) {
+    if (!tinv) return NQG_ERR_ARG;
+    // inverses of the diagonal tiles, once per factorization
+    if (!P.tinv_valid) {
+      const int nb_all = P.blk_bwd_off.back() - P.blk_bwd_off.front();
+      if (nb_all > 0) {
+        cudaEvent_t ei = P.prof_begin();
+        k_tile_inverse<<<nb_all, TB, 0, P.stream>>>(reinterpret_cast<const int2 *>(P.d_blk_items) +
+                                                        P.blk_bwd_off.front(),
+                                                    super, lpi, lpx, reinterpret_cast<const float *>(L), flagoff,
+                                                    P.d_tinv);
+        NQG_CUDA(cudaGetLastError());
+        P.nlaunch++;
+        P.prof_end(NQG_K_SOLVE, ei, 0.0, 0.0);
+      }
+      P.tinv_valid = true;
+    }
+  }
   void *args[] = {(void *)&items, (void *)&cnt, (void *)&super, (void *)&lpi, (void *)&lpx, (void *)&ls,
-                  (void *)&L, &x, &flags, (void *)&flagoff, &epoch, (void *)&vis, &ctl, &status, &xw};
+                  (void *)&L, &x, &flags, (void *)&flagoff, &epoch, (void *)&vis, &ctl, &status, &xw, &tinv};
   cudaEvent_t e0 = P.prof_begin();
   NQG_CUDA(cudaLaunchCooperativeKernel(kern, dim3(G), dim3(SW_THREADS), args, 0, P.stream));
   P.nlaunch++;
