@@ -412,10 +412,10 @@ static int upload_plan(Plan &P) {
   NQG_CUDA(cudaMemset(P.d_solve_flags, 0, (size_t)P.solve_flags_cap * sizeof(unsigned)));
   NQG_CUDA(cudaMalloc(&P.d_xw, (size_t)std::max(n, 1) * sizeof(unsigned long long)));
   NQG_CUDA(cudaMemset(P.d_xw, 0, (size_t)std::max(n, 1) * sizeof(unsigned long long)));
-  // FP32 factor with FP32 block solves: inverses of the diagonal tiles
-  // (64 x 65 floats each, one per ready flag)
+  // FP32 factor with FP32 block solves: per diagonal tile (one per ready
+  // flag) its inverse and the two last-link products, 64 x 65 floats each
   if (P.set.precision == NQG_FP32 && P.set.solve_precision == NQG_FP32)
-    NQG_CUDA(cudaMalloc(&P.d_tinv, (size_t)std::max(nflags, 1) * 64 * 65 * sizeof(float)));
+    NQG_CUDA(cudaMalloc(&P.d_tinv, (size_t)std::max(nflags, 1) * 3 * 64 * 65 * sizeof(float)));
   P.solve_small_w = small_w;
   if ((rc = dev_alloc_copy(P, &P.d_targets_lv, lvflat.data(), lvflat.size()))) return rc;
   P.lv_targets_host = lvflat;

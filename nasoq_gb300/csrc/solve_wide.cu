@@ -61,20 +61,29 @@ template <class V> __device__ void warp_trsv_lower_t(const V *T11, int m, V *xb)
   if (lane + 32 < m) xb[lane + 32] = v1;
 }
 
-// FP32 sweeps solve a diagonal tile by a product with its inverse.  The
-// inverses of all diagonal 64 x 64 tiles of the block-solved supernodes are
-// formed once per factorization: tile (s, j) at tinv + (flagoff[s] + j) * TI,
-// entry (k, c) at [c * (TB + 1) + k], zero outside the tile's m x m block.
+// FP32 sweeps solve a diagonal tile by a product with its inverse, and take
+// the last link of the dependency chain -- the block solved just before --
+// through one more precomputed product:
+//   forward   x_q = T_q (b_q - sum_{j<q-1} L(q,j) x_j) - Mf_q x_{q-1},
+//             Mf_q = T_q L(q,q-1);
+//   backward  x_j = T_j^T (b_j - sum_{i>j+1} L(i,j)^T x_i - ...) - Mb_j x_{j+1},
+//             Mb_j = T_j^T L(j+1,j)^T;
+// with T = L_qq^-1, so that once x_{q-1} arrives one 64 x 64 product remains.
+// Formed once per factorization for every diagonal tile (s, j) of the
+// block-solved supernodes: T, Mf, Mb at tinv + (flagoff[s] + j) * 3 * TI (+ 0,
+// TI, 2 TI), entry (k, c) at [c * (TB + 1) + k], zeros outside the blocks.
 constexpr int TI = TB * (TB + 1);
 
 // One CTA of TB threads per diagonal tile (items: the backward items, (s, q)
-// for column block nbd(s) - 1 - q).  Thread c forms column c by forward
-// substitution in registers; its entries above row c start at 0 and stay 0,
-// so the unrolled recurrences need no predicate.
+// for column block nbd(s) - 1 - q).  Thread c forms column c of T by forward
+// substitution in registers (its entries above row c start at 0 and stay 0,
+// so the unrolled recurrences need no predicate), then column c of Mf and of
+// Mb from T in shared memory.
 __global__ void __launch_bounds__(TB) k_tile_inverse(const int2 *items, const int *super, const int64_t *lpi,
                                                      const int64_t *lpx, const float *L, const int *flagoff,
                                                      float *tinv) {
   __shared__ float T11[TB * TB];
+  __shared__ float Ti[TI];
   const int s = items[blockIdx.x].x, q = items[blockIdx.x].y;
   const int c0 = super[s], w = super[s + 1] - c0;
   const int nrow = (int)(lpi[s + 1] - lpi[s]);
@@ -97,15 +106,54 @@ __global__ void __launch_bounds__(TB) k_tile_inverse(const int2 *items, const in
     for (int k = 0; k < i; ++k) acc = fmaf(T11[i + k * TB], x[k], acc);
     if (i > c) x[i] = -acc;
   }
-  float *out = tinv + (size_t)(flagoff[s] + j) * TI + (size_t)c * (TB + 1);
+  float *base = tinv + (size_t)(flagoff[s] + j) * 3 * TI;
+  float *out = base + (size_t)c * (TB + 1);
 #pragma unroll
-  for (int k = 0; k < TB; ++k) out[k] = (c < m && k < m) ? x[k] : 0.f;
+  for (int k = 0; k < TB; ++k) {
+    const float v = (c < m && k < m) ? x[k] : 0.f;
+    out[k] = v;
+    Ti[c * (TB + 1) + k] = v;
+  }
   out[TB] = 0.f;
+  __syncthreads();
+  // Mf(:, c) = T L(q, q-1)(:, c): the previous block is full (64 columns)
+  {
+    float g[TB];
+#pragma unroll
+    for (int k = 0; k < TB; ++k) g[k] = (j > 0 && k < m) ? S[b0 + k + (size_t)(b0 - TB + c) * nrow] : 0.f;
+    float *o = base + TI + (size_t)c * (TB + 1);
+#pragma unroll 4
+    for (int rr = 0; rr < TB; ++rr) {
+      float a = 0.f;
+#pragma unroll
+      for (int k = 0; k < TB; ++k) a = fmaf(Ti[k * (TB + 1) + rr], g[k], a);
+      o[rr] = a;
+    }
+    o[TB] = 0.f;
+  }
+  // Mb(:, c) = T^T L(j+1, j)(c, :)^T: row c of the next block's tile
+  {
+    const int mn = j + 1 < nbd ? min(TB, w - b0 - TB) : 0;
+    float h[TB];
+#pragma unroll
+    for (int k = 0; k < TB; ++k) h[k] = (c < mn && k < m) ? S[b0 + TB + c + (size_t)(b0 + k) * nrow] : 0.f;
+    float *o = base + 2 * TI + (size_t)c * (TB + 1);
+#pragma unroll 4
+    for (int rr = 0; rr < TB; ++rr) {
+      float a = 0.f;
+#pragma unroll
+      for (int k = 0; k < TB; ++k) a = fmaf(Ti[rr * (TB + 1) + k], h[k], a);
+      o[rr] = a;
+    }
+    o[TB] = 0.f;
+  }
 }
 
-// Inverse of diagonal tile (s, j) into shared memory (FP32 sweeps).
-__device__ __forceinline__ void stage_inverse(const float *tinv, const int *flagoff, int s, int j, float *Ti) {
-  const float4 *src = reinterpret_cast<const float4 *>(tinv + (size_t)(flagoff[s] + j) * TI);
+// Matrix `part` (0: T, 1: Mf, 2: Mb) of diagonal tile (s, j) into shared
+// memory (FP32 sweeps).
+__device__ __forceinline__ void stage_inverse(const float *tinv, const int *flagoff, int s, int j, float *Ti,
+                                              int part = 0) {
+  const float4 *src = reinterpret_cast<const float4 *>(tinv + ((size_t)(flagoff[s] + j) * 3 + part) * TI);
   for (int e = threadIdx.x; e < TI / 4; e += blockDim.x) reinterpret_cast<float4 *>(Ti)[e] = __ldcg(src + e);
 }
 
@@ -259,7 +307,8 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
     const bool diag = q < nbd;
     const int r0 = diag ? q * TB : w + (q - nbd) * TB;
     const int m = min(TB, (diag ? w : nrow) - r0);
-    const int jmax = diag ? q : nbd;
+    // FP32 diagonal items leave block q - 1 to the last-link product
+    const int jmax = diag ? (WORDS ? max(q - 1, 0) : q) : nbd;
     if constexpr (WORDS) {
       if (diag) stage_inverse(tinv, flagoff, s, q, Td);
     } else {
@@ -283,9 +332,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
         vn[cc] = (j + 1 < jmax && rok && cbn + cc < w) ? Lr[(size_t)(cbn + cc) * nrow] : T(0);
       const int cb = j * TB + cg * CPT;
       if constexpr (WORDS) {
-        // the block just before a diagonal item's own is the last link of
-        // the chain: its words are polled directly by every warp
-        if (j >= front && !(diag && j == q - 1)) {
+        if (j >= front) {
           __syncthreads();
           if (t < 32) {
             const int f = wait_up(fl, epoch, j, nbd, front, ctl, status, xw + c0, w);
@@ -325,15 +372,32 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
       if (t < m) yb[t] = bq - yb[t];
       __syncthreads();
       if constexpr (WORDS) {
-        // x_q = L_qq^-1 y_q
+        // c_q = T_q y_q (thread t < TB keeps entry t)
         V a = V(0);
 #pragma unroll
         for (int cc = 0; cc < CPT; ++cc)
           if (cg * CPT + cc < m) a += Td[(cg * CPT + cc) * (TB + 1) + r] * yb[cg * CPT + cc];
         red[t] = a;
         __syncthreads();
+        const V cq = t < TB ? red[t] + red[t + TB] + red[t + 2 * TB] + red[t + 3 * TB] : V(0);
+        __syncthreads();
+        V xq = cq;
+        if (q > 0) {
+          // last link: x_q = c_q - Mf_q x_{q-1}, the words of block q - 1
+          // polled directly by every warp
+          stage_inverse(tinv, flagoff, s, q, Td, 1);
+          __syncthreads();
+          const int cb = (q - 1) * TB + cg * CPT;
+          float xv[CPT];
+          if (!wait_words(xw + c0 + cb, CPT, epoch, xv, ctl, status)) return;
+          a = V(0);
+#pragma unroll
+          for (int cc = 0; cc < CPT; ++cc) a += Td[(cg * CPT + cc) * (TB + 1) + r] * xv[cc];
+          red[t] = a;
+          __syncthreads();
+          if (t < TB) xq = cq - (red[t] + red[t + TB] + red[t + 2 * TB] + red[t + 3 * TB]);
+        }
         if (t < m) {
-          const V xq = red[t] + red[t + TB] + red[t + 2 * TB] + red[t + 3 * TB];
           xs[r0 + t] = xq;
           put_word(xw + c0 + r0 + t, epoch, float(xq));
         }
@@ -417,22 +481,23 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
         if (cok[cc]) part[cc] += V(Lc[row + (size_t)cc * nrow]) * xv;
     }
     // diagonal-block rows of later blocks, in the order they become ready
+    // (FP32: block j + 1 is left to the last-link product)
+    const int ilo = WORDS ? j + 1 : j;  // blocks i > ilo
     T v[CPT], vn[CPT];
     {
       const int row = (nbd - 1) * TB + r;
 #pragma unroll
-      for (int cc = 0; cc < CPT; ++cc) v[cc] = (j < nbd - 1 && row < w && cok[cc]) ? Lc[row + (size_t)cc * nrow] : T(0);
+      for (int cc = 0; cc < CPT; ++cc) v[cc] = (ilo < nbd - 1 && row < w && cok[cc]) ? Lc[row + (size_t)cc * nrow] : T(0);
     }
-    for (int i = nbd - 1; i > j; --i) {
+    for (int i = nbd - 1; i > ilo; --i) {
       const int rown = (i - 1) * TB + r;
 #pragma unroll
       for (int cc = 0; cc < CPT; ++cc)
-        vn[cc] = (i - 1 > j && rown < w && cok[cc]) ? Lc[rown + (size_t)cc * nrow] : T(0);
+        vn[cc] = (i - 1 > ilo && rown < w && cok[cc]) ? Lc[rown + (size_t)cc * nrow] : T(0);
       const int row = i * TB + r;
       V xv;
       if constexpr (WORDS) {
-        // block j + 1 is the last link of the chain: polled directly
-        if (i < front && i != j + 1) {
+        if (i < front) {
           __syncthreads();
           if (t < 32) {
             const int f = wait_down(fl, epoch, i, j + 1, front, ctl, status, xw + c0, w);
@@ -495,15 +560,32 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
     }
     __syncthreads();
     if constexpr (WORDS) {
-      // x_j = L_jj^-T y_j
+      // c_j = T_j^T y_j (thread t < TB keeps entry t)
       V a = V(0);
 #pragma unroll
       for (int cc = 0; cc < CPT; ++cc)
         if (cg * CPT + cc < nc) a += Td[r * (TB + 1) + cg * CPT + cc] * yb[cg * CPT + cc];
       redS[t] = a;
       __syncthreads();
+      const V cj = t < TB ? redS[t] + redS[t + TB] + redS[t + 2 * TB] + redS[t + 3 * TB] : V(0);
+      __syncthreads();
+      V xj = cj;
+      if (j + 1 < nbd) {
+        // last link: x_j = c_j - Mb_j x_{j+1}, the words of block j + 1
+        // polled directly by every warp
+        stage_inverse(tinv, flagoff, s, j, Td, 2);
+        __syncthreads();
+        const int cb1 = (j + 1) * TB + cg * CPT;
+        float xv[CPT];
+        if (!wait_words(xw + c0 + cb1, min(CPT, w - cb1), epoch, xv, ctl, status)) return;
+        a = V(0);
+#pragma unroll
+        for (int cc = 0; cc < CPT; ++cc) a += Td[(cg * CPT + cc) * (TB + 1) + r] * xv[cc];
+        redS[t] = a;
+        __syncthreads();
+        if (t < TB) xj = cj - (redS[t] + redS[t + TB] + redS[t + 2 * TB] + redS[t + 3 * TB]);
+      }
       if (t < nc) {
-        const V xj = redS[t] + redS[t + TB] + redS[t + 2 * TB] + redS[t + 3 * TB];
         xs[b0 + t] = xj;
         put_word(xw + c0 + b0 + t, epoch, float(xj));
       }
