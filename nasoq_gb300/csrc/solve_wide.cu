@@ -157,6 +157,16 @@ __device__ __forceinline__ void stage_inverse(const float *tinv, const int *flag
   for (int e = threadIdx.x; e < TI / 4; e += blockDim.x) reinterpret_cast<float4 *>(Ti)[e] = __ldcg(src + e);
 }
 
+// Entries (r, c0 .. c0 + CPT - 1) of matrix `part` of diagonal tile (s, j),
+// loaded at the start of an item so that the last link finds them in
+// registers.
+__device__ __forceinline__ void load_link(const float *tinv, const int *flagoff, int s, int j, int part, int r,
+                                          int c0, float (&mv)[CPT]) {
+  const float *src = tinv + ((size_t)(flagoff[s] + j) * 3 + part) * TI + (size_t)c0 * (TB + 1) + r;
+#pragma unroll
+  for (int cc = 0; cc < CPT; ++cc) mv[cc] = __ldcg(src + (size_t)cc * (TB + 1));
+}
+
 // The m x m tile at (b0, b0) of the panel, column-major in T11.
 template <class T, class V> __device__ void stage_tile(const T *S, int nrow, int b0, int m, V *T11) {
   for (int e = threadIdx.x; e < TB * TB; e += blockDim.x) {
@@ -309,8 +319,10 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
     const int m = min(TB, (diag ? w : nrow) - r0);
     // FP32 diagonal items leave block q - 1 to the last-link product
     const int jmax = diag ? (WORDS ? max(q - 1, 0) : q) : nbd;
+    float mlink[CPT];  // FP32 diagonal items: this thread's entries of Mf_q
     if constexpr (WORDS) {
       if (diag) stage_inverse(tinv, flagoff, s, q, Td);
+      if (diag && q > 0) load_link(tinv, flagoff, s, q, 1, r, cg * CPT, mlink);
     } else {
       if (diag) stage_tile(S, nrow, r0, m, Td);
     }
@@ -385,14 +397,12 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
         if (q > 0) {
           // last link: x_q = c_q - Mf_q x_{q-1}, the words of block q - 1
           // polled directly by every warp
-          stage_inverse(tinv, flagoff, s, q, Td, 1);
-          __syncthreads();
           const int cb = (q - 1) * TB + cg * CPT;
           float xv[CPT];
           if (!wait_words(xw + c0 + cb, CPT, epoch, xv, ctl, status)) return;
           a = V(0);
 #pragma unroll
-          for (int cc = 0; cc < CPT; ++cc) a += Td[(cg * CPT + cc) * (TB + 1) + r] * xv[cc];
+          for (int cc = 0; cc < CPT; ++cc) a += mlink[cc] * xv[cc];
           red[t] = a;
           __syncthreads();
           if (t < TB) xq = cq - (red[t] + red[t + TB] + red[t + 2 * TB] + red[t + 3 * TB]);
@@ -448,8 +458,13 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
     }
     const int j = nbd - 1 - q;
     const int b0 = j * TB, nc = min(TB, w - b0);
-    if constexpr (WORDS) stage_inverse(tinv, flagoff, s, j, Td);
-    else stage_tile(S, nrow, b0, nc, Td);
+    float mlink[CPT];  // FP32: this thread's entries of Mb_j
+    if constexpr (WORDS) {
+      stage_inverse(tinv, flagoff, s, j, Td);
+      if (j + 1 < nbd) load_link(tinv, flagoff, s, j, 2, r, cg * CPT, mlink);
+    } else {
+      stage_tile(S, nrow, b0, nc, Td);
+    }
     const int cb = b0 + cg * CPT;
     const T *Lc = S + (size_t)cb * nrow;  // first of this thread's columns
     bool cok[CPT];
@@ -573,14 +588,12 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
       if (j + 1 < nbd) {
         // last link: x_j = c_j - Mb_j x_{j+1}, the words of block j + 1
         // polled directly by every warp
-        stage_inverse(tinv, flagoff, s, j, Td, 2);
-        __syncthreads();
         const int cb1 = (j + 1) * TB + cg * CPT;
         float xv[CPT];
         if (!wait_words(xw + c0 + cb1, min(CPT, w - cb1), epoch, xv, ctl, status)) return;
         a = V(0);
 #pragma unroll
-        for (int cc = 0; cc < CPT; ++cc) a += Td[(cg * CPT + cc) * (TB + 1) + r] * xv[cc];
+        for (int cc = 0; cc < CPT; ++cc) a += mlink[cc] * xv[cc];
         redS[t] = a;
         __syncthreads();
         if (t < TB) xj = cj - (redS[t] + redS[t + TB] + redS[t + 2 * TB] + redS[t + 3 * TB]);
