@@ -447,11 +447,11 @@ static int upload_plan(Plan &P) {
     int64_t wide_rows = 0;
     for (int s = 0; s < ns; ++s)
       if (S.super[s + 1] - S.super[s] > P.wide_min) wide_rows = std::max<int64_t>(wide_rows, S.lpi[s + 1] - S.lpi[s]);
-    // W of up to wide_depth pending panels (each at most nb + 1 columns) plus
-    // the two working columns of the panel kernel
+    // W of up to wide_depth + 1 pending panels (each at most nb + 1 columns)
+    // plus the two working columns of the panel kernel
     if (wide_rows > 0)
       NQG_CUDA(cudaMalloc(&P.d_wide_W,
-                          (size_t)wide_rows * (P.wide_depth * (P.wide_nb + 1) + 2) * P.val_size()));
+                          (size_t)wide_rows * ((P.wide_depth + 1) * (P.wide_nb + 1) + 2) * P.val_size()));
     // FP32: packed split-TF32 operands of the persistent tcgen05 updates,
     // blocks of 128 rows x 32 columns (hi + lo TF32 halves of 16 KB each).
     // Trailing updates of a wide supernode: row blocks of L then of W, each
@@ -466,7 +466,7 @@ static int upload_plan(Plan &P) {
           if (S.super[s + 1] - S.super[s] > P.wide_min)
             blocks = std::max<int64_t>(blocks, (S.lpi[s + 1] - S.lpi[s] + 127) / 128 +
                                                    (S.super[s + 1] - S.super[s] + 127) / 128);
-        chunks = blocks * (int64_t)std::max(P.wide_depth, 1) * ((P.wide_nb + 1 + 31) / 32);
+        chunks = blocks * (int64_t)(std::max(P.wide_depth, 1) + 1) * ((P.wide_nb + 1 + 31) / 32);
       }
       for (int q : P.pers_pair) {
         const int d = P.pair_d[q];

@@ -1681,7 +1681,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   // nkc_stride chunks each (every pending panel starts on a new chunk)
   unsigned char *pack_a = (sizeof(T) == 4 && trail == 2 && !tile_only && P) ? P->d_wide_pack : nullptr;
   const int nch_panel = (nb + 1 + t5::TK - 1) / t5::TK;
-  const int nkc_stride = std::max(depth, 1) * nch_panel;
+  const int nkc_stride = (std::max(depth, 1) + 1) * nch_panel;  // room for depth + 1 panels
   const int nrb_all = (nrow + t5::TM - 1) / t5::TM, ncb_all = (w + t5::TN - 1) / t5::TN;
   unsigned char *pack_b = pack_a ? pack_a + (size_t)nrb_all * nkc_stride * PK_BLOCK : nullptr;
   if (pack_a && cudaFuncSetAttribute(k_tc_persistent<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1730,6 +1730,13 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   // block-first launch)
   unsigned blk_seq = 0;
   bool mslot_dirty = false;
+  // width of general panels that follow a fast panel's stop (FP32 fast-panel
+  // path: 8 columns, NASOQ_GB300_PIVOT_NB overrides, 2 .. nb): the pivots of
+  // the KKT systems come singly or in 2 x 2 blocks, so the fast kernel takes
+  // over again right after them
+  int pivot_nb = fast_enabled ? std::min(nb, 8) : nb;
+  if (const char *e = std::getenv("NASOQ_GB300_PIVOT_NB"))
+    if (fast_enabled) pivot_nb = std::min(nb, std::max(2, std::atoi(e)));
   bool use_general = false;  // the next panel starts at a column that needs a pivot search
   // Delayed trailing updates (FP32 tcgen05 path): up to `depth` consecutive
   // panels are pending, their W columns side by side in Wb, and one update of
@@ -1819,7 +1826,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     return NQG_OK;
   };
   // band update before a panel at s.k0 (flushing everything before a general one)
-  auto pre = [&](State &s, bool general) -> int {
+  auto pre = [&](State &s, bool general, int kb_want) -> int {
     if (!delayed) return NQG_OK;
     int rc;
     if (general && s.npend > 0) {
@@ -1832,7 +1839,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     // a general panel may end with a 2x2 pivot one column past nb; a fast
     // panel never goes past nb, so its band stops at k0 + nb and a complete
     // fast panel leaves no remainder of its own update to apply
-    const int bend = std::min(w, s.k0 + nb + (general ? 1 : 0));
+    const int bend = std::min(w, s.k0 + kb_want + (general ? 1 : 0));
     if (s.npend > 0 && s.F < bend && (rc = apply(s.pend_k0, s.pend_K, 0, 0, s.pend_C, s.F, bend))) return rc;
     s.F = std::max(s.F, bend);
     return NQG_OK;
@@ -1848,7 +1855,11 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       s.pend_K += kb;
       s.pend_C += nch(kb);
       ++s.npend;
-      if (s.npend == depth || k1 >= w) {
+      // flush once depth * nb columns are pending (narrow panels after pivot
+      // searches do not count as whole panels), or before the buffers (room
+      // for depth + 1 panels of nb + 1 columns) could overflow
+      if (s.pend_K >= depth * nb || s.pend_C + nch(nb + 1) > nkc_stride ||
+          s.pend_K + nb + 1 > (depth + 1) * (nb + 1) || k1 >= w) {
         if ((rc = apply(s.pend_k0, s.pend_K, 0, 0, s.pend_C, s.F, w))) return rc;
         s.npend = 0;
         s.pend_K = 0;
@@ -1969,10 +1980,13 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     return NQG_OK;
   };
   while (cs.k0 < w) {
-    const int kb_want = std::min(nb, w - cs.k0);
+    // a panel on the general kernel (after a fast panel stopped at a column
+    // that needs a pivot search) is at most pivot_nb columns wide, so that the
+    // fast kernel takes over again soon after the pivots
+    const int kb_want = std::min(use_general ? pivot_nb : nb, w - cs.k0);
     const bool fast = fast_enabled && !use_general && nrow - cs.k0 - kb_want <= maxG_fast * FP_THREADS;
     if (fast && spec_ok) {
-      int rc = pre(cs, false);
+      int rc = pre(cs, false, kb_want);
       if (rc) return rc;
       const int woff = delayed ? cs.pend_K : 0;
       bool packed = false;
@@ -1989,7 +2003,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       if (rc) return rc;
       continue;  // the state may have been rewound
     }
-    int rc = pre(cs, !fast);
+    int rc = pre(cs, !fast, kb_want);
     if (rc) return rc;
     const int woff = delayed ? cs.pend_K : 0;  // this panel's W columns
     T *Wp = Wb + (size_t)woff * nrow;
