@@ -144,7 +144,7 @@ struct Plan {
   int solve_flags_cap = 0;
   unsigned solve_epoch = 0;
   int wide_nb = 64;
-  int wide_min = 256;               // supernodes wider than this use the blocked kernels
+  int wide_min = 192;               // supernodes wider than this use the blocked kernels
   int bk_small = 64;                // supernodes up to this width: shared-memory BK kernel
   int wide_depth = 8;               // wide supernodes: panels per delayed trailing update (FP32)
   bool panel_rows_serial = false;   // rows below k_bk_global blocks solved inside that kernel

@@ -666,6 +666,8 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
       float v[8], lv[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) v[q] = q < nc ? wsm[(jb + q) * FB_THREADS + tid] : 0.f;
+      // (unrolled so that the shared-memory loads of several t overlap)
+#pragma unroll 4
       for (int t = 0; t < jb; ++t) {
         const float l = wsm[t * FB_THREADS + tid] * rinv[t];
         const float4 x0 = *reinterpret_cast<const float4 *>(Rc + t * FB_LD + jb);
@@ -697,6 +699,7 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
   const int nvalid = max(0, min(FB_THREADS, min(nrow, w) - (k0 + nbR + (int)blockIdx.x * FB_THREADS)));
   for (int j = wid; j < nbR; j += FB_THREADS / 32) {
     unsigned m = 0u;
+#pragma unroll 4
     for (int t = lane; t < nvalid; t += 32) {
       const float a = fabsf(wsm[j * FB_THREADS + t]);
       if (a == a) m = max(m, __float_as_uint(a));
@@ -724,10 +727,19 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
           for (int bb = tid; bb < G; bb += FB_THREADS)
             if ((unsigned)*(volatile unsigned long long *)&slots[bb] != seq) all = false;
         } else if (q < nbR) {
-          for (int bb = p; bb < G; bb += FB_THREADS / WP_NB) {
-            const unsigned long long v = *(volatile unsigned long long *)&slots[q * FB_MAXG + bb];
-            if ((unsigned)v != seq) all = false;
-            else m = max(m, (unsigned)(v >> 32));
+          // all loads first (one L2 round trip), then the checks
+          constexpr int NW = FB_MAXG / (FB_THREADS / WP_NB);
+          unsigned long long v[NW];
+#pragma unroll
+          for (int k = 0; k < NW; ++k) {
+            const int bb = p + k * (FB_THREADS / WP_NB);
+            v[k] = bb < G ? *(volatile unsigned long long *)&slots[q * FB_MAXG + bb] : 0ull;
+          }
+#pragma unroll
+          for (int k = 0; k < NW; ++k) {
+            if (p + k * (FB_THREADS / WP_NB) >= G) continue;
+            if ((unsigned)v[k] != seq) all = false;
+            else m = max(m, (unsigned)(v[k] >> 32));
           }
         }
         if (__syncthreads_and(all)) break;
