@@ -88,6 +88,9 @@ __device__ void block_argmax(T &v, int &idx, T *sv, int *si) {
 // previously computed columns.  On return a holds L with unit diagonal and
 // zeroed 2x2 sub-diagonals; D/E get the diagonal and 2x2 sub-diagonals;
 // perm[m] = original local column now at position m.
+// Largest diagonal block k_bk_global stages in shared memory (bytes).
+constexpr size_t BKG_STAGE_MAX = 200 * 1024;
+
 template <class T>
 __device__ void bk_factor(T *a, int lda, int w, T *D, T *E, int *perm, int *status, bool *pivoted_out) {
   __shared__ T red_v[32];
@@ -605,18 +608,37 @@ __global__ void __launch_bounds__(BK_THREADS) k_bk_small(const int *targets, int
 template <class T>
 __global__ void __launch_bounds__(256) k_bk_global(const int *targets, int n, const int *super, const int64_t *lpi,
                                                    const int64_t *lpx, T *L, T *Dg, int *locperm, uint8_t *pivoted,
-                                                   int *cycle_buf, int do_rows, int *status) {
+                                                   int *cycle_buf, int do_rows, int *status, int staged) {
+  extern __shared__ __align__(16) unsigned char bkg_raw[];
   const int s = targets[blockIdx.x];
   const int c0 = super[s], w = super[s + 1] - c0;
   const int nrow = (int)(lpi[s + 1] - lpi[s]);
   T *Ls = L + lpx[s];
   int *perm = locperm + c0;
   bool piv = false;
-  bk_factor(Ls, nrow, w, Dg + c0, Dg + n + c0, perm, status, &piv);
-  // zero the strict upper triangle (never referenced, kept at 0 like the reference)
-  for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
-    int c = e / w, r = e % w;
-    if (r < c) Ls[r + (size_t)c * nrow] = T(0);
+  if (staged) {
+    // the whole diagonal block in shared memory (staged: the launch's
+    // dynamic shared memory holds w x w values), factored there, written back
+    T *a = reinterpret_cast<T *>(bkg_raw);
+    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+      const int c = e / w, r = e % w;
+      a[e] = r >= c ? Ls[r + (size_t)c * nrow] : T(0);
+    }
+    __syncthreads();
+    bk_factor(a, w, w, Dg + c0, Dg + n + c0, perm, status, &piv);
+    __syncthreads();
+    // strict upper triangle back to 0 (never referenced, kept at 0 like the reference)
+    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+      const int c = e / w, r = e % w;
+      Ls[r + (size_t)c * nrow] = r >= c ? a[e] : T(0);
+    }
+  } else {
+    bk_factor(Ls, nrow, w, Dg + c0, Dg + n + c0, perm, status, &piv);
+    // zero the strict upper triangle (never referenced, kept at 0 like the reference)
+    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+      int c = e / w, r = e % w;
+      if (r < c) Ls[r + (size_t)c * nrow] = T(0);
+    }
   }
   if (threadIdx.x == 0) pivoted[s] = piv ? 1 : 0;
   __syncthreads();
@@ -1109,9 +1131,18 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
         P.nlaunch++;
       }
       if (lv_glob_cnt[l] > 0) {
-        k_bk_global<T><<<lv_glob_cnt[l], 256, 0, st>>>(P.d_targets + lv_glob_off[l], n, P.d_super, P.d_lpi, P.d_lpx,
-                                                        L, D, P.d_locperm, P.d_pivoted, P.d_perm_tmp,
-                                                        rows_split ? 0 : 1, P.d_status);
+        // diagonal blocks staged in shared memory when the widest fits
+        int wl = 0;
+        for (int q = lv_glob_off[l]; q < lv_glob_off[l] + lv_glob_cnt[l]; ++q)
+          wl = std::max(wl, P.sym.super[order[q] + 1] - P.sym.super[order[q]]);
+        const size_t bks = (size_t)wl * wl * sizeof(T);
+        const int staged = bks <= BKG_STAGE_MAX ? 1 : 0;
+        if (staged)
+          NQG_CUDA(cudaFuncSetAttribute(k_bk_global<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)BKG_STAGE_MAX));
+        k_bk_global<T><<<lv_glob_cnt[l], 256, staged ? bks : 0, st>>>(
+            P.d_targets + lv_glob_off[l], n, P.d_super, P.d_lpi, P.d_lpx, L, D, P.d_locperm, P.d_pivoted,
+            P.d_perm_tmp, rows_split ? 0 : 1, P.d_status, staged);
         P.nlaunch++;
         if (rows_split && lv_row_cnt[l] > 0) {
           k_panel_rows<T><<<lv_row_cnt[l], 256, pr_smem, st>>>(
