@@ -487,7 +487,7 @@ static int upload_plan(Plan &P) {
 
 static void free_plan(Plan &P) {
   void *ptrs[] = {P.d_super, P.d_col2sup, P.d_ls, P.d_ls_sym, P.d_lpi, P.d_lpx, P.d_Kp, P.d_Ki, P.d_Kx,
-                  P.d_Rp, P.d_Rj, P.d_Rx, P.d_map_lo, P.d_map_hi, P.d_perm, P.d_iperm, P.d_locperm,
+                  P.d_Rp, P.d_Rj, P.d_Rx, P.d_map_lo, P.d_map_hi, P.d_Kx_spmv, P.d_perm, P.d_iperm, P.d_locperm,
                   P.d_perm_tmp, P.d_L, P.d_D, P.d_tiles, P.d_tile_list, P.d_targets, P.d_pair_s, P.d_pair_d,
                   P.d_pair_lb, P.d_pair_ub, P.d_targets_lv, P.d_pivoted, P.d_visible, P.d_hidden, P.d_status,
                   P.d_xo, P.d_bo, P.d_r, P.d_w, P.d_in, P.d_out, P.d_V, P.d_scal, P.d_wide_W, P.d_wide_ctl,
@@ -606,18 +606,35 @@ extern "C" int nqg_get_symbolic(const nqg_plan *h, const nqg_symbolic **sym) {
   return NQG_OK;
 }
 
+namespace {
+// Refinement matrix values: CSC value q of the lower triangle goes to its
+// position(s) in the full CSR (the pattern never changes).
+__global__ void k_scatter_full(int64_t nz, const int64_t *mlo, const int64_t *mhi, const double *xv, double *Rx) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nz; q += (int64_t)gridDim.x * blockDim.x) {
+    const double v = xv[q];
+    Rx[mlo[q]] = v;
+    if (mhi[q] >= 0) Rx[mhi[q]] = v;
+  }
+}
+}  // namespace
+
 extern "C" int nqg_set_values(nqg_plan *h, const double *Ax) {
   if (!h || (!Ax && h->P.n > 0)) return NQG_ERR_ARG;
   Plan &P = h->P;
+  // the host copies below overwrite buffers that earlier copies read from
+  NQG_CUDA(cudaStreamSynchronize(P.stream));
   P.K.x.assign(Ax, Ax + P.K.nnz());
   apply_perturbation(P);
-  NQG_CUDA(cudaMemcpyAsync(P.d_Kx, P.K.x.data(), P.K.x.size() * sizeof(double), cudaMemcpyHostToDevice, P.stream));
-  std::vector<int> Rp, Rj;
-  std::vector<double> Rx;
-  std::vector<int64_t> mlo, mhi;
-  build_full_csr(P.K, P.Kx_spmv, Rp, Rj, Rx, mlo, mhi);
-  NQG_CUDA(cudaMemcpyAsync(P.d_Rx, Rx.data(), Rx.size() * sizeof(double), cudaMemcpyHostToDevice, P.stream));
-  NQG_CUDA(cudaStreamSynchronize(P.stream));
+  const int64_t nz = (int64_t)P.K.nnz();
+  NQG_CUDA(cudaMemcpyAsync(P.d_Kx, P.K.x.data(), nz * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  if (nz > 0) {
+    if (!P.d_Kx_spmv) NQG_CUDA(cudaMalloc(&P.d_Kx_spmv, nz * sizeof(double)));
+    NQG_CUDA(cudaMemcpyAsync(P.d_Kx_spmv, P.Kx_spmv.data(), nz * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+    k_scatter_full<<<(int)std::min<int64_t>((nz + 255) / 256, 4096), 256, 0, P.stream>>>(nz, P.d_map_lo, P.d_map_hi,
+                                                                                          P.d_Kx_spmv, P.d_Rx);
+    P.nlaunch++;
+    NQG_CUDA(cudaGetLastError());
+  }
   P.factored = false;
   return NQG_OK;
 }

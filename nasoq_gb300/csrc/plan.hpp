@@ -85,6 +85,7 @@ struct Plan {
   int *d_Rp = nullptr, *d_Rj = nullptr;  // full (both triangles) CSR of K for the SpMV
   double *d_Rx = nullptr;
   int64_t *d_map_lo = nullptr, *d_map_hi = nullptr;  // CSC value index -> CSR positions
+  double *d_Kx_spmv = nullptr;      // staging of the refinement values (nqg_set_values)
   int *d_perm = nullptr, *d_iperm = nullptr, *d_locperm = nullptr, *d_perm_tmp = nullptr;
   void *d_L = nullptr;              // factor values (double or float)
   void *d_D = nullptr;              // 2n: diagonal then 2x2 sub-diagonal
