@@ -164,6 +164,8 @@ static void build_schedule(Plan &P) {
   P.pair_ub.clear();
   P.pair_flops.clear();
   P.pair_pers.clear();
+  P.pair_moff.clear();
+  P.map_total = 0;
   P.tile_ptr.assign(ns + 1, 0);
   P.tiles.clear();
   P.tile_ptr_tc.assign(ns + 1, 0);
@@ -199,6 +201,8 @@ static void build_schedule(Plan &P) {
         const double m = nr - lb, nc = ub - lb + 1, wd = S.super[d + 1] - S.super[d];
         P.pair_flops.push_back(2.0 * wd * (nc * m - nc * (nc - 1) / 2.0));
         P.pair_pers.push_back(0);
+        P.pair_moff.push_back(P.map_total);
+        P.map_total += nr - lb;
       }
       if (tc && S.super[d + 1] - S.super[d] >= tc_min_wd && pers_min >= 0 && P.pair_flops.back() >= pers_min) {
         P.pers_pair.push_back((int)P.pair_d.size() - 1);
@@ -207,11 +211,11 @@ static void build_schedule(Plan &P) {
       } else if (tc && S.super[d + 1] - S.super[d] >= tc_min_wd) {
         for (int ri = lb; ri < nr; ri += UPD_TC_T)
           for (int cj = lb; cj <= ub; cj += UPD_TC_T)
-            if (ri + UPD_TC_T - 1 >= cj) P.tiles_tc.push_back(UpdTile{s, d, ri, cj, ub});
+            if (ri + UPD_TC_T - 1 >= cj) P.tiles_tc.push_back(UpdTile{s, d, ri, cj, ub, (int)P.pair_d.size() - 1});
       } else {
         for (int ri = lb; ri < nr; ri += UPD_TM)
           for (int cj = lb; cj <= ub; cj += UPD_TN)
-            if (ri + UPD_TM - 1 >= cj) P.tiles.push_back(UpdTile{s, d, ri, cj, ub});
+            if (ri + UPD_TM - 1 >= cj) P.tiles.push_back(UpdTile{s, d, ri, cj, ub, (int)P.pair_d.size() - 1});
       }
     }
     P.pair_ptr[s + 1] = (int)P.pair_d.size();
@@ -311,6 +315,8 @@ static int upload_plan(Plan &P) {
   if ((rc = dev_alloc_copy(P, &P.d_pair_s, ps.data(), ps.size()))) return rc;
   if ((rc = dev_alloc_copy(P, &P.d_pair_d, P.pair_d.data(), P.pair_d.size()))) return rc;
   if ((rc = dev_alloc_copy(P, &P.d_pair_lb, P.pair_lb.data(), P.pair_lb.size()))) return rc;
+  if ((rc = dev_alloc_copy(P, &P.d_pair_moff, P.pair_moff.data(), P.pair_moff.size()))) return rc;
+  NQG_CUDA(cudaMalloc(&P.d_pair_map, (size_t)std::max<int64_t>(P.map_total, 1) * sizeof(int)));
   if ((rc = dev_alloc_copy(P, &P.d_pair_ub, P.pair_ub.data(), P.pair_ub.size()))) return rc;
   {
     // row renaming work: rows of every pair, and value-movement items sized so
@@ -491,7 +497,7 @@ static void free_plan(Plan &P) {
                   P.d_perm_tmp, P.d_L, P.d_D, P.d_tiles, P.d_tile_list, P.d_targets, P.d_pair_s, P.d_pair_d,
                   P.d_pair_lb, P.d_pair_ub, P.d_targets_lv, P.d_pivoted, P.d_visible, P.d_hidden, P.d_status,
                   P.d_xo, P.d_bo, P.d_r, P.d_w, P.d_in, P.d_out, P.d_V, P.d_scal, P.d_wide_W, P.d_wide_ctl,
-                  P.d_wide_pack, P.d_pers_map, P.d_locinv, P.d_pair_roff, P.d_rr_dest, P.d_rr_moved, P.d_rr_items, P.d_rr_stage,
+                  P.d_wide_pack, P.d_pers_map, P.d_pair_map, P.d_pair_moff, P.d_map_items, P.d_locinv, P.d_pair_roff, P.d_rr_dest, P.d_rr_moved, P.d_rr_items, P.d_rr_stage,
                   P.d_solve_flags, P.d_xw, P.d_tinv, P.d_blk_items, P.d_flagoff, P.d_xf, P.d_Z, P.d_tiles_tc,
                   P.d_tile_list_tc, P.d_row_items};
   for (void *p : ptrs)

@@ -321,6 +321,36 @@ __global__ void k_zero_targets(const int *targets, int ntargets, const int *supe
   }
 }
 
+__device__ __forceinline__ int lower_bound_i(const int *a, int len, int key);
+
+// Target row positions of the rows lb + r0 .. of descendant pair q (item
+// (q, r0), one thread per row): row r of d goes to r - cs0 inside the
+// target's diagonal block, else to its place in the target's row list.  The
+// update tiles of the level read them instead of searching per tile.
+__global__ void __launch_bounds__(256) k_pair_rowmap(const int2 *items, const int *pair_s, const int *pair_d,
+                                                     const int *pair_lb, const int64_t *moff, const int *super,
+                                                     const int64_t *lpi, const int *ls, int *map, int *status) {
+  const int q = items[blockIdx.x].x, i = items[blockIdx.x].y + threadIdx.x;
+  const int s = pair_s[q], d = pair_d[q], lb = pair_lb[q];
+  const int m = (int)(lpi[d + 1] - lpi[d]) - lb;
+  if (i >= m) return;
+  const int r = ls[lpi[d] + lb + i];
+  const int cs0 = super[s], ws = super[s + 1] - cs0;
+  const int nrs = (int)(lpi[s + 1] - lpi[s]);
+  const int *rows_s = ls + lpi[s];
+  int pos;
+  if (r < cs0 + ws) {
+    pos = r - cs0;
+  } else {
+    pos = ws + lower_bound_i(rows_s + ws, nrs - ws, r);
+    if (pos >= nrs || rows_s[pos] != r) {
+      flag_status(status, ST_BOUNDS);
+      pos = -1;
+    }
+  }
+  map[moff[q] + i] = pos;
+}
+
 __device__ __forceinline__ int lower_bound_i(const int *a, int len, int key) {
   int lo = 0, hi = len;
   while (lo < hi) {
@@ -370,7 +400,8 @@ __global__ void k_assemble(int n, const int *Kp, const int *Ki, const double *Kx
 template <class T>
 __global__ void __launch_bounds__(UPD_THREADS) k_update(const UpdTile *tiles, const int *tile_ids, int ntiles, int n,
                                                        const int *super, const int64_t *lpi, const int64_t *lpx,
-                                                       const int *ls, T *L, const T *Dg, int *status) {
+                                                       const int *ls, T *L, const T *Dg, int *status,
+                                                       const int *rowmap, const int64_t *pmoff, const int *pair_lb) {
   __shared__ T As[UPD_KC][UPD_TM + 1];
   __shared__ T Bs[UPD_KC][UPD_TN + 1];
   __shared__ T Raw[UPD_KC + 2][UPD_TM + 1];
@@ -387,24 +418,10 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(const UpdTile *tiles, co
   const int ncols = min(UPD_TN, tl.ub + 1 - tl.cj);
   const int cs0 = super[s], ws = super[s + 1] - cs0;
   const int nrs = (int)(lpi[s + 1] - lpi[s]);
-  const int *rows_s = ls + lpi[s];
   T *Lt = L + lpx[s];
-  // target positions of the tile's rows and columns
-  for (int i = tid; i < UPD_TM; i += blockDim.x) {
-    int pos = -1;
-    if (i < mrows) {
-      int r = rows_d[tl.ri + i];
-      if (r < cs0 + ws) pos = r - cs0;
-      else {
-        pos = ws + lower_bound_i(rows_s + ws, nrs - ws, r);
-        if (pos >= nrs || rows_s[pos] != r) {
-          flag_status(status, ST_BOUNDS);
-          pos = -1;
-        }
-      }
-    }
-    prow[i] = pos;
-  }
+  // target positions of the tile's rows (from the level's pair map) and columns
+  const int *pmap = rowmap + pmoff[tl.q] + (tl.ri - pair_lb[tl.q]);
+  for (int i = tid; i < UPD_TM; i += blockDim.x) prow[i] = i < mrows ? pmap[i] : -1;
   for (int j = tid; j < UPD_TN; j += blockDim.x) {
     int pos = -1;
     if (j < ncols) {
@@ -483,7 +500,9 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(const UpdTile *tiles, co
 // atomic scatter into the target from the TMEM rows (thread r owns row r).
 __global__ void __launch_bounds__(t5::THREADS) k_update_t5(const UpdTile *tiles, const int *tile_ids, int n,
                                                            const int *super, const int64_t *lpi, const int64_t *lpx,
-                                                           const int *ls, float *L, const float *Dg, int *status) {
+                                                           const int *ls, float *L, const float *Dg, int *status,
+                                                           const int *rowmap, const int64_t *pmoff,
+                                                           const int *pair_lb) {
   extern __shared__ __align__(1024) unsigned char t5_smem[];
   __shared__ int prow[UPD_TC_T], pcol[UPD_TC_T];
   const int tid = threadIdx.x;
@@ -497,22 +516,10 @@ __global__ void __launch_bounds__(t5::THREADS) k_update_t5(const UpdTile *tiles,
   const int ncols = min(UPD_TC_T, tl.ub + 1 - tl.cj);
   const int cs0 = super[s], ws = super[s + 1] - cs0;
   const int nrs = (int)(lpi[s + 1] - lpi[s]);
-  const int *rows_s = ls + lpi[s];
   float *Lt = L + lpx[s];
   {
-    // target positions of row tid and column tid of the tile
-    int pos = -1;
-    if (tid < mrows) {
-      const int r = rows_d[tl.ri + tid];
-      if (r < cs0 + ws) pos = r - cs0;
-      else {
-        pos = ws + lower_bound_i(rows_s + ws, nrs - ws, r);
-        if (pos >= nrs || rows_s[pos] != r) {
-          flag_status(status, ST_BOUNDS);
-          pos = -1;
-        }
-      }
-    }
+    // target positions of row tid (from the level's pair map) and column tid
+    int pos = tid < mrows ? rowmap[pmoff[tl.q] + (tl.ri - pair_lb[tl.q]) + tid] : -1;
     prow[tid] = pos;
     pos = -1;
     if (tid < ncols) {
@@ -960,6 +967,8 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
   std::vector<int> row_items, lv_row_off, lv_row_cnt;  // (supernode, row block) items of k_panel_rows
   std::vector<int> tile_ids, tile_ids_tc;
   std::vector<int64_t> lv_tile_off, lv_tile_cnt, lv_tc_off, lv_tc_cnt;
+  std::vector<int> map_items;  // (pair, first row) of the pair row maps, per level
+  std::vector<int64_t> lv_map_off, lv_map_cnt;
   const int nlev = (int)P.levels.size();
   for (int l = 0; l < nlev; ++l) {
     int so = (int)order.size();
@@ -999,6 +1008,20 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
         for (int64_t t = P.tile_ptr_tc[s]; t < P.tile_ptr_tc[s + 1]; ++t) tile_ids_tc.push_back((int)t);
     lv_tc_off.push_back(tco);
     lv_tc_cnt.push_back((int64_t)tile_ids_tc.size() - tco);
+    const int64_t mo = (int64_t)map_items.size() / 2;
+    for (int s : P.levels[l])
+      if (mark[s])
+        for (int q = P.pair_ptr[s]; q < P.pair_ptr[s + 1]; ++q) {
+          if (P.pair_pers[q]) continue;
+          const int d = P.pair_d[q];
+          const int m = (int)(P.sym.lpi[d + 1] - P.sym.lpi[d]) - P.pair_lb[q];
+          for (int r0 = 0; r0 < m; r0 += 256) {
+            map_items.push_back(q);
+            map_items.push_back(r0);
+          }
+        }
+    lv_map_off.push_back(mo);
+    lv_map_cnt.push_back((int64_t)map_items.size() / 2 - mo);
   }
   bool any = false;
   for (int s = 0; s < ns && !any; ++s) any = mark[s] != 0;
@@ -1046,6 +1069,14 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
                              cudaMemcpyHostToDevice, st));
   if (!tile_ids_tc.empty())
     NQG_CUDA(cudaFuncSetAttribute(k_update_t5, cudaFuncAttributeMaxDynamicSharedMemorySize, t5::smem_bytes(1)));
+  if (map_items.size() > P.map_items_cap) {
+    if (P.d_map_items) cudaFree(P.d_map_items);
+    P.map_items_cap = std::max<size_t>(map_items.size(), 128);
+    NQG_CUDA(cudaMalloc(&P.d_map_items, P.map_items_cap * sizeof(int)));
+  }
+  if (!map_items.empty())
+    NQG_CUDA(cudaMemcpyAsync(P.d_map_items, map_items.data(), map_items.size() * sizeof(int), cudaMemcpyHostToDevice,
+                             st));
   uint8_t *d_mark = P.d_pivoted + ns;  // second half of the pivoted buffer holds the marks
   NQG_CUDA(cudaMemcpyAsync(d_mark, mark.data(), ns, cudaMemcpyHostToDevice, st));
   NQG_CUDA(cudaMemsetAsync(P.d_pivoted, 0, ns, st));
@@ -1094,17 +1125,24 @@ template <class T> static int factor_impl(Plan &P, const std::vector<int> *subse
             for (int q = P.pair_ptr[s]; q < P.pair_ptr[s + 1]; ++q)
               if (!P.pair_pers[q]) fl += P.pair_flops[q];
       cudaEvent_t e0 = P.prof_begin();
+      if (lv_map_cnt[l] > 0) {
+        k_pair_rowmap<<<(unsigned)lv_map_cnt[l], 256, 0, st>>>(
+            reinterpret_cast<const int2 *>(P.d_map_items) + lv_map_off[l], P.d_pair_s, P.d_pair_d, P.d_pair_lb,
+            P.d_pair_moff, P.d_super, P.d_lpi, P.d_ls, P.d_pair_map, P.d_status);
+        P.nlaunch++;
+      }
       if (lv_tile_cnt[l] > 0) {
         k_update<T><<<(unsigned)lv_tile_cnt[l], UPD_THREADS, 0, st>>>(P.d_tiles, P.d_tile_list + lv_tile_off[l],
                                                                       (int)lv_tile_cnt[l], n, P.d_super, P.d_lpi,
-                                                                      P.d_lpx, P.d_ls, L, D, P.d_status);
+                                                                      P.d_lpx, P.d_ls, L, D, P.d_status,
+                                                                      P.d_pair_map, P.d_pair_moff, P.d_pair_lb);
         P.nlaunch++;
       }
       if constexpr (sizeof(T) == 4) {
         if (lv_tc_cnt[l] > 0) {
           k_update_t5<<<(unsigned)lv_tc_cnt[l], t5::THREADS, t5::smem_bytes(1), st>>>(
               P.d_tiles_tc, P.d_tile_list_tc + lv_tc_off[l], n, P.d_super, P.d_lpi, P.d_lpx, P.d_ls, L, D,
-              P.d_status);
+              P.d_status, P.d_pair_map, P.d_pair_moff, P.d_pair_lb);
           P.nlaunch++;
         }
       }

@@ -25,7 +25,7 @@ enum : int {
 // cols [cj, cj+TN) (positions in descendant d's row list, cols limited to
 // <= ub) of L_d D_d L_d^T, subtracted from target supernode s.
 struct UpdTile {
-  int s, d, ri, cj, ub;
+  int s, d, ri, cj, ub, q;  // q: the descendant pair
 };
 
 // One unit of row-renaming value movement: columns [c0, c0+nc) of the rows
@@ -72,6 +72,10 @@ struct Plan {
   std::vector<int> pers_ptr;        // per supernode s: range in pers_pair
   std::vector<int> pers_pair;       // pair indices
   std::vector<uint8_t> pair_pers;   // per pair: 1 if it is one of them
+  // target row positions of every pair's rows lb .. nr-1 (formed per level
+  // before its updates, read by the update tiles): offsets per pair
+  std::vector<int64_t> pair_moff;
+  int64_t map_total = 0;
   int64_t pers_map_ints = 0;        // largest rows + columns of such a pair
   std::vector<int> wide;            // supernodes factored by the blocked kernel
   int64_t ssize = 0;
@@ -138,6 +142,10 @@ struct Plan {
   void *d_wide_ctl = nullptr;       // barrier / reduction control block
   unsigned char *d_wide_pack = nullptr;  // FP32: split-TF32 operand blocks of the tcgen05 updates
   int *d_pers_map = nullptr;              // target positions of a persistent pair's rows and columns
+  int *d_pair_map = nullptr;              // target row positions of the pairs' rows (pair_moff)
+  int64_t *d_pair_moff = nullptr;
+  int *d_map_items = nullptr;             // (pair, first row) items of the per-level map kernel
+  size_t map_items_cap = 0;
   unsigned *d_solve_flags = nullptr;  // per 64-column block ready flags of the block solves
   unsigned long long *d_xw = nullptr;  // FP32 block solves: (epoch << 32) | x bits per column
   float *d_tinv = nullptr;             // FP32 block solves: inverses of the diagonal 64 x 64 tiles
