@@ -1749,6 +1749,14 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   int pivot_nb = fast_enabled ? std::min(nb, 8) : nb;
   if (const char *e = std::getenv("NASOQ_GB300_PIVOT_NB"))
     if (fast_enabled) pivot_nb = std::min(nb, std::max(2, std::atoi(e)));
+  // where pivots are dense (a fast panel stops again within nb / 4 columns)
+  // the general panels double in width, up to nb, so that fewer of them --
+  // each flushes the pending updates -- are needed; back to pivot_nb after a
+  // fast panel that stops late or not at all
+  int gen_w = pivot_nb;
+  auto after_fast = [&](bool stopped, int kept) {
+    gen_w = !stopped || kept >= nb / 4 ? pivot_nb : std::min(nb, 2 * gen_w);
+  };
   bool use_general = false;  // the next panel starts at a column that needs a pivot search
   // Delayed trailing updates (FP32 tcgen05 path): up to `depth` consecutive
   // panels are pending, their W columns side by side in Wb, and one update of
@@ -1985,17 +1993,19 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       }
       use_general = true;  // the column after the short panel needs a pivot search
       spec_limit = 1;
+      after_fast(true, kbs[i]);
     } else {
       spec_limit = std::min(SPEC_MAX, 2 * spec_limit);
+      after_fast(false, 0);
     }
     specs.clear();
     return NQG_OK;
   };
   while (cs.k0 < w) {
     // a panel on the general kernel (after a fast panel stopped at a column
-    // that needs a pivot search) is at most pivot_nb columns wide, so that the
+    // that needs a pivot search) is at most gen_w columns wide, so that the
     // fast kernel takes over again soon after the pivots
-    const int kb_want = std::min(use_general ? pivot_nb : nb, w - cs.k0);
+    const int kb_want = std::min(use_general ? gen_w : nb, w - cs.k0);
     const bool fast = fast_enabled && !use_general && nrow - cs.k0 - kb_want <= maxG_fast * FP_THREADS;
     if (fast && spec_ok) {
       int rc = pre(cs, false, kb_want);
@@ -2046,6 +2056,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     if (abort) return NQG_ERR_TIMEOUT;
     if (fast) {
       use_general = stop != 0;
+      after_fast(use_general, kb);
       if (kb <= 0) {
         if (!use_general) return NQG_ERR_TIMEOUT;
         continue;  // the first column already needs the general kernel
