@@ -876,7 +876,7 @@ void Plan::prof_end(int cls, cudaEvent_t a, double flops, double bytes) {
   }
   cudaEventRecord(e, stream);
   prof_pending.push_back(ProfRec{cls, a, e, flops, bytes});
-  if (prof_pending.size() > 8192) prof_collect();
+  if (prof_pending.size() > 8192 && !prof_hold) prof_collect();
 }
 void Plan::prof_collect() {
   if (prof_pending.empty()) return;

@@ -175,6 +175,14 @@ struct Plan {
   cudaEvent_t prof_begin();
   void prof_end(int cls, cudaEvent_t a, double flops, double bytes);
   void prof_collect();
+  // Speculative launches: records stay pending while prof_hold is set, and
+  // the work of launches that returned without running (queued behind a
+  // fast panel that stopped early) is taken back from them.
+  bool prof_hold = false;
+  size_t prof_mark() const { return prof_pending.size(); }
+  void prof_void_from(size_t i) {
+    for (size_t k = i; k < prof_pending.size(); ++k) prof_pending[k].flops = prof_pending[k].bytes = 0.0;
+  }
 
   bool factored = false;
   nqg_timings tm{};

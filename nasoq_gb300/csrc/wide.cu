@@ -1784,6 +1784,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   struct Spec {
     State st;  // state after the panel's band update, before the panel
     int kb, woff;
+    size_t prof_mark;  // measurement records after the panel's own
   };
   State cs{0, 0, 0, 0, 0, 0};
   std::vector<Spec> specs;
@@ -1984,6 +1985,8 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
     while (i < n && kbs[i] == specs[i].kb) ++i;
     if (i < n) {
       if (cudaMemsetAsync(&ctl->halt, 0, sizeof(int), st) != cudaSuccess) return NQG_ERR_CUDA;
+      // everything queued after the short panel returned without work
+      if (P) P->prof_void_from(specs[i].prof_mark);
       cs = specs[i].st;
       if (kbs[i] > 0) {
         // a short panel did not pack the rows of its diagonal block below its
@@ -1999,6 +2002,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       after_fast(false, 0);
     }
     specs.clear();
+    if (P) P->prof_hold = false;
     return NQG_OK;
   };
   while (cs.k0 < w) {
@@ -2015,7 +2019,8 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       if ((rc = launch_fast(cs.k0, kb_want, Wb + (size_t)woff * nrow, (int)specs.size(), delayed ? cs.pend_C : 0,
                             packed)))
         return rc;
-      specs.push_back(Spec{cs, kb_want, woff});
+      if (P) P->prof_hold = true;
+      specs.push_back(Spec{cs, kb_want, woff, P ? P->prof_mark() : 0});
       if ((rc = post(cs, kb_want, woff, packed))) return rc;
       if (((int)specs.size() >= spec_limit || cs.k0 >= w) && (rc = resolve())) return rc;
       continue;
