@@ -203,9 +203,11 @@ int nqg_get_launch_count(const nqg_plan *plan, long long *count);
  * cudaMalloc/cudaFree: its scratch is one fixed ~4.4 MB device array that
  * every GPU loading this library holds until the process exits, shared by
  * all calls, so calls whose GPU work overlaps (e.g. on two streams) race.
- * The first call on each device looks up that array's address and should
- * come before any stream capture.  Work runs on `stream` (NULL = default
- * stream) and the call returns when it has finished. */
+ * Every call looks up that array's device address (cudaGetSymbolAddress,
+ * which allocates nothing), so a device reset between calls is safe; the
+ * first call on each device also loads the module and should come before any
+ * stream capture.  Work runs on `stream` (NULL = default stream) and the call
+ * returns when it has finished. */
 int nqg_dense_ldlt_noalloc(int nrow, int w, double *d_A, int lda, double *d_D, int *d_perm, void *stream);
 
 /* ---- QP solve (dual active-set NASOQ over the GPU LBL) ------------------- */

@@ -3,6 +3,10 @@ CUDA kernels, the C ABI (include/nasoq_gb300.h) and the C++ drop-in classes,
 linked against the CUDA toolkit's static METIS library.
 
     python -m nasoq_gb300.build        # or nasoq_gb300.build.build()
+    python -m nasoq_gb300.build clean  # recompile every object
+
+Objects are reused when they are newer than their source and every header;
+NASOQ_GB300_REBUILD=1 (or build(clean=True)) recompiles everything.
 """
 from __future__ import annotations
 
@@ -47,9 +51,9 @@ def sources():
     return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
-def _compile(nvcc, src, flags):
+def _compile(nvcc, src, flags, clean=False):
     obj = os.path.join(OBJ, os.path.basename(src) + ".o")
-    if os.path.exists(obj) and os.path.getmtime(obj) >= max(
+    if not clean and os.path.exists(obj) and os.path.getmtime(obj) >= max(
             [os.path.getmtime(src)] + [os.path.getmtime(h) for h in glob.glob(os.path.join(CSRC, "*.h*"))]
             + [os.path.getmtime(h) for h in glob.glob(os.path.join(ROOT, "include", "**", "*.h"), recursive=True)]):
         return obj
@@ -61,7 +65,8 @@ def _compile(nvcc, src, flags):
     return obj
 
 
-def build(verbose: bool = False) -> str:
+def build(verbose: bool = False, clean: bool = False) -> str:
+    clean = clean or os.environ.get("NASOQ_GB300_REBUILD", "") not in ("", "0")
     cuda = cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(OBJ, exist_ok=True)
@@ -69,7 +74,7 @@ def build(verbose: bool = False) -> str:
                     "-I" + CSRC, "--expt-relaxed-constexpr", "-DNDEBUG"]
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda s: _compile(nvcc, s, flags), srcs))
+        objs = list(ex.map(lambda s: _compile(nvcc, s, flags, clean), srcs))
     link = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs + [metis_lib(cuda), "-cudart", "static", "-lpthread"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
@@ -80,5 +85,5 @@ def build(verbose: bool = False) -> str:
 
 
 if __name__ == "__main__":
-    build(verbose=True)
+    build(verbose=True, clean=len(sys.argv) > 1 and sys.argv[1] == "clean")
     sys.exit(0)

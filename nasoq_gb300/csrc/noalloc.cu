@@ -3,9 +3,10 @@
 //
 // All scratch lives in one file-scope device array, reserved when the
 // library is loaded on a device and kept until the process exits.  Host code
-// cannot use the array's name as a device address, so the first call on each
-// device looks the address up with cudaGetSymbolAddress (with that device
-// current) and every kernel receives pointers derived from it.
+// cannot use the array's name as a device address, so each call
+// looks the address up with cudaGetSymbolAddress (with that device
+// current) and every kernel receives pointers derived from it.  The lookup is
+// repeated on every call (see scratch_for_current_device).
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -33,24 +34,26 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
 constexpr int MAX_DEVICES = 64;
 std::mutex g_mu;
-void *g_addr[MAX_DEVICES] = {};
 int g_sms[MAX_DEVICES] = {};
 
-// Per-device set-up: device address of the scratch array and the SM count.
+// Device address of the scratch array, looked up on every call with the
+// caller's device current: a device reset or another context on the same
+// ordinal reloads the module and may move the array, so an address kept from
+// an earlier call could be stale.  The lookup allocates nothing.  The SM
+// count of each device is kept after its first call.
 int scratch_for_current_device(unsigned char **base, int *sms) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return NQG_ERR_CUDA;
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) return NQG_ERR_CUDA;
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_addr[dev]) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) return NQG_ERR_CUDA;
+  if (!g_sms[dev]) {
     int n = 0;
-    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return NQG_ERR_CUDA;
-    g_addr[dev] = p;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return NQG_ERR_CUDA;
     g_sms[dev] = n;
   }
-  *base = static_cast<unsigned char *>(g_addr[dev]);
+  *base = static_cast<unsigned char *>(p);
   *sms = g_sms[dev];
   return NQG_OK;
 }

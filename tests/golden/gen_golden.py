@@ -6,6 +6,8 @@ Run in the development container, where the reference sources live:
 
     make -C oracle && python tests/golden/gen_golden.py [/path/to/reference]
 
+(the reference path defaults to $NASOQ_REFERENCE, else /root/reference)
+
 Each fixture <case>.nqa holds the inputs (prefix ``in_``) and everything the
 reference produced (prefix ``out_``).  The reference runs single-threaded
 (OMP_NUM_THREADS=1) so its sums are in a fixed order.
@@ -157,4 +159,4 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NASOQ_REFERENCE", "/root/reference"))

@@ -82,3 +82,29 @@ def test_qp_test1json_known_answer():
     assert res.status == 1 and res.num_iter == 23
     assert rel(x, d["out_json_x"]) <= 1e-12
     assert rel(z, d["out_json_z"]) <= 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", CASES, ids=os.path.basename)
+def test_qp_fp32_factor_matches_reference(path, record_property):
+    """The mixed-precision path (FP32 factorization, FP64 flexible GMRES
+    refinement) on every QP fixture: the reference's status, KKT norms within
+    the fixture's eps_abs, and x, z within 1e-6 (relative) of the reference's
+    FP64 solution.  The active-set iteration count is recorded beside the
+    reference's; the rounding of the FP32 factor may change a decision at a
+    near-tie, so it is reported rather than required equal."""
+    d = nqa.load(path)
+    x, y, z, act, res = run(d, precision=nq.NQG_FP32)
+    ref_it = int(d["out_num_iter"][0])
+    record_property("iterations_fp32", res.num_iter)
+    record_property("iterations_reference", ref_it)
+    print(f"{os.path.basename(path)}: iterations FP32 {res.num_iter}, reference {ref_it}")
+    assert res.status == int(d["out_status"][0])
+    eps = float(d["in_eps_abs"][0])
+    assert res.cons_sat_norm <= eps and res.non_negativity_infn <= eps
+    if res.status == 1:
+        assert res.lag_res <= eps
+    assert rel(x, d["out_x"]) <= 1e-6
+    assert rel(z, d["out_z"]) <= 1e-6
+    if "out_y" in d:
+        assert rel(y, d["out_y"]) <= 1e-6

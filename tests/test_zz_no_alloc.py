@@ -6,7 +6,9 @@ the previous call's contents, so the second call must not be affected by
 them).  Same tolerance style as the other factorization parity tests: the
 two paths run the same kernels, so the factor, D and pivots must agree to
 1e-12 relative to the largest entry, and the factor's backward error must be
-below 1e-13."""
+below 1e-13.  A second test factors tall panels (rows below the diagonal
+block) of two different matrices in a row, checks them by their defining
+equations, and checks that a call leaves the device's free memory unchanged."""
 import ctypes
 
 import numpy as np
@@ -68,6 +70,52 @@ def test_noalloc_matches_plan_factor_twice():
         mag = np.abs(Lu) @ np.abs(Dm) @ np.abs(Lu).T
         assert np.abs(R).max() <= 1e-13 * mag.max()
     plan.close()
+
+
+def _check_panel(Pn, Ln, Dn, Pm, w):
+    """Pn: the nrow x w input panel (diagonal block on top), Ln/Dn/Pm: the
+    call's outputs.  P A11 P^T = L11 D L11^T and L21 = A21[:, P] L11^-T D^-1."""
+    nrow = Pn.shape[0]
+    Lu = np.tril(Ln[:w, :w], -1) + np.eye(w)
+    Dm = np.diag(Dn[:w]) + np.diag(Dn[w:2 * w - 1], -1) + np.diag(Dn[w:2 * w - 1], 1)
+    A11 = np.tril(Pn[:w, :w]) + np.tril(Pn[:w, :w], -1).T
+    Aq = A11[np.ix_(Pm, Pm)]
+    R = Aq - Lu @ Dm @ Lu.T
+    mag = np.abs(Lu) @ np.abs(Dm) @ np.abs(Lu).T
+    assert np.abs(R).max() <= 1e-13 * mag.max()
+    if nrow > w:
+        A21 = Pn[w:, :][:, Pm]
+        L21 = Ln[w:, :]
+        # L21 D L11^T must reproduce the permuted rows below
+        R2 = A21 - L21 @ Dm @ Lu.T
+        mag2 = np.abs(L21) @ np.abs(Dm) @ np.abs(Lu).T
+        assert np.abs(R2).max() <= 1e-12 * max(mag2.max(), np.abs(A21).max())
+
+
+@pytest.mark.gpu
+def test_noalloc_tall_panels_differ_and_allocate_nothing():
+    torch = pytest.importorskip("torch")
+    L = nq.lib()
+    L.nqg_dense_ldlt_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p]
+    nrow, w = 300, 200
+    for call, seed in enumerate((21, 22)):  # two different matrices in a row
+        K = _dense_sym(nrow, seed)
+        Pn = K[:, :w].copy()  # w x w symmetric block on top of nrow - w rows
+        dA = torch.from_numpy(np.ascontiguousarray(Pn.T)).cuda()
+        dD = torch.full((2 * w,), 7.0, dtype=torch.float64, device="cuda")
+        dP = torch.full((w,), -1, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        rc = L.nqg_dense_ldlt_noalloc(nrow, w, dA.data_ptr(), nrow, dD.data_ptr(), dP.data_ptr(), None)
+        torch.cuda.synchronize()
+        free1 = torch.cuda.mem_get_info()[0]
+        assert rc == 0, f"call {call}: status {rc}"
+        if call > 0:  # the first call on the device may load the module
+            assert free1 == free0, f"call {call}: free device memory changed by {free0 - free1} bytes"
+        Pm = dP.cpu().numpy()
+        assert sorted(Pm.tolist()) == list(range(w))
+        _check_panel(Pn, dA.cpu().numpy().T, dD.cpu().numpy(), Pm, w)
 
 
 @pytest.mark.gpu
