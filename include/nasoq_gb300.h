@@ -245,6 +245,70 @@ int nqg_qp_solve(int n, const int *Hp, const int *Hi, const double *Hx, const do
                  const double *z0, const double *y0, int n_as, const int *as0, double *x, double *y, double *z,
                  int *active_set, nqg_qp_result *result);
 
+/* ---- batched QP solve ------------------------------------------------------
+ * Many small QPs (min 1/2 x'Hx + q'x  s.t.  Ax = a, Bx <= b) solved together
+ * on the GPU by the reference's dual active-set method (Nasoq::solve,
+ * src/nasoq.cpp:656-710, with numeric_QP :478-610): one CTA of a persistent
+ * kernel runs one problem's whole active-set iteration -- partial
+ * refactorizations, masked solves, refinement, step lengths and active-set
+ * edits -- on the device, with no host round trip per iteration.  Problems
+ * are grouped by sparsity pattern; each pattern gets one symbolic analysis
+ * (the reference's ordering and supernodes).  The reference has no working
+ * batch path (its numeric_QP_batch, src/nasoq.cpp:1540, is unfinished); per
+ * problem the semantics are those of nqg_qp_solve. */
+typedef struct nqg_batch nqg_batch;
+
+typedef struct nqg_batch_settings {
+  nqg_qp_settings qp;   /* variant (Fixed, AUTO or PREDET), eps_abs, ...; qp.precision: NQG_FP64 or NQG_FP32
+                           factorization and triangular solves (FP64 refinement either way) */
+  int refine;           /* 0: the reference's GMRES schedule (restarts x steps from the variant);
+                           1: adaptive flexible GMRES to refine_tol */
+  double refine_tol;    /* refine == 1: stop once ||b - Kx||_2 <= refine_tol * ||b||_2 */
+  int threads;          /* CTA size, a multiple of 32 up to 256 (0: 128) */
+  int use_graph;        /* 1: the queue reset and the kernel are replayed from a captured CUDA graph */
+} nqg_batch_settings;
+
+typedef struct nqg_batch_stats {
+  int status, num_iter, active_size, flags;  /* flags: NQG_WARN_* bits of the device status */
+  int refine_steps, solves, warm_dropped, pad;  /* Krylov steps, KKT solves, warm-start rows dropped */
+  double objective, lag_res, cons_sat_norm, non_negativity_infn, complementarity_infn;
+} nqg_batch_stats;
+
+typedef struct nqg_batch_info {
+  int nprob, npatterns, grid, threads, blocks_per_sm, pad;
+  int64_t smem_bytes, slot_bytes;
+  double last_ms;       /* device time of the last nqg_batch_solve */
+} nqg_batch_info;
+
+/* Defaults: the reference's Nasoq defaults with eps_abs = 1e-8, FP64, the
+ * reference's refinement schedule, CUDA graph on. */
+void nqg_batch_default_settings(nqg_batch_settings *s);
+int nqg_batch_create(const nqg_batch_settings *s, nqg_batch **out);
+/* Adds one QP (same arrays as nqg_qp_solve); returns its index (>= 0). */
+int nqg_batch_add(nqg_batch *b, int n, const int *Hp, const int *Hi, const double *Hx, const double *q, int meq,
+                  const int *Ap, const int *Ai, const double *Ax, const double *a, int mineq, const int *Bp,
+                  const int *Bi, const double *Bx, const double *bineq);
+/* Groups by pattern, analyses each pattern, uploads; no problem can be added afterwards. */
+int nqg_batch_finalize(nqg_batch *b);
+/* New q / a / b of every problem, concatenated in problem order (NULL: unchanged). */
+int nqg_batch_set_vectors(nqg_batch *b, const double *q_all, const double *a_all, const double *b_all);
+/* Proposed active set of problem i for the next solve (n_as < 0: cold start).
+ * The solve factors the KKT system with these constraints active, drops the
+ * ones whose multipliers come out negative (up to three rounds, then a cold
+ * start), and continues the active-set iteration from there (the role of the
+ * reference's set_warm_start, src/nasoq.cpp:413-436). */
+int nqg_batch_set_warm_start(nqg_batch *b, int i, int n_as, const int *as);
+/* Solves every problem; returns when done. */
+int nqg_batch_solve(nqg_batch *b);
+/* Enqueues the solve on the batch's stream (nqg_batch_get_stream) and returns. */
+int nqg_batch_solve_async(nqg_batch *b);
+int nqg_batch_get(nqg_batch *b, int i, double *x, double *y, double *z, int *active_set, nqg_qp_result *res);
+int nqg_batch_get_all(nqg_batch *b, double *x_all, double *y_all, double *z_all, nqg_batch_stats *stats);
+int nqg_batch_get_info(const nqg_batch *b, nqg_batch_info *info);
+int nqg_batch_get_stream(const nqg_batch *b, void **stream);
+const char *nqg_batch_last_error(const nqg_batch *b);
+int nqg_batch_destroy(nqg_batch *b);
+
 #ifdef __cplusplus
 }
 #endif

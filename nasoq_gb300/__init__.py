@@ -67,6 +67,24 @@ class QPResult(C.Structure):
                 ("factor_seconds", C.c_double)]
 
 
+class BatchSettings(C.Structure):
+    _fields_ = [("qp", QPSettings), ("refine", C.c_int), ("refine_tol", C.c_double), ("threads", C.c_int),
+                ("use_graph", C.c_int)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("status", C.c_int), ("num_iter", C.c_int), ("active_size", C.c_int), ("flags", C.c_int),
+                ("refine_steps", C.c_int), ("solves", C.c_int), ("warm_dropped", C.c_int), ("pad", C.c_int),
+                ("objective", C.c_double), ("lag_res", C.c_double), ("cons_sat_norm", C.c_double),
+                ("non_negativity_infn", C.c_double), ("complementarity_infn", C.c_double)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("nprob", C.c_int), ("npatterns", C.c_int), ("grid", C.c_int), ("threads", C.c_int),
+                ("blocks_per_sm", C.c_int), ("pad", C.c_int), ("smem_bytes", C.c_int64), ("slot_bytes", C.c_int64),
+                ("last_ms", C.c_double)]
+
+
 _lib = None
 
 
@@ -113,6 +131,24 @@ def lib():
     L.nqg_qp_solve.argtypes = [C.c_int] + [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 4 + [C.c_int] + \
         [C.c_void_p] * 4 + [C.POINTER(QPSettings), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(QPResult)]
+    L.nqg_batch_default_settings.argtypes = [C.POINTER(BatchSettings)]
+    L.nqg_batch_default_settings.restype = None
+    L.nqg_batch_create.argtypes = [C.POINTER(BatchSettings), C.POINTER(C.c_void_p)]
+    L.nqg_batch_add.argtypes = [C.c_int] * 0 + [C.c_void_p, C.c_int] + [C.c_void_p] * 4 + [C.c_int] + \
+        [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 4
+    L.nqg_batch_finalize.argtypes = [C.c_void_p]
+    L.nqg_batch_set_vectors.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.nqg_batch_set_warm_start.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+    L.nqg_batch_solve.argtypes = [C.c_void_p]
+    L.nqg_batch_solve_async.argtypes = [C.c_void_p]
+    L.nqg_batch_get.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                C.POINTER(QPResult)]
+    L.nqg_batch_get_all.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.nqg_batch_get_info.argtypes = [C.c_void_p, C.POINTER(BatchInfo)]
+    L.nqg_batch_get_stream.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+    L.nqg_batch_last_error.argtypes = [C.c_void_p]
+    L.nqg_batch_last_error.restype = C.c_char_p
+    L.nqg_batch_destroy.argtypes = [C.c_void_p]
     _lib = L
     return L
 
@@ -332,3 +368,115 @@ def qp_solve(H, q, A, b, Cm, d, settings: QPSettings | None = None, warm=None):
                         nas, _ptr(as0), _ptr(x), _ptr(y), _ptr(z), _ptr(act), C.byref(res))
     _check(rc, "qp solve")
     return x, y[:meq], z[:mineq], act[:res.active_size].copy(), res
+
+
+def batch_settings(**kw) -> BatchSettings:
+    """Batch settings; QP keys (variant, eps_abs, diag_perturb, stop_tol,
+    max_iter, max_iter_nas, precision) go to the embedded QP settings."""
+    s = BatchSettings()
+    lib().nqg_batch_default_settings(C.byref(s))
+    qp_keys = {f for f, _ in QPSettings._fields_}
+    for k, v in kw.items():
+        if k == "variant" and isinstance(v, str):
+            v = VARIANTS[v.lower()]
+        if k in qp_keys:
+            setattr(s.qp, k, v)
+        else:
+            setattr(s, k, v)
+    return s
+
+
+class QPBatch:
+    """Many QPs solved together on the GPU (nqg_batch_*): each problem runs
+    the NASOQ active-set iteration to the end inside one CTA of a persistent
+    kernel.  Problems are given as (H, q, A, b, Cm, d) with CSC objects (H
+    lower-stored), the same as qp_solve."""
+
+    def __init__(self, problems, settings: BatchSettings | None = None, **kw):
+        L = lib()
+        self.settings = settings if settings is not None else batch_settings(**kw)
+        h = C.c_void_p()
+        _check(L.nqg_batch_create(C.byref(self.settings), C.byref(h)), "batch create")
+        self._h = h
+        self.sizes = []
+        arr = lambda a, t: np.ascontiguousarray(a, t)
+        for (H, q, A, b, Cm, d) in problems:
+            n, meq, mineq = int(H.ncol), int(A.nrow), int(Cm.nrow)
+            keep = [arr(H.p, np.int32), arr(H.i, np.int32), arr(H.x, np.float64), arr(q, np.float64),
+                    arr(A.p, np.int32), arr(A.i, np.int32), arr(A.x, np.float64), arr(b, np.float64),
+                    arr(Cm.p, np.int32), arr(Cm.i, np.int32), arr(Cm.x, np.float64), arr(d, np.float64)]
+            rc = L.nqg_batch_add(h, n, *[_ptr(a) for a in keep[:4]], meq, *[_ptr(a) for a in keep[4:8]], mineq,
+                                 *[_ptr(a) for a in keep[8:]])
+            self._raise(rc, "batch add")
+            self.sizes.append((n, meq, mineq))
+        self._raise(L.nqg_batch_finalize(h), "batch finalize")
+        self.n_tot = sum(s[0] for s in self.sizes)
+        self.meq_tot = sum(s[1] for s in self.sizes)
+        self.mineq_tot = sum(s[2] for s in self.sizes)
+
+    def _raise(self, rc, what):
+        if rc < 0:
+            msg = lib().nqg_batch_last_error(self._h).decode()
+            raise NasoqError(f"{what}: {lib().nqg_status_str(rc).decode()} ({rc}) {msg}")
+        return rc
+
+    def __len__(self):
+        return len(self.sizes)
+
+    def set_vectors(self, q_all=None, b_all=None, d_all=None):
+        """New q / b / d of every problem, concatenated in problem order."""
+        conv = lambda a: None if a is None else np.ascontiguousarray(a, np.float64)
+        q_all, b_all, d_all = conv(q_all), conv(b_all), conv(d_all)
+        self._raise(lib().nqg_batch_set_vectors(self._h, _ptr(q_all), _ptr(b_all), _ptr(d_all)), "set vectors")
+
+    def set_warm_start(self, i, active_set):
+        """Proposed active set of problem i (None: cold start)."""
+        if active_set is None:
+            self._raise(lib().nqg_batch_set_warm_start(self._h, int(i), -1, None), "warm start")
+            return
+        a = np.ascontiguousarray(active_set, np.int32)
+        self._raise(lib().nqg_batch_set_warm_start(self._h, int(i), len(a), _ptr(a)), "warm start")
+
+    def solve(self):
+        self._raise(lib().nqg_batch_solve(self._h), "batch solve")
+
+    def solve_async(self):
+        self._raise(lib().nqg_batch_solve_async(self._h), "batch solve")
+
+    def stream(self):
+        v = C.c_void_p()
+        self._raise(lib().nqg_batch_get_stream(self._h, C.byref(v)), "stream")
+        return v.value
+
+    def result(self, i):
+        n, meq, mineq = self.sizes[i]
+        x = np.zeros(n)
+        y = np.zeros(max(meq, 1))
+        z = np.zeros(max(mineq, 1))
+        act = np.zeros(max(mineq, 1), np.int32)
+        res = QPResult()
+        self._raise(lib().nqg_batch_get(self._h, int(i), _ptr(x), _ptr(y), _ptr(z), _ptr(act), C.byref(res)),
+                    "batch get")
+        return x, y[:meq], z[:mineq], act[:res.active_size].copy(), res
+
+    def results(self):
+        """(x_all, y_all, z_all, stats) for every problem, concatenated."""
+        x = np.zeros(max(self.n_tot, 1))
+        y = np.zeros(max(self.meq_tot, 1))
+        z = np.zeros(max(self.mineq_tot, 1))
+        st = (BatchStats * len(self.sizes))()
+        self._raise(lib().nqg_batch_get_all(self._h, _ptr(x), _ptr(y), _ptr(z), C.cast(st, C.c_void_p)), "get all")
+        return x[:self.n_tot], y[:self.meq_tot], z[:self.mineq_tot], st
+
+    def info(self) -> BatchInfo:
+        i = BatchInfo()
+        lib().nqg_batch_get_info(self._h, C.byref(i))
+        return i
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().nqg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

@@ -1,0 +1,1062 @@
+// Batched NASOQ: thousands of small QPs of uneven size, each solved to the
+// end by one CTA of a persistent kernel -- the dual active-set iteration
+// (reference Nasoq::numeric_QP, src/nasoq.cpp:478-610), its SoMod partial
+// refactorizations (update_ldl_left_sn_02_v2, src/ldl/Serial_update_ldl.cpp:
+// 18-277), masked supernodal solves and GMRES refinement all run on the
+// device; the host only fills the work queue.
+//
+// Per problem, in the CTA's scratch slot:
+//  * the supernodal factor in the reference's BCSC layout (column-major
+//    nrow x w blocks, D as diagonal + 2x2 sub-diagonal halves), the composed
+//    ordering perm/iperm and the row lists, renamed after Bunch-Kaufman
+//    pivoting as the reference's row_reordering does (without re-sorting the
+//    renamed rows: every consumer maps them through the target's row list);
+//  * the active set as a per-constraint flag.  Hidden (inactive) constraint
+//    columns are width-1 supernodes whose entries read as zero; the
+//    reference's hidden-column tree edits (linear_solver_wrapper.cpp:770-907)
+//    become a visibility test per supernode, and the supernodes to refactor
+//    after an edit are those on the elimination-tree paths from the edited
+//    column and its variables to the root;
+//  * the KKT vectors in the original numbering; the triangular solves gather
+//    them into shared memory in the factor's order.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+
+#include "batch.hpp"
+#include "bk.cuh"
+
+namespace nqg {
+
+namespace {
+
+constexpr int BT_MAX_THREADS = 256;
+constexpr int MR_CAP = BATCH_MR_CAP;  // Krylov steps per restart held in shared memory
+
+template <class T> struct Ctx {
+  // pattern
+  int n, meq, mineq, N, base, ns, nlev;
+  const int *super, *sparent, *col2sup, *lpi, *lpx, *lvl_ptr, *lvl_sn, *pair_ptr, *pair_d, *pair_lb, *pair_ub;
+  const int *Rp, *Rj, *Rq, *ent, *bt_ptr, *bt_var, *bt_q, *sn_con, *con_sn, *eq_ptr, *eq_var, *eq_q;
+  // problem
+  const double *kv, *q, *bq, *dq;
+  const uint8_t *pert;
+  double reg;
+  // slot
+  T *L, *D;
+  int *ls, *perm, *iperm, *lperm, *alist;
+  uint8_t *mark, *piv, *act;
+  double *rhs, *sol, *r, *w, *V, *tmp;
+  T *Z;
+  // shared memory
+  int *map;
+  T *xs, *B, *rowbuf, *Dsm, *Esm;
+  int *lp;
+  double *red;   // 32 doubles
+  int *redi;     // 32 ints
+  int *status;   // device status bits of this problem
+};
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+__device__ __forceinline__ int warp_id() { return threadIdx.x >> 5; }
+__device__ __forceinline__ int num_warps() { return blockDim.x >> 5; }
+
+template <class T> __device__ __forceinline__ bool visible(const Ctx<T> &c, int s) {
+  const int k = c.sn_con[s];
+  return k < 0 || c.act[k];
+}
+
+// Block-wide sum in a fixed order (per-thread strided partials, then a tree):
+// the same inputs give the same bits on every run.
+__device__ double block_sum(double v, double *red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane_id() == 0) red[warp_id()] = v;
+  __syncthreads();
+  if (warp_id() == 0) {
+    v = lane_id() < num_warps() ? red[lane_id()] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane_id() == 0) red[0] = v;
+  }
+  __syncthreads();
+  v = red[0];
+  __syncthreads();
+  return v;
+}
+
+__device__ int block_sum_int(int v, int *redi) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if (lane_id() == 0) redi[warp_id()] = v;
+  __syncthreads();
+  if (warp_id() == 0) {
+    v = lane_id() < num_warps() ? redi[lane_id()] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane_id() == 0) redi[0] = v;
+  }
+  __syncthreads();
+  v = redi[0];
+  __syncthreads();
+  return v;
+}
+
+// Block-wide selection: the largest (sel_max) or smallest value, the
+// smallest index winning ties -- the outcome of the reference's ascending
+// scans with strict comparisons.  idx < 0 marks "no candidate".
+__device__ void block_select(double &v, int &idx, bool sel_max, double *red, int *redi) {
+  auto better = [&](double ov, int oi, double cv, int ci) {
+    if (oi < 0) return false;
+    if (ci < 0) return true;
+    if (ov == cv) return oi < ci;
+    return sel_max ? ov > cv : ov < cv;
+  };
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double ov = __shfl_down_sync(0xffffffffu, v, o);
+    int oi = __shfl_down_sync(0xffffffffu, idx, o);
+    if (better(ov, oi, v, idx)) {
+      v = ov;
+      idx = oi;
+    }
+  }
+  __syncthreads();
+  if (lane_id() == 0) {
+    red[warp_id()] = v;
+    redi[warp_id()] = idx;
+  }
+  __syncthreads();
+  if (warp_id() == 0) {
+    v = lane_id() < num_warps() ? red[lane_id()] : 0.0;
+    idx = lane_id() < num_warps() ? redi[lane_id()] : -1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      double ov = __shfl_down_sync(0xffffffffu, v, o);
+      int oi = __shfl_down_sync(0xffffffffu, idx, o);
+      if (better(ov, oi, v, idx)) {
+        v = ov;
+        idx = oi;
+      }
+    }
+    if (lane_id() == 0) {
+      red[0] = v;
+      redi[0] = idx;
+    }
+  }
+  __syncthreads();
+  v = red[0];
+  idx = redi[0];
+  __syncthreads();
+}
+
+// ---- values ---------------------------------------------------------------
+// Factorization value of lower-CSC entry vq: inactive constraint entries read
+// as zero (the reference zeroes them in its ordered matrix), perturbed
+// diagonals as the regularization (find_perturbation,
+// linear_solver_wrapper.cpp:352-363).
+template <class T> __device__ __forceinline__ double fact_val(const Ctx<T> &c, int vq) {
+  const int e = c.ent[vq];
+  double v = c.kv[vq];
+  if (e >= 0) return c.act[e] ? v : 0.0;
+  if (e <= -2 && c.pert[-2 - e]) return c.reg;
+  return v;
+}
+// Refinement value: perturbed diagonals read as zero (set_diags(0),
+// linear_solver_wrapper.cpp:1359-1394).
+template <class T> __device__ __forceinline__ double ref_val(const Ctx<T> &c, int vq) {
+  const int e = c.ent[vq];
+  double v = c.kv[vq];
+  if (e >= 0) return c.act[e] ? v : 0.0;
+  if (e <= -2 && c.pert[-2 - e]) return 0.0;
+  return v;
+}
+
+// ---- factorization of one supernode (CTA scope) ------------------------------
+// Left-looking step of the reference (Serial_update_ldl.cpp:62-190): scatter
+// the matrix columns, subtract every visible descendant's L D L^T restricted
+// to the supernode, Bunch-Kaufman on the diagonal block, permute / solve /
+// scale the rows below.
+template <class T> __device__ void factor_sn(Ctx<T> &c, int s) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int c0 = c.super[s], w = c.super[s + 1] - c0;
+  const int nr = c.lpi[s + 1] - c.lpi[s];
+  const int *rows = c.ls + c.lpi[s];
+  T *B = c.B;
+  for (int p = tid; p < nr; p += nt) c.map[rows[p]] = p;
+  for (int e = tid; e < nr * w; e += nt) B[e] = T(0);
+  __syncthreads();
+  // matrix columns (symmetric neighbours j of the original column, ordered >= the column)
+  for (int m = 0; m < w; ++m) {
+    const int col = c0 + m;
+    const int j = c.perm[col];
+    for (int qq = c.Rp[j] + tid; qq < c.Rp[j + 1]; qq += nt) {
+      const int oi = c.iperm[c.Rj[qq]];
+      if (oi < col) continue;
+      const int pos = c.map[oi];
+      if (pos < 0 || pos >= nr || rows[pos] != oi) {  // not in the row list: corrupted structure
+        atomicOr(c.status, ST_BOUNDS);
+        continue;
+      }
+      B[pos + m * nr] = T(fact_val(c, c.Rq[qq]));
+    }
+  }
+  __syncthreads();
+  // descendant updates, one pair at a time (distinct targets inside a pair)
+  for (int pq = c.pair_ptr[s]; pq < c.pair_ptr[s + 1]; ++pq) {
+    const int d = c.pair_d[pq];
+    if (!visible(c, d)) continue;
+    const int lb = c.pair_lb[pq], ub = c.pair_ub[pq];
+    const int cd = c.super[d], wd = c.super[d + 1] - cd;
+    const int nrd = c.lpi[d + 1] - c.lpi[d];
+    const int *rd = c.ls + c.lpi[d];
+    const T *Ld = c.L + c.lpx[d];
+    const T *Dd = c.D + cd, *Ed = c.D + c.N + cd;
+    const int m = nrd - lb, nc = ub - lb + 1;
+    for (int e = tid; e < m * nc; e += nt) {
+      const int i = e % m, jj = e / m;
+      const int ri = rd[lb + i];
+      const int ti = c.map[ri];
+      const int tj = rd[lb + jj] - c0;
+      if (ti < 0 || ti >= nr || rows[ti] != ri || tj < 0 || tj >= w) {
+        atomicOr(c.status, ST_BOUNDS);
+        continue;
+      }
+      if (ti < tj) continue;  // lower triangle of the target only
+      double acc = 0.0;
+      for (int k = 0; k < wd; ++k) {
+        const double lik = (double)Ld[lb + i + (size_t)k * nrd];
+        const double ek = (double)Ed[k];
+        if (ek == 0.0 || k + 1 >= wd) {
+          acc += lik * (double)Dd[k] * (double)Ld[lb + jj + (size_t)k * nrd];
+        } else {
+          // 2x2 block (k, k+1): (D L^T)_k,j = d1 L_jk + e L_j,k+1; (D L^T)_k+1,j = e L_jk + d2 L_j,k+1
+          const double ljk = (double)Ld[lb + jj + (size_t)k * nrd], ljk1 = (double)Ld[lb + jj + (size_t)(k + 1) * nrd];
+          const double lik1 = (double)Ld[lb + i + (size_t)(k + 1) * nrd];
+          acc += lik * ((double)Dd[k] * ljk + ek * ljk1) + lik1 * (ek * ljk + (double)Dd[k + 1] * ljk1);
+          ++k;
+        }
+      }
+      B[ti + tj * nr] -= T(acc);
+    }
+    __syncthreads();
+  }
+  // Bunch-Kaufman on the diagonal block, then the rows below
+  bool pivoted = false;
+  bk_factor<T>(B, nr, w, c.Dsm, c.Esm, c.lp, c.status, &pivoted);
+  __syncthreads();
+  if (nr > w) panel_solve_rows<T>(B, nr, w, B, nr, c.Dsm, c.Esm, c.lp, c.rowbuf, blockDim.x, pivoted);
+  __syncthreads();
+  T *Ls = c.L + c.lpx[s];
+  for (int e = tid; e < nr * w; e += nt) {
+    T v = B[e];
+    if (!(v == v) || isinf((double)v)) atomicOr(c.status, ST_NONFINITE);
+    Ls[e] = v;
+  }
+  for (int m = tid; m < w; m += nt) {
+    c.D[c0 + m] = c.Dsm[m];
+    c.D[c.N + c0 + m] = c.Esm[m];
+    c.lperm[c0 + m] = c.lp[m];
+  }
+  if (tid == 0) c.piv[s] = pivoted ? 1 : 0;
+  __syncthreads();
+}
+
+// Factor every marked supernode (leaves first), then fold the pivots into the
+// row lists of the descendants (row_reordering, Sym_BLAS.cpp:327-490) and
+// into the ordering (reorder_matrix, linear_solver_wrapper.cpp:1432-1460).
+template <class T> __device__ void factor_marked(Ctx<T> &c) {
+  for (int l = 0; l < c.nlev; ++l)
+    for (int q = c.lvl_ptr[l]; q < c.lvl_ptr[l + 1]; ++q) {
+      const int s = c.lvl_sn[q];
+      if (c.mark[s]) factor_sn(c, s);
+    }
+  // renaming: rows of descendants that fall into a pivoted supernode
+  for (int s = 0; s < c.ns; ++s) {
+    if (!c.mark[s] || !c.piv[s]) continue;
+    const int c0 = c.super[s], w = c.super[s + 1] - c0;
+    // inverse of the local pivot order: old local position -> new position
+    for (int m = threadIdx.x; m < w; m += blockDim.x) c.lp[c.lperm[c0 + m]] = m;
+    __syncthreads();
+    for (int pq = c.pair_ptr[s]; pq < c.pair_ptr[s + 1]; ++pq) {
+      const int d = c.pair_d[pq];
+      int *rd = c.ls + c.lpi[d];
+      const int lb = c.pair_lb[pq], ub = c.pair_ub[pq];
+      for (int i = lb + threadIdx.x; i <= ub; i += blockDim.x) {
+        const int o = rd[i] - c0;
+        if (o >= 0 && o < w) rd[i] = c0 + c.lp[o];
+        else atomicOr(c.status, ST_BOUNDS);
+      }
+    }
+    // composed ordering: new position m holds the column that was at lperm[m]
+    // (old values staged in the free row map)
+    for (int m = threadIdx.x; m < w; m += blockDim.x) c.map[m] = c.perm[c0 + c.lperm[c0 + m]];
+    __syncthreads();
+    for (int m = threadIdx.x; m < w; m += blockDim.x) c.perm[c0 + m] = c.map[m];
+    __syncthreads();
+    for (int m = threadIdx.x; m < w; m += blockDim.x) c.iperm[c.perm[c0 + m]] = c0 + m;
+    __syncthreads();
+  }
+  for (int s = threadIdx.x; s < c.ns; s += blockDim.x) c.mark[s] = 0;
+  __syncthreads();
+}
+
+// ---- triangular solves (factor order, vector in shared memory) ---------------
+// Forward: per level, every visible supernode pulls the products of its
+// visible descendants' rows that fall into it, then solves its unit lower
+// diagonal block (the reference pushes the same products with atomics,
+// Triangular_BCSC.cpp:378-446).  Wide levels: a thread per supernode, narrow
+// levels: a warp per supernode.
+template <class T> __device__ void fwd_thread(Ctx<T> &c, int s) {
+  T *x = c.xs;
+  const int c0 = c.super[s], w = c.super[s + 1] - c0, nr = c.lpi[s + 1] - c.lpi[s];
+  for (int pq = c.pair_ptr[s]; pq < c.pair_ptr[s + 1]; ++pq) {
+    const int d = c.pair_d[pq];
+    if (!visible(c, d)) continue;
+    const int lb = c.pair_lb[pq], ub = c.pair_ub[pq];
+    const int cd = c.super[d], wd = c.super[d + 1] - cd, nrd = c.lpi[d + 1] - c.lpi[d];
+    const int *rd = c.ls + c.lpi[d];
+    const T *Ld = c.L + c.lpx[d];
+    for (int i = lb; i <= ub; ++i) {
+      T acc = T(0);
+      for (int k = 0; k < wd; ++k) acc += Ld[i + (size_t)k * nrd] * x[cd + k];
+      const int r = rd[i];
+      if (r >= c0 && r < c0 + w) x[r] -= acc;
+    }
+  }
+  const T *Ls = c.L + c.lpx[s];
+  for (int j = 0; j < w - 1; ++j) {
+    const T xj = x[c0 + j];
+    for (int i = j + 1; i < w; ++i) x[c0 + i] -= Ls[i + (size_t)j * nr] * xj;
+  }
+}
+
+template <class T> __device__ void fwd_warp(Ctx<T> &c, int s) {
+  T *x = c.xs;
+  const int lane = lane_id();
+  const int c0 = c.super[s], w = c.super[s + 1] - c0, nr = c.lpi[s + 1] - c.lpi[s];
+  for (int pq = c.pair_ptr[s]; pq < c.pair_ptr[s + 1]; ++pq) {
+    const int d = c.pair_d[pq];
+    if (!visible(c, d)) continue;
+    const int lb = c.pair_lb[pq], ub = c.pair_ub[pq];
+    const int cd = c.super[d], wd = c.super[d + 1] - cd, nrd = c.lpi[d + 1] - c.lpi[d];
+    const int *rd = c.ls + c.lpi[d];
+    const T *Ld = c.L + c.lpx[d];
+    for (int i = lb + lane; i <= ub; i += 32) {
+      T acc = T(0);
+      for (int k = 0; k < wd; ++k) acc += Ld[i + (size_t)k * nrd] * x[cd + k];
+      const int r = rd[i];
+      if (r >= c0 && r < c0 + w) x[r] -= acc;
+    }
+    __syncwarp();
+  }
+  const T *Ls = c.L + c.lpx[s];
+  for (int j = 0; j < w - 1; ++j) {
+    const T xj = x[c0 + j];
+    __syncwarp();
+    for (int i = j + 1 + lane; i < w; i += 32) x[c0 + i] -= Ls[i + (size_t)j * nr] * xj;
+    __syncwarp();
+  }
+}
+
+// Backward (Triangular_BCSC.cpp:534-600): x1 -= L21^T x(rows below), then the
+// transposed unit triangle.
+template <class T> __device__ void bwd_thread(Ctx<T> &c, int s) {
+  T *x = c.xs;
+  const int c0 = c.super[s], w = c.super[s + 1] - c0, nr = c.lpi[s + 1] - c.lpi[s];
+  const int *rows = c.ls + c.lpi[s];
+  const T *Ls = c.L + c.lpx[s];
+  for (int j = 0; j < w; ++j) {
+    T acc = T(0);
+    for (int r = w; r < nr; ++r) {
+      const int rr = rows[r];
+      if ((unsigned)rr < (unsigned)c.N) acc += Ls[r + (size_t)j * nr] * x[rr];
+    }
+    x[c0 + j] -= acc;
+  }
+  for (int i = w - 1; i > 0; --i) {
+    const T xi = x[c0 + i];
+    for (int j = 0; j < i; ++j) x[c0 + j] -= Ls[i + (size_t)j * nr] * xi;
+  }
+}
+
+template <class T> __device__ void bwd_warp(Ctx<T> &c, int s) {
+  T *x = c.xs;
+  const int lane = lane_id();
+  const int c0 = c.super[s], w = c.super[s + 1] - c0, nr = c.lpi[s + 1] - c.lpi[s];
+  const int *rows = c.ls + c.lpi[s];
+  const T *Ls = c.L + c.lpx[s];
+  for (int j = 0; j < w; ++j) {
+    T acc = T(0);
+    for (int r = w + lane; r < nr; r += 32) {
+      const int rr = rows[r];
+      if ((unsigned)rr < (unsigned)c.N) acc += Ls[r + (size_t)j * nr] * x[rr];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) x[c0 + j] -= acc;
+  }
+  __syncwarp();
+  for (int i = w - 1; i > 0; --i) {
+    const T xi = x[c0 + i];
+    __syncwarp();
+    for (int j = lane; j < i; j += 32) x[c0 + j] -= Ls[i + (size_t)j * nr] * xi;
+    __syncwarp();
+  }
+}
+
+// x <- (L D L^T)^-1 x on the visible part, in the factor's order.
+template <class T> __device__ void ldlt_solve_smem(Ctx<T> &c) {
+  const int nw = num_warps();
+  for (int l = 0; l < c.nlev; ++l) {
+    const int a = c.lvl_ptr[l], b = c.lvl_ptr[l + 1];
+    if (b - a > 2 * nw) {
+      for (int q = a + threadIdx.x; q < b; q += blockDim.x) {
+        const int s = c.lvl_sn[q];
+        if (visible(c, s)) fwd_thread(c, s);
+      }
+    } else {
+      for (int q = a + warp_id(); q < b; q += nw) {
+        const int s = c.lvl_sn[q];
+        if (visible(c, s)) fwd_warp(c, s);
+      }
+    }
+    __syncthreads();
+  }
+  // D solve: 1x1 by division, 2x2 by Cramer's rule (blocked_2by2_solver, Sym_BLAS.cpp:492-529)
+  for (int i = threadIdx.x; i < c.N; i += blockDim.x) {
+    if (!visible(c, c.col2sup[i])) continue;
+    if (i > 0 && c.D[c.N + i - 1] != T(0)) continue;  // second column of a 2x2 block
+    const T e = i + 1 < c.N ? c.D[c.N + i] : T(0);
+    if (e == T(0)) {
+      c.xs[i] = c.xs[i] / c.D[i];
+    } else {
+      const T d1 = c.D[i], d2 = c.D[i + 1];
+      const T inv = T(1) / (d1 * d2 - e * e);
+      const T x1 = c.xs[i], x2 = c.xs[i + 1];
+      c.xs[i] = (x1 * d2 - x2 * e) * inv;
+      c.xs[i + 1] = (x2 * d1 - x1 * e) * inv;
+    }
+  }
+  __syncthreads();
+  for (int l = c.nlev - 1; l >= 0; --l) {
+    const int a = c.lvl_ptr[l], b = c.lvl_ptr[l + 1];
+    if (b - a > 2 * nw) {
+      for (int q = a + threadIdx.x; q < b; q += blockDim.x) {
+        const int s = c.lvl_sn[q];
+        if (visible(c, s)) bwd_thread(c, s);
+      }
+    } else {
+      for (int q = a + warp_id(); q < b; q += nw) {
+        const int s = c.lvl_sn[q];
+        if (visible(c, s)) bwd_warp(c, s);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// out = M^-1 v (original numbering; hidden rows give zero).  Vectors in
+// global memory, the solve in shared memory.
+template <class T, class VI, class VO> __device__ void precond(Ctx<T> &c, const VI *v, VO *out) {
+  for (int i = threadIdx.x; i < c.N; i += blockDim.x) c.xs[i] = visible(c, c.col2sup[i]) ? T(v[c.perm[i]]) : T(0);
+  __syncthreads();
+  ldlt_solve_smem(c);
+  for (int i = threadIdx.x; i < c.N; i += blockDim.x) out[c.perm[i]] = VO(c.xs[i]);
+  __syncthreads();
+}
+
+// y = K x with the refinement values (original numbering).
+template <class T> __device__ void spmv_ref(const Ctx<T> &c, const double *x, double *y) {
+  for (int i = threadIdx.x; i < c.N; i += blockDim.x) {
+    double acc = 0.0;
+    for (int qq = c.Rp[i]; qq < c.Rp[i + 1]; ++qq) acc += ref_val(c, c.Rq[qq]) * x[c.Rj[qq]];
+    y[i] = acc;
+  }
+  __syncthreads();
+}
+
+template <class T> __device__ double dot(const Ctx<T> &c, const double *a, const double *b) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < c.N; i += blockDim.x) s += a[i] * b[i];
+  return block_sum(s, c.red);
+}
+
+// ---- refinement (reference pmgmres_ldlt_auto, src/gmres/mgmres.cpp:1015-1211)
+struct GmresSmall {
+  double h[MR_CAP + 1][MR_CAP], cs[MR_CAP + 1], sn[MR_CAP + 1], g[MR_CAP + 1], y[MR_CAP + 1];
+  double scal[4];
+};
+
+// Solves K x = b (x holds the preconditioned solution on entry).  flexible:
+// right-preconditioned FGMRES with stored directions Z (Saad 1993) -- the
+// residual it minimises is the FP64 b - Kx itself; else the reference's
+// left-preconditioned GMRES.  adaptive: stop once the residual estimate is
+// below rtol * ||b||; else the reference's rule (rho <= tol_rel * rho0 and
+// rho <= tol_abs).  Returns the Krylov steps taken.
+template <class T>
+__device__ int refine(Ctx<T> &c, const double *b, double *x, int itr_max, int mr, bool flexible, bool adaptive,
+                      double rtol, double tol_abs, double tol_rel, GmresSmall &gs) {
+  if (itr_max <= 0 || mr <= 0) return 0;
+  mr = min(mr, MR_CAP);
+  const int N = c.N;
+  const double delta = 1.0e-03;
+  double *r = c.r, *V = c.V;
+  double rho = 0.0, rho_tol = 0.0, stop_abs = tol_abs;
+  int used = 0;
+  if (adaptive) {
+    const double nb = sqrt(dot(c, b, b));
+    stop_abs = rtol * nb;
+  }
+  for (int itr = 0; itr < itr_max; ++itr) {
+    spmv_ref(c, x, r);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) r[i] = b[i] - r[i];
+    __syncthreads();
+    if (!flexible) precond(c, r, r);
+    rho = sqrt(dot(c, r, r));
+    if (adaptive ? rho <= stop_abs : rho < tol_abs) return used;
+    if (itr == 0) rho_tol = rho * tol_rel;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) V[i] = r[i] / rho;
+    if (threadIdx.x == 0) {
+      gs.g[0] = rho;
+      for (int i = 1; i <= mr; ++i) gs.g[i] = 0.0;
+      for (int i = 0; i <= mr; ++i)
+        for (int j = 0; j < mr; ++j) gs.h[i][j] = 0.0;
+    }
+    __syncthreads();
+    int k_copy = 0;
+    bool stop = false;
+    for (int k = 0; k < mr; ++k) {
+      k_copy = k;
+      double *vk = V + (size_t)k * N, *vk1 = V + (size_t)(k + 1) * N;
+      if (flexible) {
+        T *zk = c.Z + (size_t)k * N;
+        precond(c, vk, zk);
+        // A z_k in FP64 (z widened)
+        for (int i = threadIdx.x; i < N; i += blockDim.x) c.w[i] = (double)zk[i];
+        __syncthreads();
+        spmv_ref(c, c.w, vk1);
+      } else {
+        spmv_ref(c, vk, vk1);
+        precond(c, vk1, vk1);
+      }
+      const double av = sqrt(dot(c, vk1, vk1));
+      for (int j = 0; j <= k; ++j) {
+        const double hj = dot(c, vk1, V + (size_t)j * N);
+        for (int i = threadIdx.x; i < N; i += blockDim.x) vk1[i] -= hj * V[(size_t)j * N + i];
+        if (threadIdx.x == 0) gs.h[j][k] = hj;
+        __syncthreads();
+      }
+      double hk1 = sqrt(dot(c, vk1, vk1));
+      if ((av + delta * hk1) == av) {
+        for (int j = 0; j <= k; ++j) {
+          const double ht = dot(c, vk1, V + (size_t)j * N);
+          for (int i = threadIdx.x; i < N; i += blockDim.x) vk1[i] -= ht * V[(size_t)j * N + i];
+          if (threadIdx.x == 0) gs.h[j][k] += ht;
+          __syncthreads();
+        }
+        hk1 = sqrt(dot(c, vk1, vk1));
+      }
+      if (hk1 != 0.0)
+        for (int i = threadIdx.x; i < N; i += blockDim.x) vk1[i] = vk1[i] / hk1;
+      if (threadIdx.x == 0) {
+        gs.h[k + 1][k] = hk1;
+        if (0 < k) {
+          for (int j = 0; j < k; ++j) {  // previous Givens rotations
+            const double g1 = gs.cs[j] * gs.h[j][k] - gs.sn[j] * gs.h[j + 1][k];
+            const double g2 = gs.sn[j] * gs.h[j][k] + gs.cs[j] * gs.h[j + 1][k];
+            gs.h[j][k] = g1;
+            gs.h[j + 1][k] = g2;
+          }
+        }
+        const double mu = sqrt(gs.h[k][k] * gs.h[k][k] + gs.h[k + 1][k] * gs.h[k + 1][k]);
+        gs.scal[0] = mu;
+        if (mu != 0.0) {
+          gs.cs[k] = gs.h[k][k] / mu;
+          gs.sn[k] = -gs.h[k + 1][k] / mu;
+          gs.h[k][k] = gs.cs[k] * gs.h[k][k] - gs.sn[k] * gs.h[k + 1][k];
+          gs.h[k + 1][k] = 0.0;
+          const double g1 = gs.cs[k] * gs.g[k] - gs.sn[k] * gs.g[k + 1];
+          const double g2 = gs.sn[k] * gs.g[k] + gs.cs[k] * gs.g[k + 1];
+          gs.g[k] = g1;
+          gs.g[k + 1] = g2;
+        }
+      }
+      __syncthreads();
+      if (gs.scal[0] == 0.0) return used;
+      rho = fabs(gs.g[k + 1]);
+      used++;
+      stop = adaptive ? rho <= stop_abs : (rho <= rho_tol && rho <= tol_abs);
+      if (stop) break;
+    }
+    const int k = k_copy;
+    if (gs.h[k][k] == 0.0) return used;
+    if (threadIdx.x == 0) {
+      gs.y[k] = gs.g[k] / gs.h[k][k];
+      for (int i = k - 1; 0 <= i; i--) {
+        double yi = gs.g[i];
+        for (int j = i + 1; j < k + 1; j++) yi = yi - gs.h[i][j] * gs.y[j];
+        gs.y[i] = yi / gs.h[i][i];
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      double acc = 0.0;
+      if (flexible)
+        for (int j = 0; j <= k; ++j) acc += (double)c.Z[(size_t)j * N + i] * gs.y[j];
+      else
+        for (int j = 0; j <= k; ++j) acc += V[(size_t)j * N + i] * gs.y[j];
+      x[i] += acc;
+    }
+    __syncthreads();
+    if (stop) break;
+  }
+  return used;
+}
+
+// ---- NASOQ on one problem ------------------------------------------------------
+// Marks the supernodes on the elimination-tree path from supernode s to the
+// root (the reference marks the visible ones of its edited tree, which are a
+// subset; refactoring an unchanged supernode reproduces it).
+template <class T> __device__ void mark_path(Ctx<T> &c, int s) {
+  for (; s >= 0; s = c.sparent[s]) c.mark[s] = 1;
+}
+
+// KKT edit of constraint k (reference edit_kkt -> add_del_matrix_qp,
+// linear_solver_wrapper.cpp:1020-1137): the constraint's entries become
+// visible / hidden, and the paths of its column and of its variables are
+// marked for the next partial refactorization.  Thread 0 only.
+template <class T> __device__ void edit_constraint(Ctx<T> &c, int k, bool add) {
+  c.act[k] = add ? 1 : 0;
+  mark_path(c, c.con_sn[k]);
+  for (int e = c.bt_ptr[k]; e < c.bt_ptr[k + 1]; ++e) mark_path(c, c.col2sup[c.iperm[c.bt_var[e]]]);
+}
+
+}  // namespace
+
+template <class T>
+__global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double red[32];
+  __shared__ int redi[32];
+  __shared__ int s_status, s_prob;
+  __shared__ GmresSmall gs;
+  __shared__ int s_int[8];
+  __shared__ double s_dbl[8];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  // shared-memory carve-up (sizes from the largest pattern of the batch)
+  unsigned char *sp = smem;
+  int *map = reinterpret_cast<int *>(sp);
+  sp += ((size_t)a.N_max * sizeof(int) + 15) / 16 * 16;
+  T *xs = reinterpret_cast<T *>(sp);
+  sp += ((size_t)a.N_max * sizeof(T) + 15) / 16 * 16;
+  T *Bm = reinterpret_cast<T *>(sp);
+  sp += ((size_t)a.nr_max * a.w_max * sizeof(T) + 15) / 16 * 16;
+  T *rowbuf = reinterpret_cast<T *>(sp);
+  sp += ((size_t)a.w_max * nt * sizeof(T) + 15) / 16 * 16;
+  T *Dsm = reinterpret_cast<T *>(sp);
+  sp += ((size_t)a.w_max * sizeof(T) + 15) / 16 * 16;
+  T *Esm = reinterpret_cast<T *>(sp);
+  sp += ((size_t)a.w_max * sizeof(T) + 15) / 16 * 16;
+  int *lp = reinterpret_cast<int *>(sp);
+
+  unsigned char *slot = a.slots + (size_t)blockIdx.x * a.slot.bytes;
+  for (;;) {
+    if (tid == 0) {
+      const int qi = atomicAdd(a.head, 1);
+      s_prob = qi < a.nprob ? a.order[qi] : -1;
+      s_status = 0;
+    }
+    __syncthreads();
+    const int pi = s_prob;
+    if (pi < 0) break;
+    const BProb &P = a.probs[pi];
+    const BPat &pt = a.pats[P.pat];
+    Ctx<T> c;
+    c.n = pt.n;
+    c.meq = pt.meq;
+    c.mineq = pt.mineq;
+    c.N = pt.N;
+    c.base = pt.base;
+    c.ns = pt.ns;
+    c.nlev = pt.nlev;
+    const int *ip = a.ipool;
+    c.super = ip + pt.o_super;
+    c.sparent = ip + pt.o_sparent;
+    c.col2sup = ip + pt.o_col2sup;
+    c.lpi = ip + pt.o_lpi;
+    c.lpx = ip + pt.o_lpx;
+    c.lvl_ptr = ip + pt.o_lvl_ptr;
+    c.lvl_sn = ip + pt.o_lvl_sn;
+    c.pair_ptr = ip + pt.o_pair_ptr;
+    c.pair_d = ip + pt.o_pair_d;
+    c.pair_lb = ip + pt.o_pair_lb;
+    c.pair_ub = ip + pt.o_pair_ub;
+    c.Rp = ip + pt.o_Rp;
+    c.Rj = ip + pt.o_Rj;
+    c.Rq = ip + pt.o_Rq;
+    c.ent = ip + pt.o_ent;
+    c.bt_ptr = ip + pt.o_bt_ptr;
+    c.bt_var = ip + pt.o_bt_var;
+    c.bt_q = ip + pt.o_bt_q;
+    c.sn_con = ip + pt.o_sn_con;
+    c.con_sn = ip + pt.o_con_sn;
+    c.eq_ptr = ip + pt.o_eq_ptr;
+    c.eq_var = ip + pt.o_eq_var;
+    c.eq_q = ip + pt.o_eq_q;
+    c.kv = a.dpool + P.o_kv;
+    c.q = a.dpool + P.o_q;
+    c.bq = a.dpool + P.o_b;
+    c.dq = a.dpool + P.o_d;
+    c.pert = reinterpret_cast<const uint8_t *>(a.dpool) + P.o_pert;
+    c.reg = P.reg;
+    c.L = reinterpret_cast<T *>(slot + a.slot.o_L);
+    c.D = reinterpret_cast<T *>(slot + a.slot.o_D);
+    c.ls = reinterpret_cast<int *>(slot + a.slot.o_ls);
+    c.perm = reinterpret_cast<int *>(slot + a.slot.o_perm);
+    c.iperm = reinterpret_cast<int *>(slot + a.slot.o_iperm);
+    c.lperm = reinterpret_cast<int *>(slot + a.slot.o_lperm);
+    c.mark = slot + a.slot.o_mark;
+    c.piv = slot + a.slot.o_piv;
+    c.act = slot + a.slot.o_act;
+    c.alist = reinterpret_cast<int *>(slot + a.slot.o_alist);
+    c.rhs = reinterpret_cast<double *>(slot + a.slot.o_rhs);
+    c.sol = reinterpret_cast<double *>(slot + a.slot.o_sol);
+    c.r = reinterpret_cast<double *>(slot + a.slot.o_r);
+    c.w = reinterpret_cast<double *>(slot + a.slot.o_w);
+    c.V = reinterpret_cast<double *>(slot + a.slot.o_V);
+    c.Z = reinterpret_cast<T *>(slot + a.slot.o_Z);
+    c.tmp = reinterpret_cast<double *>(slot + a.slot.o_tmp);
+    c.map = map;
+    c.xs = xs;
+    c.B = Bm;
+    c.rowbuf = rowbuf;
+    c.Dsm = Dsm;
+    c.Esm = Esm;
+    c.lp = lp;
+    c.red = red;
+    c.redi = redi;
+    c.status = &s_status;
+    double *xv = a.dout + P.o_x, *yv = a.dout + P.o_y, *zv = a.dout + P.o_z;
+    int *as_out = a.iout + P.o_as;
+    const int n = c.n, meq = c.meq, mineq = c.mineq, N = c.N;
+    const bool flexible = sizeof(T) == 4 || a.refine == 1;
+    const bool adaptive = a.refine == 1;
+    int steps = 0, solves = 0, warm_dropped = 0;
+
+    // ---- set-up: pattern state into the slot
+    for (int i = tid; i < N; i += nt) {
+      const int p0 = ip[pt.o_perm0 + i];
+      c.perm[i] = p0;
+      c.iperm[p0] = i;
+      c.D[i] = T(0);
+      c.D[N + i] = T(0);
+    }
+    for (int i = tid; i < pt.ssize; i += nt) c.ls[i] = ip[pt.o_ls0 + i];
+    for (int i = tid; i < pt.xsize; i += nt) c.L[i] = T(0);
+    for (int s = tid; s < c.ns; s += nt) {
+      c.mark[s] = 0;
+      c.piv[s] = 0;
+    }
+    for (int k = tid; k < mineq; k += nt) c.act[k] = 0;
+    __syncthreads();
+    int nact = 0;
+    // warm start: proposed active set (constraints listed in as_out), then
+    // the equality-constrained solution on it (below)
+    const bool warm = P.ws_n >= 0;
+    if (warm) {
+      for (int t = tid; t < P.ws_n; t += nt) {
+        const int k = as_out[t];
+        if (k >= 0 && k < mineq) c.act[k] = 1;
+      }
+      __syncthreads();
+    }
+    // ---- initial factorization and solution (reference initialize_x,
+    // src/nasoq.cpp:448-476): every visible supernode; rhs [-q; b; d on the
+    // active rows]
+    for (int round = 0; round < (warm ? 4 : 1); ++round) {
+      for (int s = tid; s < c.ns; s += nt) c.mark[s] = warm ? 1 : (visible(c, s) ? 1 : 0);
+      __syncthreads();
+      factor_marked(c);
+      for (int i = tid; i < N; i += nt) {
+        double v = 0.0;
+        if (i < n) v = -c.q[i];
+        else if (i < c.base) v = c.bq[i - n];
+        else if (c.act[i - c.base]) v = c.dq[i - c.base];
+        c.rhs[i] = v;
+      }
+      __syncthreads();
+      precond(c, c.rhs, c.sol);
+      solves++;
+      steps += refine(c, c.rhs, c.sol, P.outer, P.inner, flexible, adaptive, a.refine_tol, P.tol_abs, P.tol_rel, gs);
+      if (!warm) break;
+      // drop proposed constraints with negative multipliers, then solve again
+      int ndrop = 0;
+      for (int k = tid; k < mineq; k += nt)
+        if (c.act[k] && c.sol[c.base + k] < 0.0) {
+          c.act[k] = 0;
+          ndrop++;
+        }
+      ndrop = block_sum_int(ndrop, redi);
+      warm_dropped += ndrop;
+      if (ndrop == 0) break;
+      if (round == 2) {  // no consistent set after three rounds: cold start
+        for (int k = tid; k < mineq; k += nt) c.act[k] = 0;
+        __syncthreads();
+      }
+    }
+    for (int i = tid; i < n; i += nt) xv[i] = c.sol[i];
+    for (int i = tid; i < meq; i += nt) yv[i] = c.sol[n + i];
+    for (int k = tid; k < mineq; k += nt) zv[k] = c.act[k] ? c.sol[c.base + k] : 0.0;
+    __syncthreads();
+    if (tid == 0) {
+      for (int k = 0; k < mineq; ++k)
+        if (c.act[k]) c.alist[nact++] = k;
+      s_int[0] = nact;
+    }
+    __syncthreads();
+    nact = s_int[0];
+
+    // ---- the dual active-set iteration (reference numeric_QP)
+    int num_iter = 0, converged = 0, nxt_active = -1, nxt_drop = -1, to_add = 1;
+    int typ = 0;  // 0 solve, 1 update (partial refactorization first)
+    const double DMAX = DBL_MAX;
+    for (;;) {
+      if (num_iter > P.max_iter_nas) {
+        converged = 0;
+        break;
+      }
+      if (to_add == 1) {
+        // primal_feasibility (src/nasoq.cpp:787-840): most violated row beyond eps_abs
+        int viol = 0;
+        double best = P.eps_abs;
+        int bi = -1;
+        for (int k = tid; k < mineq; k += nt) {
+          double t = 0.0;
+          for (int e = c.bt_ptr[k]; e < c.bt_ptr[k + 1]; ++e) t += c.kv[c.bt_q[e]] * xv[c.bt_var[e]];
+          t -= c.dq[k];
+          if (t > P.eps_abs) viol++;
+          if (t > best) {
+            best = t;
+            bi = k;
+          }
+        }
+        viol = block_sum_int(viol, redi);
+        block_select(best, bi, true, red, redi);
+        if (viol == 0) {
+          converged = 1;
+          break;
+        }
+        if (bi < 0) {
+          converged = 0;
+          break;
+        }
+        nxt_active = bi;
+        // update_rhs (src/nasoq.cpp:880-889): the constraint's row as the rhs
+        for (int i = tid; i < N; i += nt) c.rhs[i] = 0.0;
+        __syncthreads();
+        for (int e = c.bt_ptr[nxt_active] + tid; e < c.bt_ptr[nxt_active + 1]; e += nt)
+          c.rhs[c.bt_var[e]] = c.kv[c.bt_q[e]];
+        __syncthreads();
+      }
+      // solve_kkt (src/nasoq.cpp:918-957)
+      if (typ == 1) factor_marked(c);
+      precond(c, c.rhs, c.sol);
+      solves++;
+      steps += refine(c, c.rhs, c.sol, P.outer, P.inner, flexible, adaptive, a.refine_tol, P.tol_abs, P.tol_rel, gs);
+      // step lengths (src/nasoq.cpp:852-878)
+      double dual_step = DMAX;
+      int drop = -1;
+      for (int t = tid; t < nact; t += nt) {
+        const int k = c.alist[t];
+        const double lm = c.sol[c.base + k];
+        if (lm > 0.0) {
+          const double ratio = zv[k] / lm;
+          if (drop < 0 || ratio < dual_step || (ratio == dual_step && k < drop)) {
+            dual_step = ratio;
+            drop = k;
+          }
+        }
+      }
+      block_select(dual_step, drop, false, red, redi);
+      if (drop < 0) dual_step = DMAX;
+      if (tid == 0) {
+        double bdotx = 0.0, ddotb = 0.0;
+        for (int e = c.bt_ptr[nxt_active]; e < c.bt_ptr[nxt_active + 1]; ++e) {
+          bdotx += c.kv[c.bt_q[e]] * xv[c.bt_var[e]];
+          ddotb += c.kv[c.bt_q[e]] * c.sol[c.bt_var[e]];
+        }
+        double prime_step = DMAX;
+        if (!(ddotb < P.zero_thresh)) prime_step = -(c.dq[nxt_active] - bdotx) / ddotb;
+        s_dbl[0] = prime_step;
+      }
+      __syncthreads();
+      const double prime_step = s_dbl[0];
+      if (drop >= 0) nxt_drop = drop;
+      const double step = prime_step > dual_step ? dual_step : prime_step;
+      if (step == DMAX) {
+        converged = 0;
+        break;
+      }
+      const bool dual_only = prime_step == DMAX && step == dual_step;
+      // update_primal / update_dual (src/nasoq.cpp:612-632)
+      if (!dual_only)
+        for (int i = tid; i < n; i += nt) xv[i] = xv[i] - step * c.sol[i];
+      for (int i = tid; i < meq; i += nt) yv[i] -= step * c.sol[n + i];
+      for (int t = tid; t < nact; t += nt) {
+        const int k = c.alist[t];
+        zv[k] -= step * c.sol[c.base + k];
+      }
+      __syncthreads();
+      if (tid == 0) {
+        zv[nxt_active] = zv[nxt_active] + step;
+        int add = -1, del = -1;
+        if (dual_only) del = nxt_drop;
+        else if (step == prime_step) add = nxt_active;
+        else if (step == dual_step) del = nxt_drop;
+        if (add >= 0) {
+          const bool fresh = !c.act[add];
+          edit_constraint(c, add, true);
+          if (fresh && nact < mineq) c.alist[nact++] = add;
+          s_int[1] = 1;
+        } else if (del >= 0) {
+          edit_constraint(c, del, false);
+          int pos = -1;
+          for (int t = 0; t < nact; ++t)
+            if (c.alist[t] == del) pos = t;
+          if (pos >= 0) {
+            for (int t = pos; t + 1 < nact; ++t) c.alist[t] = c.alist[t + 1];
+            nact--;
+          }
+          s_int[1] = 0;
+        } else {
+          s_int[1] = -1;
+        }
+        s_int[0] = nact;
+      }
+      __syncthreads();
+      nact = s_int[0];
+      if (s_int[1] >= 0) {
+        to_add = s_int[1];
+        typ = 1;
+      }
+      num_iter++;
+    }
+
+    // ---- results: objective and KKT norms (src/nasoq.cpp:712-728, 1013-1106)
+    // Hx, Ax, Cx and H x + A^T y + C^T z from the original values
+    for (int i = tid; i < N; i += nt) {
+      double v = 0.0;
+      if (i < n) v = xv[i];
+      c.w[i] = v;
+      double u = v;
+      if (i >= n && i < c.base) u = yv[i - n];
+      else if (i >= c.base) u = zv[i - c.base];
+      c.tmp[i] = u;
+    }
+    __syncthreads();
+    double quad = 0.0, lin = 0.0, lag = 0.0;
+    for (int i = tid; i < n; i += nt) {
+      double hx = 0.0, full = 0.0;
+      for (int qq = c.Rp[i]; qq < c.Rp[i + 1]; ++qq) {
+        const int j = c.Rj[qq];
+        const double v = c.kv[c.Rq[qq]];
+        if (j < n) hx += v * c.w[j];
+        full += v * c.tmp[j];
+      }
+      quad += hx * xv[i];
+      lin += c.q[i] * xv[i];
+      lag = fmax(lag, fabs(full + c.q[i]));
+    }
+    double cons = 0.0, dual_obj = 0.0, nonneg = 0.0, comp = 0.0;
+    for (int k = tid; k < mineq; k += nt) {
+      double t = 0.0;
+      for (int e = c.bt_ptr[k]; e < c.bt_ptr[k + 1]; ++e) t += c.kv[c.bt_q[e]] * xv[c.bt_var[e]];
+      t -= c.dq[k];
+      cons = fmax(cons, t < 0.0 ? 0.0 : t);
+      dual_obj += t * zv[k];
+      nonneg = fmax(nonneg, zv[k] > 0.0 ? 0.0 : fabs(zv[k]));
+      comp = fmax(comp, fabs(zv[k] * t));
+    }
+    for (int r = tid; r < meq; r += nt) {
+      double t = 0.0;
+      for (int e = c.eq_ptr[r]; e < c.eq_ptr[r + 1]; ++e) t += c.kv[c.eq_q[e]] * xv[c.eq_var[e]];
+      cons = fmax(cons, fabs(t - c.bq[r]));
+    }
+    quad = block_sum(quad, red);
+    lin = block_sum(lin, red);
+    dual_obj = block_sum(dual_obj, red);
+    double mx[4] = {lag, cons, nonneg, comp};
+    for (int m = 0; m < 4; ++m) {
+      double v = mx[m];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+      __syncthreads();
+      if (lane_id() == 0) red[warp_id()] = v;
+      __syncthreads();
+      if (tid == 0) {
+        double w = 0.0;
+        for (int t = 0; t < num_warps(); ++t) w = fmax(w, red[t]);
+        s_dbl[m] = w;
+      }
+      __syncthreads();
+      mx[m] = s_dbl[m];
+      __syncthreads();
+    }
+    for (int t = tid; t < mineq; t += nt) as_out[t] = t < nact ? c.alist[t] : -1;
+    if (tid == 0) {
+      BResult &R = a.res[pi];
+      R.num_iter = num_iter;
+      R.active_size = nact;
+      R.flags = s_status;
+      R.refine_steps = steps;
+      R.solves = solves;
+      R.warm_dropped = warm_dropped;
+      R.primal_obj = 0.5 * quad + lin;
+      R.dual_obj = dual_obj;
+      R.objective = R.primal_obj + dual_obj;
+      R.lag_res = mx[0];
+      R.cons_sat_norm = mx[1];
+      R.non_negativity_infn = mx[2];
+      R.complementarity_infn = mx[3];
+      int st;
+      if (!converged) st = 0;  // check_solve_status: Infeasible when the loop did not converge
+      else if (mx[0] <= P.eps_abs && mx[1] <= P.eps_abs && mx[2] <= P.eps_abs) st = 1;
+      else if (mx[1] <= P.eps_abs) st = 2;
+      else st = 3;
+      R.status = st;
+    }
+    __syncthreads();
+  }
+}
+
+size_t batch_smem_bytes(int N_max, int nr_max, int w_max, int threads, size_t tsize) {
+  auto up = [](size_t b) { return (b + 15) / 16 * 16; };
+  return up((size_t)N_max * sizeof(int)) + up((size_t)N_max * tsize) + up((size_t)nr_max * w_max * tsize) +
+         up((size_t)w_max * threads * tsize) + 2 * up((size_t)w_max * tsize) + up((size_t)w_max * sizeof(int));
+}
+
+template <class T> int batch_prepare(int threads, size_t smem, int *blocks_per_sm) {
+  if (cudaFuncSetAttribute(k_nasoq_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return NQG_ERR_CUDA;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_nasoq_batch<T>, threads, smem) != cudaSuccess)
+    return NQG_ERR_CUDA;
+  return NQG_OK;
+}
+
+// The dynamic shared-memory limit was raised by batch_prepare (outside any
+// stream capture).
+template <class T> int launch_batch(const BArgs &a, int grid, int threads, size_t smem, cudaStream_t st) {
+  k_nasoq_batch<T><<<grid, threads, smem, st>>>(a);
+  return cudaGetLastError() == cudaSuccess ? NQG_OK : NQG_ERR_CUDA;
+}
+
+template int launch_batch<double>(const BArgs &, int, int, size_t, cudaStream_t);
+template int launch_batch<float>(const BArgs &, int, int, size_t, cudaStream_t);
+template int batch_prepare<double>(int, size_t, int *);
+template int batch_prepare<float>(int, size_t, int *);
+
+}  // namespace nqg

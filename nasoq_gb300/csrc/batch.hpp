@@ -1,0 +1,100 @@
+// Device layout of the batched QP solver (batch.cu): many small QPs solved by
+// NASOQ's dual active-set method (reference src/nasoq.cpp:478-610) in one
+// persistent kernel, one CTA per QP, with no host round trip per iteration.
+//
+// Problems are grouped by sparsity pattern.  Each distinct pattern of the
+// super-KKT matrix [H A^T C^T; A 0 0; C 0 0] (reference
+// SolverSettings::build_super_matrix, src/QP/linear_solver_wrapper.cpp:246)
+// gets one host symbolic analysis (the same ordering and supernodes as the
+// reference) and one set of integer work lists; every problem of the pattern
+// only brings its values.  All integer arrays of all patterns live in one
+// pool and are addressed by the offsets below.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace nqg {
+
+constexpr int BATCH_MR_CAP = 10;  // largest number of Krylov steps per restart
+
+struct BPat {
+  int n, meq, mineq, N, base;  // N = n + meq + mineq; base = n + meq (first constraint column)
+  int ns, nlev, xsize, ssize, nnzK, max_w, max_nr;
+  // int-pool offsets
+  int o_super;     // ns+1   first (ordered) column of each supernode
+  int o_sparent;   // ns     supernodal elimination tree (-1 at roots)
+  int o_col2sup;   // N      ordered column -> supernode
+  int o_lpi;       // ns+1   start of each supernode's row list
+  int o_lpx;       // ns+1   start of each supernode's values (column-major nrow x w)
+  int o_ls0;       // ssize  row lists of the analysis (ordered indices, sorted)
+  int o_perm0;     // N      fill-reducing order: perm0[c] = original column at position c
+  int o_lvl_ptr;   // nlev+1 supernodes grouped by tree level (leaves first)
+  int o_lvl_sn;    // ns
+  int o_pair_ptr;  // ns+1   descendants of every supernode (elimination-tree reach)
+  int o_pair_d, o_pair_lb, o_pair_ub;  // per pair: descendant, first / last row of it inside the target
+  int o_Rp, o_Rj, o_Rq;  // full symmetric CSR of K (original numbering); Rq = index of the lower-CSC value
+  int o_ent;       // nnzK   per lower-CSC value: constraint k of an entry in constraint row k (>= 0),
+                   //        -2-col for the diagonal of column col, -1 otherwise
+  int o_bt_ptr, o_bt_var, o_bt_q;  // per constraint: its variables and the lower-CSC value index of each entry
+  int o_sn_con;    // ns     constraint whose (single) column a supernode holds, -1 otherwise
+  int o_con_sn;    // mineq  supernode of each constraint column
+  int o_eq_ptr, o_eq_var, o_eq_q;  // per equality row: its variables and value indices
+};
+
+// One QP of the batch: where its values are, its derived settings, and where
+// its results go.
+struct BProb {
+  int pat;
+  int outer, inner;          // refinement restarts x inner steps
+  int max_iter_nas;
+  int ws_n;                  // warm start: size of the proposed active set (-1: cold start)
+  int64_t o_kv;              // nnzK values of K (original, every constraint entry present)
+  int64_t o_pert;            // N bytes: diagonal replaced by the regularization
+  int64_t o_q, o_b, o_d;     // n, meq, mineq
+  int64_t o_x, o_y, o_z;     // n, meq, mineq (results; warm start in)
+  int64_t o_as;              // mineq ints: final active set (insertion order); warm-start set in
+  double reg, zero_thresh, eps_abs, tol_abs, tol_rel;
+};
+
+// Results of one QP (reference Nasoq fields of the same names).
+struct BResult {
+  int status;        // nasoq_status: 1 Optimal, 2 Inaccurate, 3 NotConverged, 0 Infeasible
+  int num_iter, active_size, flags;  // flags: device status bits (zero pivot, non-finite)
+  int refine_steps, solves, warm_dropped, pad;
+  double objective, primal_obj, dual_obj;
+  double lag_res, cons_sat_norm, non_negativity_infn, complementarity_infn;
+};
+
+// Per-CTA scratch: one problem at a time, sized for the largest pattern.
+struct BSlot {
+  int64_t o_L, o_D, o_ls, o_perm, o_iperm, o_lperm, o_mark, o_piv, o_act, o_alist;
+  int64_t o_rhs, o_sol, o_r, o_w, o_V, o_Z, o_tmp;
+  int64_t bytes;
+};
+
+struct BArgs {
+  const BPat *pats;
+  const BProb *probs;
+  const int *ipool;
+  const double *dpool;       // problem values and vectors (BProb offsets)
+  double *dout;              // problem results (x, y, z)
+  int *iout;                 // active sets
+  BResult *res;
+  const int *order;          // queue order of the problems
+  int *head;                 // work-queue counter (reset before every launch)
+  int nprob;
+  unsigned char *slots;      // per-CTA scratch
+  BSlot slot;                // layout of one slot
+  int refine;                // 0: reference GMRES schedule, 1: adaptive flexible GMRES
+  double refine_tol;         // adaptive: relative residual target
+  int mr_max;                // capacity of the Krylov arrays
+  int N_max, w_max, nr_max;  // shared-memory sizing
+};
+
+size_t batch_smem_bytes(int N_max, int nr_max, int w_max, int threads, size_t tsize);
+template <class T> int batch_prepare(int threads, size_t smem, int *blocks_per_sm);
+template <class T> int launch_batch(const BArgs &a, int grid, int threads, size_t smem, cudaStream_t st);
+
+}  // namespace nqg

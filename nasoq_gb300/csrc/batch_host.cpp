@@ -1,0 +1,834 @@
+// Host side of the batched QP solver: problem intake, grouping by sparsity
+// pattern, one symbolic analysis per pattern (the reference's ordering and
+// supernodes, reference SolverSettings::symbolic_analysis,
+// src/QP/linear_solver_wrapper.cpp:396-536), the integer work lists of each
+// pattern, per-problem values and settings, device layout, the CUDA-graph
+// launch of the persistent kernel (batch.cu), and the C ABI
+// (include/nasoq_gb300.h, nqg_batch_*).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/nasoq_gb300.h"
+#include "batch.hpp"
+#include "plan.hpp"
+#include "qp_rules.hpp"
+#include "symbolic.hpp"
+
+namespace {
+
+using nqg::BPat;
+using nqg::BProb;
+using nqg::BResult;
+
+struct HostQP {
+  int n = 0, meq = 0, mineq = 0;
+  std::vector<int> Hp, Hi, Ap, Ai, Cp, Ci;
+  std::vector<double> Hx, q, Ax, b, Cx, d;
+  int pat = -1;
+  std::vector<int> ws;  // proposed active set (warm start)
+  bool warm = false;
+};
+
+struct HostPattern {
+  int rep = -1;  // a problem of this pattern
+  BPat P{};
+  nqg::Symbolic S;
+  // integer arrays of this pattern, in BPat offset order (filled by build_pattern)
+  std::vector<int> super, sparent, col2sup, lpi, lpx, ls0, perm0, lvl_ptr, lvl_sn, pair_ptr, pair_d, pair_lb,
+      pair_ub, Rp, Rj, Rq, ent, bt_ptr, bt_var, bt_q, sn_con, con_sn, eq_ptr, eq_var, eq_q;
+  std::vector<int> diag_q;  // per column: value index of its diagonal
+};
+
+uint64_t fnv(uint64_t h, const void *p, size_t bytes) {
+  const unsigned char *c = static_cast<const unsigned char *>(p);
+  for (size_t k = 0; k < bytes; ++k) {
+    h ^= c[k];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+uint64_t pattern_key(const HostQP &Q) {
+  uint64_t h = 1469598103934665603ull;
+  int dims[3] = {Q.n, Q.meq, Q.mineq};
+  h = fnv(h, dims, sizeof dims);
+  for (const std::vector<int> *v : {&Q.Hp, &Q.Hi, &Q.Ap, &Q.Ai, &Q.Cp, &Q.Ci}) h = fnv(h, v->data(), v->size() * 4);
+  return h;
+}
+
+bool same_pattern(const HostQP &a, const HostQP &b) {
+  return a.n == b.n && a.meq == b.meq && a.mineq == b.mineq && a.Hp == b.Hp && a.Hi == b.Hi && a.Ap == b.Ap &&
+         a.Ai == b.Ai && a.Cp == b.Cp && a.Ci == b.Ci;
+}
+
+// Lower CSC pattern of the super-KKT [H; A; C] (the reference's
+// build_super_matrix: H columns, then the equality rows, then the
+// inequality rows; one diagonal entry per constraint column) and, when
+// `vals`, the original values with every constraint entry present.
+void super_kkt(const HostQP &Q, nqg::Csc &K, std::vector<double> *vals) {
+  const int n = Q.n, N = Q.n + Q.meq + Q.mineq, base = Q.n + Q.meq;
+  K.n = N;
+  K.p.assign(N + 1, 0);
+  K.i.clear();
+  if (vals) vals->clear();
+  for (int j = 0; j < n; ++j) {
+    for (int q = Q.Hp[j]; q < Q.Hp[j + 1]; ++q) {
+      K.i.push_back(Q.Hi[q]);
+      if (vals) vals->push_back(Q.Hx[q]);
+    }
+    if (Q.meq)
+      for (int q = Q.Ap[j]; q < Q.Ap[j + 1]; ++q) {
+        K.i.push_back(n + Q.Ai[q]);
+        if (vals) vals->push_back(Q.Ax[q]);
+      }
+    if (Q.mineq)
+      for (int q = Q.Cp[j]; q < Q.Cp[j + 1]; ++q) {
+        K.i.push_back(base + Q.Ci[q]);
+        if (vals) vals->push_back(Q.Cx[q]);
+      }
+    K.p[j + 1] = (int)K.i.size();
+  }
+  for (int k = n; k < N; ++k) {
+    K.i.push_back(k);
+    if (vals) vals->push_back(0.0);
+    K.p[k + 1] = (int)K.i.size();
+  }
+}
+
+std::string build_pattern(const HostQP &Q, HostPattern &H, const int nrelax[3], const double zrelax[3]) {
+  const int n = Q.n, meq = Q.meq, mineq = Q.mineq, N = n + meq + mineq, base = n + meq;
+  nqg::Csc K;
+  super_kkt(Q, K, nullptr);
+  std::vector<int> extra(N, 0);
+  for (int j = base; j < N; ++j) extra[j] = 1;
+  nqg::Symbolic &S = H.S;
+  std::string err = nqg::analyze(K, extra.data(), nrelax, zrelax, S);
+  if (!err.empty()) return err;
+  const int ns = S.nsuper;
+  if (S.xsize > (1ll << 30) || (int64_t)S.ls.size() > (1ll << 30)) return "pattern too large for the batched solver";
+  BPat &P = H.P;
+  P.n = n;
+  P.meq = meq;
+  P.mineq = mineq;
+  P.N = N;
+  P.base = base;
+  P.ns = ns;
+  P.xsize = (int)S.xsize;
+  P.ssize = (int)S.ls.size();
+  P.nnzK = (int)K.nnz();
+  H.super = S.super;
+  H.sparent = S.sparent;
+  H.col2sup = S.col2sup;
+  H.lpi.assign(S.lpi.begin(), S.lpi.end());
+  H.lpx.assign(S.lpx.begin(), S.lpx.end());
+  H.ls0 = S.ls;
+  H.perm0 = S.perm;
+  P.max_w = 0;
+  P.max_nr = 0;
+  for (int s = 0; s < ns; ++s) {
+    P.max_w = std::max(P.max_w, S.super[s + 1] - S.super[s]);
+    P.max_nr = std::max(P.max_nr, (int)(S.lpi[s + 1] - S.lpi[s]));
+  }
+  // levels (leaves first)
+  std::vector<int> lev(ns, 0);
+  int maxl = 0;
+  for (int s = 0; s < ns; ++s) {
+    const int p = S.sparent[s];
+    if (p >= 0) lev[p] = std::max(lev[p], lev[s] + 1);
+    maxl = std::max(maxl, lev[s]);
+  }
+  P.nlev = ns ? maxl + 1 : 0;
+  H.lvl_ptr.assign(P.nlev + 1, 0);
+  for (int s = 0; s < ns; ++s) H.lvl_ptr[lev[s] + 1]++;
+  for (int l = 0; l < P.nlev; ++l) H.lvl_ptr[l + 1] += H.lvl_ptr[l];
+  H.lvl_sn.assign(ns, 0);
+  {
+    std::vector<int> pos(H.lvl_ptr.begin(), H.lvl_ptr.end() - (P.nlev ? 1 : 0));
+    for (int s = 0; s < ns; ++s) H.lvl_sn[pos[lev[s]]++] = s;
+  }
+  // descendant pairs from the elimination-tree reach (reference ereach_sn)
+  nqg::Csc up;
+  nqg::sym_permute(K, S.iperm, nullptr, &up);
+  std::vector<int> mark(ns, 0), stack, lst;
+  H.pair_ptr.assign(ns + 1, 0);
+  for (int s = 0; s < ns; ++s) {
+    nqg::ereach_sn(S, up, s, S.sparent, mark, stack, lst);
+    const int c1 = S.super[s], c2 = S.super[s + 1];
+    for (int d : lst) {
+      const int *rows = S.ls.data() + S.lpi[d];
+      const int nr = (int)(S.lpi[d + 1] - S.lpi[d]);
+      const int lb = (int)(std::lower_bound(rows, rows + nr, c1) - rows);
+      const int ub = (int)(std::lower_bound(rows, rows + nr, c2) - rows) - 1;
+      if (lb >= nr || ub < lb) continue;
+      H.pair_d.push_back(d);
+      H.pair_lb.push_back(lb);
+      H.pair_ub.push_back(ub);
+    }
+    H.pair_ptr[s + 1] = (int)H.pair_d.size();
+  }
+  // full symmetric CSR of K in the original numbering, with value indices
+  const int nz = (int)K.nnz();
+  H.Rp.assign(N + 1, 0);
+  for (int j = 0; j < N; ++j)
+    for (int q = K.p[j]; q < K.p[j + 1]; ++q) {
+      H.Rp[j + 1]++;
+      if (K.i[q] != j) H.Rp[K.i[q] + 1]++;
+    }
+  for (int r = 0; r < N; ++r) H.Rp[r + 1] += H.Rp[r];
+  H.Rj.assign(H.Rp[N], 0);
+  H.Rq.assign(H.Rp[N], 0);
+  {
+    std::vector<int> pos(H.Rp.begin(), H.Rp.end() - 1);
+    for (int j = 0; j < N; ++j)
+      for (int q = K.p[j]; q < K.p[j + 1]; ++q) {
+        const int i = K.i[q];
+        H.Rj[pos[j]] = i;
+        H.Rq[pos[j]++] = q;
+        if (i != j) {
+          H.Rj[pos[i]] = j;
+          H.Rq[pos[i]++] = q;
+        }
+      }
+  }
+  // entry kinds, constraint and equality row lists
+  H.ent.assign(nz, -1);
+  H.diag_q.assign(N, -1);
+  std::vector<std::vector<int>> btv(mineq), btq(mineq), eqv(meq), eqq(meq);
+  for (int j = 0; j < N; ++j) {
+    for (int q = K.p[j]; q < K.p[j + 1]; ++q) {
+      const int i = K.i[q];
+      if (i == j) {
+        H.ent[q] = -2 - j;
+        H.diag_q[j] = q;
+      } else if (i >= base) {
+        H.ent[q] = i - base;
+        btv[i - base].push_back(j);
+        btq[i - base].push_back(q);
+      } else if (i >= n) {
+        eqv[i - n].push_back(j);
+        eqq[i - n].push_back(q);
+      }
+    }
+    if (H.diag_q[j] != K.p[j]) return "every column of H needs its diagonal entry stored first";
+  }
+  auto flatten = [](const std::vector<std::vector<int>> &v, const std::vector<std::vector<int>> &w,
+                    std::vector<int> &ptr, std::vector<int> &a, std::vector<int> &b) {
+    ptr.assign(v.size() + 1, 0);
+    for (size_t k = 0; k < v.size(); ++k) {
+      ptr[k + 1] = ptr[k] + (int)v[k].size();
+      a.insert(a.end(), v[k].begin(), v[k].end());
+      b.insert(b.end(), w[k].begin(), w[k].end());
+    }
+  };
+  flatten(btv, btq, H.bt_ptr, H.bt_var, H.bt_q);
+  flatten(eqv, eqq, H.eq_ptr, H.eq_var, H.eq_q);
+  H.sn_con.assign(ns, -1);
+  H.con_sn.assign(mineq, -1);
+  for (int k = 0; k < mineq; ++k) {
+    const int oc = S.iperm[base + k];
+    const int s = S.col2sup[oc];
+    if (S.super[s + 1] - S.super[s] != 1) return "an inequality column is not a single-column supernode";
+    H.con_sn[k] = s;
+    H.sn_con[s] = k;
+  }
+  return "";
+}
+
+}  // namespace
+
+struct nqg_batch {
+  nqg_batch_settings set{};
+  std::vector<HostQP> qp;
+  std::vector<HostPattern> pats;
+  bool finalized = false;
+  std::string last_error;
+  // device
+  cudaStream_t stream = nullptr;
+  nqg::BArgs args{};
+  BPat *d_pats = nullptr;
+  BProb *d_probs = nullptr;
+  int *d_ipool = nullptr, *d_order = nullptr, *d_head = nullptr, *d_iout = nullptr;
+  double *d_dpool = nullptr, *d_dout = nullptr;
+  BResult *d_res = nullptr;
+  unsigned char *d_slots = nullptr;
+  std::vector<BProb> h_probs;
+  std::vector<double> h_dpool;  // doubles part of the value pool (pert bytes follow on the device)
+  int64_t n_dbl = 0, n_pert_bytes = 0, n_dout = 0, n_iout = 0;
+  int grid = 0, threads = 128, blocks_per_sm = 0, num_sms = 0;
+  size_t smem = 0;
+  cudaGraphExec_t gexec = nullptr;
+  cudaGraph_t graph = nullptr;
+  double last_ms = 0.0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+};
+
+namespace {
+
+int fail(nqg_batch *b, int code, const std::string &msg) {
+  b->last_error = msg;
+  return code;
+}
+
+#define BQ_CUDA(call)                                                             \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess) return fail(b, NQG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+void free_device(nqg_batch *b) {
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->gexec = nullptr;
+  b->graph = nullptr;
+  for (void *p : {(void *)b->d_pats, (void *)b->d_probs, (void *)b->d_ipool, (void *)b->d_order, (void *)b->d_head,
+                  (void *)b->d_iout, (void *)b->d_dpool, (void *)b->d_dout, (void *)b->d_res, (void *)b->d_slots})
+    if (p) cudaFree(p);
+  b->d_pats = nullptr;
+  b->d_probs = nullptr;
+  b->d_ipool = b->d_order = b->d_head = b->d_iout = nullptr;
+  b->d_dpool = b->d_dout = nullptr;
+  b->d_res = nullptr;
+  b->d_slots = nullptr;
+}
+
+// Derived settings of one problem (reference Nasoq::symbolic_QP,
+// src/nasoq.cpp:222-280): regularization, refinement counts and tolerance
+// from the variant.
+int problem_settings(const nqg_batch_settings &st, const HostQP &Q, BProb &P) {
+  const nqg_qp_settings &s = st.qp;
+  double reg = s.diag_perturb, tol = s.stop_tol;
+  int outer = s.max_iter, inner = s.max_iter;
+  const size_t total_nnz = (size_t)Q.Hp[Q.n] + (size_t)(Q.mineq ? Q.Cp[Q.n] : 0);
+  const double H_norm2 = nqg::qp_frob_lower(Q.n, Q.Hp.data(), Q.Hi.data(), Q.Hx.data());
+  if (s.variant == 1) {  // AUTO
+    nqg::qp_auto_perturbation2(Q.n, total_nnz, H_norm2, 0.0, Q.mineq, Q.mineq / double(Q.n), s.eps_abs, reg, outer,
+                               inner, tol);
+  } else if (s.variant == 0) {  // Fixed
+    nqg::qp_determine_iterations(total_nnz, s.eps_abs, outer, inner);
+    tol = 1e-15;
+    reg = H_norm2 < 1 ? 1e-7 : 1e-9;
+  } else if (s.variant == 2) {
+    return NQG_ERR_ARG;  // Tuned (four repeated solves) is not offered in batches
+  }
+  if (st.qp.precision == NQG_FP32) {  // FP32 factor: refinement always runs
+    outer = std::max(outer, 2);
+    inner = std::max(inner, 2);
+  }
+  if (inner > nqg::BATCH_MR_CAP) return NQG_ERR_SIZE;
+  P.reg = reg;
+  P.zero_thresh = reg;
+  P.tol_abs = P.tol_rel = tol;
+  P.outer = std::max(outer, 0);
+  P.inner = std::max(inner, 0);
+  P.eps_abs = s.eps_abs;
+  P.max_iter_nas = s.max_iter_nas;
+  return NQG_OK;
+}
+
+// Values of problem i into the host pool (original K values and the
+// perturbed-diagonal flags).
+void fill_values(nqg_batch *b, int i, std::vector<unsigned char> &pert_pool) {
+  const HostQP &Q = b->qp[i];
+  BProb &P = b->h_probs[i];
+  nqg::Csc K;
+  std::vector<double> kv;
+  super_kkt(Q, K, &kv);
+  std::copy(kv.begin(), kv.end(), b->h_dpool.begin() + P.o_kv);
+  std::copy(Q.q.begin(), Q.q.end(), b->h_dpool.begin() + P.o_q);
+  std::copy(Q.b.begin(), Q.b.end(), b->h_dpool.begin() + P.o_b);
+  std::copy(Q.d.begin(), Q.d.end(), b->h_dpool.begin() + P.o_d);
+  const int N = K.n;
+  unsigned char *pf = pert_pool.data() + (P.o_pert - b->n_dbl * (int64_t)sizeof(double));
+  for (int j = 0; j < N; ++j) pf[j] = std::abs(kv[K.p[j]]) < P.reg ? 1 : 0;
+}
+
+template <class T> int prepare(nqg_batch *b, int threads, size_t smem, int *bps) {
+  return nqg::batch_prepare<T>(threads, smem, bps);
+}
+
+int launch(nqg_batch *b) {
+  if (b->set.qp.precision == NQG_FP32)
+    return nqg::launch_batch<float>(b->args, b->grid, b->threads, b->smem, b->stream);
+  return nqg::launch_batch<double>(b->args, b->grid, b->threads, b->smem, b->stream);
+}
+
+}  // namespace
+
+extern "C" void nqg_batch_default_settings(nqg_batch_settings *s) {
+  if (!s) return;
+  nqg_qp_default_settings(&s->qp);
+  s->qp.eps_abs = 1e-8;
+  s->refine = 0;
+  s->refine_tol = 1e-12;
+  s->threads = 0;
+  s->use_graph = 1;
+}
+
+extern "C" int nqg_batch_create(const nqg_batch_settings *s, nqg_batch **out) {
+  if (!out) return NQG_ERR_ARG;
+  auto *b = new nqg_batch;
+  if (s) b->set = *s;
+  else nqg_batch_default_settings(&b->set);
+  if (b->set.qp.precision != NQG_FP64 && b->set.qp.precision != NQG_FP32) {
+    delete b;
+    return NQG_ERR_ARG;
+  }
+  *out = b;
+  return NQG_OK;
+}
+
+extern "C" int nqg_batch_add(nqg_batch *b, int n, const int *Hp, const int *Hi, const double *Hx, const double *q,
+                             int meq, const int *Ap, const int *Ai, const double *Ax, const double *a, int mineq,
+                             const int *Bp, const int *Bi, const double *Bx, const double *bineq) {
+  if (!b || b->finalized) return NQG_ERR_STATE;
+  if (n <= 0 || !Hp || !Hi || !Hx || !q || meq < 0 || mineq < 0) return NQG_ERR_ARG;
+  if (meq > 0 && (!Ap || !Ai || !Ax || !a)) return NQG_ERR_ARG;
+  if (mineq > 0 && (!Bp || !Bi || !Bx || !bineq)) return NQG_ERR_ARG;
+  HostQP Q;
+  Q.n = n;
+  Q.meq = meq;
+  Q.mineq = mineq;
+  Q.Hp.assign(Hp, Hp + n + 1);
+  Q.Hi.assign(Hi, Hi + Hp[n]);
+  Q.Hx.assign(Hx, Hx + Hp[n]);
+  Q.q.assign(q, q + n);
+  for (int j = 0; j < n; ++j) {
+    if (Hp[j + 1] < Hp[j]) return NQG_ERR_ARG;
+    for (int k = Hp[j]; k < Hp[j + 1]; ++k)
+      if (Hi[k] < j || Hi[k] >= n || (k > Hp[j] && Hi[k] <= Hi[k - 1])) return NQG_ERR_ARG;
+  }
+  auto take = [n](int m, const int *p, const int *ii, const double *x, std::vector<int> &P, std::vector<int> &I,
+                  std::vector<double> &X) {
+    P.assign(p, p + n + 1);
+    I.assign(ii, ii + p[n]);
+    X.assign(x, x + p[n]);
+    for (int j = 0; j < n; ++j)
+      for (int k = p[j]; k < p[j + 1]; ++k)
+        if (ii[k] < 0 || ii[k] >= m || (k > p[j] && ii[k] <= ii[k - 1])) return false;
+    return true;
+  };
+  if (meq > 0) {
+    if (!take(meq, Ap, Ai, Ax, Q.Ap, Q.Ai, Q.Ax)) return NQG_ERR_ARG;
+    Q.b.assign(a, a + meq);
+  } else {
+    Q.Ap.assign(n + 1, 0);
+  }
+  if (mineq > 0) {
+    if (!take(mineq, Bp, Bi, Bx, Q.Cp, Q.Ci, Q.Cx)) return NQG_ERR_ARG;
+    Q.d.assign(bineq, bineq + mineq);
+  } else {
+    Q.Cp.assign(n + 1, 0);
+  }
+  b->qp.push_back(std::move(Q));
+  return (int)b->qp.size() - 1;
+}
+
+extern "C" int nqg_batch_finalize(nqg_batch *b) {
+  if (!b || b->finalized) return NQG_ERR_STATE;
+  const int np = (int)b->qp.size();
+  if (np == 0) return NQG_ERR_ARG;
+  // ---- patterns
+  const int nrelax[3] = {4, 16, 48};
+  const double zrelax[3] = {0.8, 0.1, 0.05};
+  std::unordered_map<uint64_t, std::vector<int>> by_key;
+  for (int i = 0; i < np; ++i) {
+    HostQP &Q = b->qp[i];
+    const uint64_t key = pattern_key(Q);
+    int found = -1;
+    for (int pidx : by_key[key])
+      if (same_pattern(b->qp[b->pats[pidx].rep], Q)) found = pidx;
+    if (found < 0) {
+      HostPattern H;
+      H.rep = i;
+      std::string err = build_pattern(Q, H, nrelax, zrelax);
+      if (!err.empty()) return fail(b, NQG_ERR_SYMBOLIC, err);
+      found = (int)b->pats.size();
+      b->pats.push_back(std::move(H));
+      by_key[key].push_back(found);
+    }
+    Q.pat = found;
+  }
+  // ---- integer pool
+  std::vector<int> ipool;
+  std::vector<BPat> hp;
+  int N_max = 0, nr_max = 1, w_max = 1, xs_max = 0, ss_max = 0, ns_max = 0, mi_max = 0;
+  for (HostPattern &H : b->pats) {
+    BPat &P = H.P;
+    auto put = [&ipool](const std::vector<int> &v) {
+      const int o = (int)ipool.size();
+      ipool.insert(ipool.end(), v.begin(), v.end());
+      ipool.push_back(0);  // keeps every offset valid for empty arrays
+      return o;
+    };
+    P.o_super = put(H.super);
+    P.o_sparent = put(H.sparent);
+    P.o_col2sup = put(H.col2sup);
+    P.o_lpi = put(H.lpi);
+    P.o_lpx = put(H.lpx);
+    P.o_ls0 = put(H.ls0);
+    P.o_perm0 = put(H.perm0);
+    P.o_lvl_ptr = put(H.lvl_ptr);
+    P.o_lvl_sn = put(H.lvl_sn);
+    P.o_pair_ptr = put(H.pair_ptr);
+    P.o_pair_d = put(H.pair_d);
+    P.o_pair_lb = put(H.pair_lb);
+    P.o_pair_ub = put(H.pair_ub);
+    P.o_Rp = put(H.Rp);
+    P.o_Rj = put(H.Rj);
+    P.o_Rq = put(H.Rq);
+    P.o_ent = put(H.ent);
+    P.o_bt_ptr = put(H.bt_ptr);
+    P.o_bt_var = put(H.bt_var);
+    P.o_bt_q = put(H.bt_q);
+    P.o_sn_con = put(H.sn_con);
+    P.o_con_sn = put(H.con_sn);
+    P.o_eq_ptr = put(H.eq_ptr);
+    P.o_eq_var = put(H.eq_var);
+    P.o_eq_q = put(H.eq_q);
+    hp.push_back(P);
+    N_max = std::max(N_max, P.N);
+    nr_max = std::max(nr_max, P.max_nr);
+    w_max = std::max(w_max, P.max_w);
+    xs_max = std::max(xs_max, P.xsize);
+    ss_max = std::max(ss_max, P.ssize);
+    ns_max = std::max(ns_max, P.ns);
+    mi_max = std::max(mi_max, P.mineq);
+  }
+  if (ipool.size() > (size_t)INT32_MAX) return fail(b, NQG_ERR_SIZE, "integer work lists exceed 2^31 entries");
+  // ---- per-problem settings and value layout
+  b->h_probs.assign(np, BProb{});
+  int64_t od = 0, oo = 0, oi = 0;
+  int mr_max = 1;
+  for (int i = 0; i < np; ++i) {
+    const HostQP &Q = b->qp[i];
+    const BPat &P = b->pats[Q.pat].P;
+    BProb &R = b->h_probs[i];
+    R.pat = Q.pat;
+    int rc = problem_settings(b->set, Q, R);
+    if (rc) return fail(b, rc, "unsupported settings (Tuned variant, or more than 10 refinement steps per restart)");
+    mr_max = std::max(mr_max, R.inner);
+    R.ws_n = -1;
+    R.o_kv = od;
+    od += P.nnzK;
+    R.o_q = od;
+    od += Q.n;
+    R.o_b = od;
+    od += Q.meq;
+    R.o_d = od;
+    od += Q.mineq;
+    R.o_x = oo;
+    oo += Q.n;
+    R.o_y = oo;
+    oo += Q.meq;
+    R.o_z = oo;
+    oo += Q.mineq;
+    R.o_as = oi;
+    oi += std::max(Q.mineq, 1);
+  }
+  b->n_dbl = od;
+  int64_t pb = 0;
+  for (int i = 0; i < np; ++i) {
+    b->h_probs[i].o_pert = od * (int64_t)sizeof(double) + pb;
+    pb += b->pats[b->qp[i].pat].P.N;
+  }
+  b->n_pert_bytes = pb;
+  b->n_dout = oo;
+  b->n_iout = oi;
+  b->h_dpool.assign(od, 0.0);
+  std::vector<unsigned char> pert(std::max<int64_t>(pb, 1), 0);
+  for (int i = 0; i < np; ++i) fill_values(b, i, pert);
+  // ---- slot layout (one problem at a time per CTA)
+  const size_t ts = b->set.qp.precision == NQG_FP32 ? sizeof(float) : sizeof(double);
+  nqg::BSlot sl{};
+  int64_t off = 0;
+  auto seg = [&off](int64_t bytes) {
+    const int64_t o = off;
+    off += (bytes + 255) / 256 * 256;
+    return o;
+  };
+  sl.o_L = seg((int64_t)xs_max * ts);
+  sl.o_D = seg((int64_t)2 * N_max * ts);
+  sl.o_ls = seg((int64_t)ss_max * 4);
+  sl.o_perm = seg((int64_t)N_max * 4);
+  sl.o_iperm = seg((int64_t)N_max * 4);
+  sl.o_lperm = seg((int64_t)N_max * 4);
+  sl.o_mark = seg(ns_max);
+  sl.o_piv = seg(ns_max);
+  sl.o_act = seg(std::max(mi_max, 1));
+  sl.o_alist = seg((int64_t)std::max(mi_max, 1) * 4);
+  sl.o_rhs = seg((int64_t)N_max * 8);
+  sl.o_sol = seg((int64_t)N_max * 8);
+  sl.o_r = seg((int64_t)N_max * 8);
+  sl.o_w = seg((int64_t)N_max * 8);
+  sl.o_tmp = seg((int64_t)N_max * 8);
+  sl.o_V = seg((int64_t)(mr_max + 1) * N_max * 8);
+  sl.o_Z = seg((int64_t)mr_max * N_max * ts);
+  sl.bytes = off;
+  // ---- launch shape
+  BQ_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  int dev = 0;
+  BQ_CUDA(cudaGetDevice(&dev));
+  BQ_CUDA(cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, dev));
+  b->threads = b->set.threads > 0 ? b->set.threads : 128;
+  if (b->threads % 32 || b->threads > 256) return fail(b, NQG_ERR_ARG, "threads must be a multiple of 32, at most 256");
+  b->smem = nqg::batch_smem_bytes(N_max, nr_max, w_max, b->threads, ts);
+  if (b->smem > 200 * 1024) return fail(b, NQG_ERR_SIZE, "largest pattern exceeds the batched solver's shared memory");
+  int bps = 0;
+  int rc = b->set.qp.precision == NQG_FP32 ? prepare<float>(b, b->threads, b->smem, &bps)
+                                          : prepare<double>(b, b->threads, b->smem, &bps);
+  if (rc || bps <= 0) return fail(b, NQG_ERR_CUDA, "no resident CTA fits the batched kernel");
+  b->blocks_per_sm = bps;
+  b->grid = std::min(np, bps * b->num_sms);
+  // queue order: largest problems first (longest-processing-time order)
+  std::vector<int> order(np);
+  for (int i = 0; i < np; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    const BPat &A = b->pats[b->qp[x].pat].P, &B = b->pats[b->qp[y].pat].P;
+    const double cx = (double)A.xsize * (A.mineq + 1), cy = (double)B.xsize * (B.mineq + 1);
+    return cx > cy;
+  });
+  // ---- device
+  BQ_CUDA(cudaMalloc(&b->d_pats, hp.size() * sizeof(BPat)));
+  BQ_CUDA(cudaMemcpy(b->d_pats, hp.data(), hp.size() * sizeof(BPat), cudaMemcpyHostToDevice));
+  BQ_CUDA(cudaMalloc(&b->d_probs, np * sizeof(BProb)));
+  BQ_CUDA(cudaMalloc(&b->d_ipool, ipool.size() * sizeof(int)));
+  BQ_CUDA(cudaMemcpy(b->d_ipool, ipool.data(), ipool.size() * sizeof(int), cudaMemcpyHostToDevice));
+  BQ_CUDA(cudaMalloc(&b->d_dpool, od * sizeof(double) + std::max<int64_t>(pb, 1)));
+  BQ_CUDA(cudaMemcpy(b->d_dpool, b->h_dpool.data(), od * sizeof(double), cudaMemcpyHostToDevice));
+  BQ_CUDA(cudaMemcpy(reinterpret_cast<unsigned char *>(b->d_dpool) + od * sizeof(double), pert.data(), pb,
+                     cudaMemcpyHostToDevice));
+  BQ_CUDA(cudaMalloc(&b->d_dout, std::max<int64_t>(oo, 1) * sizeof(double)));
+  BQ_CUDA(cudaMemset(b->d_dout, 0, std::max<int64_t>(oo, 1) * sizeof(double)));
+  BQ_CUDA(cudaMalloc(&b->d_iout, std::max<int64_t>(oi, 1) * sizeof(int)));
+  BQ_CUDA(cudaMalloc(&b->d_res, np * sizeof(BResult)));
+  BQ_CUDA(cudaMalloc(&b->d_order, np * sizeof(int)));
+  BQ_CUDA(cudaMemcpy(b->d_order, order.data(), np * sizeof(int), cudaMemcpyHostToDevice));
+  BQ_CUDA(cudaMalloc(&b->d_head, sizeof(int)));
+  BQ_CUDA(cudaMalloc(&b->d_slots, (size_t)b->grid * sl.bytes));
+  BQ_CUDA(cudaMemcpy(b->d_probs, b->h_probs.data(), np * sizeof(BProb), cudaMemcpyHostToDevice));
+  BQ_CUDA(cudaEventCreate(&b->e0));
+  BQ_CUDA(cudaEventCreate(&b->e1));
+  nqg::BArgs &A = b->args;
+  A.pats = b->d_pats;
+  A.probs = b->d_probs;
+  A.ipool = b->d_ipool;
+  A.dpool = b->d_dpool;
+  A.dout = b->d_dout;
+  A.iout = b->d_iout;
+  A.res = b->d_res;
+  A.order = b->d_order;
+  A.head = b->d_head;
+  A.nprob = np;
+  A.slots = b->d_slots;
+  A.slot = sl;
+  A.refine = b->set.refine;
+  A.refine_tol = b->set.refine_tol;
+  A.mr_max = mr_max;
+  A.N_max = N_max;
+  A.w_max = w_max;
+  A.nr_max = nr_max;
+  b->finalized = true;
+  return NQG_OK;
+}
+
+extern "C" int nqg_batch_set_vectors(nqg_batch *b, const double *q_all, const double *beq_all,
+                                     const double *d_all) {
+  // New q / b / d for every problem, concatenated in problem order (any may
+  // be NULL: unchanged).
+  if (!b || !b->finalized) return NQG_ERR_STATE;
+  const int np = (int)b->qp.size();
+  int64_t oq = 0, ob = 0, odd = 0;
+  for (int i = 0; i < np; ++i) {
+    HostQP &Q = b->qp[i];
+    const BProb &P = b->h_probs[i];
+    if (q_all) {
+      std::copy(q_all + oq, q_all + oq + Q.n, Q.q.begin());
+      BQ_CUDA(cudaMemcpyAsync(b->d_dpool + P.o_q, q_all + oq, Q.n * sizeof(double), cudaMemcpyHostToDevice,
+                              b->stream));
+    }
+    if (beq_all && Q.meq) {
+      std::copy(beq_all + ob, beq_all + ob + Q.meq, Q.b.begin());
+      BQ_CUDA(cudaMemcpyAsync(b->d_dpool + P.o_b, beq_all + ob, Q.meq * sizeof(double), cudaMemcpyHostToDevice,
+                              b->stream));
+    }
+    if (d_all && Q.mineq) {
+      std::copy(d_all + odd, d_all + odd + Q.mineq, Q.d.begin());
+      BQ_CUDA(cudaMemcpyAsync(b->d_dpool + P.o_d, d_all + odd, Q.mineq * sizeof(double), cudaMemcpyHostToDevice,
+                              b->stream));
+    }
+    oq += Q.n;
+    ob += Q.meq;
+    odd += Q.mineq;
+  }
+  BQ_CUDA(cudaStreamSynchronize(b->stream));
+  return NQG_OK;
+}
+
+extern "C" int nqg_batch_set_warm_start(nqg_batch *b, int i, int n_as, const int *as) {
+  // Proposed active set of problem i for the next solve (n_as < 0: cold start).
+  if (!b || !b->finalized) return NQG_ERR_STATE;
+  if (i < 0 || i >= (int)b->qp.size()) return NQG_ERR_ARG;
+  HostQP &Q = b->qp[i];
+  BProb &P = b->h_probs[i];
+  if (n_as < 0) {
+    P.ws_n = -1;
+  } else {
+    if (n_as > Q.mineq || (n_as > 0 && !as)) return NQG_ERR_ARG;
+    for (int t = 0; t < n_as; ++t)
+      if (as[t] < 0 || as[t] >= Q.mineq) return NQG_ERR_ARG;
+    P.ws_n = n_as;
+    if (n_as > 0)
+      BQ_CUDA(cudaMemcpyAsync(b->d_iout + P.o_as, as, n_as * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  }
+  BQ_CUDA(cudaMemcpyAsync(b->d_probs + i, &P, sizeof(BProb), cudaMemcpyHostToDevice, b->stream));
+  BQ_CUDA(cudaStreamSynchronize(b->stream));
+  return NQG_OK;
+}
+
+extern "C" int nqg_batch_solve_async(nqg_batch *b) {
+  // Enqueues one solve of every problem on the batch's stream (captured once
+  // into a CUDA graph of the queue reset and the persistent kernel).
+  if (!b || !b->finalized) return NQG_ERR_STATE;
+  if (b->set.use_graph) {
+    if (!b->gexec) {
+      BQ_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      cudaMemsetAsync(b->d_head, 0, sizeof(int), b->stream);
+      int rc = launch(b);
+      cudaGraph_t g = nullptr;
+      cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
+      if (rc || ec != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(b, NQG_ERR_CUDA, "graph capture of the batched solve failed");
+      }
+      b->graph = g;
+      BQ_CUDA(cudaGraphInstantiate(&b->gexec, g, 0));
+    }
+    BQ_CUDA(cudaGraphLaunch(b->gexec, b->stream));
+  } else {
+    BQ_CUDA(cudaMemsetAsync(b->d_head, 0, sizeof(int), b->stream));
+    int rc = launch(b);
+    if (rc) return fail(b, rc, "launch of the batched kernel failed");
+  }
+  return NQG_OK;
+}
+
+extern "C" int nqg_batch_solve(nqg_batch *b) {
+  if (!b || !b->finalized) return NQG_ERR_STATE;
+  BQ_CUDA(cudaEventRecord(b->e0, b->stream));
+  int rc = nqg_batch_solve_async(b);
+  if (rc) return rc;
+  BQ_CUDA(cudaEventRecord(b->e1, b->stream));
+  BQ_CUDA(cudaStreamSynchronize(b->stream));
+  float ms = 0.f;
+  BQ_CUDA(cudaEventElapsedTime(&ms, b->e0, b->e1));
+  b->last_ms = ms;
+  return NQG_OK;
+}
+
+extern "C" int nqg_batch_get(nqg_batch *b, int i, double *x, double *y, double *z, int *active_set,
+                             nqg_qp_result *res) {
+  if (!b || !b->finalized) return NQG_ERR_STATE;
+  if (i < 0 || i >= (int)b->qp.size()) return NQG_ERR_ARG;
+  const HostQP &Q = b->qp[i];
+  const BProb &P = b->h_probs[i];
+  BResult R{};
+  BQ_CUDA(cudaMemcpy(&R, b->d_res + i, sizeof(BResult), cudaMemcpyDeviceToHost));
+  if (x) BQ_CUDA(cudaMemcpy(x, b->d_dout + P.o_x, Q.n * sizeof(double), cudaMemcpyDeviceToHost));
+  if (y && Q.meq) BQ_CUDA(cudaMemcpy(y, b->d_dout + P.o_y, Q.meq * sizeof(double), cudaMemcpyDeviceToHost));
+  if (z && Q.mineq) BQ_CUDA(cudaMemcpy(z, b->d_dout + P.o_z, Q.mineq * sizeof(double), cudaMemcpyDeviceToHost));
+  if (active_set && Q.mineq)
+    BQ_CUDA(cudaMemcpy(active_set, b->d_iout + P.o_as, Q.mineq * sizeof(int), cudaMemcpyDeviceToHost));
+  if (res) {
+    res->status = R.status;
+    res->num_iter = R.num_iter;
+    res->active_size = R.active_size;
+    res->objective = R.objective;
+    res->primal_obj = R.primal_obj;
+    res->dual_obj = R.dual_obj;
+    res->lag_res = R.lag_res;
+    res->cons_sat_norm = R.cons_sat_norm;
+    res->non_negativity_infn = R.non_negativity_infn;
+    res->complementarity_infn = R.complementarity_infn;
+    res->total_seconds = b->last_ms * 1e-3;
+    res->factor_seconds = 0.0;
+  }
+  return R.flags & nqg::ST_NONFINITE ? NQG_WARN_NONFINITE : (R.flags & nqg::ST_ZERO_PIVOT ? NQG_WARN_ZERO_PIVOT : NQG_OK);
+}
+
+extern "C" int nqg_batch_get_all(nqg_batch *b, double *x_all, double *y_all, double *z_all, nqg_batch_stats *stats) {
+  // Every problem's x / y / z, concatenated in problem order (any may be NULL),
+  // and per-problem statistics (nprob entries).
+  if (!b || !b->finalized) return NQG_ERR_STATE;
+  const int np = (int)b->qp.size();
+  std::vector<double> out(std::max<int64_t>(b->n_dout, 1));
+  BQ_CUDA(cudaMemcpyAsync(out.data(), b->d_dout, b->n_dout * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  std::vector<BResult> R(np);
+  BQ_CUDA(cudaMemcpyAsync(R.data(), b->d_res, np * sizeof(BResult), cudaMemcpyDeviceToHost, b->stream));
+  BQ_CUDA(cudaStreamSynchronize(b->stream));
+  int64_t ox = 0, oy = 0, oz = 0;
+  for (int i = 0; i < np; ++i) {
+    const HostQP &Q = b->qp[i];
+    const BProb &P = b->h_probs[i];
+    if (x_all) std::copy(out.begin() + P.o_x, out.begin() + P.o_x + Q.n, x_all + ox);
+    if (y_all) std::copy(out.begin() + P.o_y, out.begin() + P.o_y + Q.meq, y_all + oy);
+    if (z_all) std::copy(out.begin() + P.o_z, out.begin() + P.o_z + Q.mineq, z_all + oz);
+    ox += Q.n;
+    oy += Q.meq;
+    oz += Q.mineq;
+    if (stats) {
+      nqg_batch_stats &s = stats[i];
+      s.status = R[i].status;
+      s.num_iter = R[i].num_iter;
+      s.active_size = R[i].active_size;
+      s.flags = R[i].flags;
+      s.refine_steps = R[i].refine_steps;
+      s.solves = R[i].solves;
+      s.warm_dropped = R[i].warm_dropped;
+      s.objective = R[i].objective;
+      s.lag_res = R[i].lag_res;
+      s.cons_sat_norm = R[i].cons_sat_norm;
+      s.non_negativity_infn = R[i].non_negativity_infn;
+      s.complementarity_infn = R[i].complementarity_infn;
+    }
+  }
+  return NQG_OK;
+}
+
+extern "C" int nqg_batch_get_info(const nqg_batch *b, nqg_batch_info *info) {
+  if (!b || !info) return NQG_ERR_ARG;
+  info->nprob = (int)b->qp.size();
+  info->npatterns = (int)b->pats.size();
+  info->grid = b->grid;
+  info->threads = b->threads;
+  info->blocks_per_sm = b->blocks_per_sm;
+  info->smem_bytes = (int64_t)b->smem;
+  info->slot_bytes = b->args.slot.bytes;
+  info->last_ms = b->last_ms;
+  return NQG_OK;
+}
+
+extern "C" int nqg_batch_get_stream(const nqg_batch *b, void **stream) {
+  if (!b || !stream || !b->finalized) return NQG_ERR_ARG;
+  *stream = b->stream;
+  return NQG_OK;
+}
+
+extern "C" const char *nqg_batch_last_error(const nqg_batch *b) { return b ? b->last_error.c_str() : ""; }
+
+extern "C" int nqg_batch_destroy(nqg_batch *b) {
+  if (!b) return NQG_ERR_ARG;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  free_device(b);
+  if (b->e0) cudaEventDestroy(b->e0);
+  if (b->e1) cudaEventDestroy(b->e1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return NQG_OK;
+}

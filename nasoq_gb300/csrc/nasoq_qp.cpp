@@ -13,6 +13,7 @@
 #include <limits>
 
 #include "nasoq_gb300.h"
+#include "qp_rules.hpp"
 
 namespace nasoq {
 
@@ -105,17 +106,7 @@ static double inf_norm(size_t n, const double *v) {
   return m;
 }
 
-static double frob_lower(const CSC *H) {
-  double frob = 0, s = 0;
-  for (size_t j = 0; j < H->ncol; ++j)
-    for (int q = H->p[j]; q < H->p[j + 1]; ++q) {
-      int i = H->i[q];
-      s = std::abs(H->x[q]);
-      if (i == (int)j) frob += s * s;
-      else if (i > (int)j) frob += 2 * s * s;
-    }
-  return std::isfinite(s) ? std::sqrt(frob) : 0.0;
-}
+static double frob_lower(const CSC *H) { return nqg::qp_frob_lower((int)H->ncol, H->p, H->i, H->x); }
 
 // ---- construction ---------------------------------------------------------
 Nasoq::Nasoq(size_t H_size, int *Hp, int *Hi, double *Hx, double *q_in, size_t B_row, size_t B_col, int *Bp, int *Bi,
@@ -228,48 +219,11 @@ void Nasoq::default_setting() {
 void Nasoq::auto_perturbation2(size_t dim, size_t total_nnz, double H_norm2, double range, int n_ineq,
                                double ineq_ratio, double acc_thresh, double &reg, int &outer, int &inner,
                                double &tol) {
-  // reference :320-371
-  reg = std::pow(10, -8);
-  int iter_low = 2, iter_high = 9, iter_large = 0;
-  if (acc_thresh >= 1e-3) {
-    iter_low /= 2;
-    iter_high /= 2;
-  } else if (acc_thresh < 1e-8) {
-    iter_low *= 2;
-    iter_large *= 2;
-    iter_large += 1;
-  }
-  inner = outer = iter_large;
-  if (total_nnz < 3e5) {
-    inner = outer = iter_low;
-    tol = 1e-10;
-    if (H_norm2 < 1) {
-      reg = std::pow(10, -7);
-      inner = outer = iter_low;
-      tol = 1e-15;
-    } else if (ineq_ratio > 2.5) {
-      reg = std::pow(10, -10);
-      tol = 1e-16;
-      inner = outer = iter_low;
-    } else if (dim > 1e4 && n_ineq >= 1e4) {
-      reg = std::pow(10, -11);
-      inner = outer = iter_high;
-      tol = 1e-15;
-    }
-  } else if (H_norm2 < 1) {
-    reg = std::pow(10, -7);
-    inner = outer = 2;
-    tol = 1e-15;
-  }
+  nqg::qp_auto_perturbation2(dim, total_nnz, H_norm2, range, n_ineq, ineq_ratio, acc_thresh, reg, outer, inner, tol);
 }
 
 void Nasoq::determine_iterations(size_t total_nnz, double acc_thresh, int &outer, int &inner) {
-  // reference :373-395
-  if (acc_thresh >= 1e-3) inner = outer = 0;
-  else if (acc_thresh <= 1e-4 && acc_thresh > 1e-7) inner = outer = 1;
-  else if (acc_thresh <= 1e-7 && acc_thresh > 1e-10) inner = outer = 2;
-  else inner = outer = 4;
-  if (total_nnz <= 20000) inner = outer = 3;
+  nqg::qp_determine_iterations(total_nnz, acc_thresh, outer, inner);
 }
 
 int Nasoq::symbolic_QP() {
@@ -298,6 +252,13 @@ int Nasoq::symbolic_QP() {
     diag_perturb = H_norm2 < 1 ? std::pow(10, -7) : std::pow(10, -9);
   } else {
     outer_iter_ref = inner_iter_ref = max_iter;
+  }
+  // An FP32 factorization is only the preconditioner of the FP64 refinement:
+  // without refinement its solutions carry FP32 rounding into every
+  // active-set decision, so at least two restarts of two steps run.
+  if (gpu_precision) {
+    outer_iter_ref = std::max(outer_iter_ref, 2);
+    inner_iter_ref = std::max(inner_iter_ref, 2);
   }
   ss->tol_abs = ss->tol_rel = stop_tol;
   ss->req_ref_iter = outer_iter_ref;

@@ -282,3 +282,59 @@ def sym_indefinite(seed: int, n: int, density: float, zero_diag: bool = True) ->
             if rng.random() < density:
                 rows.append(i); cols.append(j); vals.append(rng.standard_normal())
     return csc_from_coo(n, n, rows, cols, vals)
+
+
+def mpc_batch_specs(count: int, seed: int = 0, horizons=(10, 100)):
+    """(seed, horizon) of each problem of an uneven MPC batch: horizons drawn
+    uniformly from [horizons[0], horizons[1]], problem seeds seed*100003+i.
+    count=4096 with horizons (10, 100) is the batched MPC workload."""
+    rng = np.random.default_rng(seed)
+    hz = rng.integers(horizons[0], horizons[1] + 1, size=count)
+    return [(seed * 100003 + i, int(hz[i])) for i in range(count)]
+
+
+def mpc_batch(count: int, seed: int = 0, horizons=(10, 100)):
+    """The QPs of mpc_batch_specs (see qp_mpc)."""
+    return [qp_mpc(s, h) for s, h in mpc_batch_specs(count, seed, horizons)]
+
+
+@dataclass
+class ParametricQP:
+    """min 1/2 x'Hx + (P theta)'x  s.t.  A x = b,  C x <= d0 + S theta."""
+
+    base: QP
+    P: np.ndarray   # n x p
+    d0: np.ndarray  # mineq
+    S: np.ndarray   # mineq x p
+
+    def q_of(self, theta):
+        return self.P @ theta
+
+    def d_of(self, theta):
+        return self.d0 + self.S @ theta
+
+
+def mpc_parametric(seed: int = 0, horizon: int = 50, p: int = 32, scale: float = 0.1) -> ParametricQP:
+    """Parametric QP family on the MPC structure (qp_mpc at the given horizon;
+    horizon 50: n = 450, 300 equalities, 900 inequalities): q = P theta and
+    d = d0 + S theta, theta in R^p ~ N(0, I), P dense N(0, scale) (standard
+    deviation `scale`).  S moves each variable's box as a whole: a dense
+    N(0, scale) shift s_v = (G theta)_v enters the two rows of the box of
+    variable v with opposite signs (x_v <= ub + s_v, -x_v <= ub - s_v), so the
+    box [-ub + s_v, ub + s_v] is never empty; independent perturbations of the
+    two rows would make some instances infeasible."""
+    base = qp_mpc(seed, horizon)
+    rng = np.random.default_rng(seed + 7919)
+    n = base.n
+    P = rng.normal(0.0, scale, (n, p))
+    G = rng.normal(0.0, scale, (n, p))
+    S = np.empty((base.C.nrow, p))
+    S[0::2] = G
+    S[1::2] = -G
+    return ParametricQP(base, P, base.d.copy(), S)
+
+
+def qp_checksum(qp: QP) -> float:
+    """Sum of |entries| of every input array: detects a change of a generator."""
+    return float(sum(np.abs(np.asarray(a, np.float64)).sum()
+                     for a in (qp.H.x, qp.q, qp.A.x, qp.b, qp.C.x, qp.d)))
