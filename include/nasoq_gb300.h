@@ -265,7 +265,9 @@ typedef struct nqg_batch_settings {
                            1: adaptive flexible GMRES to refine_tol */
   double refine_tol;    /* refine == 1: stop once ||b - Kx||_2 <= refine_tol * ||b||_2 */
   int threads;          /* CTA size, a multiple of 32 up to 256 (0: 128) */
-  int use_graph;        /* 1: the queue reset and the kernel are replayed from a captured CUDA graph */
+  int use_graph;        /* 1: the queue resets and the kernels are replayed from a captured CUDA graph */
+  int stage;            /* 1: a problem's factor and row lists stay in shared memory when they fit
+                           (problems grouped into shared-memory tiers, one launch per tier) */
 } nqg_batch_settings;
 
 typedef struct nqg_batch_stats {
@@ -306,6 +308,16 @@ int nqg_batch_get(nqg_batch *b, int i, double *x, double *y, double *z, int *act
 int nqg_batch_get_all(nqg_batch *b, double *x_all, double *y_all, double *z_all, nqg_batch_stats *stats);
 int nqg_batch_get_info(const nqg_batch *b, nqg_batch_info *info);
 int nqg_batch_get_stream(const nqg_batch *b, void **stream);
+/* Per-phase SM-cycle counters of the solves (summed over problems), for
+ * profiling: on = 1 enables them for the next solves.  get_profile copies up
+ * to n counters and resets them: [0] total, [1] set-up and first solve,
+ * [2] partial refactorizations, [3] triangular-solve applications, [4] SpMVs,
+ * [5] refinement (solves included), [6] entering-constraint selection,
+ * [7] steps and edits, [8] supernodes factored, [9] active-set iterations,
+ * and inside [3]: [10] forward sweeps of wide levels, [11] of narrow levels,
+ * [12] diagonal solves, [13] backward sweeps, [14] gathers and scatters. */
+int nqg_batch_set_profiling(nqg_batch *b, int on);
+int nqg_batch_get_profile(nqg_batch *b, unsigned long long *counters, int n);
 const char *nqg_batch_last_error(const nqg_batch *b);
 int nqg_batch_destroy(nqg_batch *b);
 

@@ -69,7 +69,7 @@ class QPResult(C.Structure):
 
 class BatchSettings(C.Structure):
     _fields_ = [("qp", QPSettings), ("refine", C.c_int), ("refine_tol", C.c_double), ("threads", C.c_int),
-                ("use_graph", C.c_int)]
+                ("use_graph", C.c_int), ("stage", C.c_int)]
 
 
 class BatchStats(C.Structure):
@@ -134,7 +134,7 @@ def lib():
     L.nqg_batch_default_settings.argtypes = [C.POINTER(BatchSettings)]
     L.nqg_batch_default_settings.restype = None
     L.nqg_batch_create.argtypes = [C.POINTER(BatchSettings), C.POINTER(C.c_void_p)]
-    L.nqg_batch_add.argtypes = [C.c_int] * 0 + [C.c_void_p, C.c_int] + [C.c_void_p] * 4 + [C.c_int] + \
+    L.nqg_batch_add.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 4 + [C.c_int] + \
         [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 4
     L.nqg_batch_finalize.argtypes = [C.c_void_p]
     L.nqg_batch_set_vectors.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -149,6 +149,8 @@ def lib():
     L.nqg_batch_last_error.argtypes = [C.c_void_p]
     L.nqg_batch_last_error.restype = C.c_char_p
     L.nqg_batch_destroy.argtypes = [C.c_void_p]
+    L.nqg_batch_set_profiling.argtypes = [C.c_void_p, C.c_int]
+    L.nqg_batch_get_profile.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
     _lib = L
     return L
 
@@ -467,6 +469,18 @@ class QPBatch:
         st = (BatchStats * len(self.sizes))()
         self._raise(lib().nqg_batch_get_all(self._h, _ptr(x), _ptr(y), _ptr(z), C.cast(st, C.c_void_p)), "get all")
         return x[:self.n_tot], y[:self.meq_tot], z[:self.mineq_tot], st
+
+    PROFILE_PHASES = ("total", "setup", "refactor", "precond", "spmv", "refine", "select", "update",
+                      "supernodes", "iterations", "fwd_wide", "fwd_narrow", "diag", "bwd", "gather")
+
+    def set_profiling(self, on=True):
+        self._raise(lib().nqg_batch_set_profiling(self._h, 1 if on else 0), "set profiling")
+
+    def profile(self):
+        """Per-phase SM cycles summed over problems (and counts), then reset."""
+        v = (C.c_ulonglong * len(self.PROFILE_PHASES))()
+        self._raise(lib().nqg_batch_get_profile(self._h, C.cast(v, C.c_void_p), len(v)), "get profile")
+        return dict(zip(self.PROFILE_PHASES, list(v)))
 
     def info(self) -> BatchInfo:
         i = BatchInfo()

@@ -5,18 +5,24 @@
 // 18-277), masked supernodal solves and GMRES refinement all run on the
 // device; the host only fills the work queue.
 //
-// Per problem, in the CTA's scratch slot:
+// Per problem, in the CTA's scratch slot (or, for the factor and its row
+// lists, in shared memory when they fit the launch's staging space):
 //  * the supernodal factor in the reference's BCSC layout (column-major
 //    nrow x w blocks, D as diagonal + 2x2 sub-diagonal halves), the composed
 //    ordering perm/iperm and the row lists, renamed after Bunch-Kaufman
 //    pivoting as the reference's row_reordering does (without re-sorting the
-//    renamed rows: every consumer maps them through the target's row list);
+//    renamed rows: every consumer maps them through the target's row list).
+//    Once a supernode is factored, the unit lower triangle of its diagonal
+//    block is replaced by its inverse, which is all the solves need of it;
 //  * the active set as a per-constraint flag.  Hidden (inactive) constraint
 //    columns are width-1 supernodes whose entries read as zero; the
 //    reference's hidden-column tree edits (linear_solver_wrapper.cpp:770-907)
-//    become a visibility test per supernode, and the supernodes to refactor
-//    after an edit are those on the elimination-tree paths from the edited
-//    column and its variables to the root;
+//    become a visibility flag per supernode plus, per supernode, a bit mask
+//    of its active constraint-column descendants, and the supernodes to
+//    refactor after an edit are those on the elimination-tree paths from the
+//    edited column and its variables to the root;
+//  * two copies of K's values in CSR order (factorization values with the
+//    regularization, refinement values without it), edited in place;
 //  * the KKT vectors in the original numbering; the triangular solves gather
 //    them into shared memory in the factor's order.
 #include <cuda_runtime.h>
@@ -35,36 +41,74 @@ constexpr int BT_MAX_THREADS = 256;
 constexpr int MR_CAP = BATCH_MR_CAP;  // Krylov steps per restart held in shared memory
 
 template <class T> struct Ctx {
-  // pattern
-  int n, meq, mineq, N, base, ns, nlev;
-  const int *super, *sparent, *col2sup, *lpi, *lpx, *lvl_ptr, *lvl_sn, *pair_ptr, *pair_d, *pair_lb, *pair_ub;
-  const int *Rp, *Rj, *Rq, *ent, *bt_ptr, *bt_var, *bt_q, *sn_con, *con_sn, *eq_ptr, *eq_var, *eq_q;
+  // pattern (read-only)
+  int n, meq, mineq, N, base, ns, nlev, nnzR, cmask_ok;
+  const int *__restrict__ super, *__restrict__ sparent, *__restrict__ col2sup, *__restrict__ lpi, *__restrict__ lpx;
+  const int *__restrict__ lvl_ptr, *__restrict__ lvl_sn, *__restrict__ lev;
+  const int *__restrict__ Rp, *__restrict__ Rj, *__restrict__ Rq, *__restrict__ ent;
+  const int *__restrict__ bt_ptr, *__restrict__ bt_var, *__restrict__ bt_q, *__restrict__ bt_rpos;
+  const int *__restrict__ sn_con, *__restrict__ con_sn, *__restrict__ eq_ptr, *__restrict__ eq_var,
+      *__restrict__ eq_q;
+  const int4 *__restrict__ snrec;  // 2 per supernode: {c0, w, nrow, value offset}, {row-list offset, pairs}
+  const int4 *__restrict__ prec;   // per pair: {descendant, lb, ub, descendant's row-list offset}
+  const int *__restrict__ con_ptr, *__restrict__ con_tgt;
   // problem
-  const double *kv, *q, *bq, *dq;
-  const uint8_t *pert;
-  double reg;
+  const double *__restrict__ kv, *__restrict__ q, *__restrict__ bq, *__restrict__ dq;
+  const uint8_t *__restrict__ pert;
+  double reg, reg32;
   // slot
   T *L, *D;
-  int *ls, *perm, *iperm, *lperm, *alist;
-  uint8_t *mark, *piv, *act;
+  int *ls, *perm, *iperm, *lperm, *alist, *vlist, *mlist;
+  uint8_t *mark, *piv;
+  double *Fv, *Rv;  // factorization / refinement values of K in CSR order
+  unsigned long long *cmask;  // per supernode: active constraint-column descendants (bit = pair - pair_mid)
   double *rhs, *sol, *r, *w, *V, *tmp;
   T *Z;
   // shared memory
   int *map;
-  T *xs, *B, *rowbuf, *Dsm, *Esm;
+  T *xs, *B, *rowbuf, *Dsm, *Esm, *Binv;
   int *lp;
+  uint8_t *vis;  // per supernode: visible (structural, or the column of an active constraint)
+  uint8_t *act;  // per constraint: active
+  int *vlvl;     // visible supernodes of each level: vlist[vlvl[l] .. vlvl[l+1])
+  int *nmark;    // length of mlist
   double *red;   // 32 doubles
   int *redi;     // 32 ints
   int *status;   // device status bits of this problem
+  unsigned long long *cyc;  // per-phase SM cycles of this CTA (profiling), or null
 };
+
+// Counters of nqg_batch_get_profile.
+enum { PH_TOTAL, PH_INIT, PH_FACTOR, PH_PRECOND, PH_SPMV, PH_REFINE, PH_SELECT, PH_UPDATE, PH_SN, PH_ITER,
+       PH_FWD_WIDE, PH_FWD_NARROW, PH_DIAG, PH_BWD, PH_GATHER, PH_N };
+static_assert(PH_N <= BATCH_PROFILE_COUNTERS, "profile counters");
+#define BQ_T0(c) const long long t0_ = (c).cyc ? clock64() : 0
+#define BQ_T1(c, ph) \
+  if ((c).cyc && threadIdx.x == 0) (c).cyc[ph] += (unsigned long long)(clock64() - t0_)
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 __device__ __forceinline__ int warp_id() { return threadIdx.x >> 5; }
 __device__ __forceinline__ int num_warps() { return blockDim.x >> 5; }
 
-template <class T> __device__ __forceinline__ bool visible(const Ctx<T> &c, int s) {
-  const int k = c.sn_con[s];
-  return k < 0 || c.act[k];
+template <class T> __device__ __forceinline__ bool visible(const Ctx<T> &c, int s) { return c.vis[s] != 0; }
+
+// Calls f(pair) for every descendant pair of s whose descendant is visible:
+// the structural ones, then the active constraint columns (bit mask, or a
+// scan when a supernode has more than 64 of them).
+template <class T, class F> __device__ __forceinline__ void for_visible_pairs(const Ctx<T> &c, int s, int pp, int pm,
+                                                                              int pe, F &&f) {
+  for (int pq = pp; pq < pm; ++pq) f(pq);
+  if (c.cmask_ok) {
+    unsigned long long m = c.cmask[s];
+    while (m) {
+      const int b = __ffsll((long long)m) - 1;
+      m &= m - 1ull;
+      f(pm + b);
+    }
+  } else {
+    for (int pq = pm; pq < pe; ++pq)
+      if (c.vis[c.prec[pq].x]) f(pq);
+  }
 }
 
 // Block-wide sum in a fixed order (per-thread strided partials, then a tree):
@@ -153,16 +197,26 @@ __device__ void block_select(double &v, int &idx, bool sel_max, double *red, int
   __syncthreads();
 }
 
+
 // ---- values ---------------------------------------------------------------
 // Factorization value of lower-CSC entry vq: inactive constraint entries read
 // as zero (the reference zeroes them in its ordered matrix), perturbed
 // diagonals as the regularization (find_perturbation,
 // linear_solver_wrapper.cpp:352-363).
+//
+// An FP32 factor also gets a sign-keeping floor reg32 on its diagonal: pivots
+// as small as the 1e-9 regularization create element growth of ~1e9 under
+// Bunch-Kaufman restricted to supernode diagonal blocks, beyond what FP32
+// carries; the factor is only the preconditioner of the FP64 refinement,
+// whose matrix keeps the reference's values.
 template <class T> __device__ __forceinline__ double fact_val(const Ctx<T> &c, int vq) {
   const int e = c.ent[vq];
   double v = c.kv[vq];
   if (e >= 0) return c.act[e] ? v : 0.0;
-  if (e <= -2 && c.pert[-2 - e]) return c.reg;
+  if (e <= -2) {
+    if (c.pert[-2 - e]) v = c.reg;
+    if (sizeof(T) == 4 && fabs(v) < c.reg32) v = v < 0.0 ? -c.reg32 : c.reg32;
+  }
   return v;
 }
 // Refinement value: perturbed diagonals read as zero (set_diags(0),
@@ -175,6 +229,85 @@ template <class T> __device__ __forceinline__ double ref_val(const Ctx<T> &c, in
   return v;
 }
 
+// Panel rows [w, nr) of the supernode block B (ld nr): columns permuted by
+// the pivot order, solved with the unit lower L11^T, scaled by D^-1 (1x1:
+// times 1/d; 2x2: Cramer's rule, the arithmetic of blocked_2by2_solver,
+// Sym_BLAS.cpp:492-529).  Warp 0, one lane per row, rows staged in rowbuf
+// (w x 32).
+template <class T> __device__ void panel_rows_warp0(Ctx<T> &c, T *B, int nr, int w, bool permute) {
+  if (warp_id() != 0) return;
+  const int lane = lane_id();
+  T *rb = c.rowbuf;
+  const T *D = c.Dsm, *E = c.Esm;
+  for (int r0 = w; r0 < nr; r0 += 32) {
+    const int r = r0 + lane;
+    if (r < nr) {
+      for (int j = 0; j < w; ++j) rb[j * 32 + lane] = B[r + (size_t)(permute ? c.lp[j] : j) * nr];
+      for (int j = 0; j < w; ++j) {
+        T x = rb[j * 32 + lane];
+        for (int t = 0; t < j; ++t) x -= rb[t * 32 + lane] * B[j + (size_t)t * nr];
+        rb[j * 32 + lane] = x;
+      }
+      for (int j = 0; j < w; ++j) {
+        if (E[j] == T(0) || j + 1 >= w) {
+          B[r + (size_t)j * nr] = rb[j * 32 + lane] * (T(1) / D[j]);
+        } else {
+          const T e = E[j];
+          const T inv = T(1) / (D[j] * D[j + 1] - e * e);
+          const T x1 = rb[j * 32 + lane], x2 = rb[(j + 1) * 32 + lane];
+          B[r + (size_t)j * nr] = (x1 * D[j + 1] - x2 * e) * inv;
+          B[r + (size_t)(j + 1) * nr] = (x2 * D[j] - x1 * e) * inv;
+          ++j;
+        }
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// Subtracts descendant d's L D L^T restricted to target s (rows lb.. of d,
+// columns lb..ub) from the staged target block B.  One warp per pair; pairs
+// of different warps may hit the same entries, so the subtraction is atomic
+// (the summation order of a target entry varies between runs, as in the
+// reference's threaded factorization).
+template <class T> __device__ void sub_update_warp(Ctx<T> &c, int pq, int d, int c0, int w, int nr, const int *rows) {
+  const int lane = lane_id();
+  const int4 pr = c.prec[pq], d0 = c.snrec[2 * d];
+  const int lb = pr.y, ub = pr.z;
+  const int cd = d0.x, wd = d0.y, nrd = d0.z;
+  const int *rd = c.ls + pr.w;
+  const T *Ld = c.L + d0.w;
+  const T *Dd = c.D + cd, *Ed = c.D + c.N + cd;
+  const int m = nrd - lb, nc = ub - lb + 1;
+  T *B = c.B;
+  for (int e = lane; e < m * nc; e += 32) {
+    const int i = e % m, jj = e / m;
+    const int ri = rd[lb + i];
+    const int ti = c.map[ri];
+    const int tj = rd[lb + jj] - c0;
+    if (ti < 0 || ti >= nr || rows[ti] != ri || tj < 0 || tj >= w) {
+      atomicOr(c.status, ST_BOUNDS);
+      continue;
+    }
+    if (ti < tj) continue;  // lower triangle of the target only
+    double acc = 0.0;
+    for (int k = 0; k < wd; ++k) {
+      const double lik = (double)Ld[lb + i + (size_t)k * nrd];
+      const double ek = (double)Ed[k];
+      if (ek == 0.0 || k + 1 >= wd) {
+        acc += lik * (double)Dd[k] * (double)Ld[lb + jj + (size_t)k * nrd];
+      } else {
+        // 2x2 block (k, k+1): (D L^T)_k,j = d1 L_jk + e L_j,k+1; (D L^T)_k+1,j = e L_jk + d2 L_j,k+1
+        const double ljk = (double)Ld[lb + jj + (size_t)k * nrd], ljk1 = (double)Ld[lb + jj + (size_t)(k + 1) * nrd];
+        const double lik1 = (double)Ld[lb + i + (size_t)(k + 1) * nrd];
+        acc += lik * ((double)Dd[k] * ljk + ek * ljk1) + lik1 * (ek * ljk + (double)Dd[k + 1] * ljk1);
+        ++k;
+      }
+    }
+    atomicAdd(&B[ti + tj * nr], T(-acc));
+  }
+}
+
 // ---- factorization of one supernode (CTA scope) ------------------------------
 // Left-looking step of the reference (Serial_update_ldl.cpp:62-190): scatter
 // the matrix columns, subtract every visible descendant's L D L^T restricted
@@ -182,14 +315,15 @@ template <class T> __device__ __forceinline__ double ref_val(const Ctx<T> &c, in
 // scale the rows below.
 template <class T> __device__ void factor_sn(Ctx<T> &c, int s) {
   const int tid = threadIdx.x, nt = blockDim.x;
-  const int c0 = c.super[s], w = c.super[s + 1] - c0;
-  const int nr = c.lpi[s + 1] - c.lpi[s];
-  const int *rows = c.ls + c.lpi[s];
+  if (c.cyc && tid == 0) c.cyc[PH_SN] += 1;
+  const int4 r0 = c.snrec[2 * s], r1 = c.snrec[2 * s + 1];
+  const int c0 = r0.x, w = r0.y, nr = r0.z;
+  const int *rows = c.ls + r1.x;
   T *B = c.B;
   for (int p = tid; p < nr; p += nt) c.map[rows[p]] = p;
   for (int e = tid; e < nr * w; e += nt) B[e] = T(0);
   __syncthreads();
-  // matrix columns (symmetric neighbours j of the original column, ordered >= the column)
+  // matrix columns (symmetric neighbours of the original column, ordered >= the column)
   for (int m = 0; m < w; ++m) {
     const int col = c0 + m;
     const int j = c.perm[col];
@@ -201,56 +335,46 @@ template <class T> __device__ void factor_sn(Ctx<T> &c, int s) {
         atomicOr(c.status, ST_BOUNDS);
         continue;
       }
-      B[pos + m * nr] = T(fact_val(c, c.Rq[qq]));
+      B[pos + m * nr] = T(c.Fv[qq]);
     }
   }
   __syncthreads();
-  // descendant updates, one pair at a time (distinct targets inside a pair)
-  for (int pq = c.pair_ptr[s]; pq < c.pair_ptr[s + 1]; ++pq) {
-    const int d = c.pair_d[pq];
-    if (!visible(c, d)) continue;
-    const int lb = c.pair_lb[pq], ub = c.pair_ub[pq];
-    const int cd = c.super[d], wd = c.super[d + 1] - cd;
-    const int nrd = c.lpi[d + 1] - c.lpi[d];
-    const int *rd = c.ls + c.lpi[d];
-    const T *Ld = c.L + c.lpx[d];
-    const T *Dd = c.D + cd, *Ed = c.D + c.N + cd;
-    const int m = nrd - lb, nc = ub - lb + 1;
-    for (int e = tid; e < m * nc; e += nt) {
-      const int i = e % m, jj = e / m;
-      const int ri = rd[lb + i];
-      const int ti = c.map[ri];
-      const int tj = rd[lb + jj] - c0;
-      if (ti < 0 || ti >= nr || rows[ti] != ri || tj < 0 || tj >= w) {
-        atomicOr(c.status, ST_BOUNDS);
-        continue;
-      }
-      if (ti < tj) continue;  // lower triangle of the target only
-      double acc = 0.0;
-      for (int k = 0; k < wd; ++k) {
-        const double lik = (double)Ld[lb + i + (size_t)k * nrd];
-        const double ek = (double)Ed[k];
-        if (ek == 0.0 || k + 1 >= wd) {
-          acc += lik * (double)Dd[k] * (double)Ld[lb + jj + (size_t)k * nrd];
-        } else {
-          // 2x2 block (k, k+1): (D L^T)_k,j = d1 L_jk + e L_j,k+1; (D L^T)_k+1,j = e L_jk + d2 L_j,k+1
-          const double ljk = (double)Ld[lb + jj + (size_t)k * nrd], ljk1 = (double)Ld[lb + jj + (size_t)(k + 1) * nrd];
-          const double lik1 = (double)Ld[lb + i + (size_t)(k + 1) * nrd];
-          acc += lik * ((double)Dd[k] * ljk + ek * ljk1) + lik1 * (ek * ljk + (double)Dd[k + 1] * ljk1);
-          ++k;
-        }
-      }
-      B[ti + tj * nr] -= T(acc);
-    }
-    __syncthreads();
+  // descendant updates: descendants that never hide, then the active
+  // constraint columns; warp wi takes every num_warps()-th of them
+  {
+    int t = 0;
+    const int wi = warp_id(), nw = num_warps();
+    for_visible_pairs(c, s, r1.y, r1.z, r1.w, [&](int pq) {
+      if (t++ % nw == wi) sub_update_warp(c, pq, c.prec[pq].x, c0, w, nr, rows);
+    });
   }
+  __syncthreads();
   // Bunch-Kaufman on the diagonal block, then the rows below
   bool pivoted = false;
   bk_factor<T>(B, nr, w, c.Dsm, c.Esm, c.lp, c.status, &pivoted);
   __syncthreads();
-  if (nr > w) panel_solve_rows<T>(B, nr, w, B, nr, c.Dsm, c.Esm, c.lp, c.rowbuf, blockDim.x, pivoted);
+  if (nr > w) panel_rows_warp0(c, B, nr, w, pivoted);
   __syncthreads();
-  T *Ls = c.L + c.lpx[s];
+  // The solves apply the diagonal block through the inverse of its unit
+  // lower triangle (one product instead of w dependent steps); nothing else
+  // reads L11 once the rows below are solved, so the inverse replaces it.
+  // Column j of the inverse by thread j: X[i][j] = -sum_{j<=k<i} L[i][k] X[k][j].
+  for (int j = tid; j < w; j += nt) {
+    T *X = c.Binv;
+    X[j + j * w] = T(1);
+    for (int i = j + 1; i < w; ++i) {
+      T acc = B[i + (size_t)j * nr];
+      for (int k = j + 1; k < i; ++k) acc += B[i + (size_t)k * nr] * X[k + j * w];
+      X[i + j * w] = -acc;
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < w * w; e += nt) {
+    const int i = e % w, j = e / w;
+    if (i > j) B[i + (size_t)j * nr] = c.Binv[i + j * w];
+  }
+  __syncthreads();
+  T *Ls = c.L + r0.w;
   for (int e = tid; e < nr * w; e += nt) {
     T v = B[e];
     if (!(v == v) || isinf((double)v)) atomicOr(c.status, ST_NONFINITE);
@@ -265,110 +389,109 @@ template <class T> __device__ void factor_sn(Ctx<T> &c, int s) {
   __syncthreads();
 }
 
-// Factor every marked supernode (leaves first), then fold the pivots into the
-// row lists of the descendants (row_reordering, Sym_BLAS.cpp:327-490) and
-// into the ordering (reorder_matrix, linear_solver_wrapper.cpp:1432-1460).
+// Factor the supernodes of mlist (ascending ids: children before parents,
+// the reference's order of mod_indices), then fold the pivots into the row
+// lists of the descendants (row_reordering, Sym_BLAS.cpp:327-490) and into
+// the ordering (reorder_matrix, linear_solver_wrapper.cpp:1432-1460).
 template <class T> __device__ void factor_marked(Ctx<T> &c) {
-  for (int l = 0; l < c.nlev; ++l)
-    for (int q = c.lvl_ptr[l]; q < c.lvl_ptr[l + 1]; ++q) {
-      const int s = c.lvl_sn[q];
-      if (c.mark[s]) factor_sn(c, s);
-    }
+  const int m = *c.nmark;
+  for (int t = 0; t < m; ++t) factor_sn(c, c.mlist[t]);
   // renaming: rows of descendants that fall into a pivoted supernode
-  for (int s = 0; s < c.ns; ++s) {
-    if (!c.mark[s] || !c.piv[s]) continue;
-    const int c0 = c.super[s], w = c.super[s + 1] - c0;
+  for (int t = 0; t < m; ++t) {
+    const int s = c.mlist[t];
+    if (!c.piv[s]) continue;
+    const int4 r0 = c.snrec[2 * s], r1 = c.snrec[2 * s + 1];
+    const int c0 = r0.x, w = r0.y;
     // inverse of the local pivot order: old local position -> new position
-    for (int m = threadIdx.x; m < w; m += blockDim.x) c.lp[c.lperm[c0 + m]] = m;
+    for (int q = threadIdx.x; q < w; q += blockDim.x) c.lp[c.lperm[c0 + q]] = q;
     __syncthreads();
-    for (int pq = c.pair_ptr[s]; pq < c.pair_ptr[s + 1]; ++pq) {
-      const int d = c.pair_d[pq];
-      int *rd = c.ls + c.lpi[d];
-      const int lb = c.pair_lb[pq], ub = c.pair_ub[pq];
-      for (int i = lb + threadIdx.x; i <= ub; i += blockDim.x) {
+    for (int pq = r1.y; pq < r1.w; ++pq) {
+      const int4 pr = c.prec[pq];
+      int *rd = c.ls + pr.w;
+      for (int i = pr.y + threadIdx.x; i <= pr.z; i += blockDim.x) {
         const int o = rd[i] - c0;
         if (o >= 0 && o < w) rd[i] = c0 + c.lp[o];
         else atomicOr(c.status, ST_BOUNDS);
       }
     }
-    // composed ordering: new position m holds the column that was at lperm[m]
+    // composed ordering: new position q holds the column that was at lperm[q]
     // (old values staged in the free row map)
-    for (int m = threadIdx.x; m < w; m += blockDim.x) c.map[m] = c.perm[c0 + c.lperm[c0 + m]];
+    for (int q = threadIdx.x; q < w; q += blockDim.x) c.map[q] = c.perm[c0 + c.lperm[c0 + q]];
     __syncthreads();
-    for (int m = threadIdx.x; m < w; m += blockDim.x) c.perm[c0 + m] = c.map[m];
+    for (int q = threadIdx.x; q < w; q += blockDim.x) c.perm[c0 + q] = c.map[q];
     __syncthreads();
-    for (int m = threadIdx.x; m < w; m += blockDim.x) c.iperm[c.perm[c0 + m]] = c0 + m;
+    for (int q = threadIdx.x; q < w; q += blockDim.x) c.iperm[c.perm[c0 + q]] = c0 + q;
     __syncthreads();
   }
-  for (int s = threadIdx.x; s < c.ns; s += blockDim.x) c.mark[s] = 0;
+  for (int t = threadIdx.x; t < m; t += blockDim.x) c.mark[c.mlist[t]] = 0;
+  __syncthreads();
+  if (threadIdx.x == 0) *c.nmark = 0;
   __syncthreads();
 }
 
 // ---- triangular solves (factor order, vector in shared memory) ---------------
-// Forward: per level, every visible supernode pulls the products of its
-// visible descendants' rows that fall into it, then solves its unit lower
-// diagonal block (the reference pushes the same products with atomics,
-// Triangular_BCSC.cpp:378-446).  Wide levels: a thread per supernode, narrow
-// levels: a warp per supernode.
+// Forward step of one supernode (reference H2LeveledBlockedLsolve,
+// Triangular_BCSC.cpp:378-446): x_s <- L11^-1 x_s through the stored inverse,
+// then the rows below push -L21 x_s into their (ancestor) entries; pushes of
+// supernodes of the same level may meet, so they are atomic, as in the
+// reference's threaded solve (:435).  Wide levels: a thread per supernode,
+// narrow levels: a warp per supernode.
 template <class T> __device__ void fwd_thread(Ctx<T> &c, int s) {
   T *x = c.xs;
-  const int c0 = c.super[s], w = c.super[s + 1] - c0, nr = c.lpi[s + 1] - c.lpi[s];
-  for (int pq = c.pair_ptr[s]; pq < c.pair_ptr[s + 1]; ++pq) {
-    const int d = c.pair_d[pq];
-    if (!visible(c, d)) continue;
-    const int lb = c.pair_lb[pq], ub = c.pair_ub[pq];
-    const int cd = c.super[d], wd = c.super[d + 1] - cd, nrd = c.lpi[d + 1] - c.lpi[d];
-    const int *rd = c.ls + c.lpi[d];
-    const T *Ld = c.L + c.lpx[d];
-    for (int i = lb; i <= ub; ++i) {
-      T acc = T(0);
-      for (int k = 0; k < wd; ++k) acc += Ld[i + (size_t)k * nrd] * x[cd + k];
-      const int r = rd[i];
-      if (r >= c0 && r < c0 + w) x[r] -= acc;
-    }
+  const int4 r0 = c.snrec[2 * s], r1 = c.snrec[2 * s + 1];
+  const int c0 = r0.x, w = r0.y, nr = r0.z;
+  const T *Ls = c.L + r0.w;
+  const int *rows = c.ls + r1.x;
+  for (int i = w - 1; i > 0; --i) {  // bottom-up: row i reads x_j, j < i, not yet replaced
+    T acc = x[c0 + i];
+    for (int j = 0; j < i; ++j) acc += Ls[i + (size_t)j * nr] * x[c0 + j];
+    x[c0 + i] = acc;
   }
-  const T *Ls = c.L + c.lpx[s];
-  for (int j = 0; j < w - 1; ++j) {
-    const T xj = x[c0 + j];
-    for (int i = j + 1; i < w; ++i) x[c0 + i] -= Ls[i + (size_t)j * nr] * xj;
+  for (int r = w; r < nr; ++r) {
+    T y = T(0);
+    for (int k = 0; k < w; ++k) y += Ls[r + (size_t)k * nr] * x[c0 + k];
+    const int rr = rows[r];
+    if ((unsigned)rr < (unsigned)c.N) atomicAdd(&x[rr], -y);
   }
 }
 
 template <class T> __device__ void fwd_warp(Ctx<T> &c, int s) {
   T *x = c.xs;
   const int lane = lane_id();
-  const int c0 = c.super[s], w = c.super[s + 1] - c0, nr = c.lpi[s + 1] - c.lpi[s];
-  for (int pq = c.pair_ptr[s]; pq < c.pair_ptr[s + 1]; ++pq) {
-    const int d = c.pair_d[pq];
-    if (!visible(c, d)) continue;
-    const int lb = c.pair_lb[pq], ub = c.pair_ub[pq];
-    const int cd = c.super[d], wd = c.super[d + 1] - cd, nrd = c.lpi[d + 1] - c.lpi[d];
-    const int *rd = c.ls + c.lpi[d];
-    const T *Ld = c.L + c.lpx[d];
-    for (int i = lb + lane; i <= ub; i += 32) {
-      T acc = T(0);
-      for (int k = 0; k < wd; ++k) acc += Ld[i + (size_t)k * nrd] * x[cd + k];
-      const int r = rd[i];
-      if (r >= c0 && r < c0 + w) x[r] -= acc;
+  const int4 r0 = c.snrec[2 * s], r1 = c.snrec[2 * s + 1];
+  const int c0 = r0.x, w = r0.y, nr = r0.z;
+  const T *Ls = c.L + r0.w;
+  const int *rows = c.ls + r1.x;
+  // x_s <- L11^-1 x_s: lanes form rows of the product, then write; chunks
+  // of 32 rows from the bottom (a chunk reads only rows above it)
+  for (int i0 = ((w - 1) / 32) * 32; i0 >= 0; i0 -= 32) {
+    const int i = i0 + lane;
+    T acc = T(0);
+    if (i < w) {
+      acc = x[c0 + i];
+      for (int j = 0; j < i; ++j) acc += Ls[i + (size_t)j * nr] * x[c0 + j];
     }
     __syncwarp();
-  }
-  const T *Ls = c.L + c.lpx[s];
-  for (int j = 0; j < w - 1; ++j) {
-    const T xj = x[c0 + j];
-    __syncwarp();
-    for (int i = j + 1 + lane; i < w; i += 32) x[c0 + i] -= Ls[i + (size_t)j * nr] * xj;
+    if (i < w) x[c0 + i] = acc;
     __syncwarp();
   }
+  for (int r = w + lane; r < nr; r += 32) {
+    T y = T(0);
+    for (int k = 0; k < w; ++k) y += Ls[r + (size_t)k * nr] * x[c0 + k];
+    const int rr = rows[r];
+    if ((unsigned)rr < (unsigned)c.N) atomicAdd(&x[rr], -y);
+  }
+  __syncwarp();
 }
 
-// Backward (Triangular_BCSC.cpp:534-600): x1 -= L21^T x(rows below), then the
-// transposed unit triangle.
+// Backward (Triangular_BCSC.cpp:534-600): x1 -= L21^T x(rows below), then
+// x1 <- L11^-T x1 through the stored inverse.
 template <class T> __device__ void bwd_thread(Ctx<T> &c, int s) {
   T *x = c.xs;
-  const int c0 = c.super[s], w = c.super[s + 1] - c0, nr = c.lpi[s + 1] - c.lpi[s];
-  const int *rows = c.ls + c.lpi[s];
-  const T *Ls = c.L + c.lpx[s];
+  const int4 r0 = c.snrec[2 * s], r1 = c.snrec[2 * s + 1];
+  const int c0 = r0.x, w = r0.y, nr = r0.z;
+  const int *rows = c.ls + r1.x;
+  const T *Ls = c.L + r0.w;
   for (int j = 0; j < w; ++j) {
     T acc = T(0);
     for (int r = w; r < nr; ++r) {
@@ -377,18 +500,21 @@ template <class T> __device__ void bwd_thread(Ctx<T> &c, int s) {
     }
     x[c0 + j] -= acc;
   }
-  for (int i = w - 1; i > 0; --i) {
-    const T xi = x[c0 + i];
-    for (int j = 0; j < i; ++j) x[c0 + j] -= Ls[i + (size_t)j * nr] * xi;
+  // top-down: entry j reads x_i, i > j, not yet replaced
+  for (int j = 0; j + 1 < w; ++j) {
+    T acc = x[c0 + j];
+    for (int i = j + 1; i < w; ++i) acc += Ls[i + (size_t)j * nr] * x[c0 + i];
+    x[c0 + j] = acc;
   }
 }
 
 template <class T> __device__ void bwd_warp(Ctx<T> &c, int s) {
   T *x = c.xs;
   const int lane = lane_id();
-  const int c0 = c.super[s], w = c.super[s + 1] - c0, nr = c.lpi[s + 1] - c.lpi[s];
-  const int *rows = c.ls + c.lpi[s];
-  const T *Ls = c.L + c.lpx[s];
+  const int4 r0 = c.snrec[2 * s], r1 = c.snrec[2 * s + 1];
+  const int c0 = r0.x, w = r0.y, nr = r0.z;
+  const int *rows = c.ls + r1.x;
+  const T *Ls = c.L + r0.w;
   for (int j = 0; j < w; ++j) {
     T acc = T(0);
     for (int r = w + lane; r < nr; r += 32) {
@@ -400,10 +526,16 @@ template <class T> __device__ void bwd_warp(Ctx<T> &c, int s) {
     if (lane == 0) x[c0 + j] -= acc;
   }
   __syncwarp();
-  for (int i = w - 1; i > 0; --i) {
-    const T xi = x[c0 + i];
+  // x_s <- L11^-T x_s: lanes form entries of the product, chunks of 32 from the top
+  for (int j0 = 0; j0 < w; j0 += 32) {
+    const int j = j0 + lane;
+    T acc = T(0);
+    if (j < w) {
+      acc = x[c0 + j];
+      for (int i = j + 1; i < w; ++i) acc += Ls[i + (size_t)j * nr] * x[c0 + i];
+    }
     __syncwarp();
-    for (int j = lane; j < i; j += 32) x[c0 + j] -= Ls[i + (size_t)j * nr] * xi;
+    if (j < w) x[c0 + j] = acc;
     __syncwarp();
   }
 }
@@ -412,71 +544,110 @@ template <class T> __device__ void bwd_warp(Ctx<T> &c, int s) {
 template <class T> __device__ void ldlt_solve_smem(Ctx<T> &c) {
   const int nw = num_warps();
   for (int l = 0; l < c.nlev; ++l) {
-    const int a = c.lvl_ptr[l], b = c.lvl_ptr[l + 1];
-    if (b - a > 2 * nw) {
-      for (int q = a + threadIdx.x; q < b; q += blockDim.x) {
-        const int s = c.lvl_sn[q];
-        if (visible(c, s)) fwd_thread(c, s);
-      }
+    BQ_T0(c);
+    const int a = c.vlvl[l], b = c.vlvl[l + 1];
+    const bool wide = b - a > 2 * nw;
+    if (wide) {
+      for (int q = a + threadIdx.x; q < b; q += blockDim.x) fwd_thread(c, c.vlist[q]);
     } else {
-      for (int q = a + warp_id(); q < b; q += nw) {
-        const int s = c.lvl_sn[q];
-        if (visible(c, s)) fwd_warp(c, s);
+      for (int q = a + warp_id(); q < b; q += nw) fwd_warp(c, c.vlist[q]);
+    }
+    __syncthreads();
+    BQ_T1(c, wide ? PH_FWD_WIDE : PH_FWD_NARROW);
+  }
+  {
+    BQ_T0(c);
+    // D solve: 1x1 by division, 2x2 by Cramer's rule (blocked_2by2_solver, Sym_BLAS.cpp:492-529)
+    for (int i = threadIdx.x; i < c.N; i += blockDim.x) {
+      if (!visible(c, c.col2sup[i])) continue;
+      if (i > 0 && c.D[c.N + i - 1] != T(0)) continue;  // second column of a 2x2 block
+      const T e = i + 1 < c.N ? c.D[c.N + i] : T(0);
+      if (e == T(0)) {
+        c.xs[i] = c.xs[i] / c.D[i];
+      } else {
+        const T d1 = c.D[i], d2 = c.D[i + 1];
+        const T inv = T(1) / (d1 * d2 - e * e);
+        const T x1 = c.xs[i], x2 = c.xs[i + 1];
+        c.xs[i] = (x1 * d2 - x2 * e) * inv;
+        c.xs[i + 1] = (x2 * d1 - x1 * e) * inv;
       }
     }
     __syncthreads();
+    BQ_T1(c, PH_DIAG);
   }
-  // D solve: 1x1 by division, 2x2 by Cramer's rule (blocked_2by2_solver, Sym_BLAS.cpp:492-529)
-  for (int i = threadIdx.x; i < c.N; i += blockDim.x) {
-    if (!visible(c, c.col2sup[i])) continue;
-    if (i > 0 && c.D[c.N + i - 1] != T(0)) continue;  // second column of a 2x2 block
-    const T e = i + 1 < c.N ? c.D[c.N + i] : T(0);
-    if (e == T(0)) {
-      c.xs[i] = c.xs[i] / c.D[i];
-    } else {
-      const T d1 = c.D[i], d2 = c.D[i + 1];
-      const T inv = T(1) / (d1 * d2 - e * e);
-      const T x1 = c.xs[i], x2 = c.xs[i + 1];
-      c.xs[i] = (x1 * d2 - x2 * e) * inv;
-      c.xs[i + 1] = (x2 * d1 - x1 * e) * inv;
-    }
-  }
-  __syncthreads();
+  BQ_T0(c);
   for (int l = c.nlev - 1; l >= 0; --l) {
-    const int a = c.lvl_ptr[l], b = c.lvl_ptr[l + 1];
+    const int a = c.vlvl[l], b = c.vlvl[l + 1];
     if (b - a > 2 * nw) {
-      for (int q = a + threadIdx.x; q < b; q += blockDim.x) {
-        const int s = c.lvl_sn[q];
-        if (visible(c, s)) bwd_thread(c, s);
-      }
+      for (int q = a + threadIdx.x; q < b; q += blockDim.x) bwd_thread(c, c.vlist[q]);
     } else {
-      for (int q = a + warp_id(); q < b; q += nw) {
-        const int s = c.lvl_sn[q];
-        if (visible(c, s)) bwd_warp(c, s);
-      }
+      for (int q = a + warp_id(); q < b; q += nw) bwd_warp(c, c.vlist[q]);
     }
     __syncthreads();
+  }
+  BQ_T1(c, PH_BWD);
+}
+
+// Visible supernodes grouped by level (after every change of the active set),
+// each level in the pattern's order.
+template <class T> __device__ void build_vlist(Ctx<T> &c) {
+  for (int l = threadIdx.x; l <= c.nlev; l += blockDim.x) c.vlvl[l] = 0;
+  __syncthreads();
+  for (int s = threadIdx.x; s < c.ns; s += blockDim.x)
+    if (c.vis[s]) atomicAdd(&c.vlvl[c.lev[s] + 1], 1);
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int l = 0; l < c.nlev; ++l) c.vlvl[l + 1] += c.vlvl[l];
+  __syncthreads();
+  for (int l = 0; l < c.nlev; ++l) {
+    const int a = c.lvl_ptr[l], b = c.lvl_ptr[l + 1];
+    int base = c.vlvl[l];
+    for (int q0 = a; q0 < b; q0 += blockDim.x) {
+      const int q = q0 + threadIdx.x;
+      const int sn = q < b ? c.lvl_sn[q] : -1;
+      const int f = (sn >= 0 && c.vis[sn]) ? 1 : 0;
+      const unsigned bal = __ballot_sync(0xffffffffu, f);
+      const int wpre = __popc(bal & ((1u << lane_id()) - 1u));
+      if (lane_id() == 0) c.redi[warp_id()] = __popc(bal);
+      __syncthreads();
+      int before = 0, total = 0;
+      for (int t = 0; t < num_warps(); ++t) {
+        if (t < warp_id()) before += c.redi[t];
+        total += c.redi[t];
+      }
+      if (f) c.vlist[base + before + wpre] = sn;
+      base += total;
+      __syncthreads();
+    }
   }
 }
 
 // out = M^-1 v (original numbering; hidden rows give zero).  Vectors in
 // global memory, the solve in shared memory.
 template <class T, class VI, class VO> __device__ void precond(Ctx<T> &c, const VI *v, VO *out) {
+  BQ_T0(c);
+  const long long tg0 = c.cyc ? clock64() : 0;
   for (int i = threadIdx.x; i < c.N; i += blockDim.x) c.xs[i] = visible(c, c.col2sup[i]) ? T(v[c.perm[i]]) : T(0);
   __syncthreads();
+  if (c.cyc && threadIdx.x == 0) c.cyc[PH_GATHER] += (unsigned long long)(clock64() - tg0);
   ldlt_solve_smem(c);
+  const long long tg1 = c.cyc ? clock64() : 0;
   for (int i = threadIdx.x; i < c.N; i += blockDim.x) out[c.perm[i]] = VO(c.xs[i]);
   __syncthreads();
+  if (c.cyc && threadIdx.x == 0) c.cyc[PH_GATHER] += (unsigned long long)(clock64() - tg1);
+  BQ_T1(c, PH_PRECOND);
 }
 
 // y = K x with the refinement values (original numbering).
 template <class T> __device__ void spmv_ref(const Ctx<T> &c, const double *x, double *y) {
+  BQ_T0(c);
   for (int i = threadIdx.x; i < c.N; i += blockDim.x) {
     double acc = 0.0;
-    for (int qq = c.Rp[i]; qq < c.Rp[i + 1]; ++qq) acc += ref_val(c, c.Rq[qq]) * x[c.Rj[qq]];
+    for (int qq = c.Rp[i]; qq < c.Rp[i + 1]; ++qq) acc += c.Rv[qq] * x[c.Rj[qq]];
     y[i] = acc;
   }
   __syncthreads();
+  BQ_T1(c, PH_SPMV);
 }
 
 template <class T> __device__ double dot(const Ctx<T> &c, const double *a, const double *b) {
@@ -619,20 +790,112 @@ __device__ int refine(Ctx<T> &c, const double *b, double *x, int itr_max, int mr
 
 // ---- NASOQ on one problem ------------------------------------------------------
 // Marks the supernodes on the elimination-tree path from supernode s to the
-// root (the reference marks the visible ones of its edited tree, which are a
-// subset; refactoring an unchanged supernode reproduces it).
+// root and appends them to mlist (the reference marks the visible ones of its
+// edited tree, which are a subset; refactoring an unchanged supernode
+// reproduces it).  Thread 0 only.
 template <class T> __device__ void mark_path(Ctx<T> &c, int s) {
-  for (; s >= 0; s = c.sparent[s]) c.mark[s] = 1;
+  for (; s >= 0; s = c.sparent[s])
+    if (!c.mark[s]) {
+      c.mark[s] = 1;
+      c.mlist[(*c.nmark)++] = s;
+    }
 }
 
 // KKT edit of constraint k (reference edit_kkt -> add_del_matrix_qp,
 // linear_solver_wrapper.cpp:1020-1137): the constraint's entries become
-// visible / hidden, and the paths of its column and of its variables are
-// marked for the next partial refactorization.  Thread 0 only.
+// visible / hidden in both value copies and in the descendant masks of its
+// targets, and the paths of its column and of its variables are marked for
+// the next partial refactorization.  Thread 0 only.
 template <class T> __device__ void edit_constraint(Ctx<T> &c, int k, bool add) {
   c.act[k] = add ? 1 : 0;
+  c.vis[c.con_sn[k]] = add ? 1 : 0;
+  for (int e = c.bt_ptr[k]; e < c.bt_ptr[k + 1]; ++e) {
+    const int qq = c.bt_rpos[e];
+    const double v = add ? c.kv[c.bt_q[e]] : 0.0;
+    c.Fv[qq] = v;
+    c.Rv[qq] = v;
+  }
+  const int row = c.base + k;
+  for (int qq = c.Rp[row]; qq < c.Rp[row + 1]; ++qq)
+    if (c.Rj[qq] != row) {
+      const double v = add ? c.kv[c.Rq[qq]] : 0.0;
+      c.Fv[qq] = v;
+      c.Rv[qq] = v;
+    }
+  for (int e = c.con_ptr[k]; e < c.con_ptr[k + 1]; ++e) {
+    const int tg = c.con_tgt[2 * e], bit = c.con_tgt[2 * e + 1];
+    if (bit < 64) {
+      if (add) c.cmask[tg] |= 1ull << bit;
+      else c.cmask[tg] &= ~(1ull << bit);
+    }
+  }
   mark_path(c, c.con_sn[k]);
   for (int e = c.bt_ptr[k]; e < c.bt_ptr[k + 1]; ++e) mark_path(c, c.col2sup[c.iperm[c.bt_var[e]]]);
+}
+
+// Marks every supernode (visible ones only when `only_visible`), in
+// ascending order.
+template <class T> __device__ void mark_all(Ctx<T> &c, bool only_visible) {
+  int base = 0;
+  for (int q0 = 0; q0 < c.ns; q0 += blockDim.x) {
+    const int q = q0 + threadIdx.x;
+    const int f = (q < c.ns && (!only_visible || c.vis[q])) ? 1 : 0;
+    if (q < c.ns) c.mark[q] = (uint8_t)f;
+    const unsigned bal = __ballot_sync(0xffffffffu, f);
+    const int wpre = __popc(bal & ((1u << lane_id()) - 1u));
+    if (lane_id() == 0) c.redi[warp_id()] = __popc(bal);
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int t = 0; t < num_warps(); ++t) {
+      if (t < warp_id()) before += c.redi[t];
+      total += c.redi[t];
+    }
+    if (f) c.mlist[base + before + wpre] = q;
+    base += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *c.nmark = base;
+  __syncthreads();
+}
+
+// Sorts mlist ascending (children before parents).  Thread 0; the lists of
+// partial refactorizations are a few tree paths long.
+template <class T> __device__ void sort_mlist(Ctx<T> &c) {
+  if (threadIdx.x == 0) {
+    const int m = *c.nmark;
+    for (int i = 1; i < m; ++i) {
+      const int v = c.mlist[i];
+      int j = i - 1;
+      while (j >= 0 && c.mlist[j] > v) {
+        c.mlist[j + 1] = c.mlist[j];
+        --j;
+      }
+      c.mlist[j + 1] = v;
+    }
+  }
+  __syncthreads();
+}
+
+// Visibility, descendant masks and both value copies of K from the active set.
+template <class T> __device__ void load_state(Ctx<T> &c) {
+  for (int s = threadIdx.x; s < c.ns; s += blockDim.x) {
+    const int k = c.sn_con[s];
+    c.vis[s] = (k < 0 || c.act[k]) ? 1 : 0;
+    c.cmask[s] = 0ull;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < c.mineq; k += blockDim.x)
+    if (c.act[k])
+      for (int e = c.con_ptr[k]; e < c.con_ptr[k + 1]; ++e) {
+        const int bit = c.con_tgt[2 * e + 1];
+        if (bit < 64) atomicOr(c.cmask + c.con_tgt[2 * e], 1ull << bit);
+      }
+  for (int qq = threadIdx.x; qq < c.nnzR; qq += blockDim.x) {
+    const int vq = c.Rq[qq];
+    c.Fv[qq] = fact_val(c, vq);
+    c.Rv[qq] = ref_val(c, vq);
+  }
+  __syncthreads();
 }
 
 }  // namespace
@@ -646,22 +909,37 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
   __shared__ GmresSmall gs;
   __shared__ int s_int[8];
   __shared__ double s_dbl[8];
+  __shared__ int s_nmark;
+  __shared__ Ctx<T> sc;  // the problem's context, read by every thread
+  __shared__ unsigned long long s_cyc[PH_N];
   const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid < PH_N) s_cyc[tid] = 0;
   // shared-memory carve-up (sizes from the largest pattern of the batch)
+  auto up16 = [](size_t v) { return (v + 15) / 16 * 16; };
   unsigned char *sp = smem;
   int *map = reinterpret_cast<int *>(sp);
-  sp += ((size_t)a.N_max * sizeof(int) + 15) / 16 * 16;
+  sp += up16((size_t)a.N_max * sizeof(int));
   T *xs = reinterpret_cast<T *>(sp);
-  sp += ((size_t)a.N_max * sizeof(T) + 15) / 16 * 16;
+  sp += up16((size_t)a.N_max * sizeof(T));
   T *Bm = reinterpret_cast<T *>(sp);
-  sp += ((size_t)a.nr_max * a.w_max * sizeof(T) + 15) / 16 * 16;
+  sp += up16((size_t)a.nr_max * a.w_max * sizeof(T));
   T *rowbuf = reinterpret_cast<T *>(sp);
-  sp += ((size_t)a.w_max * nt * sizeof(T) + 15) / 16 * 16;
+  sp += up16((size_t)a.w_max * 32 * sizeof(T));
   T *Dsm = reinterpret_cast<T *>(sp);
-  sp += ((size_t)a.w_max * sizeof(T) + 15) / 16 * 16;
+  sp += up16((size_t)a.w_max * sizeof(T));
   T *Esm = reinterpret_cast<T *>(sp);
-  sp += ((size_t)a.w_max * sizeof(T) + 15) / 16 * 16;
+  sp += up16((size_t)a.w_max * sizeof(T));
   int *lp = reinterpret_cast<int *>(sp);
+  sp += up16((size_t)a.w_max * sizeof(int));
+  T *Binv = reinterpret_cast<T *>(sp);
+  sp += up16((size_t)a.w_max * a.w_max * sizeof(T));
+  int *vlvl = reinterpret_cast<int *>(sp);
+  sp += up16((size_t)(a.nlev_max + 1) * sizeof(int));
+  uint8_t *vis = sp;
+  sp += up16((size_t)a.ns_max);
+  uint8_t *act = sp;
+  sp += up16((size_t)a.mi_max);
+  unsigned char *stage = sp;  // the factor and row lists of a problem that fits
 
   unsigned char *slot = a.slots + (size_t)blockIdx.x * a.slot.bytes;
   for (;;) {
@@ -669,77 +947,105 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
       const int qi = atomicAdd(a.head, 1);
       s_prob = qi < a.nprob ? a.order[qi] : -1;
       s_status = 0;
+      s_nmark = 0;
     }
     __syncthreads();
     const int pi = s_prob;
     if (pi < 0) break;
     const BProb &P = a.probs[pi];
     const BPat &pt = a.pats[P.pat];
-    Ctx<T> c;
-    c.n = pt.n;
-    c.meq = pt.meq;
-    c.mineq = pt.mineq;
-    c.N = pt.N;
-    c.base = pt.base;
-    c.ns = pt.ns;
-    c.nlev = pt.nlev;
+    Ctx<T> &c = sc;
+    if (tid == 0) {
+      const int *ip = a.ipool;
+      c.n = pt.n;
+      c.meq = pt.meq;
+      c.mineq = pt.mineq;
+      c.N = pt.N;
+      c.base = pt.base;
+      c.ns = pt.ns;
+      c.nlev = pt.nlev;
+      c.nnzR = pt.nnzR;
+      c.cmask_ok = pt.cmask_ok;
+      c.super = ip + pt.o_super;
+      c.sparent = ip + pt.o_sparent;
+      c.col2sup = ip + pt.o_col2sup;
+      c.lpi = ip + pt.o_lpi;
+      c.lpx = ip + pt.o_lpx;
+      c.lvl_ptr = ip + pt.o_lvl_ptr;
+      c.lvl_sn = ip + pt.o_lvl_sn;
+      c.lev = ip + pt.o_lev;
+      c.Rp = ip + pt.o_Rp;
+      c.Rj = ip + pt.o_Rj;
+      c.Rq = ip + pt.o_Rq;
+      c.ent = ip + pt.o_ent;
+      c.bt_ptr = ip + pt.o_bt_ptr;
+      c.bt_var = ip + pt.o_bt_var;
+      c.bt_q = ip + pt.o_bt_q;
+      c.bt_rpos = ip + pt.o_bt_rpos;
+      c.sn_con = ip + pt.o_sn_con;
+      c.con_sn = ip + pt.o_con_sn;
+      c.eq_ptr = ip + pt.o_eq_ptr;
+      c.eq_var = ip + pt.o_eq_var;
+      c.eq_q = ip + pt.o_eq_q;
+      c.snrec = reinterpret_cast<const int4 *>(ip + pt.o_snrec);
+      c.prec = reinterpret_cast<const int4 *>(ip + pt.o_prec);
+      c.con_ptr = ip + pt.o_con_ptr;
+      c.con_tgt = ip + pt.o_con_tgt;
+      c.kv = a.dpool + P.o_kv;
+      c.q = a.dpool + P.o_q;
+      c.bq = a.dpool + P.o_b;
+      c.dq = a.dpool + P.o_d;
+      c.pert = reinterpret_cast<const uint8_t *>(a.dpool) + P.o_pert;
+      c.reg = P.reg;
+      c.reg32 = P.reg32;
+      // the factor and the row lists live in shared memory when they fit
+      const size_t lbytes = ((size_t)pt.xsize * sizeof(T) + 15) / 16 * 16;
+      if (lbytes + (size_t)pt.ssize * sizeof(int) <= (size_t)a.stage_bytes) {
+        c.L = reinterpret_cast<T *>(stage);
+        c.ls = reinterpret_cast<int *>(stage + lbytes);
+      } else {
+        c.L = reinterpret_cast<T *>(slot + a.slot.o_L);
+        c.ls = reinterpret_cast<int *>(slot + a.slot.o_ls);
+      }
+      c.D = reinterpret_cast<T *>(slot + a.slot.o_D);
+      c.perm = reinterpret_cast<int *>(slot + a.slot.o_perm);
+      c.iperm = reinterpret_cast<int *>(slot + a.slot.o_iperm);
+      c.lperm = reinterpret_cast<int *>(slot + a.slot.o_lperm);
+      c.mark = slot + a.slot.o_mark;
+      c.piv = slot + a.slot.o_piv;
+      c.alist = reinterpret_cast<int *>(slot + a.slot.o_alist);
+      c.vlist = reinterpret_cast<int *>(slot + a.slot.o_vlist);
+      c.mlist = reinterpret_cast<int *>(slot + a.slot.o_mlist);
+      c.Fv = reinterpret_cast<double *>(slot + a.slot.o_Fv);
+      c.Rv = reinterpret_cast<double *>(slot + a.slot.o_Rv);
+      c.cmask = reinterpret_cast<unsigned long long *>(slot + a.slot.o_cmask);
+      c.rhs = reinterpret_cast<double *>(slot + a.slot.o_rhs);
+      c.sol = reinterpret_cast<double *>(slot + a.slot.o_sol);
+      c.r = reinterpret_cast<double *>(slot + a.slot.o_r);
+      c.w = reinterpret_cast<double *>(slot + a.slot.o_w);
+      c.V = reinterpret_cast<double *>(slot + a.slot.o_V);
+      c.Z = reinterpret_cast<T *>(slot + a.slot.o_Z);
+      c.tmp = reinterpret_cast<double *>(slot + a.slot.o_tmp);
+      c.map = map;
+      c.xs = xs;
+      c.B = Bm;
+      c.rowbuf = rowbuf;
+      c.Dsm = Dsm;
+      c.Esm = Esm;
+      c.Binv = Binv;
+      c.lp = lp;
+      c.vis = vis;
+      c.act = act;
+      c.vlvl = vlvl;
+      c.nmark = &s_nmark;
+      c.red = red;
+      c.redi = redi;
+      c.status = &s_status;
+      c.cyc = a.prof ? s_cyc : nullptr;
+    }
+    __syncthreads();
+    const long long tp0 = clock64();
     const int *ip = a.ipool;
-    c.super = ip + pt.o_super;
-    c.sparent = ip + pt.o_sparent;
-    c.col2sup = ip + pt.o_col2sup;
-    c.lpi = ip + pt.o_lpi;
-    c.lpx = ip + pt.o_lpx;
-    c.lvl_ptr = ip + pt.o_lvl_ptr;
-    c.lvl_sn = ip + pt.o_lvl_sn;
-    c.pair_ptr = ip + pt.o_pair_ptr;
-    c.pair_d = ip + pt.o_pair_d;
-    c.pair_lb = ip + pt.o_pair_lb;
-    c.pair_ub = ip + pt.o_pair_ub;
-    c.Rp = ip + pt.o_Rp;
-    c.Rj = ip + pt.o_Rj;
-    c.Rq = ip + pt.o_Rq;
-    c.ent = ip + pt.o_ent;
-    c.bt_ptr = ip + pt.o_bt_ptr;
-    c.bt_var = ip + pt.o_bt_var;
-    c.bt_q = ip + pt.o_bt_q;
-    c.sn_con = ip + pt.o_sn_con;
-    c.con_sn = ip + pt.o_con_sn;
-    c.eq_ptr = ip + pt.o_eq_ptr;
-    c.eq_var = ip + pt.o_eq_var;
-    c.eq_q = ip + pt.o_eq_q;
-    c.kv = a.dpool + P.o_kv;
-    c.q = a.dpool + P.o_q;
-    c.bq = a.dpool + P.o_b;
-    c.dq = a.dpool + P.o_d;
-    c.pert = reinterpret_cast<const uint8_t *>(a.dpool) + P.o_pert;
-    c.reg = P.reg;
-    c.L = reinterpret_cast<T *>(slot + a.slot.o_L);
-    c.D = reinterpret_cast<T *>(slot + a.slot.o_D);
-    c.ls = reinterpret_cast<int *>(slot + a.slot.o_ls);
-    c.perm = reinterpret_cast<int *>(slot + a.slot.o_perm);
-    c.iperm = reinterpret_cast<int *>(slot + a.slot.o_iperm);
-    c.lperm = reinterpret_cast<int *>(slot + a.slot.o_lperm);
-    c.mark = slot + a.slot.o_mark;
-    c.piv = slot + a.slot.o_piv;
-    c.act = slot + a.slot.o_act;
-    c.alist = reinterpret_cast<int *>(slot + a.slot.o_alist);
-    c.rhs = reinterpret_cast<double *>(slot + a.slot.o_rhs);
-    c.sol = reinterpret_cast<double *>(slot + a.slot.o_sol);
-    c.r = reinterpret_cast<double *>(slot + a.slot.o_r);
-    c.w = reinterpret_cast<double *>(slot + a.slot.o_w);
-    c.V = reinterpret_cast<double *>(slot + a.slot.o_V);
-    c.Z = reinterpret_cast<T *>(slot + a.slot.o_Z);
-    c.tmp = reinterpret_cast<double *>(slot + a.slot.o_tmp);
-    c.map = map;
-    c.xs = xs;
-    c.B = Bm;
-    c.rowbuf = rowbuf;
-    c.Dsm = Dsm;
-    c.Esm = Esm;
-    c.lp = lp;
-    c.red = red;
-    c.redi = redi;
-    c.status = &s_status;
     double *xv = a.dout + P.o_x, *yv = a.dout + P.o_y, *zv = a.dout + P.o_z;
     int *as_out = a.iout + P.o_as;
     const int n = c.n, meq = c.meq, mineq = c.mineq, N = c.N;
@@ -778,8 +1084,9 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
     // src/nasoq.cpp:448-476): every visible supernode; rhs [-q; b; d on the
     // active rows]
     for (int round = 0; round < (warm ? 4 : 1); ++round) {
-      for (int s = tid; s < c.ns; s += nt) c.mark[s] = warm ? 1 : (visible(c, s) ? 1 : 0);
-      __syncthreads();
+      load_state(c);
+      build_vlist(c);
+      mark_all(c, !warm);
       factor_marked(c);
       for (int i = tid; i < N; i += nt) {
         double v = 0.0;
@@ -819,6 +1126,7 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
     }
     __syncthreads();
     nact = s_int[0];
+    if (c.cyc && tid == 0) c.cyc[PH_INIT] += (unsigned long long)(clock64() - tp0);
 
     // ---- the dual active-set iteration (reference numeric_QP)
     int num_iter = 0, converged = 0, nxt_active = -1, nxt_drop = -1, to_add = 1;
@@ -830,6 +1138,7 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
         break;
       }
       if (to_add == 1) {
+        BQ_T0(c);
         // primal_feasibility (src/nasoq.cpp:787-840): most violated row beyond eps_abs
         int viol = 0;
         double best = P.eps_abs;
@@ -861,12 +1170,25 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
         for (int e = c.bt_ptr[nxt_active] + tid; e < c.bt_ptr[nxt_active + 1]; e += nt)
           c.rhs[c.bt_var[e]] = c.kv[c.bt_q[e]];
         __syncthreads();
+        BQ_T1(c, PH_SELECT);
       }
       // solve_kkt (src/nasoq.cpp:918-957)
-      if (typ == 1) factor_marked(c);
-      precond(c, c.rhs, c.sol);
-      solves++;
-      steps += refine(c, c.rhs, c.sol, P.outer, P.inner, flexible, adaptive, a.refine_tol, P.tol_abs, P.tol_rel, gs);
+      if (typ == 1) {
+        BQ_T0(c);
+        sort_mlist(c);
+        factor_marked(c);
+        build_vlist(c);
+        typ = 0;
+        BQ_T1(c, PH_FACTOR);
+      }
+      {
+        BQ_T0(c);
+        precond(c, c.rhs, c.sol);
+        solves++;
+        steps += refine(c, c.rhs, c.sol, P.outer, P.inner, flexible, adaptive, a.refine_tol, P.tol_abs, P.tol_rel, gs);
+        BQ_T1(c, PH_REFINE);
+      }
+      const long long tu0 = clock64();
       // step lengths (src/nasoq.cpp:852-878)
       double dual_step = DMAX;
       int drop = -1;
@@ -944,6 +1266,10 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
         typ = 1;
       }
       num_iter++;
+      if (c.cyc && tid == 0) {
+        c.cyc[PH_UPDATE] += (unsigned long long)(clock64() - tu0);
+        c.cyc[PH_ITER] += 1;
+      }
     }
 
     // ---- results: objective and KKT norms (src/nasoq.cpp:712-728, 1013-1106)
@@ -1028,27 +1354,33 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
       else if (mx[1] <= P.eps_abs) st = 2;
       else st = 3;
       R.status = st;
+      if (c.cyc) c.cyc[PH_TOTAL] += (unsigned long long)(clock64() - tp0);
     }
     __syncthreads();
   }
+  if (a.prof && tid < PH_N) atomicAdd(a.prof + tid, s_cyc[tid]);
 }
 
-size_t batch_smem_bytes(int N_max, int nr_max, int w_max, int threads, size_t tsize) {
+
+size_t batch_smem_bytes(const BArgs &a, size_t tsize) {
   auto up = [](size_t b) { return (b + 15) / 16 * 16; };
-  return up((size_t)N_max * sizeof(int)) + up((size_t)N_max * tsize) + up((size_t)nr_max * w_max * tsize) +
-         up((size_t)w_max * threads * tsize) + 2 * up((size_t)w_max * tsize) + up((size_t)w_max * sizeof(int));
+  return up((size_t)a.N_max * sizeof(int)) + up((size_t)a.N_max * tsize) + up((size_t)a.nr_max * a.w_max * tsize) +
+         up((size_t)a.w_max * 32 * tsize) + 2 * up((size_t)a.w_max * tsize) + up((size_t)a.w_max * sizeof(int)) +
+         up((size_t)a.w_max * a.w_max * tsize) + up((size_t)(a.nlev_max + 1) * sizeof(int)) + up((size_t)a.ns_max) +
+         up((size_t)a.mi_max) + (size_t)a.stage_bytes;
 }
 
-template <class T> int batch_prepare(int threads, size_t smem, int *blocks_per_sm) {
-  if (cudaFuncSetAttribute(k_nasoq_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+// Raises the kernel's dynamic shared-memory limit to smem_attr (outside any
+// stream capture) and returns how many CTAs of `smem` bytes fit on an SM.
+template <class T> int batch_prepare(int threads, size_t smem_attr, size_t smem, int *blocks_per_sm) {
+  if (cudaFuncSetAttribute(k_nasoq_batch<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_attr) !=
+      cudaSuccess)
     return NQG_ERR_CUDA;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_nasoq_batch<T>, threads, smem) != cudaSuccess)
     return NQG_ERR_CUDA;
   return NQG_OK;
 }
 
-// The dynamic shared-memory limit was raised by batch_prepare (outside any
-// stream capture).
 template <class T> int launch_batch(const BArgs &a, int grid, int threads, size_t smem, cudaStream_t st) {
   k_nasoq_batch<T><<<grid, threads, smem, st>>>(a);
   return cudaGetLastError() == cudaSuccess ? NQG_OK : NQG_ERR_CUDA;
@@ -1056,7 +1388,7 @@ template <class T> int launch_batch(const BArgs &a, int grid, int threads, size_
 
 template int launch_batch<double>(const BArgs &, int, int, size_t, cudaStream_t);
 template int launch_batch<float>(const BArgs &, int, int, size_t, cudaStream_t);
-template int batch_prepare<double>(int, size_t, int *);
-template int batch_prepare<float>(int, size_t, int *);
+template int batch_prepare<double>(int, size_t, size_t, int *);
+template int batch_prepare<float>(int, size_t, size_t, int *);
 
 }  // namespace nqg

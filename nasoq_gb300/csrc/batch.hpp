@@ -18,10 +18,11 @@
 namespace nqg {
 
 constexpr int BATCH_MR_CAP = 10;  // largest number of Krylov steps per restart
+constexpr int BATCH_PROFILE_COUNTERS = 16;
 
 struct BPat {
   int n, meq, mineq, N, base;  // N = n + meq + mineq; base = n + meq (first constraint column)
-  int ns, nlev, xsize, ssize, nnzK, max_w, max_nr;
+  int ns, nlev, xsize, ssize, nnzK, nnzR, max_w, max_nr;
   // int-pool offsets
   int o_super;     // ns+1   first (ordered) column of each supernode
   int o_sparent;   // ns     supernodal elimination tree (-1 at roots)
@@ -32,15 +33,22 @@ struct BPat {
   int o_perm0;     // N      fill-reducing order: perm0[c] = original column at position c
   int o_lvl_ptr;   // nlev+1 supernodes grouped by tree level (leaves first)
   int o_lvl_sn;    // ns
-  int o_pair_ptr;  // ns+1   descendants of every supernode (elimination-tree reach)
+  int o_lev;       // ns     tree level of each supernode
+  int o_pair_ptr;  // ns+1   descendants of every supernode (elimination-tree reach): descendants
+  int o_pair_mid;  // ns     that never hide first, then the constraint columns (from pair_mid[s])
   int o_pair_d, o_pair_lb, o_pair_ub;  // per pair: descendant, first / last row of it inside the target
   int o_Rp, o_Rj, o_Rq;  // full symmetric CSR of K (original numbering); Rq = index of the lower-CSC value
   int o_ent;       // nnzK   per lower-CSC value: constraint k of an entry in constraint row k (>= 0),
                    //        -2-col for the diagonal of column col, -1 otherwise
   int o_bt_ptr, o_bt_var, o_bt_q;  // per constraint: its variables and the lower-CSC value index of each entry
+  int o_bt_rpos;   // per constraint entry: its position in the CSR row of its variable
   int o_sn_con;    // ns     constraint whose (single) column a supernode holds, -1 otherwise
   int o_con_sn;    // mineq  supernode of each constraint column
   int o_eq_ptr, o_eq_var, o_eq_q;  // per equality row: its variables and value indices
+  int o_snrec;     // 8 ints per supernode: c0, w, nrow, value offset, row-list offset, pair start, pair_mid, pair end
+  int o_prec;      // 4 ints per pair: descendant, lb, ub, descendant's row-list offset
+  int o_con_ptr, o_con_tgt;  // per constraint: (target supernode, bit) of every pair whose descendant is its column
+  int cmask_ok;    // every supernode has at most 64 constraint-column descendants (bit masks apply)
 };
 
 // One QP of the batch: where its values are, its derived settings, and where
@@ -56,6 +64,7 @@ struct BProb {
   int64_t o_x, o_y, o_z;     // n, meq, mineq (results; warm start in)
   int64_t o_as;              // mineq ints: final active set (insertion order); warm-start set in
   double reg, zero_thresh, eps_abs, tol_abs, tol_rel;
+  double reg32;              // FP32 factor: sign-keeping floor of its diagonal (3e-5 max |k_ij|)
 };
 
 // Results of one QP (reference Nasoq fields of the same names).
@@ -69,7 +78,9 @@ struct BResult {
 
 // Per-CTA scratch: one problem at a time, sized for the largest pattern.
 struct BSlot {
-  int64_t o_L, o_D, o_ls, o_perm, o_iperm, o_lperm, o_mark, o_piv, o_act, o_alist;
+  int64_t o_L, o_D, o_ls, o_perm, o_iperm, o_lperm, o_mark, o_piv, o_alist, o_vlist, o_mlist;
+  int64_t o_Fv, o_Rv;  // factorization / refinement values of K in CSR order (inactive rows zeroed)
+  int64_t o_cmask;     // per supernode: bit mask of its active constraint-column descendants
   int64_t o_rhs, o_sol, o_r, o_w, o_V, o_Z, o_tmp;
   int64_t bytes;
 };
@@ -90,11 +101,13 @@ struct BArgs {
   int refine;                // 0: reference GMRES schedule, 1: adaptive flexible GMRES
   double refine_tol;         // adaptive: relative residual target
   int mr_max;                // capacity of the Krylov arrays
-  int N_max, w_max, nr_max;  // shared-memory sizing
+  int N_max, w_max, nr_max, ns_max, mi_max, nlev_max;  // shared-memory sizing
+  unsigned long long *prof;  // per-phase SM cycles summed over CTAs, or null
+  int stage_bytes;           // shared memory for the factor and row lists of problems that fit
 };
 
-size_t batch_smem_bytes(int N_max, int nr_max, int w_max, int threads, size_t tsize);
-template <class T> int batch_prepare(int threads, size_t smem, int *blocks_per_sm);
+size_t batch_smem_bytes(const BArgs &a, size_t tsize);
+template <class T> int batch_prepare(int threads, size_t smem_attr, size_t smem, int *blocks_per_sm);
 template <class T> int launch_batch(const BArgs &a, int grid, int threads, size_t smem, cudaStream_t st);
 
 }  // namespace nqg

@@ -41,8 +41,9 @@ struct HostPattern {
   BPat P{};
   nqg::Symbolic S;
   // integer arrays of this pattern, in BPat offset order (filled by build_pattern)
-  std::vector<int> super, sparent, col2sup, lpi, lpx, ls0, perm0, lvl_ptr, lvl_sn, pair_ptr, pair_d, pair_lb,
-      pair_ub, Rp, Rj, Rq, ent, bt_ptr, bt_var, bt_q, sn_con, con_sn, eq_ptr, eq_var, eq_q;
+  std::vector<int> super, sparent, col2sup, lpi, lpx, ls0, perm0, lvl_ptr, lvl_sn, lev, pair_ptr, pair_mid, pair_d,
+      pair_lb, pair_ub, Rp, Rj, Rq, ent, bt_ptr, bt_var, bt_q, bt_rpos, sn_con, con_sn, eq_ptr, eq_var, eq_q,
+      snrec, prec, con_ptr, con_tgt;
   std::vector<int> diag_q;  // per column: value index of its diagonal
 };
 
@@ -136,6 +137,17 @@ std::string build_pattern(const HostQP &Q, HostPattern &H, const int nrelax[3], 
     P.max_w = std::max(P.max_w, S.super[s + 1] - S.super[s]);
     P.max_nr = std::max(P.max_nr, (int)(S.lpi[s + 1] - S.lpi[s]));
   }
+  H.sn_con.assign(ns, -1);
+  H.con_sn.assign(mineq, -1);
+  for (int k = 0; k < mineq; ++k) {
+    const int oc = S.iperm[base + k];
+    const int s = S.col2sup[oc];
+    if (S.super[s + 1] - S.super[s] != 1) return "an inequality column is not a single-column supernode";
+    H.con_sn[k] = s;
+    H.sn_con[s] = k;
+  }
+  for (int s = 0; s < ns; ++s)
+    if (S.sparent[s] >= 0 && S.sparent[s] <= s) return "supernodes are not numbered in postorder";
   // levels (leaves first)
   std::vector<int> lev(ns, 0);
   int maxl = 0;
@@ -153,14 +165,19 @@ std::string build_pattern(const HostQP &Q, HostPattern &H, const int nrelax[3], 
     std::vector<int> pos(H.lvl_ptr.begin(), H.lvl_ptr.end() - (P.nlev ? 1 : 0));
     for (int s = 0; s < ns; ++s) H.lvl_sn[pos[lev[s]]++] = s;
   }
+  H.lev = lev;
   // descendant pairs from the elimination-tree reach (reference ereach_sn)
   nqg::Csc up;
   nqg::sym_permute(K, S.iperm, nullptr, &up);
   std::vector<int> mark(ns, 0), stack, lst;
   H.pair_ptr.assign(ns + 1, 0);
+  H.pair_mid.assign(ns, 0);
   for (int s = 0; s < ns; ++s) {
     nqg::ereach_sn(S, up, s, S.sparent, mark, stack, lst);
+    // descendants that never hide first, then the constraint columns
+    std::stable_partition(lst.begin(), lst.end(), [&](int d) { return H.sn_con[d] < 0; });
     const int c1 = S.super[s], c2 = S.super[s + 1];
+    int nstruct = 0;
     for (int d : lst) {
       const int *rows = S.ls.data() + S.lpi[d];
       const int nr = (int)(S.lpi[d + 1] - S.lpi[d]);
@@ -170,7 +187,9 @@ std::string build_pattern(const HostQP &Q, HostPattern &H, const int nrelax[3], 
       H.pair_d.push_back(d);
       H.pair_lb.push_back(lb);
       H.pair_ub.push_back(ub);
+      if (H.sn_con[d] < 0) nstruct++;
     }
+    H.pair_mid[s] = H.pair_ptr[s] + nstruct;
     H.pair_ptr[s + 1] = (int)H.pair_d.size();
   }
   // full symmetric CSR of K in the original numbering, with value indices
@@ -228,20 +247,67 @@ std::string build_pattern(const HostQP &Q, HostPattern &H, const int nrelax[3], 
     }
   };
   flatten(btv, btq, H.bt_ptr, H.bt_var, H.bt_q);
-  flatten(eqv, eqq, H.eq_ptr, H.eq_var, H.eq_q);
-  H.sn_con.assign(ns, -1);
-  H.con_sn.assign(mineq, -1);
-  for (int k = 0; k < mineq; ++k) {
-    const int oc = S.iperm[base + k];
-    const int s = S.col2sup[oc];
-    if (S.super[s + 1] - S.super[s] != 1) return "an inequality column is not a single-column supernode";
-    H.con_sn[k] = s;
-    H.sn_con[s] = k;
+  H.bt_rpos.assign(H.bt_var.size(), -1);
+  for (int k = 0; k < mineq; ++k)
+    for (int e = H.bt_ptr[k]; e < H.bt_ptr[k + 1]; ++e) {
+      const int v = H.bt_var[e];
+      for (int qq = H.Rp[v]; qq < H.Rp[v + 1]; ++qq)
+        if (H.Rj[qq] == base + k) H.bt_rpos[e] = qq;
+      if (H.bt_rpos[e] < 0) return "constraint entry missing from the symmetric pattern";
+    }
+  P.nnzR = H.Rp[N];
+  // packed records: one load brings a supernode's or a pair's numbers
+  H.snrec.assign((size_t)8 * ns, 0);
+  for (int s = 0; s < ns; ++s) {
+    int *r = H.snrec.data() + 8 * (size_t)s;
+    r[0] = S.super[s];
+    r[1] = S.super[s + 1] - S.super[s];
+    r[2] = (int)(S.lpi[s + 1] - S.lpi[s]);
+    r[3] = (int)S.lpx[s];
+    r[4] = (int)S.lpi[s];
+    r[5] = H.pair_ptr[s];
+    r[6] = H.pair_mid[s];
+    r[7] = H.pair_ptr[s + 1];
   }
+  const int npairs = (int)H.pair_d.size();
+  H.prec.assign((size_t)4 * npairs, 0);
+  std::vector<std::vector<int>> ctg(mineq);
+  P.cmask_ok = 1;
+  for (int s = 0; s < ns; ++s) {
+    if (H.pair_ptr[s + 1] - H.pair_mid[s] > 64) P.cmask_ok = 0;
+    for (int pq = H.pair_ptr[s]; pq < H.pair_ptr[s + 1]; ++pq) {
+      const int d = H.pair_d[pq];
+      int *r = H.prec.data() + 4 * (size_t)pq;
+      r[0] = d;
+      r[1] = H.pair_lb[pq];
+      r[2] = H.pair_ub[pq];
+      r[3] = (int)S.lpi[d];
+      if (pq >= H.pair_mid[s]) {
+        const int k = H.sn_con[d];
+        ctg[k].push_back(s);
+        ctg[k].push_back(pq - H.pair_mid[s]);
+      }
+    }
+  }
+  H.con_ptr.assign(mineq + 1, 0);
+  for (int k = 0; k < mineq; ++k) {
+    H.con_ptr[k + 1] = H.con_ptr[k] + (int)ctg[k].size() / 2;
+    H.con_tgt.insert(H.con_tgt.end(), ctg[k].begin(), ctg[k].end());
+  }
+  flatten(eqv, eqq, H.eq_ptr, H.eq_var, H.eq_q);
   return "";
 }
 
 }  // namespace
+
+struct TierLaunch {
+  nqg::BArgs args{};
+  size_t smem = 0;
+  int grid = 0, bps = 0, nprob = 0, order_off = 0;
+  int64_t slot_off = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+};
 
 struct nqg_batch {
   nqg_batch_settings set{};
@@ -266,7 +332,9 @@ struct nqg_batch {
   cudaGraphExec_t gexec = nullptr;
   cudaGraph_t graph = nullptr;
   double last_ms = 0.0;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, efork = nullptr;
+  std::vector<TierLaunch> tiers;
+  unsigned long long *d_prof = nullptr;
 };
 
 namespace {
@@ -287,6 +355,8 @@ void free_device(nqg_batch *b) {
   if (b->graph) cudaGraphDestroy(b->graph);
   b->gexec = nullptr;
   b->graph = nullptr;
+  if (b->d_prof) cudaFree(b->d_prof);
+  b->d_prof = nullptr;
   for (void *p : {(void *)b->d_pats, (void *)b->d_probs, (void *)b->d_ipool, (void *)b->d_order, (void *)b->d_head,
                   (void *)b->d_iout, (void *)b->d_dpool, (void *)b->d_dout, (void *)b->d_res, (void *)b->d_slots})
     if (p) cudaFree(p);
@@ -347,16 +417,28 @@ void fill_values(nqg_batch *b, int i, std::vector<unsigned char> &pert_pool) {
   const int N = K.n;
   unsigned char *pf = pert_pool.data() + (P.o_pert - b->n_dbl * (int64_t)sizeof(double));
   for (int j = 0; j < N; ++j) pf[j] = std::abs(kv[K.p[j]]) < P.reg ? 1 : 0;
+  double amax = 0.0;
+  for (double v : kv) amax = std::max(amax, std::abs(v));
+  P.reg32 = 3e-5 * (amax > 0 ? amax : 1.0);
 }
 
-template <class T> int prepare(nqg_batch *b, int threads, size_t smem, int *bps) {
-  return nqg::batch_prepare<T>(threads, smem, bps);
-}
-
+// Queue resets and one persistent launch per tier, forked from the batch's
+// stream and joined back into it.
 int launch(nqg_batch *b) {
-  if (b->set.qp.precision == NQG_FP32)
-    return nqg::launch_batch<float>(b->args, b->grid, b->threads, b->smem, b->stream);
-  return nqg::launch_batch<double>(b->args, b->grid, b->threads, b->smem, b->stream);
+  if (cudaEventRecord(b->efork, b->stream) != cudaSuccess) return NQG_ERR_CUDA;
+  for (size_t t = 0; t < b->tiers.size(); ++t) {
+    TierLaunch &L = b->tiers[t];
+    if (cudaStreamWaitEvent(L.stream, b->efork, 0) != cudaSuccess) return NQG_ERR_CUDA;
+    if (cudaMemsetAsync(L.args.head, 0, sizeof(int), L.stream) != cudaSuccess) return NQG_ERR_CUDA;
+    L.args.prof = b->args.prof;
+    const int rc = b->set.qp.precision == NQG_FP32
+                       ? nqg::launch_batch<float>(L.args, L.grid, b->threads, L.smem, L.stream)
+                       : nqg::launch_batch<double>(L.args, L.grid, b->threads, L.smem, L.stream);
+    if (rc) return rc;
+    if (cudaEventRecord(L.done, L.stream) != cudaSuccess) return NQG_ERR_CUDA;
+    if (cudaStreamWaitEvent(b->stream, L.done, 0) != cudaSuccess) return NQG_ERR_CUDA;
+  }
+  return NQG_OK;
 }
 
 }  // namespace
@@ -369,6 +451,7 @@ extern "C" void nqg_batch_default_settings(nqg_batch_settings *s) {
   s->refine_tol = 1e-12;
   s->threads = 0;
   s->use_graph = 1;
+  s->stage = 0;
 }
 
 extern "C" int nqg_batch_create(const nqg_batch_settings *s, nqg_batch **out) {
@@ -458,7 +541,7 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
   // ---- integer pool
   std::vector<int> ipool;
   std::vector<BPat> hp;
-  int N_max = 0, nr_max = 1, w_max = 1, xs_max = 0, ss_max = 0, ns_max = 0, mi_max = 0;
+  int N_max = 0, nr_max = 1, w_max = 1, xs_max = 0, ss_max = 0, ns_max = 1, mi_max = 1, nlev_max = 1, nR_max = 1;
   for (HostPattern &H : b->pats) {
     BPat &P = H.P;
     auto put = [&ipool](const std::vector<int> &v) {
@@ -476,7 +559,9 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
     P.o_perm0 = put(H.perm0);
     P.o_lvl_ptr = put(H.lvl_ptr);
     P.o_lvl_sn = put(H.lvl_sn);
+    P.o_lev = put(H.lev);
     P.o_pair_ptr = put(H.pair_ptr);
+    P.o_pair_mid = put(H.pair_mid);
     P.o_pair_d = put(H.pair_d);
     P.o_pair_lb = put(H.pair_lb);
     P.o_pair_ub = put(H.pair_ub);
@@ -487,11 +572,19 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
     P.o_bt_ptr = put(H.bt_ptr);
     P.o_bt_var = put(H.bt_var);
     P.o_bt_q = put(H.bt_q);
+    P.o_bt_rpos = put(H.bt_rpos);
     P.o_sn_con = put(H.sn_con);
     P.o_con_sn = put(H.con_sn);
     P.o_eq_ptr = put(H.eq_ptr);
     P.o_eq_var = put(H.eq_var);
     P.o_eq_q = put(H.eq_q);
+    // records start on 16-byte boundaries (int4 loads)
+    while (ipool.size() % 4) ipool.push_back(0);
+    P.o_snrec = put(H.snrec);
+    while (ipool.size() % 4) ipool.push_back(0);
+    P.o_prec = put(H.prec);
+    P.o_con_ptr = put(H.con_ptr);
+    P.o_con_tgt = put(H.con_tgt);
     hp.push_back(P);
     N_max = std::max(N_max, P.N);
     nr_max = std::max(nr_max, P.max_nr);
@@ -500,6 +593,8 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
     ss_max = std::max(ss_max, P.ssize);
     ns_max = std::max(ns_max, P.ns);
     mi_max = std::max(mi_max, P.mineq);
+    nlev_max = std::max(nlev_max, P.nlev);
+    nR_max = std::max(nR_max, P.nnzR);
   }
   if (ipool.size() > (size_t)INT32_MAX) return fail(b, NQG_ERR_SIZE, "integer work lists exceed 2^31 entries");
   // ---- per-problem settings and value layout
@@ -561,8 +656,12 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
   sl.o_lperm = seg((int64_t)N_max * 4);
   sl.o_mark = seg(ns_max);
   sl.o_piv = seg(ns_max);
-  sl.o_act = seg(std::max(mi_max, 1));
-  sl.o_alist = seg((int64_t)std::max(mi_max, 1) * 4);
+  sl.o_alist = seg((int64_t)mi_max * 4);
+  sl.o_vlist = seg((int64_t)ns_max * 4);
+  sl.o_mlist = seg((int64_t)ns_max * 4);
+  sl.o_Fv = seg((int64_t)nR_max * 8);
+  sl.o_Rv = seg((int64_t)nR_max * 8);
+  sl.o_cmask = seg((int64_t)ns_max * 8);
   sl.o_rhs = seg((int64_t)N_max * 8);
   sl.o_sol = seg((int64_t)N_max * 8);
   sl.o_r = seg((int64_t)N_max * 8);
@@ -571,29 +670,89 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
   sl.o_V = seg((int64_t)(mr_max + 1) * N_max * 8);
   sl.o_Z = seg((int64_t)mr_max * N_max * ts);
   sl.bytes = off;
-  // ---- launch shape
+  // ---- launch shape: shared-memory tiers.  A problem whose factor and row
+  // lists fit in a tier's staging space keeps them on chip while it runs;
+  // each tier is one persistent launch (its queue, its slots), and the tiers
+  // run side by side on forked streams.  Problems that fit no tier (or all
+  // of them, with staging off) keep them in their slot (L2 / HBM).
   BQ_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   int dev = 0;
   BQ_CUDA(cudaGetDevice(&dev));
   BQ_CUDA(cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, dev));
+  int smem_optin = 0;
+  BQ_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   b->threads = b->set.threads > 0 ? b->set.threads : 128;
   if (b->threads % 32 || b->threads > 256) return fail(b, NQG_ERR_ARG, "threads must be a multiple of 32, at most 256");
-  b->smem = nqg::batch_smem_bytes(N_max, nr_max, w_max, b->threads, ts);
-  if (b->smem > 200 * 1024) return fail(b, NQG_ERR_SIZE, "largest pattern exceeds the batched solver's shared memory");
-  int bps = 0;
-  int rc = b->set.qp.precision == NQG_FP32 ? prepare<float>(b, b->threads, b->smem, &bps)
-                                          : prepare<double>(b, b->threads, b->smem, &bps);
-  if (rc || bps <= 0) return fail(b, NQG_ERR_CUDA, "no resident CTA fits the batched kernel");
-  b->blocks_per_sm = bps;
-  b->grid = std::min(np, bps * b->num_sms);
-  // queue order: largest problems first (longest-processing-time order)
+  nqg::BArgs base_args{};
+  base_args.N_max = N_max;
+  base_args.w_max = w_max;
+  base_args.nr_max = nr_max;
+  base_args.ns_max = ns_max;
+  base_args.mi_max = mi_max;
+  base_args.nlev_max = nlev_max;
+  base_args.stage_bytes = 0;
+  const size_t base_smem = nqg::batch_smem_bytes(base_args, ts);
+  const size_t static_smem = 8 * 1024;  // the kernel's own __shared__ variables, rounded up
+  if ((int64_t)base_smem + (int64_t)static_smem > smem_optin)
+    return fail(b, NQG_ERR_SIZE, "largest pattern exceeds the batched solver's shared memory");
+  const int64_t stage_max = smem_optin - (int64_t)base_smem - (int64_t)static_smem;
+  std::vector<int64_t> need(np);
+  for (int i = 0; i < np; ++i) {
+    const BPat &P = b->pats[b->qp[i].pat].P;
+    need[i] = ((int64_t)P.xsize * (int64_t)ts + 15) / 16 * 16 + (int64_t)P.ssize * 4;
+  }
+  std::vector<int64_t> budgets;
+  if (b->set.stage) {
+    for (int64_t kb : {16, 32, 48, 64, 96, 128, 160, 192, 224})
+      if (kb * 1024 <= stage_max) budgets.push_back(kb * 1024);
+    if (budgets.empty() || budgets.back() < stage_max) budgets.push_back(stage_max / 16 * 16);
+  }
+  std::vector<int> tier_of(np, -1);  // index into budgets, -1: slot memory
+  for (int i = 0; i < np; ++i)
+    for (size_t t = 0; t < budgets.size(); ++t)
+      if (need[i] <= budgets[t]) {
+        tier_of[i] = (int)t;
+        break;
+      }
+  // queue order inside every tier: largest problems first (longest-processing-time order)
   std::vector<int> order(np);
   for (int i = 0; i < np; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    if (tier_of[x] != tier_of[y]) return tier_of[x] == -1 ? true : (tier_of[y] == -1 ? false : tier_of[x] > tier_of[y]);
     const BPat &A = b->pats[b->qp[x].pat].P, &B = b->pats[b->qp[y].pat].P;
     const double cx = (double)A.xsize * (A.mineq + 1), cy = (double)B.xsize * (B.mineq + 1);
     return cx > cy;
   });
+  b->tiers.clear();
+  for (int q = 0; q < np;) {
+    const int t = tier_of[order[q]];
+    int e = q;
+    while (e < np && tier_of[order[e]] == t) ++e;
+    TierLaunch L;
+    L.args = base_args;
+    L.args.stage_bytes = t < 0 ? 0 : (int)budgets[t];
+    L.smem = base_smem + (size_t)L.args.stage_bytes;
+    L.order_off = q;
+    L.nprob = e - q;
+    b->tiers.push_back(L);
+    q = e;
+  }
+  size_t smem_top = 0;
+  for (auto &L : b->tiers) smem_top = std::max(smem_top, L.smem);
+  int64_t nslots = 0;
+  for (auto &L : b->tiers) {
+    int bps = 0;
+    int rc = b->set.qp.precision == NQG_FP32 ? nqg::batch_prepare<float>(b->threads, smem_top, L.smem, &bps)
+                                            : nqg::batch_prepare<double>(b->threads, smem_top, L.smem, &bps);
+    if (rc || bps <= 0) return fail(b, NQG_ERR_CUDA, "no resident CTA fits the batched kernel");
+    L.bps = bps;
+    L.grid = std::min(L.nprob, bps * b->num_sms);
+    L.slot_off = nslots;
+    nslots += L.grid;
+  }
+  b->smem = smem_top;
+  b->grid = (int)nslots;
+  b->blocks_per_sm = b->tiers.empty() ? 0 : b->tiers.front().bps;
   // ---- device
   BQ_CUDA(cudaMalloc(&b->d_pats, hp.size() * sizeof(BPat)));
   BQ_CUDA(cudaMemcpy(b->d_pats, hp.data(), hp.size() * sizeof(BPat), cudaMemcpyHostToDevice));
@@ -610,30 +769,35 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
   BQ_CUDA(cudaMalloc(&b->d_res, np * sizeof(BResult)));
   BQ_CUDA(cudaMalloc(&b->d_order, np * sizeof(int)));
   BQ_CUDA(cudaMemcpy(b->d_order, order.data(), np * sizeof(int), cudaMemcpyHostToDevice));
-  BQ_CUDA(cudaMalloc(&b->d_head, sizeof(int)));
-  BQ_CUDA(cudaMalloc(&b->d_slots, (size_t)b->grid * sl.bytes));
+  BQ_CUDA(cudaMalloc(&b->d_head, std::max<size_t>(b->tiers.size(), 1) * sizeof(int)));
+  BQ_CUDA(cudaMalloc(&b->d_slots, (size_t)std::max<int64_t>(nslots, 1) * sl.bytes));
   BQ_CUDA(cudaMemcpy(b->d_probs, b->h_probs.data(), np * sizeof(BProb), cudaMemcpyHostToDevice));
-  BQ_CUDA(cudaEventCreate(&b->e0));
-  BQ_CUDA(cudaEventCreate(&b->e1));
-  nqg::BArgs &A = b->args;
-  A.pats = b->d_pats;
-  A.probs = b->d_probs;
-  A.ipool = b->d_ipool;
-  A.dpool = b->d_dpool;
-  A.dout = b->d_dout;
-  A.iout = b->d_iout;
-  A.res = b->d_res;
-  A.order = b->d_order;
-  A.head = b->d_head;
-  A.nprob = np;
-  A.slots = b->d_slots;
-  A.slot = sl;
-  A.refine = b->set.refine;
-  A.refine_tol = b->set.refine_tol;
-  A.mr_max = mr_max;
-  A.N_max = N_max;
-  A.w_max = w_max;
-  A.nr_max = nr_max;
+  BQ_CUDA(cudaEventCreateWithFlags(&b->e0, cudaEventDefault));
+  BQ_CUDA(cudaEventCreateWithFlags(&b->e1, cudaEventDefault));
+  BQ_CUDA(cudaEventCreateWithFlags(&b->efork, cudaEventDisableTiming));
+  for (size_t t = 0; t < b->tiers.size(); ++t) {
+    TierLaunch &L = b->tiers[t];
+    BQ_CUDA(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
+    BQ_CUDA(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));
+    nqg::BArgs &A = L.args;
+    A.pats = b->d_pats;
+    A.probs = b->d_probs;
+    A.ipool = b->d_ipool;
+    A.dpool = b->d_dpool;
+    A.dout = b->d_dout;
+    A.iout = b->d_iout;
+    A.res = b->d_res;
+    A.order = b->d_order + L.order_off;
+    A.head = b->d_head + t;
+    A.nprob = L.nprob;
+    A.slots = b->d_slots + (size_t)L.slot_off * sl.bytes;
+    A.slot = sl;
+    A.refine = b->set.refine;
+    A.refine_tol = b->set.refine_tol;
+    A.mr_max = mr_max;
+    A.prof = nullptr;
+  }
+  b->args.slot = sl;
   b->finalized = true;
   return NQG_OK;
 }
@@ -699,7 +863,6 @@ extern "C" int nqg_batch_solve_async(nqg_batch *b) {
   if (b->set.use_graph) {
     if (!b->gexec) {
       BQ_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-      cudaMemsetAsync(b->d_head, 0, sizeof(int), b->stream);
       int rc = launch(b);
       cudaGraph_t g = nullptr;
       cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
@@ -712,7 +875,6 @@ extern "C" int nqg_batch_solve_async(nqg_batch *b) {
     }
     BQ_CUDA(cudaGraphLaunch(b->gexec, b->stream));
   } else {
-    BQ_CUDA(cudaMemsetAsync(b->d_head, 0, sizeof(int), b->stream));
     int rc = launch(b);
     if (rc) return fail(b, rc, "launch of the batched kernel failed");
   }
@@ -814,6 +976,36 @@ extern "C" int nqg_batch_get_info(const nqg_batch *b, nqg_batch_info *info) {
   return NQG_OK;
 }
 
+extern "C" int nqg_batch_set_profiling(nqg_batch *b, int on) {
+  // Per-phase cycle counters of the next solves (summed over problems); a
+  // change rebuilds the CUDA graph.
+  if (!b || !b->finalized) return NQG_ERR_STATE;
+  if (on && !b->d_prof) {
+    BQ_CUDA(cudaMalloc(&b->d_prof, nqg::BATCH_PROFILE_COUNTERS * sizeof(unsigned long long)));
+    BQ_CUDA(cudaMemset(b->d_prof, 0, nqg::BATCH_PROFILE_COUNTERS * sizeof(unsigned long long)));
+  }
+  b->args.prof = on ? b->d_prof : nullptr;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->gexec = nullptr;
+  b->graph = nullptr;
+  return NQG_OK;
+}
+
+extern "C" int nqg_batch_get_profile(nqg_batch *b, unsigned long long *counters, int n) {
+  // Copies (and resets) the per-phase counters (see include/nasoq_gb300.h).
+  if (!b || !b->finalized || !counters || n <= 0) return NQG_ERR_ARG;
+  if (!b->d_prof) {
+    for (int k = 0; k < n; ++k) counters[k] = 0;
+    return NQG_OK;
+  }
+  unsigned long long h[nqg::BATCH_PROFILE_COUNTERS] = {};
+  BQ_CUDA(cudaMemcpy(h, b->d_prof, sizeof h, cudaMemcpyDeviceToHost));
+  BQ_CUDA(cudaMemset(b->d_prof, 0, sizeof h));
+  for (int k = 0; k < n && k < nqg::BATCH_PROFILE_COUNTERS; ++k) counters[k] = h[k];
+  return NQG_OK;
+}
+
 extern "C" int nqg_batch_get_stream(const nqg_batch *b, void **stream) {
   if (!b || !stream || !b->finalized) return NQG_ERR_ARG;
   *stream = b->stream;
@@ -826,6 +1018,11 @@ extern "C" int nqg_batch_destroy(nqg_batch *b) {
   if (!b) return NQG_ERR_ARG;
   if (b->stream) cudaStreamSynchronize(b->stream);
   free_device(b);
+  for (auto &L : b->tiers) {
+    if (L.stream) cudaStreamDestroy(L.stream);
+    if (L.done) cudaEventDestroy(L.done);
+  }
+  if (b->efork) cudaEventDestroy(b->efork);
   if (b->e0) cudaEventDestroy(b->e0);
   if (b->e1) cudaEventDestroy(b->e1);
   if (b->stream) cudaStreamDestroy(b->stream);

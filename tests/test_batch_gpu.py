@@ -113,7 +113,9 @@ def test_batch_mixed_precision_meets_tolerance(record_property):
 
 @pytest.mark.gpu
 def test_batch_repeat_and_new_vectors():
-    """A second solve (graph replay) gives identical bits; new q / d for the
+    """A second solve (graph replay) makes the same decisions (iteration
+    counts) and the same solution to 1e-12 (the triangular solves push with
+    atomics, so the last bits may differ between runs); new q / d for the
     parametric instances give the results of a batch built with them."""
     d, qps = fixture()
     sel = [q for q, k in zip(qps, d["spec"].reshape(-1, 5)[:, 0]) if k == KIND_PARAM]
@@ -121,7 +123,8 @@ def test_batch_repeat_and_new_vectors():
     x1, y1, z1, s1 = b.results()
     b.solve()
     x2, y2, z2, s2 = b.results()
-    assert np.array_equal(x1, x2) and np.array_equal(z1, z2)
+    assert [s.num_iter for s in s1] == [s.num_iter for s in s2]
+    assert rel(x2, x1) <= 1e-12 and rel(z2, z1) <= 1e-12
     fam = P.mpc_parametric(0)
     ths = [np.random.default_rng(5000 + t).standard_normal(32) for t in range(len(sel))]
     b.set_vectors(q_all=np.concatenate([fam.q_of(t) for t in ths]), d_all=np.concatenate([fam.d_of(t) for t in ths]))
@@ -130,7 +133,7 @@ def test_batch_repeat_and_new_vectors():
     fresh = [P.QP(fam.base.H, fam.q_of(t), fam.base.A, fam.base.b, fam.base.C, fam.d_of(t)) for t in ths]
     b2 = _run(d, fresh, precision=nq.NQG_FP64, refine=0)
     x4, _, z4, s4 = b2.results()
-    assert np.array_equal(x3, x4) and np.array_equal(z3, z4)
+    assert rel(x3, x4) <= 1e-12 and rel(z3, z4) <= 1e-12
     assert [s.num_iter for s in s3] == [s.num_iter for s in s4]
     b.close()
     b2.close()
