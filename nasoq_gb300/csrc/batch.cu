@@ -52,6 +52,7 @@ template <class T> struct Ctx {
   const int4 *__restrict__ snrec;  // 2 per supernode: {c0, w, nrow, value offset}, {row-list offset, pairs}
   const int4 *__restrict__ prec;   // per pair: {descendant, lb, ub, descendant's row-list offset}
   const int *__restrict__ con_ptr, *__restrict__ con_tgt;
+  const uint8_t *__restrict__ sn_big;  // per supernode: solved by a warp (wide or tall block)
   // problem
   const double *__restrict__ kv, *__restrict__ q, *__restrict__ bq, *__restrict__ dq;
   const uint8_t *__restrict__ pert;
@@ -70,7 +71,9 @@ template <class T> struct Ctx {
   int *lp;
   uint8_t *vis;  // per supernode: visible (structural, or the column of an active constraint)
   uint8_t *act;  // per constraint: active
-  int *vlvl;     // visible supernodes of each level: vlist[vlvl[l] .. vlvl[l+1])
+  int *vlvl;     // visible supernodes of each level: vlist[vlvl[l] .. vlvl[l+1]),
+  int *vmid;     // the small ones (a thread each) before vmid[l], the big ones (a warp each) after
+  int *vfill;    // 2 * (nlev + 1) fill counters of build_vlist
   int *nmark;    // length of mlist
   double *red;   // 32 doubles
   int *redi;     // 32 ints
@@ -308,6 +311,169 @@ template <class T> __device__ void sub_update_warp(Ctx<T> &c, int pq, int d, int
   }
 }
 
+// Warp-wide argmax of |value| with the smallest index winning ties (the
+// LAPACK idamax convention); every lane returns the winner.
+template <class T> __device__ __forceinline__ void warp_argmax(T &v, int &idx) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const T ov = __shfl_xor_sync(0xffffffffu, v, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+    if (oi >= 0 && (idx < 0 || ov > v || (ov == v && oi < idx))) {
+      v = ov;
+      idx = oi;
+    }
+  }
+}
+
+template <class T> __device__ __forceinline__ void s_flag_store(Ctx<T> &c, bool f) { c.redi[31] = f ? 1 : 0; }
+
+// Bunch-Kaufman (alpha = (1+sqrt(17))/8, the LAPACK dsytf2('L') pivot rule
+// and the reference's reorder_after_sytrf form: explicit interchanges, L with
+// unit diagonal, D / E the diagonal and 2x2 sub-diagonals, perm[m] = original
+// local column at position m) on a w <= 32 wide lower-stored block, by one
+// warp: the steps and the arithmetic of each entry are those of the CTA-wide
+// bk_factor.  wk holds 2 (w - 2) multipliers of a 2x2 step.  Returns whether
+// any interchange happened.
+template <class T>
+__device__ bool bk_factor_warp(T *a, int lda, int w, T *D, T *E, int *perm, int *status, T *wk) {
+  const T alpha = (T)((1.0 + sqrt(17.0)) / 8.0);
+  const int lane = lane_id();
+  bool pivoted = false;
+  for (int m = lane; m < w; m += 32) perm[m] = m;
+  __syncwarp();
+  int k = 0;
+  while (k < w) {
+    const T absakk = tabs(a[k + (size_t)k * lda]);
+    T cv = T(-1);
+    int ci = -1;
+    for (int i = k + 1 + lane; i < w; i += 32) {
+      const T v = tabs(a[i + (size_t)k * lda]);
+      if (ci < 0 || v > cv) {
+        cv = v;
+        ci = i;
+      }
+    }
+    warp_argmax(cv, ci);
+    const T colmax = ci >= 0 ? cv : T(0);
+    const int imax = ci;
+    int kp = k, kstep = 1, zero = 0;
+    if ((absakk >= colmax ? absakk : colmax) == T(0) || absakk != absakk) {
+      zero = 1;
+    } else if (absakk >= alpha * colmax) {
+      kp = k;
+    } else {
+      T rv = T(-1);
+      int ri = -1;
+      for (int j = k + lane; j < w; j += 32) {
+        if (j == imax) continue;
+        const T v = j < imax ? tabs(a[imax + (size_t)j * lda]) : tabs(a[j + (size_t)imax * lda]);
+        if (ri < 0 || v > rv) {
+          rv = v;
+          ri = j;
+        }
+      }
+      warp_argmax(rv, ri);
+      const T rowmax = rv;
+      if (absakk >= alpha * colmax * (colmax / rowmax)) {
+        kp = k;
+      } else if (tabs(a[imax + (size_t)imax * lda]) >= alpha * rowmax) {
+        kp = imax;
+      } else {
+        kp = imax;
+        kstep = 2;
+      }
+    }
+    const int kk = k + kstep - 1;
+    if (zero && lane == 0) atomicOr(status, ST_ZERO_PIVOT);
+    if (kp != kk) {  // symmetric interchange of kk and kp (kp > kk)
+      pivoted = true;
+      for (int i = kp + 1 + lane; i < w; i += 32) {
+        const T t = a[i + (size_t)kk * lda];
+        a[i + (size_t)kk * lda] = a[i + (size_t)kp * lda];
+        a[i + (size_t)kp * lda] = t;
+      }
+      for (int j = kk + 1 + lane; j < kp; j += 32) {
+        const T t = a[j + (size_t)kk * lda];
+        a[j + (size_t)kk * lda] = a[kp + (size_t)j * lda];
+        a[kp + (size_t)j * lda] = t;
+      }
+      const int ncols_left = kstep == 2 ? k + 1 : k;
+      for (int cc = lane; cc < ncols_left; cc += 32) {
+        const T t = a[kk + (size_t)cc * lda];
+        a[kk + (size_t)cc * lda] = a[kp + (size_t)cc * lda];
+        a[kp + (size_t)cc * lda] = t;
+      }
+      if (lane == 0) {
+        const T t = a[kk + (size_t)kk * lda];
+        a[kk + (size_t)kk * lda] = a[kp + (size_t)kp * lda];
+        a[kp + (size_t)kp * lda] = t;
+        const int pt = perm[kk];
+        perm[kk] = perm[kp];
+        perm[kp] = pt;
+      }
+    }
+    __syncwarp();
+    if (kstep == 1) {
+      if (!zero) {
+        const T r1 = T(1) / a[k + (size_t)k * lda];
+        const int m = w - k - 1;
+        for (int e = lane; e < m * m; e += 32) {
+          const int jj = e / m, ii = e % m;
+          if (ii < jj) continue;
+          const int i = k + 1 + ii, j = k + 1 + jj;
+          a[i + (size_t)j * lda] -= r1 * a[j + (size_t)k * lda] * a[i + (size_t)k * lda];
+        }
+        __syncwarp();
+        for (int i = k + 1 + lane; i < w; i += 32) a[i + (size_t)k * lda] *= r1;
+      }
+      if (lane == 0) {
+        D[k] = a[k + (size_t)k * lda];
+        E[k] = T(0);
+      }
+    } else {
+      // 2x2 pivot on rows/cols k, k+1
+      T d21 = a[k + 1 + (size_t)k * lda];
+      const T d11 = a[k + 1 + (size_t)(k + 1) * lda] / d21;
+      const T d22 = a[k + (size_t)k * lda] / d21;
+      const T t = T(1) / (d11 * d22 - T(1));
+      d21 = t / d21;
+      const int m = w - k - 2;
+      for (int q = lane; q < m; q += 32) {
+        const int j = k + 2 + q;
+        const T ajk = a[j + (size_t)k * lda], ajk1 = a[j + (size_t)(k + 1) * lda];
+        wk[2 * q] = d21 * (d11 * ajk - ajk1);
+        wk[2 * q + 1] = d21 * (d22 * ajk1 - ajk);
+      }
+      __syncwarp();
+      for (int e = lane; e < m * m; e += 32) {
+        const int q = e / m, ii = e % m;
+        const int j = k + 2 + q, i = k + 2 + ii;
+        if (i < j) continue;
+        a[i + (size_t)j * lda] -= a[i + (size_t)k * lda] * wk[2 * q] + a[i + (size_t)(k + 1) * lda] * wk[2 * q + 1];
+      }
+      __syncwarp();
+      for (int q = lane; q < m; q += 32) {
+        const int j = k + 2 + q;
+        a[j + (size_t)k * lda] = wk[2 * q];
+        a[j + (size_t)(k + 1) * lda] = wk[2 * q + 1];
+      }
+      __syncwarp();
+      if (lane == 0) {
+        D[k] = a[k + (size_t)k * lda];
+        D[k + 1] = a[k + 1 + (size_t)(k + 1) * lda];
+        E[k] = a[k + 1 + (size_t)k * lda];
+        E[k + 1] = T(0);
+        a[k + 1 + (size_t)k * lda] = T(0);
+      }
+    }
+    __syncwarp();
+    k += kstep;
+  }
+  for (int m = lane; m < w; m += 32) a[m + (size_t)m * lda] = T(1);
+  __syncwarp();
+  return pivoted;
+}
+
 // ---- factorization of one supernode (CTA scope) ------------------------------
 // Left-looking step of the reference (Serial_update_ldl.cpp:62-190): scatter
 // the matrix columns, subtract every visible descendant's L D L^T restricted
@@ -323,11 +489,14 @@ template <class T> __device__ void factor_sn(Ctx<T> &c, int s) {
   for (int p = tid; p < nr; p += nt) c.map[rows[p]] = p;
   for (int e = tid; e < nr * w; e += nt) B[e] = T(0);
   __syncthreads();
-  // matrix columns (symmetric neighbours of the original column, ordered >= the column)
-  for (int m = 0; m < w; ++m) {
+  // matrix columns (symmetric neighbours of the original column, ordered >=
+  // the column): g threads per column, all columns at once
+  const int g = w < nt ? nt / w : 1;
+  for (int t = tid; t < w * g; t += nt) {
+    const int m = t % w, k0 = t / w;
     const int col = c0 + m;
     const int j = c.perm[col];
-    for (int qq = c.Rp[j] + tid; qq < c.Rp[j + 1]; qq += nt) {
+    for (int qq = c.Rp[j] + k0; qq < c.Rp[j + 1]; qq += g) {
       const int oi = c.iperm[c.Rj[qq]];
       if (oi < col) continue;
       const int pos = c.map[oi];
@@ -349,9 +518,19 @@ template <class T> __device__ void factor_sn(Ctx<T> &c, int s) {
     });
   }
   __syncthreads();
-  // Bunch-Kaufman on the diagonal block, then the rows below
+  // Bunch-Kaufman on the diagonal block (one warp up to 32 columns), then the rows below
   bool pivoted = false;
-  bk_factor<T>(B, nr, w, c.Dsm, c.Esm, c.lp, c.status, &pivoted);
+  if (w <= 32) {
+    if (warp_id() == 0) {
+      const bool pv = bk_factor_warp<T>(B, nr, w, c.Dsm, c.Esm, c.lp, c.status, c.rowbuf);
+      if (lane_id() == 0) s_flag_store(c, pv);
+    }
+    __syncthreads();
+    pivoted = c.redi[31] != 0;
+    __syncthreads();
+  } else {
+    bk_factor<T>(B, nr, w, c.Dsm, c.Esm, c.lp, c.status, &pivoted);
+  }
   __syncthreads();
   if (nr > w) panel_rows_warp0(c, B, nr, w, pivoted);
   __syncthreads();
@@ -540,20 +719,20 @@ template <class T> __device__ void bwd_warp(Ctx<T> &c, int s) {
   }
 }
 
-// x <- (L D L^T)^-1 x on the visible part, in the factor's order.
+// x <- (L D L^T)^-1 x on the visible part, in the factor's order.  Per
+// level, small supernodes take a thread each and big ones a warp each, in
+// the same pass (supernodes of one level are independent).
 template <class T> __device__ void ldlt_solve_smem(Ctx<T> &c) {
   const int nw = num_warps();
-  for (int l = 0; l < c.nlev; ++l) {
+  {
     BQ_T0(c);
-    const int a = c.vlvl[l], b = c.vlvl[l + 1];
-    const bool wide = b - a > 2 * nw;
-    if (wide) {
-      for (int q = a + threadIdx.x; q < b; q += blockDim.x) fwd_thread(c, c.vlist[q]);
-    } else {
-      for (int q = a + warp_id(); q < b; q += nw) fwd_warp(c, c.vlist[q]);
+    for (int l = 0; l < c.nlev; ++l) {
+      const int a = c.vlvl[l], m = c.vmid[l], b = c.vlvl[l + 1];
+      for (int q = a + threadIdx.x; q < m; q += blockDim.x) fwd_thread(c, c.vlist[q]);
+      for (int q = m + warp_id(); q < b; q += nw) fwd_warp(c, c.vlist[q]);
+      __syncthreads();
     }
-    __syncthreads();
-    BQ_T1(c, wide ? PH_FWD_WIDE : PH_FWD_NARROW);
+    BQ_T1(c, PH_FWD_WIDE);
   }
   {
     BQ_T0(c);
@@ -577,49 +756,39 @@ template <class T> __device__ void ldlt_solve_smem(Ctx<T> &c) {
   }
   BQ_T0(c);
   for (int l = c.nlev - 1; l >= 0; --l) {
-    const int a = c.vlvl[l], b = c.vlvl[l + 1];
-    if (b - a > 2 * nw) {
-      for (int q = a + threadIdx.x; q < b; q += blockDim.x) bwd_thread(c, c.vlist[q]);
-    } else {
-      for (int q = a + warp_id(); q < b; q += nw) bwd_warp(c, c.vlist[q]);
-    }
+    const int a = c.vlvl[l], m = c.vmid[l], b = c.vlvl[l + 1];
+    for (int q = a + threadIdx.x; q < m; q += blockDim.x) bwd_thread(c, c.vlist[q]);
+    for (int q = m + warp_id(); q < b; q += nw) bwd_warp(c, c.vlist[q]);
     __syncthreads();
   }
   BQ_T1(c, PH_BWD);
 }
 
-// Visible supernodes grouped by level (after every change of the active set),
-// each level in the pattern's order.
+// Visible supernodes grouped by level (after every change of the active set):
+// per level the small ones, then the big ones.
 template <class T> __device__ void build_vlist(Ctx<T> &c) {
-  for (int l = threadIdx.x; l <= c.nlev; l += blockDim.x) c.vlvl[l] = 0;
+  const int L1 = c.nlev + 1;
+  for (int l = threadIdx.x; l < 2 * L1; l += blockDim.x) c.vfill[l] = 0;
   __syncthreads();
   for (int s = threadIdx.x; s < c.ns; s += blockDim.x)
-    if (c.vis[s]) atomicAdd(&c.vlvl[c.lev[s] + 1], 1);
+    if (c.vis[s]) atomicAdd(&c.vfill[c.lev[s] + (c.sn_big[s] ? L1 : 0)], 1);
   __syncthreads();
-  if (threadIdx.x == 0)
-    for (int l = 0; l < c.nlev; ++l) c.vlvl[l + 1] += c.vlvl[l];
-  __syncthreads();
-  for (int l = 0; l < c.nlev; ++l) {
-    const int a = c.lvl_ptr[l], b = c.lvl_ptr[l + 1];
-    int base = c.vlvl[l];
-    for (int q0 = a; q0 < b; q0 += blockDim.x) {
-      const int q = q0 + threadIdx.x;
-      const int sn = q < b ? c.lvl_sn[q] : -1;
-      const int f = (sn >= 0 && c.vis[sn]) ? 1 : 0;
-      const unsigned bal = __ballot_sync(0xffffffffu, f);
-      const int wpre = __popc(bal & ((1u << lane_id()) - 1u));
-      if (lane_id() == 0) c.redi[warp_id()] = __popc(bal);
-      __syncthreads();
-      int before = 0, total = 0;
-      for (int t = 0; t < num_warps(); ++t) {
-        if (t < warp_id()) before += c.redi[t];
-        total += c.redi[t];
-      }
-      if (f) c.vlist[base + before + wpre] = sn;
-      base += total;
-      __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int l = 0; l < c.nlev; ++l) {
+      c.vlvl[l] = acc;
+      acc += c.vfill[l];
+      c.vmid[l] = acc;
+      acc += c.vfill[L1 + l];
+      c.vfill[l] = c.vlvl[l];     // next free position of the small ones
+      c.vfill[L1 + l] = c.vmid[l];  // and of the big ones
     }
+    c.vlvl[c.nlev] = acc;
   }
+  __syncthreads();
+  for (int s = threadIdx.x; s < c.ns; s += blockDim.x)
+    if (c.vis[s]) c.vlist[atomicAdd(&c.vfill[c.lev[s] + (c.sn_big[s] ? L1 : 0)], 1)] = s;
+  __syncthreads();
 }
 
 // out = M^-1 v (original numbering; hidden rows give zero).  Vectors in
@@ -935,6 +1104,10 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
   sp += up16((size_t)a.w_max * a.w_max * sizeof(T));
   int *vlvl = reinterpret_cast<int *>(sp);
   sp += up16((size_t)(a.nlev_max + 1) * sizeof(int));
+  int *vmid = reinterpret_cast<int *>(sp);
+  sp += up16((size_t)(a.nlev_max + 1) * sizeof(int));
+  int *vfill = reinterpret_cast<int *>(sp);
+  sp += up16((size_t)2 * (a.nlev_max + 1) * sizeof(int));
   uint8_t *vis = sp;
   sp += up16((size_t)a.ns_max);
   uint8_t *act = sp;
@@ -991,6 +1164,7 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
       c.prec = reinterpret_cast<const int4 *>(ip + pt.o_prec);
       c.con_ptr = ip + pt.o_con_ptr;
       c.con_tgt = ip + pt.o_con_tgt;
+      c.sn_big = reinterpret_cast<const uint8_t *>(ip + pt.o_sn_big);
       c.kv = a.dpool + P.o_kv;
       c.q = a.dpool + P.o_q;
       c.bq = a.dpool + P.o_b;
@@ -1037,6 +1211,8 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
       c.vis = vis;
       c.act = act;
       c.vlvl = vlvl;
+      c.vmid = vmid;
+      c.vfill = vfill;
       c.nmark = &s_nmark;
       c.red = red;
       c.redi = redi;
@@ -1366,7 +1542,7 @@ size_t batch_smem_bytes(const BArgs &a, size_t tsize) {
   auto up = [](size_t b) { return (b + 15) / 16 * 16; };
   return up((size_t)a.N_max * sizeof(int)) + up((size_t)a.N_max * tsize) + up((size_t)a.nr_max * a.w_max * tsize) +
          up((size_t)a.w_max * 32 * tsize) + 2 * up((size_t)a.w_max * tsize) + up((size_t)a.w_max * sizeof(int)) +
-         up((size_t)a.w_max * a.w_max * tsize) + up((size_t)(a.nlev_max + 1) * sizeof(int)) + up((size_t)a.ns_max) +
+         up((size_t)a.w_max * a.w_max * tsize) + 4 * up((size_t)(a.nlev_max + 1) * sizeof(int)) + up((size_t)a.ns_max) +
          up((size_t)a.mi_max) + (size_t)a.stage_bytes;
 }
 

@@ -48,6 +48,7 @@ struct BPat {
   int o_snrec;     // 8 ints per supernode: c0, w, nrow, value offset, row-list offset, pair start, pair_mid, pair end
   int o_prec;      // 4 ints per pair: descendant, lb, ub, descendant's row-list offset
   int o_con_ptr, o_con_tgt;  // per constraint: (target supernode, bit) of every pair whose descendant is its column
+  int o_sn_big;    // ns bytes (packed in ints): 1 where a warp solves the supernode (w > 4 or nrow * w > 64)
   int cmask_ok;    // every supernode has at most 64 constraint-column descendants (bit masks apply)
 };
 

@@ -43,7 +43,7 @@ struct HostPattern {
   // integer arrays of this pattern, in BPat offset order (filled by build_pattern)
   std::vector<int> super, sparent, col2sup, lpi, lpx, ls0, perm0, lvl_ptr, lvl_sn, lev, pair_ptr, pair_mid, pair_d,
       pair_lb, pair_ub, Rp, Rj, Rq, ent, bt_ptr, bt_var, bt_q, bt_rpos, sn_con, con_sn, eq_ptr, eq_var, eq_q,
-      snrec, prec, con_ptr, con_tgt;
+      snrec, prec, con_ptr, con_tgt, sn_big;
   std::vector<int> diag_q;  // per column: value index of its diagonal
 };
 
@@ -288,6 +288,12 @@ std::string build_pattern(const HostQP &Q, HostPattern &H, const int nrelax[3], 
         ctg[k].push_back(pq - H.pair_mid[s]);
       }
     }
+  }
+  // supernodes the solves give a warp: wide or tall blocks (one flag byte each, packed in ints)
+  H.sn_big.assign((ns + 3) / 4 + 1, 0);
+  for (int s = 0; s < ns; ++s) {
+    const int w = S.super[s + 1] - S.super[s], nr = (int)(S.lpi[s + 1] - S.lpi[s]);
+    if (w > 4 || (int64_t)nr * w > 64) reinterpret_cast<unsigned char *>(H.sn_big.data())[s] = 1;
   }
   H.con_ptr.assign(mineq + 1, 0);
   for (int k = 0; k < mineq; ++k) {
@@ -585,6 +591,7 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
     P.o_prec = put(H.prec);
     P.o_con_ptr = put(H.con_ptr);
     P.o_con_tgt = put(H.con_tgt);
+    P.o_sn_big = put(H.sn_big);
     hp.push_back(P);
     N_max = std::max(N_max, P.N);
     nr_max = std::max(nr_max, P.max_nr);
