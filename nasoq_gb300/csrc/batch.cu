@@ -626,6 +626,7 @@ template <class T> __device__ void fwd_thread(Ctx<T> &c, int s) {
     for (int j = 0; j < i; ++j) acc += Ls[i + (size_t)j * nr] * x[c0 + j];
     x[c0 + i] = acc;
   }
+#pragma unroll 4
   for (int r = w; r < nr; ++r) {
     T y = T(0);
     for (int k = 0; k < w; ++k) y += Ls[r + (size_t)k * nr] * x[c0 + k];
@@ -673,6 +674,7 @@ template <class T> __device__ void bwd_thread(Ctx<T> &c, int s) {
   const T *Ls = c.L + r0.w;
   for (int j = 0; j < w; ++j) {
     T acc = T(0);
+#pragma unroll 4
     for (int r = w; r < nr; ++r) {
       const int rr = rows[r];
       if ((unsigned)rr < (unsigned)c.N) acc += Ls[r + (size_t)j * nr] * x[rr];
@@ -1308,6 +1310,7 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
     int num_iter = 0, converged = 0, nxt_active = -1, nxt_drop = -1, to_add = 1;
     int typ = 0;  // 0 solve, 1 update (partial refactorization first)
     const double DMAX = DBL_MAX;
+    for (int pol = 0;; ++pol) {
     for (;;) {
       if (num_iter > P.max_iter_nas) {
         converged = 0;
@@ -1446,6 +1449,54 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
         c.cyc[PH_UPDATE] += (unsigned long long)(clock64() - tu0);
         c.cyc[PH_ITER] += 1;
       }
+    }
+    // Polish (adaptive refinement only): the updates x -= step * descent
+    // carry each solve's residual (1e-12 relative) through every iteration,
+    // so the final point is recomputed as the equality-constrained solution
+    // on the final active set.  Kept when its multipliers stay non-negative;
+    // if it then violates a constraint, the active-set iteration continues
+    // from it (at most twice).  The reference's fixed schedule runs to 1e-15
+    // and needs none of this.
+    if (!adaptive || !converged || pol >= 2) break;
+    if (*c.nmark > 0) {
+      sort_mlist(c);
+      factor_marked(c);
+      build_vlist(c);
+    }
+    typ = 0;
+    for (int i = tid; i < N; i += nt) {
+      double v = 0.0;
+      if (i < n) v = -c.q[i];
+      else if (i < c.base) v = c.bq[i - n];
+      else if (c.act[i - c.base]) v = c.dq[i - c.base];
+      c.rhs[i] = v;
+    }
+    __syncthreads();
+    precond(c, c.rhs, c.sol);
+    solves++;
+    steps += refine(c, c.rhs, c.sol, P.outer, P.inner, flexible, adaptive, a.refine_tol, P.tol_abs, P.tol_rel, gs);
+    int negz = 0;
+    for (int t = tid; t < nact; t += nt)
+      if (c.sol[c.base + c.alist[t]] < 0.0) negz++;
+    negz = block_sum_int(negz, redi);
+    if (negz > 0) break;  // keep the iteration's own point
+    for (int i = tid; i < n; i += nt) xv[i] = c.sol[i];
+    for (int i = tid; i < meq; i += nt) yv[i] = c.sol[n + i];
+    for (int t = tid; t < nact; t += nt) {
+      const int k = c.alist[t];
+      zv[k] = c.sol[c.base + k];
+    }
+    __syncthreads();
+    int viol = 0;
+    for (int k = tid; k < mineq; k += nt) {
+      double t = 0.0;
+      for (int e = c.bt_ptr[k]; e < c.bt_ptr[k + 1]; ++e) t += c.kv[c.bt_q[e]] * xv[c.bt_var[e]];
+      if (t - c.dq[k] > P.eps_abs) viol++;
+    }
+    viol = block_sum_int(viol, redi);
+    if (viol == 0) break;
+    converged = 0;
+    to_add = 1;
     }
 
     // ---- results: objective and KKT norms (src/nasoq.cpp:712-728, 1013-1106)
