@@ -300,6 +300,15 @@ int nqg_batch_set_vectors(nqg_batch *b, const double *q_all, const double *a_all
  * start), and continues the active-set iteration from there (the role of the
  * reference's set_warm_start, src/nasoq.cpp:413-436). */
 int nqg_batch_set_warm_start(nqg_batch *b, int i, int n_as, const int *as);
+/* Warm-start sets of every problem from device-resident scores (row i, ld
+ * floats apart: one score per inequality of problem i, e.g. the logits of an
+ * nqg_mlp): each problem proposes its constraints scoring above `threshold`,
+ * skipping one parallel to a constraint already proposed (the two sides of a
+ * box); a problem without proposal starts cold.  Enqueued on the batch's
+ * stream. */
+int nqg_batch_warm_start_from_scores(nqg_batch *b, const float *d_scores, int ld, float threshold);
+/* Every problem back to a cold start. */
+int nqg_batch_clear_warm_starts(nqg_batch *b);
 /* Solves every problem; returns when done. */
 int nqg_batch_solve(nqg_batch *b);
 /* Enqueues the solve on the batch's stream (nqg_batch_get_stream) and returns. */
@@ -320,6 +329,30 @@ int nqg_batch_set_profiling(nqg_batch *b, int on);
 int nqg_batch_get_profile(nqg_batch *b, unsigned long long *counters, int n);
 const char *nqg_batch_last_error(const nqg_batch *b);
 int nqg_batch_destroy(nqg_batch *b);
+
+/* ---- active-set model (learned warm start) ----------------------------------
+ * No counterpart in the reference (its warm-start entry, Nasoq::set_warm_start,
+ * src/nasoq.cpp:413-436, takes a given set).  A multilayer perceptron theta ->
+ * one logit per inequality of a parametric QP family (ReLU hidden layers,
+ * BF16 weights with FP32 master copies, FP32 accumulation), trained on the
+ * GPU by its own forward / backward kernels with Adam on a weighted sigmoid
+ * cross-entropy; its logits feed nqg_batch_warm_start_from_scores.
+ * sizes[0] inputs, sizes[1 .. nsizes-2] hidden widths, sizes[nsizes-1]
+ * outputs; weights row-major (out x in), layer after layer. */
+typedef struct nqg_mlp nqg_mlp;
+int nqg_mlp_create(int nsizes, const int *sizes, unsigned long long seed, nqg_mlp **out);
+int nqg_mlp_num_params(const nqg_mlp *m, long *n_weights, long *n_biases);
+int nqg_mlp_set_weights(nqg_mlp *m, const float *w_all, const float *b_all);
+int nqg_mlp_get_weights(nqg_mlp *m, float *w_all, float *b_all);
+int nqg_mlp_forward(nqg_mlp *m, int rows, const float *x, float *logits);
+int nqg_mlp_forward_device(nqg_mlp *m, int rows, const float *d_x, float *d_logits, void *stream);
+int nqg_mlp_loss_grad(nqg_mlp *m, int rows, const float *x, const float *y, float pos_weight, double *loss,
+                      float *gw_all, float *gb_all);
+int nqg_mlp_set_data(nqg_mlp *m, int n, const float *x, const float *y);
+int nqg_mlp_train(nqg_mlp *m, int epochs, int batch, float lr, float pos_weight, unsigned long long seed,
+                  double *epoch_loss);
+const char *nqg_mlp_last_error(const nqg_mlp *m);
+int nqg_mlp_destroy(nqg_mlp *m);
 
 #ifdef __cplusplus
 }

@@ -149,6 +149,21 @@ def lib():
     L.nqg_batch_last_error.argtypes = [C.c_void_p]
     L.nqg_batch_last_error.restype = C.c_char_p
     L.nqg_batch_destroy.argtypes = [C.c_void_p]
+    L.nqg_batch_warm_start_from_scores.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_float]
+    L.nqg_batch_clear_warm_starts.argtypes = [C.c_void_p]
+    L.nqg_mlp_create.argtypes = [C.c_int, C.c_void_p, C.c_ulonglong, C.POINTER(C.c_void_p)]
+    L.nqg_mlp_num_params.argtypes = [C.c_void_p, C.POINTER(C.c_long), C.POINTER(C.c_long)]
+    L.nqg_mlp_set_weights.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.nqg_mlp_get_weights.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.nqg_mlp_forward.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    L.nqg_mlp_forward_device.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.nqg_mlp_loss_grad.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_float,
+                                    C.POINTER(C.c_double), C.c_void_p, C.c_void_p]
+    L.nqg_mlp_set_data.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    L.nqg_mlp_train.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_ulonglong, C.c_void_p]
+    L.nqg_mlp_last_error.argtypes = [C.c_void_p]
+    L.nqg_mlp_last_error.restype = C.c_char_p
+    L.nqg_mlp_destroy.argtypes = [C.c_void_p]
     L.nqg_batch_set_profiling.argtypes = [C.c_void_p, C.c_int]
     L.nqg_batch_get_profile.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
     _lib = L
@@ -439,6 +454,15 @@ class QPBatch:
         a = np.ascontiguousarray(active_set, np.int32)
         self._raise(lib().nqg_batch_set_warm_start(self._h, int(i), len(a), _ptr(a)), "warm start")
 
+    def warm_start_from_scores(self, d_scores_ptr, ld, threshold=0.0):
+        """Warm-start sets from device-resident scores (one row of ld floats
+        per problem, e.g. model logits)."""
+        self._raise(lib().nqg_batch_warm_start_from_scores(self._h, C.c_void_p(d_scores_ptr), int(ld),
+                                                           float(threshold)), "warm start from scores")
+
+    def clear_warm_starts(self):
+        self._raise(lib().nqg_batch_clear_warm_starts(self._h), "clear warm starts")
+
     def solve(self):
         self._raise(lib().nqg_batch_solve(self._h), "batch solve")
 
@@ -490,6 +514,86 @@ class QPBatch:
     def close(self):
         if getattr(self, "_h", None):
             lib().nqg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class MLP:
+    """Active-set model (nqg_mlp_*): sizes = (inputs, hidden..., outputs),
+    ReLU hidden layers, BF16 weights with FP32 master copies, trained on the
+    GPU by the library's own kernels."""
+
+    def __init__(self, sizes, seed=0):
+        L = lib()
+        self.sizes = tuple(int(v) for v in sizes)
+        arr = (C.c_int * len(self.sizes))(*self.sizes)
+        h = C.c_void_p()
+        _check(L.nqg_mlp_create(len(self.sizes), C.cast(arr, C.c_void_p), int(seed), C.byref(h)), "mlp create")
+        self._h = h
+        nw, nb = C.c_long(), C.c_long()
+        L.nqg_mlp_num_params(h, C.byref(nw), C.byref(nb))
+        self.n_weights, self.n_biases = nw.value, nb.value
+
+    def _raise(self, rc, what):
+        if rc < 0:
+            raise NasoqError(f"{what}: {lib().nqg_status_str(rc).decode()} ({rc}) "
+                             f"{lib().nqg_mlp_last_error(self._h).decode()}")
+
+    def get_weights(self):
+        w = np.zeros(self.n_weights, np.float32)
+        b = np.zeros(self.n_biases, np.float32)
+        self._raise(lib().nqg_mlp_get_weights(self._h, _ptr(w), _ptr(b)), "get weights")
+        return w, b
+
+    def set_weights(self, w, b):
+        w = np.ascontiguousarray(w, np.float32)
+        b = np.ascontiguousarray(b, np.float32)
+        self._raise(lib().nqg_mlp_set_weights(self._h, _ptr(w), _ptr(b)), "set weights")
+
+    def layers(self):
+        """[(W (out x in), b)] of the FP32 master weights."""
+        w, b = self.get_weights()
+        out, ow, ob = [], 0, 0
+        for i, o in zip(self.sizes[:-1], self.sizes[1:]):
+            out.append((w[ow:ow + i * o].reshape(o, i), b[ob:ob + o]))
+            ow += i * o
+            ob += o
+        return out
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.zeros((x.shape[0], self.sizes[-1]), np.float32)
+        self._raise(lib().nqg_mlp_forward(self._h, x.shape[0], _ptr(x), _ptr(y)), "forward")
+        return y
+
+    def forward_device(self, rows, d_x, d_logits, stream=None):
+        self._raise(lib().nqg_mlp_forward_device(self._h, int(rows), C.c_void_p(d_x), C.c_void_p(d_logits),
+                                                 C.c_void_p(stream) if stream else None), "forward")
+
+    def loss_grad(self, x, y, pos_weight=1.0):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        gw = np.zeros(self.n_weights, np.float32)
+        gb = np.zeros(self.n_biases, np.float32)
+        loss = C.c_double()
+        self._raise(lib().nqg_mlp_loss_grad(self._h, x.shape[0], _ptr(x), _ptr(y), float(pos_weight),
+                                            C.byref(loss), _ptr(gw), _ptr(gb)), "loss grad")
+        return loss.value, gw, gb
+
+    def fit(self, x, y, epochs=10, batch=1024, lr=1e-3, pos_weight=1.0, seed=0):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        self._raise(lib().nqg_mlp_set_data(self._h, x.shape[0], _ptr(x), _ptr(y)), "set data")
+        losses = np.zeros(epochs)
+        self._raise(lib().nqg_mlp_train(self._h, int(epochs), int(batch), float(lr), float(pos_weight), int(seed),
+                                        _ptr(losses)), "train")
+        return losses
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().nqg_mlp_destroy(self._h)
             self._h = None
 
     def __del__(self):

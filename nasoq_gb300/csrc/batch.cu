@@ -1261,10 +1261,11 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
     // ---- initial factorization and solution (reference initialize_x,
     // src/nasoq.cpp:448-476): every visible supernode; rhs [-q; b; d on the
     // active rows]
-    for (int round = 0; round < (warm ? 4 : 1); ++round) {
+    bool cold = !warm;
+    for (int round = 0; round < 5; ++round) {
       load_state(c);
       build_vlist(c);
-      mark_all(c, !warm);
+      mark_all(c, cold);
       factor_marked(c);
       for (int i = tid; i < N; i += nt) {
         double v = 0.0;
@@ -1277,7 +1278,21 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
       precond(c, c.rhs, c.sol);
       solves++;
       steps += refine(c, c.rhs, c.sol, P.outer, P.inner, flexible, adaptive, a.refine_tol, P.tol_abs, P.tol_rel, gs);
-      if (!warm) break;
+      if (cold) break;
+      // a proposed set that makes the KKT matrix singular (dependent
+      // constraints): start cold instead
+      int bad = 0;
+      for (int i = tid; i < N; i += nt)
+        if (!isfinite(c.sol[i])) bad++;
+      bad = block_sum_int(bad, redi);
+      if (bad > 0 || (s_status & (ST_ZERO_PIVOT | ST_NONFINITE))) {
+        for (int k = tid; k < mineq; k += nt) c.act[k] = 0;
+        __syncthreads();
+        if (tid == 0) s_status = 0;
+        cold = true;
+        __syncthreads();
+        continue;
+      }
       // drop proposed constraints with negative multipliers, then solve again
       int ndrop = 0;
       for (int k = tid; k < mineq; k += nt)
@@ -1288,8 +1303,9 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
       ndrop = block_sum_int(ndrop, redi);
       warm_dropped += ndrop;
       if (ndrop == 0) break;
-      if (round == 2) {  // no consistent set after three rounds: cold start
+      if (round >= 2) {  // no consistent set after three rounds: cold start
         for (int k = tid; k < mineq; k += nt) c.act[k] = 0;
+        cold = true;
         __syncthreads();
       }
     }
@@ -1588,6 +1604,60 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
   if (a.prof && tid < PH_N) atomicAdd(a.prof + tid, s_cyc[tid]);
 }
 
+
+
+// Warm-start sets from per-constraint scores (e.g. the logits of the active-set
+// model): problem i proposes every constraint k with scores[i * ld + k] >
+// threshold, in ascending order, except one parallel to a constraint it
+// already proposed (same variables, proportional coefficients -- the two
+// sides of a box): both active would make the KKT matrix singular.  A
+// problem with no proposal keeps a cold start.  One thread per problem.
+__global__ void k_ws_scores(int nprob, BProb *probs, const BPat *pats, const int *ipool, const double *dpool,
+                            int *iout, const float *scores, int ld, float thr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nprob) return;
+  BProb &P = probs[i];
+  const BPat &pt = pats[P.pat];
+  const int *bt_ptr = ipool + pt.o_bt_ptr, *bt_var = ipool + pt.o_bt_var, *bt_q = ipool + pt.o_bt_q;
+  const double *kv = dpool + P.o_kv;
+  int *as = iout + P.o_as;
+  const float *sc = scores + (size_t)i * ld;
+  int cnt = 0;
+  const int mi = min(pt.mineq, ld);
+  for (int k = 0; k < mi; ++k) {
+    if (!(sc[k] > thr)) continue;
+    const int ka = bt_ptr[k], kn = bt_ptr[k + 1] - ka;
+    bool parallel = false;
+    for (int t = 0; t < cnt && !parallel; ++t) {
+      const int j = as[t], ja = bt_ptr[j], jn = bt_ptr[j + 1] - ja;
+      if (jn != kn || kn == 0) continue;
+      bool same = true;
+      const double r = kv[bt_q[ka]] / kv[bt_q[ja]];
+      for (int e = 0; e < kn && same; ++e)
+        same = bt_var[ka + e] == bt_var[ja + e] && fabs(kv[bt_q[ka + e]] - r * kv[bt_q[ja + e]]) <=
+                                                        1e-12 * fabs(kv[bt_q[ka + e]]);
+      parallel = same;
+    }
+    if (!parallel) as[cnt++] = k;
+  }
+  P.ws_n = cnt > 0 ? cnt : -1;
+}
+
+__global__ void k_ws_clear(int nprob, BProb *probs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nprob) probs[i].ws_n = -1;
+}
+
+int batch_ws_from_scores(int nprob, BProb *probs, const BPat *pats, const int *ipool, const double *dpool, int *iout,
+                         const float *scores, int ld, float thr, cudaStream_t st) {
+  k_ws_scores<<<(nprob + 127) / 128, 128, 0, st>>>(nprob, probs, pats, ipool, dpool, iout, scores, ld, thr);
+  return cudaGetLastError() == cudaSuccess ? NQG_OK : NQG_ERR_CUDA;
+}
+
+int batch_ws_clear(int nprob, BProb *probs, cudaStream_t st) {
+  k_ws_clear<<<(nprob + 127) / 128, 128, 0, st>>>(nprob, probs);
+  return cudaGetLastError() == cudaSuccess ? NQG_OK : NQG_ERR_CUDA;
+}
 
 size_t batch_smem_bytes(const BArgs &a, size_t tsize) {
   auto up = [](size_t b) { return (b + 15) / 16 * 16; };

@@ -108,6 +108,9 @@ struct BArgs {
 };
 
 size_t batch_smem_bytes(const BArgs &a, size_t tsize);
+int batch_ws_from_scores(int nprob, BProb *probs, const BPat *pats, const int *ipool, const double *dpool, int *iout,
+                         const float *scores, int ld, float thr, cudaStream_t st);
+int batch_ws_clear(int nprob, BProb *probs, cudaStream_t st);
 template <class T> int batch_prepare(int threads, size_t smem_attr, size_t smem, int *blocks_per_sm);
 template <class T> int launch_batch(const BArgs &a, int grid, int threads, size_t smem, cudaStream_t st);
 

@@ -863,6 +863,30 @@ extern "C" int nqg_batch_set_warm_start(nqg_batch *b, int i, int n_as, const int
   return NQG_OK;
 }
 
+extern "C" int nqg_batch_warm_start_from_scores(nqg_batch *b, const float *d_scores, int ld, float threshold) {
+  // Warm-start sets of every problem from device-resident scores (row i:
+  // problem i's constraints); see k_ws_scores.  Runs on the batch's stream.
+  if (!b || !b->finalized) return NQG_ERR_STATE;
+  if (!d_scores || ld <= 0) return NQG_ERR_ARG;
+  const int np = (int)b->qp.size();
+  int rc = nqg::batch_ws_from_scores(np, b->d_probs, b->d_pats, b->d_ipool, b->d_dpool, b->d_iout, d_scores, ld,
+                                     threshold, b->stream);
+  if (rc) return fail(b, rc, "warm-start kernel launch failed");
+  for (auto &P : b->h_probs) P.ws_n = 0;  // device copies now hold the sets
+  return NQG_OK;
+}
+
+extern "C" int nqg_batch_clear_warm_starts(nqg_batch *b) {
+  // Every problem back to a cold start.
+  if (!b || !b->finalized) return NQG_ERR_STATE;
+  const int np = (int)b->qp.size();
+  int rc = nqg::batch_ws_clear(np, b->d_probs, b->stream);
+  if (rc) return fail(b, rc, "warm-start kernel launch failed");
+  for (auto &P : b->h_probs) P.ws_n = -1;
+  BQ_CUDA(cudaStreamSynchronize(b->stream));
+  return NQG_OK;
+}
+
 extern "C" int nqg_batch_solve_async(nqg_batch *b) {
   // Enqueues one solve of every problem on the batch's stream (captured once
   // into a CUDA graph of the queue reset and the persistent kernel).
