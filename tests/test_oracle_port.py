@@ -76,3 +76,22 @@ def test_port_refined_solution(path):
         pytest.skip("reference refinement diverges on this singular refinement matrix")
     g = np.abs(d["out_valL"]).max()
     assert np.linalg.norm(out["x"] - xr) <= max(1e-11, 1e-15 * g) * np.linalg.norm(xr)
+
+
+def test_port_qp_matches_reference_batch_fixture():
+    """The oracle's QP restatement (NASOQ loop over the partial
+    refactorization, masked solves, the reference's GMRES) against the
+    reference's own solves of the batch fixture (every 3rd problem: MPC of
+    uneven horizon, random convex QPs with dropped constraints, parametric
+    instances): same status and iteration count, x within 1e-7."""
+    import test_batch_gpu as TB
+    from oracle import port
+
+    port.set_threads(1)
+    d, qps = TB.fixture()
+    for i in range(0, len(qps), 3):
+        r = port.qp_solve(qps[i], variant=0, eps_abs=1e-8)
+        assert r["status"] == int(d["status"][i]), f"problem {i}"
+        assert r["num_iter"] == int(d["num_iter"][i]), f"problem {i}"
+        assert TB.rel(r["x"], TB.part(d, "x", i)) <= 1e-7, f"problem {i}"
+        assert sorted(r["active"].tolist()) == sorted(TB.part(d, "act", i).tolist()), f"problem {i}"
