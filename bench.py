@@ -1,29 +1,38 @@
 #!/usr/bin/env python3
-"""Benchmark of the GB300 LBL path on the symmetric-indefinite KKT workload
-K = [H A^T; A -1e-8 I], H = 3D 7-point Laplacian on 64^3 (n = 262,144), A =
-20,000 x n with 6 random N(0,1) entries per row, rhs ~ N(0,1) (N = 282,144),
-seeded synthetic data.
+"""Benchmark: QP solves/s at a 1e-8 KKT tolerance of the mixed-precision,
+batched, learned-warm-start NASOQ path on one GB300, against the plain FP64
+GPU path and the reference's CPU method.
 
-One step = one KKT solve to a relative residual below 1e-10: numeric
-supernodal Bunch-Kaufman LDL^T factorization (FP32 factor, diagonal floor for
-FP32) + supernodal solves + FP64 GMRES refinement on the unperturbed matrix.
-The symbolic analysis (ordering, supernodes) is per sparsity pattern and runs
-once, outside the timed region.
+Workload (seeded synthetic; the reference's benchmark suites are not
+available): the parametric MPC family at horizon 50 (n = 450, 300 equality
+rows, 900 box rows), q = P theta, box shifts S theta, theta in R^32 ~ N(0, I),
+P and S dense N(0, 0.1) (nasoq_gb300.problems.mpc_parametric).  One step = one
+batch of 4096 fresh theta: model logits on the GPU, warm-start sets, and the
+batched NASOQ solve (one CTA per QP), FP32 factorization with FP64 flexible
+GMRES refinement, every QP checked at eps_abs = 1e-8.  The active-set model is
+trained at start-up by the library's own kernels on plain-NASOQ solves of
+200k random theta (outside the timed region; reported).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-Prints one JSON line (rank 0).  `value` is device-resident throughput (matrix
-values and rhs already in HBM); `e2e` is the same through the C ABI with host
-buffers (matrix values and rhs copied in, solution copied out, every step);
-`plain_fp64` is the FP64 factorization path on the same GPU; `cpu_baseline`
-is the oracle restatement (reference algorithm over OpenBLAS) on the host
-cores.  For N > 1 (torchrun) every rank solves its own replica: the path has
-no data exchange to shard.
+Prints one JSON line (rank 0).  `value`: device-resident throughput (theta,
+q and d already in HBM; model forward, warm start and solve timed with CUDA
+events); `e2e`: the same through the C ABI from host buffers (q, d computed
+from theta on the host and copied in, x copied out, every step);
+`plain_fp64_batched`: the same batches solved by the plain FP64 path (FP64
+factor, the reference's refinement schedule, cold start) on the same GPU;
+`plain_fp64_single`: the per-QP FP64 GPU path (one problem at a time, host
+loop over the C ABI) on a sample; `cpu_baseline`: the oracle restatement of
+the reference's method on the host cores.  Secondary sections: `c3`, the
+uneven MPC batch (4096 problems, horizons 10..100), and `lbl_c2`, the
+symmetric-indefinite KKT solve of the 64^3 Laplacian workload.  For N > 1
+(torchrun) every rank solves its own batches (no data exchange).
 """
 from __future__ import annotations
 
 import argparse
 import json
+import multiprocessing as mp
 import os
 import statistics
 import subprocess
@@ -37,41 +46,24 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "QP solves/sec at 1e-8 KKT tol: mixed+batched+warm-start vs plain GPU FP64"
+BATCH = 4096
+EPS = 1e-8
+N_TRAIN = 200_000
+REFINE_TOL = 1e-12
+THETA_SEED = 20261204
+CPU_SAMPLE_PER_PROC = 48
+# DRAM bytes (read + write) of one batch-kernel launch on this workload,
+# scaled from one ncu capture of a 1024-problem batch (profiles/); None
+# until captured
+NCU_BATCH_TRAFFIC = None
+# LBL section: K = [H A^T; A -1e-8 I], H 3D 7-point Laplacian on 64^3, A 20000 x n, 6 N(0,1) per row
 GRID, MCON, PER_ROW, DELTA, SEED = 64, 20000, 6, 1e-8, 0
-SAMPLE_GRID, SAMPLE_M = 48, 8000          # CPU baseline sample of the same family (~9% of the flops)
+SAMPLE_GRID, SAMPLE_M = 48, 8000
 TARGET_RELRES = 1e-10
-# DRAM bytes (read + write) per launch of the dominant kernel classes, scaled
-# from one ncu capture of the 48^3 / m=8000 case of this workload family (see
-# profiles/); None where no capture exists yet
-NCU_TRAFFIC = {}
-INNER = 8  # cap on the FGMRES inner steps of the refinement (one restart)
-STOP_REL = 1e-12  # FGMRES stops once its residual estimate is below STOP_REL * ||b|| (100x under the target)
+LBL_INNER, LBL_STOP_REL = 8, 1e-12
 
 
-def workload_name(g, m):
-    return f"lbl_kkt_lap3d_{g}cube_m{m}"
-
-
-def sym_spmv(K, x):
-    cols = np.repeat(np.arange(K.ncol), np.diff(K.p))
-    y = np.zeros(K.ncol)
-    np.add.at(y, K.i, K.x * x[cols])
-    off = K.i != cols
-    np.add.at(y, cols[off], K.x[off] * x[K.i[off]])
-    return y
-
-
-def relres(K, x, b):
-    return float(np.linalg.norm(b - sym_spmv(K, x)) / np.linalg.norm(b))
-
-
-def factor_flops(sym):
-    w = np.diff(sym.super).astype(np.float64)
-    r = np.diff(sym.lpi).astype(np.float64)
-    # sum over supernodes of sum_{k<w} (r-k)^2
-    return float(np.sum(w * r * r - r * w * (w - 1) + (w - 1) * w * (2 * w - 1) / 6.0))
-
-
+# ---------------------------------------------------------------------------
 class ClockSampler:
     """nvidia-smi SM clock / throttle sampling during the timed region."""
 
@@ -127,80 +119,367 @@ class ClockSampler:
 
 
 def dist_setup():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
 
 
-def cpu_sample():
-    """Oracle restatement on the sample instance with all host threads."""
-    from nasoq_gb300 import Symbolic
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "MEASURED_PEAKS.json"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def thetas_for(step, rank):
+    return np.random.default_rng([THETA_SEED, rank, step]).standard_normal((BATCH, 32))
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle restatement of the reference's method (cold start),
+# one single-threaded process per host core, each on its own slice.
+def _cpu_worker(args):
+    start, count, step = args
+    import nasoq_gb300 as nq
     from nasoq_gb300 import problems as P
     from oracle import port
 
-    K, rhs = P.lbl_kkt(seed=SEED, grid3d=SAMPLE_GRID, m=SAMPLE_M, per_row=PER_ROW, delta=DELTA)
-    sym = Symbolic(K.ncol, K.p, K.i)
-    ax = K.x.copy()
-    dg = K.p[:-1]
-    ax[dg] = np.where(np.abs(ax[dg]) < 1e-9, 1e-9, ax[dg])
-    threads = os.cpu_count() or 1
-    port.set_threads(threads)
+    port.set_threads(1)
+    fam = P.mpc_parametric(0)
+    th = np.random.default_rng([THETA_SEED, 7777, step]).standard_normal((start + count, 32))[start:]
+    N, Kp, Ki, _ = port.super_kkt(fam.base)
+    ex = np.zeros(N, np.int32)
+    ex[fam.base.n + fam.base.A.nrow:] = 1
+    sym = nq.Symbolic(N, Kp, Ki, extra_cols=ex)
     t0 = time.perf_counter()
-    out = port.solve(K.ncol, K.p, K.i, ax, K.x, sym, rhs, req_ref_iter=2, max_inner_iter=2)
-    dt = time.perf_counter() - t0
-    return {"seconds": dt, "flops": factor_flops(sym), "threads": threads, "N": K.ncol,
-            "relres": relres(K, out["x"], rhs), "factor_s": out["factor_s"], "solve_s": out["solve_s"]}
+    ok = 0
+    iters = 0
+    for t in th:
+        qp = P.QP(fam.base.H, fam.q_of(t), fam.base.A, fam.base.b, fam.base.C, fam.d_of(t))
+        r = port.qp_solve(qp, variant=0, eps_abs=EPS, sym=sym)
+        ok += r["status"] == 1
+        iters += r["num_iter"]
+    return time.perf_counter() - t0, ok, iters
+
+
+def cpu_qp_sample(step=0, per_proc=CPU_SAMPLE_PER_PROC):
+    procs = os.cpu_count() or 1
+    jobs = [(i * per_proc, per_proc, step) for i in range(procs)]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_cpu_worker, jobs)
+    wall = time.perf_counter() - t0
+    n = procs * per_proc
+    slowest = max(r[0] for r in res)
+    return {"value": n / slowest, "unit": "QP solves/s", "cores": procs, "kind": "port", "wall_seconds": wall,
+            "sample": f"{n} QPs of the same family ({per_proc} per process, fresh theta), one single-threaded "
+                      f"process per host core, cold start (the reference's method), eps_abs={EPS:g}; value = "
+                      f"QPs / solve time of the slowest process ({slowest:.2f}s; {wall:.2f}s with process start)",
+            "optimal_fraction": sum(r[1] for r in res) / n, "mean_iterations": sum(r[2] for r in res) / n,
+            "per_process_seconds": max(r[0] for r in res)}
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return 0
-    from nasoq_gb300 import Symbolic
-    from nasoq_gb300 import problems as P
-
-    Kc, _ = P.lbl_kkt(seed=SEED, grid3d=args.grid, m=args.mcon, per_row=PER_ROW, delta=DELTA)
-    F_full = factor_flops(Symbolic(Kc.ncol, Kc.p, Kc.i))
-    for _ in range(args.warmup):
-        cpu_sample()
-    times, samples = [], []
-    for _ in range(args.steps):
-        s = cpu_sample()
+    for w in range(args.warmup):
+        cpu_qp_sample(step=1000 + w, per_proc=8)
+    vals, samples = [], []
+    for k in range(args.steps):
+        s = cpu_qp_sample(step=k)
         samples.append(s)
-        times.append(s["seconds"])
-    tot = sum(times)
-    # flop-scaled to the full workload: seconds per full solve = F_full / (F_sample / t_sample)
-    sec_full = statistics.median(times) * F_full / samples[0]["flops"]
-    value = 1.0 / sec_full
-    line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / max(args.steps, 1),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(args.grid, args.mcon), "N": Kc.ncol},
-        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": samples[0]["threads"], "kind": "port",
-                         "sample": f"each step: full factor + refined solve of the same KKT family at "
-                                   f"{SAMPLE_GRID}^3 grid, m={SAMPLE_M} (N={samples[0]['N']}, "
-                                   f"F={samples[0]['flops']:.3e}); value scaled to the full workload by "
-                                   f"F_full={F_full:.3e}",
-                         "sample_gflops": samples[0]["flops"] / statistics.median(times) / 1e9},
-        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
+        vals.append(s["value"])
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "QP solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * statistics.mean(s["wall_seconds"] for s in samples),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "qp_mpc50_parametric_theta32", "batch": BATCH, "eps_abs": EPS,
+                       "variant": "Fixed", "warm_start": "none (the reference's method)"},
+            "cpu_baseline": dict(samples[0], value=value),
+            "e2e": {"value": value, "unit": "QP solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+# ---------------------------------------------------------------------------
+def qp_section(args, world, rank, local, torch, nq, P, learn, pk, pk_src):
+    fam = P.mpc_parametric(0)
+    n, mi = fam.base.n, fam.base.C.nrow
+    # model: trained on plain-NASOQ solves (outside the timed region)
+    model, rep = learn.train_model(fam, n_train=args.n_train, seed=11 + rank, epochs=20, batch=1024, lr=1e-3,
+                                   solver=dict(variant=0, eps_abs=EPS, precision=nq.NQG_FP32, refine=1,
+                                               refine_tol=REFINE_TOL))
+    mixed = dict(variant=0, eps_abs=EPS, precision=nq.NQG_FP32, refine=1, refine_tol=REFINE_TOL)
+    batch = learn.family_batch(fam, BATCH, **mixed)
+    ws = learn.WarmStarter(batch, model, fam)
+    bstream = torch.cuda.ExternalStream(batch.stream())
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+
+    def device_step(thetas):
+        """Inputs made resident first (untimed), then forward + warm start + solve timed on the batch stream."""
+        learn.set_theta(batch, fam, thetas)
+        ws.d_theta.copy_(torch.from_numpy(np.ascontiguousarray(thetas, np.float32)))
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(bstream)
+        model.forward_device(BATCH, ws.d_theta.data_ptr(), ws.d_logits.data_ptr(), stream=batch.stream())
+        batch.warm_start_from_scores(ws.d_logits.data_ptr(), mi, 0.0)
+        batch.solve_async()
+        e1.record(bstream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    def e2e_step(thetas):
+        """Host theta in, host x out, through the C ABI."""
+        t0 = time.perf_counter()
+        learn.set_theta(batch, fam, thetas)           # q, d from theta on the host, copied in
+        ws.propose(thetas)                            # theta copied in, model logits, warm-start sets
+        batch.solve()
+        x, _, z, st = batch.results()                 # x, z and statistics copied out
+        return (time.perf_counter() - t0) * 1e3, x, z, st
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for w in range(args.warmup):
+        device_step(thetas_for(10_000 + w, rank))
+    barrier()
+    with ClockSampler(local) as clk:
+        barrier()
+        ms = [device_step(thetas_for(k, rank)) for k in range(args.steps)]
+        barrier()
+    t_ms = float(sum(ms))
+    if world > 1:
+        tt = torch.tensor([t_ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    value = world * args.steps * BATCH / (t_ms / 1e3)
+    _, _, _, st = batch.results()
+    kernel_ms = batch.info().last_ms
+
+    # end to end
+    e2e_step(thetas_for(20_000, rank))
+    e2e_ms, warm_stats = [], None
+    for k in range(args.steps):
+        ms_k, xw, zw, warm_stats = e2e_step(thetas_for(k, rank))
+        e2e_ms.append(ms_k)
+    e2e_value = BATCH / (statistics.median(e2e_ms) / 1e3) * world
+    th_last = thetas_for(args.steps - 1, rank)
+    warm_it = np.array([s.num_iter for s in warm_stats])
+    warm_ok = np.mean([s.status == 1 for s in warm_stats])
+    lag_max = max(s.lag_res for s in warm_stats)
+    cons_max = max(s.cons_sat_norm for s in warm_stats)
+    compl_max = max(s.complementarity_infn for s in warm_stats)
+
+    # the same batch cold (mixed precision), and plain FP64 batched (reference schedule, cold)
+    def cold_run(settings):
+        b = learn.family_batch(fam, BATCH, **settings)
+        learn.set_theta(b, fam, th_last)
+        b.solve()
+        times = []
+        for _ in range(2):
+            b.solve()
+            times.append(b.info().last_ms)
+        x, _, z, s = b.results()
+        b.close()
+        return min(times), x, z, s
+
+    cold_ms, xc, zc, sc = cold_run(mixed)
+    f64_ms, x64, z64, s64 = cold_run(dict(variant=0, eps_abs=EPS, precision=nq.NQG_FP64, refine=0))
+    xr = np.abs(xw - x64).reshape(BATCH, n).max(axis=1) / np.maximum(np.abs(x64).reshape(BATCH, n).max(axis=1), 1)
+
+    # plain FP64 single-QP path (host loop over the C ABI) on a sample
+    single = None
+    if not args.no_single:
+        st64 = nq.qp_settings(variant=0, eps_abs=EPS, precision=nq.NQG_FP64)
+        ns_ = args.single_sample
+        t0 = time.perf_counter()
+        its = []
+        for t in th_last[:ns_]:
+            x1, y1, z1, a1, r1 = nq.qp_solve(fam.base.H, fam.q_of(t), fam.base.A, fam.base.b, fam.base.C,
+                                            fam.d_of(t), settings=st64)
+            its.append(r1.num_iter)
+        dt = time.perf_counter() - t0
+        single = {"value": ns_ / dt, "unit": "QP solves/s", "sample": ns_, "mean_iterations": float(np.mean(its)),
+                  "path": "nqg_qp_solve: host active-set loop, GPU FP64 factor / refactor / solve per iteration"}
+
+    # error against the oracle (the reference's method restated, FP64) on a few problems
+    oracle_err = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            from oracle import port
+            N, Kp, Ki, _ = port.super_kkt(fam.base)
+            ex = np.zeros(N, np.int32)
+            ex[n + fam.base.A.nrow:] = 1
+            sym = nq.Symbolic(N, Kp, Ki, extra_cols=ex)
+            errs = []
+            for i in range(8):
+                t = th_last[i]
+                qp = P.QP(fam.base.H, fam.q_of(t), fam.base.A, fam.base.b, fam.base.C, fam.d_of(t))
+                r = port.qp_solve(qp, variant=0, eps_abs=EPS, sym=sym)
+                xi = xw[i * n:(i + 1) * n]
+                errs.append(float(np.linalg.norm(xi - r["x"]) / max(np.linalg.norm(r["x"]), 1e-300)))
+            oracle_err = {"max_rel_x_error": max(errs), "problems": 8}
+        except Exception as e:
+            oracle_err = {"unavailable": str(e)[:200]}
+
+    # roofline of the batch kernel: algorithmic bytes = factor entries read by
+    # the triangular solves (forward + backward per preconditioner
+    # application) plus the factor written by each refactorization
+    batch.set_profiling(True)
+    device_step(th_last)
+    prof = batch.profile()
+    batch.set_profiling(False)
+    _, _, _, stp = batch.results()
+    elt = 4  # FP32 factor
+    sym_fam = _family_symbolic(nq, fam)
+    xsize = int(sym_fam.colp[-1])
+    applications = sum(s.solves + s.refine_steps for s in stp)
+    sn_factored = prof["supernodes"]
+    avg_sn_bytes = xsize * elt / max(len(sym_fam.super) - 1, 1)
+    alg_bytes = applications * 2 * xsize * elt + sn_factored * avg_sn_bytes
+    ach = alg_bytes / (batch.info().last_ms / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": ach, "peak": pk.get("hbm_gbs", 6800.0), "unit": "GB/s",
+            "frac": ach / pk.get("hbm_gbs", 6800.0), "traffic": NCU_BATCH_TRAFFIC, "kernel": "k_nasoq_batch<float>",
+            "launches_per_step": 1, "avg_launch_ms": batch.info().last_ms, "peak_source": pk_src,
+            "algorithmic_bytes_per_launch": alg_bytes,
+            "note": "one CTA per QP runs its whole active-set loop; bound by dependent on-chip latency, not DRAM",
+            "phase_share": {k: prof[k] / max(prof["total"], 1) for k in
+                            ("setup", "refactor", "precond", "spmv", "refine", "select", "update")}}
+    out = {
+        "value": value, "ms_per_step": t_ms / args.steps,
+        "e2e": {"value": e2e_value, "unit": "QP solves/s",
+                "h2d_bytes_per_step": int(BATCH * (n + mi) * 8 + BATCH * 32 * 4),
+                "d2h_bytes_per_step": int(BATCH * (n + mi) * 8 + BATCH * 64),
+                "ms_per_step": statistics.median(e2e_ms)},
+        "check": {"optimal_fraction": float(warm_ok), "max_lag_res": lag_max, "max_cons_sat": cons_max,
+                  "max_complementarity": compl_max, "eps_abs": EPS,
+                  "max_rel_x_error_vs_fp64_gpu": float(xr.max()), "error_vs_oracle": oracle_err},
+        "iterations": {"warm_mean": float(warm_it.mean()), "warm_max": int(warm_it.max()),
+                       "cold_mean": float(np.mean([s.num_iter for s in sc])),
+                       "warm_dropped_mean": float(np.mean([s.warm_dropped for s in warm_stats]))},
+        "mixed_cold_batched": {"value": BATCH / (cold_ms / 1e3), "unit": "QP solves/s",
+                               "optimal_fraction": float(np.mean([s.status == 1 for s in sc]))},
+        "plain_fp64_batched": {"value": BATCH / (f64_ms / 1e3), "unit": "QP solves/s",
+                               "optimal_fraction": float(np.mean([s.status == 1 for s in s64])),
+                               "precision": "FP64 factor and solves, the reference's GMRES schedule, cold start"},
+        "plain_fp64_single": single,
+        "model": {"sizes": list(model.sizes), "n_train": rep.n_train, "label_seconds": rep.label_seconds,
+                  "train_seconds": rep.train_seconds, "loss_first": rep.losses[0], "loss_last": rep.losses[-1],
+                  "active_fraction": rep.active_mean},
+        "roofline": roof, "clocks": clk.summary(), "kernel_ms": kernel_ms,
+        "gpu_launches": 1 + (len(model.sizes) - 1) + 1,
+    }
+    batch.close()
+    model.close()
+    return out
+
+
+def _family_symbolic(nq, fam):
+    from nasoq_gb300 import problems as P  # noqa: F401
+    b = fam.base
+    n, meq, mi = b.n, b.A.nrow, b.C.nrow
+    N = n + meq + mi
+    cols = []
+    for j in range(n):
+        r = list(b.H.i[b.H.p[j]:b.H.p[j + 1]]) + [n + i for i in b.A.i[b.A.p[j]:b.A.p[j + 1]]] + \
+            [n + meq + i for i in b.C.i[b.C.p[j]:b.C.p[j + 1]]]
+        cols.append(r)
+    for k in range(n, N):
+        cols.append([k])
+    Kp = np.cumsum([0] + [len(c) for c in cols]).astype(np.int32)
+    Ki = np.concatenate([np.asarray(c, np.int32) for c in cols])
+    ex = np.zeros(N, np.int32)
+    ex[n + meq:] = 1
+    return nq.Symbolic(N, Kp, Ki, extra_cols=ex)
+
+
+def c3_section(nq, P):
+    qps = P.mpc_batch(BATCH, seed=0)
+    probs = [(q.H, q.q, q.A, q.b, q.C, q.d) for q in qps]
+    out = {"workload": "qp_mpc_uneven_horizon10-100_b4096"}
+    for name, kw in (("mixed", dict(precision=nq.NQG_FP32, refine=1, refine_tol=REFINE_TOL)),
+                     ("plain_fp64", dict(precision=nq.NQG_FP64, refine=0))):
+        t0 = time.perf_counter()
+        b = nq.QPBatch(probs, settings=nq.batch_settings(variant=0, eps_abs=EPS, **kw))
+        fin = time.perf_counter() - t0
+        b.solve()
+        b.solve()
+        ms = b.info().last_ms
+        _, _, _, st = b.results()
+        out[name] = {"value": BATCH / (ms / 1e3), "unit": "QP solves/s", "ms": ms,
+                     "optimal_fraction": float(np.mean([s.status == 1 for s in st])),
+                     "iterations_total": int(sum(s.num_iter for s in st)), "patterns": b.info().npatterns,
+                     "setup_seconds": fin}
+        b.close()
+    return out
+
+
+def lbl_section(args, torch, nq, P, pk):
+    """The symmetric-indefinite KKT solve (FP32 factor + FP64 FGMRES-IR)."""
+    K, rhs = P.lbl_kkt(seed=SEED, grid3d=GRID, m=MCON, per_row=PER_ROW, delta=DELTA)
+    n = K.ncol
+    st32 = nq.default_settings(precision=nq.NQG_FP32, solve_precision=nq.NQG_FP32, req_ref_iter=1,
+                               max_inner_iter=LBL_INNER, tol_abs=LBL_STOP_REL * float(np.linalg.norm(rhs)),
+                               tol_rel=1.0, reg_diag=1e-9)
+    stream = torch.cuda.current_stream()
+    t0 = time.perf_counter()
+    plan = nq.Plan(n, K.p, K.i, K.x, settings=st32)
+    analysis_s = time.perf_counter() - t0
+    plan.set_stream(stream.cuda_stream)
+    d_rhs = torch.from_numpy(rhs).cuda()
+    d_x = torch.empty(n, dtype=torch.float64, device="cuda")
+
+    def step():
+        plan.factor()
+        plan.solve_device(d_rhs.data_ptr(), d_x.data_ptr())
+
+    for _ in range(2):
+        step()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = args.lbl_steps
+    ev0.record(stream)
+    for _ in range(steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    x32 = d_x.cpu().numpy()
+    cols = np.repeat(np.arange(n), np.diff(K.p))
+    y = np.zeros(n)
+    np.add.at(y, K.i, K.x * x32[cols])
+    off = K.i != cols
+    np.add.at(y, cols[off], K.x[off] * x32[K.i[off]])
+    rr = float(np.linalg.norm(rhs - y) / np.linalg.norm(rhs))
+    plan.set_profiling(True)
+    step()
+    stats = plan.kernel_stats()
+    plan.set_profiling(False)
+    plan.close()
+    return {"workload": f"lbl_kkt_lap3d_{GRID}cube_m{MCON}", "N": n, "value": 1000.0 / ms, "unit": "solves/s",
+            "ms_per_step": ms, "relres": rr, "meets_target": bool(rr <= TARGET_RELRES), "analysis_s": analysis_s,
+            "kernels_ms": {k: v["total_ms"] for k, v in stats.items()}}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison step")
+    ap.add_argument("--n-train", type=int, default=N_TRAIN)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--grid", type=int, default=GRID, help="Laplacian grid edge (smaller cases for profiler captures)")
-    ap.add_argument("--mcon", type=int, default=MCON, help="constraint rows")
-    ap.add_argument("--profile-once", action="store_true",
-                    help="analysis + exactly one timed step and nothing else (for profiler launch lists)")
+    ap.add_argument("--no-single", action="store_true", help="skip the single-QP FP64 sample")
+    ap.add_argument("--single-sample", type=int, default=32)
+    ap.add_argument("--no-c3", action="store_true")
+    ap.add_argument("--no-lbl", action="store_true")
+    ap.add_argument("--lbl-steps", type=int, default=3)
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
@@ -209,196 +488,41 @@ def main():
     import torch
 
     import nasoq_gb300 as nq
+    from nasoq_gb300 import learn
     from nasoq_gb300 import problems as P
 
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    stream = torch.cuda.current_stream()
-
-    K, rhs = P.lbl_kkt(seed=SEED, grid3d=args.grid, m=args.mcon, per_row=PER_ROW, delta=DELTA)
-    n = K.ncol
-    # FGMRES residual estimates are of the true residual b - K x: stop at
-    # STOP_REL * ||b|| (tol_rel = 1 leaves the absolute bound in charge)
-    st32 = nq.default_settings(precision=nq.NQG_FP32, solve_precision=nq.NQG_FP32, req_ref_iter=1,
-                               max_inner_iter=INNER, tol_abs=STOP_REL * float(np.linalg.norm(rhs)), tol_rel=1.0,
-                               reg_diag=1e-9)
-    t0 = time.perf_counter()
-    plan = nq.Plan(n, K.p, K.i, K.x, settings=st32)
-    analysis_s = time.perf_counter() - t0
-    plan.set_stream(stream.cuda_stream)
-    F = factor_flops(plan.symbolic)
-    d_rhs = torch.from_numpy(rhs).cuda()
-    d_x = torch.empty(n, dtype=torch.float64, device="cuda")
-
-    def step():
-        plan.factor()
-        plan.solve_device(d_rhs.data_ptr(), d_x.data_ptr())
-
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-
-    if args.profile_once:
-        barrier()
-        t1 = time.perf_counter()
-        step()
-        barrier()
-        print(json.dumps({"profile_once_step_s": time.perf_counter() - t1, "launches": plan.launch_count()}))
-        plan.close()
-        return 0
-    for _ in range(args.warmup):
-        step()
-    barrier()
-    l0 = plan.launch_count()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        barrier()
-        ev0.record(stream)
-        for _ in range(args.steps):
-            step()
-        ev1.record(stream)
-        barrier()
-    launches = (plan.launch_count() - l0) / max(args.steps, 1)
-    t_ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        tt = torch.tensor([t_ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_ms = float(tt.item())
-    value = world * args.steps / (t_ms / 1000.0)
-    x32 = d_x.cpu().numpy()
-    rr32 = relres(K, x32, rhs)
-    inner_used = plan.timings().num_ref_iter
-
-    # end to end through the C ABI with host buffers (values + rhs in, x out)
-    ax = np.ascontiguousarray(K.x)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    plan.set_values(ax)
-    plan.factor()
-    xh = plan.solve(rhs)
-    barrier()
-    e0.record(stream)
-    for _ in range(args.steps):
-        plan.set_values(ax)
-        plan.factor()
-        xh = plan.solve(rhs)
-    e1.record(stream)
-    barrier()
-    e2e_ms = e0.elapsed_time(e1)
-    e2e_value = world * args.steps / (e2e_ms / 1000.0)
-
-    # per-kernel-class device time over identical steps (CUDA events per launch)
-    plan.set_profiling(True)
-    for _ in range(2):
-        step()
-    stats = plan.kernel_stats()
-    plan.set_profiling(False)
-    torch.cuda.synchronize()
-
-    # plain FP64 factorization path on the same GPU
-    fp64 = None
-    if not args.no_fp64:
-        st64 = nq.default_settings(precision=nq.NQG_FP64, req_ref_iter=1, max_inner_iter=2, tol_abs=0.0,
-                                   tol_rel=0.0, reg_diag=1e-9)
-        p64 = nq.Plan(n, K.p, K.i, K.x, settings=st64)
-        p64.set_stream(stream.cuda_stream)
-        d_x64 = torch.empty(n, dtype=torch.float64, device="cuda")
-        p64.factor()
-        p64.solve_device(d_rhs.data_ptr(), d_x64.data_ptr())
-        torch.cuda.synchronize()
-        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
-        p64.factor()
-        p64.solve_device(d_rhs.data_ptr(), d_x64.data_ptr())
-        f1.record(stream)
-        torch.cuda.synchronize()
-        ms64 = f0.elapsed_time(f1)
-        x64 = d_x64.cpu().numpy()
-        fp64 = {"value": 1000.0 / ms64, "unit": "solves/s", "ms_per_step": ms64, "relres": relres(K, x64, rhs),
-                "steps": 1}
-        err_vs_fp64 = float(np.linalg.norm(x32 - x64) / np.linalg.norm(x64))
-        p64.close()
-        del d_x64
-    else:
-        err_vs_fp64 = None
-
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except OSError:
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    bf16_peak = peaks.get("bf16_tflops", 1900.0)
-    dom = max(stats, key=lambda k: stats[k]["total_ms"])
-    ds = stats[dom]
-    avg_ms = ds["total_ms"] / max(ds["launches"], 1)
-    if dom in ("solve", "spmv", "pack"):
-        ach = ds["alg_bytes"] / (ds["total_ms"] / 1000.0) / 1e9
-        roof = {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak}
-    else:
-        ach = ds["alg_flops"] / (ds["total_ms"] / 1000.0) / 1e12
-        # FP32 CUDA-core work measured against the measured dense bf16 tensor peak
-        roof = {"bound": "tensor", "achieved": ach, "peak": bf16_peak, "unit": "TFLOP/s", "frac": ach / bf16_peak,
-                "fp32_cuda_core_nominal_tflops": 80.5, "frac_of_fp32_nominal": ach / 80.5}
-    roof.update({"kernel": dom, "launches_per_step": ds["launches"] / 2, "avg_launch_ms": avg_ms,
-                 "traffic": NCU_TRAFFIC.get(dom), "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"})
-    # every class: factor classes against the measured tensor peak (the tcgen05
-    # classes do 3 split-TF32 MMAs per useful multiply-add), solves and SpMV
-    # against the measured copy bandwidth
-    by_class = {}
-    for k, v in stats.items():
-        sec = v["total_ms"] / 1000.0
-        if sec <= 0:
-            continue
-        if k in ("solve", "spmv", "pack"):
-            a = v["alg_bytes"] / sec / 1e9
-            by_class[k] = {"bound": "hbm", "achieved": a, "unit": "GB/s", "frac": a / hbm_peak}
-        else:
-            a = v["alg_flops"] / sec / 1e12
-            e = {"bound": "tensor", "achieved": a, "unit": "TFLOP/s", "frac": a / bf16_peak}
-            if k in ("update", "wide_trailing"):
-                e["mma_tflops"] = 3 * a
-            by_class[k] = e
-    roof["by_class"] = by_class
-    kinfo = {k: {"ms_per_step": v["total_ms"] / 2, "launches_per_step": v["launches"] / 2} for k, v in stats.items()}
-
+    pk, pk_src = peaks()
+    qp = qp_section(args, world, rank, local, torch, nq, P, learn, pk, pk_src)
+    c3 = None if args.no_c3 else c3_section(nq, P)
+    lbl = None if args.no_lbl else lbl_section(args, torch, nq, P, pk)
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
-            s = cpu_sample()
-            sec_full = s["seconds"] * F / s["flops"]
-            cpu = {"value": 1.0 / sec_full, "unit": "solves/s", "cores": s["threads"], "kind": "port",
-                   "sample": f"full factor + refined solve of the same KKT family at {SAMPLE_GRID}^3 grid, "
-                             f"m={SAMPLE_M} (N={s['N']}, F={s['flops']:.3e}) in {s['seconds']:.2f}s; value "
-                             f"scaled to the full workload by F_full={F:.3e}",
-                   "sample_gflops": s["flops"] / s["seconds"] / 1e9, "sample_relres": s["relres"]}
+            cpu = cpu_qp_sample(step=0)
         except Exception as e:  # the CPU baseline must not hide the GPU line
             cpu = {"value": None, "unavailable": str(e)[:200]}
-
     if rank == 0:
-        h2d = K.x.nbytes + rhs.nbytes
         line = {
-            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "metric": METRIC, "value": qp["value"], "unit": "QP solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": qp["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32-factor+fp64-refine", "data": "synthetic",
-            "config": {"workload": workload_name(args.grid, args.mcon), "N": n, "nnz_K_lower": int(K.nnz),
-                       "seed": SEED, "delta": DELTA, "factor_flops": F, "precision": "fp32 factor and triangular solves, fp64 flexible GMRES-IR",
-                       "refinement": f"FGMRES, 1 restart, stop at residual {STOP_REL:g}*||b|| (at most {INNER} "
-                                     f"inner steps; {inner_used} used)", "target_relres": TARGET_RELRES,
-                       "l2": "inputs larger than L2 (FP32 factor 4 GB)", "analysis_s": analysis_s,
-                       "parallelism": f"replicas x{world}"},
-            "relres": rr32, "meets_target": bool(rr32 <= TARGET_RELRES), "error_vs_fp64_gpu": err_vs_fp64,
-            "plain_fp64": fp64,
-            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(n * 8), "ms_per_step": e2e_ms / args.steps},
-            "roofline": roof, "kernels": kinfo, "cpu_baseline": cpu, "clocks": clk.summary(),
-            "gpu_launches": int(round(launches)),
+            "config": {"workload": "qp_mpc50_parametric_theta32", "batch": BATCH, "n": 450, "meq": 300,
+                       "mineq": 900, "eps_abs": EPS, "variant": "Fixed",
+                       "precision": "FP32 factor and triangular solves, FP64 flexible GMRES to 1e-12 relative "
+                                    "residual, final polish on the active set",
+                       "warm_start": "learned (MLP 32-256-256-900, BF16 weights, FP32 accumulation)",
+                       "l2": "256 MB written between timed steps (L2 flush)", "parallelism": f"replicas x{world}"},
+            "e2e": qp["e2e"], "check": qp["check"], "iterations": qp["iterations"],
+            "mixed_cold_batched": qp["mixed_cold_batched"], "plain_fp64_batched": qp["plain_fp64_batched"],
+            "plain_fp64_single": qp["plain_fp64_single"], "model": qp["model"], "roofline": qp["roofline"],
+            "cpu_baseline": cpu, "clocks": qp["clocks"], "gpu_launches": qp["gpu_launches"], "c3": c3,
+            "lbl_c2": lbl,
         }
         print(json.dumps(line), flush=True)
-    plan.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
