@@ -1261,12 +1261,21 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
     // ---- initial factorization and solution (reference initialize_x,
     // src/nasoq.cpp:448-476): every visible supernode; rhs [-q; b; d on the
     // active rows]
-    bool cold = !warm;
+    // Only visible supernodes are factored: a hidden one contributes zeros
+    // and is skipped by the solves.  After the first warm round, dropped
+    // constraints are hidden by the partial refactorization of their paths.
+    bool cold = !warm, full = true;
     for (int round = 0; round < 5; ++round) {
-      load_state(c);
-      build_vlist(c);
-      mark_all(c, cold);
-      factor_marked(c);
+      if (full) {
+        load_state(c);
+        build_vlist(c);
+        mark_all(c, true);
+        factor_marked(c);
+      } else {
+        sort_mlist(c);
+        factor_marked(c);
+        build_vlist(c);
+      }
       for (int i = tid; i < N; i += nt) {
         double v = 0.0;
         if (i < n) v = -c.q[i];
@@ -1290,22 +1299,33 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
         __syncthreads();
         if (tid == 0) s_status = 0;
         cold = true;
+        full = true;
         __syncthreads();
         continue;
       }
       // drop proposed constraints with negative multipliers, then solve again
-      int ndrop = 0;
-      for (int k = tid; k < mineq; k += nt)
-        if (c.act[k] && c.sol[c.base + k] < 0.0) {
-          c.act[k] = 0;
-          ndrop++;
-        }
-      ndrop = block_sum_int(ndrop, redi);
+      if (tid == 0) {
+        int nd = 0;
+        for (int k = 0; k < mineq; ++k)
+          if (c.act[k] && c.sol[c.base + k] < 0.0) {
+            edit_constraint(c, k, false);
+            nd++;
+          }
+        s_int[2] = nd;
+      }
+      __syncthreads();
+      const int ndrop = s_int[2];
       warm_dropped += ndrop;
       if (ndrop == 0) break;
+      full = false;
       if (round >= 2) {  // no consistent set after three rounds: cold start
         for (int k = tid; k < mineq; k += nt) c.act[k] = 0;
+        if (tid == 0) {
+          for (int t = 0; t < *c.nmark; ++t) c.mark[c.mlist[t]] = 0;
+          *c.nmark = 0;
+        }
         cold = true;
+        full = true;
         __syncthreads();
       }
     }
@@ -1469,10 +1489,11 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
     // Polish (adaptive refinement only): the updates x -= step * descent
     // carry each solve's residual (1e-12 relative) through every iteration,
     // so the final point is recomputed as the equality-constrained solution
-    // on the final active set.  Kept when its multipliers stay non-negative;
-    // if it then violates a constraint, the active-set iteration continues
-    // from it (at most twice).  The reference's fixed schedule runs to 1e-15
-    // and needs none of this.
+    // on the final active set (constraints whose multipliers come out
+    // negative are dropped and the solve repeated); if the point then
+    // violates a constraint, the active-set iteration continues from it (at
+    // most twice).  The reference's fixed schedule runs to 1e-15 and needs
+    // none of this.
     if (!adaptive || !converged || pol >= 2) break;
     if (*c.nmark > 0) {
       sort_mlist(c);
@@ -1491,11 +1512,40 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
     precond(c, c.rhs, c.sol);
     solves++;
     steps += refine(c, c.rhs, c.sol, P.outer, P.inner, flexible, adaptive, a.refine_tol, P.tol_abs, P.tol_rel, gs);
-    int negz = 0;
-    for (int t = tid; t < nact; t += nt)
-      if (c.sol[c.base + c.alist[t]] < 0.0) negz++;
-    negz = block_sum_int(negz, redi);
-    if (negz > 0) break;  // keep the iteration's own point
+    // a negative multiplier: that constraint does not belong to the active
+    // set of this point; drop it and solve again (at most three times)
+    for (int rep = 0; rep < 3; ++rep) {
+      if (tid == 0) {
+        int nd = 0;
+        for (int t = 0; t < nact;) {
+          const int k = c.alist[t];
+          if (c.sol[c.base + k] < 0.0) {
+            edit_constraint(c, k, false);
+            for (int u = t; u + 1 < nact; ++u) c.alist[u] = c.alist[u + 1];
+            nact--;
+            nd++;
+          } else {
+            ++t;
+          }
+        }
+        s_int[0] = nact;
+        s_int[2] = nd;
+      }
+      __syncthreads();
+      nact = s_int[0];
+      if (s_int[2] == 0) break;
+      sort_mlist(c);
+      factor_marked(c);
+      build_vlist(c);
+      for (int i = c.base + tid; i < N; i += nt)
+        if (!c.act[i - c.base]) c.rhs[i] = 0.0;
+      __syncthreads();
+      precond(c, c.rhs, c.sol);
+      solves++;
+      steps += refine(c, c.rhs, c.sol, P.outer, P.inner, flexible, adaptive, a.refine_tol, P.tol_abs, P.tol_rel, gs);
+    }
+    for (int k = tid; k < mineq; k += nt)
+      if (!c.act[k]) zv[k] = 0.0;
     for (int i = tid; i < n; i += nt) xv[i] = c.sol[i];
     for (int i = tid; i < meq; i += nt) yv[i] = c.sol[n + i];
     for (int t = tid; t < nact; t += nt) {
