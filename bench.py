@@ -51,6 +51,7 @@ EPS = 1e-8
 N_TRAIN = 200_000
 REFINE_TOL = 1e-12
 THETA_SEED = 20261204
+WS_THRESHOLD = 1.0  # logit above which a constraint is proposed (swept 0..5: 1.0 fastest, every QP optimal)
 CPU_SAMPLE_PER_PROC = 48
 # DRAM bytes (read + write) of one batch-kernel launch on this workload,
 # scaled from one ncu capture of a 1024-problem batch (profiles/); None
@@ -213,7 +214,7 @@ def qp_section(args, world, rank, local, torch, nq, P, learn, pk, pk_src):
                                                refine_tol=REFINE_TOL))
     mixed = dict(variant=0, eps_abs=EPS, precision=nq.NQG_FP32, refine=1, refine_tol=REFINE_TOL)
     batch = learn.family_batch(fam, BATCH, **mixed)
-    ws = learn.WarmStarter(batch, model, fam)
+    ws = learn.WarmStarter(batch, model, fam, threshold=WS_THRESHOLD)
     bstream = torch.cuda.ExternalStream(batch.stream())
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
@@ -226,7 +227,7 @@ def qp_section(args, world, rank, local, torch, nq, P, learn, pk, pk_src):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(bstream)
         model.forward_device(BATCH, ws.d_theta.data_ptr(), ws.d_logits.data_ptr(), stream=batch.stream())
-        batch.warm_start_from_scores(ws.d_logits.data_ptr(), mi, 0.0)
+        batch.warm_start_from_scores(ws.d_logits.data_ptr(), mi, WS_THRESHOLD)
         batch.solve_async()
         e1.record(bstream)
         e1.synchronize()
@@ -514,7 +515,8 @@ def main():
                        "mineq": 900, "eps_abs": EPS, "variant": "Fixed",
                        "precision": "FP32 factor and triangular solves, FP64 flexible GMRES to 1e-12 relative "
                                     "residual, final polish on the active set",
-                       "warm_start": "learned (MLP 32-256-256-900, BF16 weights, FP32 accumulation)",
+                       "warm_start": f"learned (MLP 32-256-256-900, BF16 weights, FP32 accumulation; logit > "
+                                     f"{WS_THRESHOLD:g} proposes a constraint)",
                        "l2": "256 MB written between timed steps (L2 flush)", "parallelism": f"replicas x{world}"},
             "e2e": qp["e2e"], "check": qp["check"], "iterations": qp["iterations"],
             "mixed_cold_batched": qp["mixed_cold_batched"], "plain_fp64_batched": qp["plain_fp64_batched"],
