@@ -136,6 +136,11 @@ def thetas_for(step, rank):
     return np.random.default_rng([THETA_SEED, rank, step]).standard_normal((BATCH, 32))
 
 
+def set_batch(b):
+    global BATCH
+    BATCH = int(b)
+
+
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle restatement of the reference's method (cold start),
 # one single-threaded process per host core, each on its own slice.
@@ -250,6 +255,10 @@ def qp_section(args, world, rank, local, torch, nq, P, learn, pk, pk_src):
     for w in range(args.warmup):
         device_step(thetas_for(10_000 + w, rank))
     barrier()
+    if args.profile_once:  # exactly one measured step, for profiler launch lists
+        ms1 = device_step(thetas_for(0, rank))
+        print(json.dumps({"profile_once_ms": ms1, "batch": BATCH}), flush=True)
+        return None
     with ClockSampler(local) as clk:
         barrier()
         ms = [device_step(thetas_for(k, rank)) for k in range(args.steps)]
@@ -481,6 +490,9 @@ def main():
     ap.add_argument("--no-c3", action="store_true")
     ap.add_argument("--no-lbl", action="store_true")
     ap.add_argument("--lbl-steps", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=BATCH, help="QPs per step (smaller cases for profiler captures)")
+    ap.add_argument("--profile-once", action="store_true",
+                    help="train, then exactly one measured step and nothing else (profiler launch lists)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
@@ -497,7 +509,10 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     pk, pk_src = peaks()
+    set_batch(args.batch)
     qp = qp_section(args, world, rank, local, torch, nq, P, learn, pk, pk_src)
+    if qp is None:
+        return 0
     c3 = None if args.no_c3 else c3_section(nq, P)
     lbl = None if args.no_lbl else lbl_section(args, torch, nq, P, pk)
     cpu = None
