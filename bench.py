@@ -213,10 +213,21 @@ def run_reference(args, world, rank):
 def qp_section(args, world, rank, local, torch, nq, P, learn, pk, pk_src):
     fam = P.mpc_parametric(0)
     n, mi = fam.base.n, fam.base.C.nrow
-    # model: trained on plain-NASOQ solves (outside the timed region)
-    model, rep = learn.train_model(fam, n_train=args.n_train, seed=11 + rank, epochs=20, batch=1024, lr=1e-3,
-                                   solver=dict(variant=0, eps_abs=EPS, precision=nq.NQG_FP32, refine=1,
-                                               refine_tol=REFINE_TOL))
+    # model: trained on plain-NASOQ solves (outside the timed region), or
+    # weights saved by an earlier run (profiler captures skip the training)
+    if args.load_model:
+        z = np.load(args.load_model)
+        model = nq.MLP(tuple(int(v) for v in z["sizes"]))
+        model.set_weights(z["w"], z["b"])
+        rep = learn.TrainReport(int(z["n_train"]), 0.0, 0.0, [float(v) for v in z["losses"]], float(z["active"]))
+    else:
+        model, rep = learn.train_model(fam, n_train=args.n_train, seed=11 + rank, epochs=20, batch=1024, lr=1e-3,
+                                       solver=dict(variant=0, eps_abs=EPS, precision=nq.NQG_FP32, refine=1,
+                                                   refine_tol=REFINE_TOL))
+        if args.save_model and rank == 0:
+            w, b = model.get_weights()
+            np.savez(args.save_model, sizes=np.array(model.sizes), w=w, b=b, n_train=rep.n_train,
+                     losses=np.array(rep.losses), active=rep.active_mean)
     mixed = dict(variant=0, eps_abs=EPS, precision=nq.NQG_FP32, refine=1, refine_tol=REFINE_TOL)
     batch = learn.family_batch(fam, BATCH, **mixed)
     ws = learn.WarmStarter(batch, model, fam, threshold=WS_THRESHOLD)
@@ -493,6 +504,8 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH, help="QPs per step (smaller cases for profiler captures)")
     ap.add_argument("--profile-once", action="store_true",
                     help="train, then exactly one measured step and nothing else (profiler launch lists)")
+    ap.add_argument("--save-model", default=None, help="write the trained model's weights (.npz)")
+    ap.add_argument("--load-model", default=None, help="use saved weights instead of training")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

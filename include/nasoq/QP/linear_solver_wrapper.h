@@ -104,6 +104,7 @@ struct SolverSettings {
   nqg_plan *plan;             // device plan, created by symbolic_analysis()
   std::vector<std::vector<long long>> const_val_idx;  // QP mode: SM value index of every entry of each constraint
   int last_gpu_status;        // status of the last C-ABI call
+  bool own_simplicial;        // l_pb / l_pe / l_i allocated by convert_supernode_to_simplicial()
 
   SolverSettings(CSC *Amat, double *rhs_in);
   SolverSettings(CSC *Amat, double *rhs_in, CSC *Bmat);
@@ -115,21 +116,51 @@ struct SolverSettings {
   void default_setting();
   int build_super_matrix();
   void find_perturbation(double tol);
+  // +tol on the diagonals of the first A->ncol columns of AorSM, -tol on the
+  // rest (host values; the plan applies the same rule when regularization != 1)
+  void apply_perturbation(double tol);
+  // the same on the host ordered copy A_ord (the plan factors the perturbed
+  // matrix and refines with the unperturbed one by itself)
+  void add_perturbation(double tol);
+  void remove_perturbation(double tol);
   int symbolic_analysis();
   void reset_symbolic_factor();
+  // level sets of the supernodal tree (s_level_*) when num_thread > thread_thresh
+  void architecture_related_params();
+  // host workspaces ws / ws_int / ws_zeroed, with the reference's sizes
+  void allocate_workspace();
   int numerical_factorization();
   int delete_node_tree_simple(int k);
   int add_node_tree_simple(int k);
   void bfs_tree(int cur_sn);
+  // column-tree variants (etree_mod / child_ptr / child_no, built on first use)
+  int delete_node_tree(int k);
+  int add_node_tree(int k);
   int add_del_matrix_qp(int add_del, std::vector<int> add_drp_const);
   int update_somod(std::vector<int> add_drp_const, const int n_rhs, const double *new_rhs);
   int downdate_somod(std::vector<int> add_drp_const, int n_rhs);
   int update_factorization();
+  // placeholders with the reference's return values (1, 1, NULL, 1, NULL)
+  int edit_matrix();
+  int edit_rhs();
+  double *edit_solve_rhs();
+  int edit_update_factorization(int add_del, std::vector<int> add_drp_const);
+  double *update_solve();
   double *solve_only();
   double *solve_only(const int n_rhs, double *rhs_in);
+  // refinement alone, started from x = rhs (x returned)
+  double *iterative_ref_only();
+  // brings L->Perm / L->IPerm and A_ord up to the permutation of the last
+  // factorization (the GPU folds the pivots into it while factoring)
+  void reorder_matrix();
   void compute_norms();
   double backward_error();
+  // column pointers / row indices of the factor in simplicial form (l_pb, l_pe, l_i)
+  void convert_supernode_to_simplicial();
+  void copy_lsuper_to_l();
   void set_diags(double d);
+  // downloads the factor; 1 when every value is finite and the permutation is one
+  int check_ldlt_factor();
   // Copies the GPU factor into valL / d_val and the current permutation into
   // L->Perm / L->IPerm (host buffers owned by this object).
   int download_factor();

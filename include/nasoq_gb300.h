@@ -41,7 +41,12 @@ typedef struct nqg_settings {
   double tol_abs;       /* GMRES absolute tolerance (reference tol_abs) */
   double tol_rel;       /* GMRES relative tolerance (reference tol_rel) */
   double reg_diag;      /* diagonal perturbation (reference reg_diag) */
-  int regularization;   /* 1: |a_jj| < reg_diag -> a_jj = reg_diag (reference find_perturbation) */
+  /* 1: |a_jj| < reg_diag -> a_jj = reg_diag, the refinement sees 0 there
+   *    (reference find_perturbation / set_diags);
+   * 0: a_jj += reg_diag on columns [0, perturb_plus_cols), a_jj -= reg_diag
+   *    on the others, the refinement sees the unperturbed matrix (reference
+   *    apply_perturbation / remove_perturbation / add_perturbation). */
+  int regularization;
   int n_relax[3];       /* supernode relaxation (reference n_relax) */
   double z_relax[3];    /* supernode relaxation (reference z_relax) */
   /* FP32 factor only: diagonal entries smaller than this in magnitude are
@@ -56,6 +61,9 @@ typedef struct nqg_settings {
    * enough when the refined residual still meets the tolerance; on
    * ill-conditioned systems it can stall the refinement earlier). */
   int solve_precision;
+  /* regularization 0: number of leading columns perturbed by +reg_diag (the
+   * reference's A->ncol: the Hessian block of a QP); < 0: every column. */
+  int perturb_plus_cols;
 } nqg_settings;
 
 /* Reference defaults (src/QP/linear_solver_wrapper.cpp:205-244). */
@@ -112,6 +120,13 @@ int nqg_plan_destroy(nqg_plan *plan);
 /* Work on the given CUDA stream (cudaStream_t passed as void*; NULL = the
  * plan's own stream). */
 int nqg_set_stream(nqg_plan *plan, void *stream);
+/* Polls before a cross-CTA wait of this plan gives up (grid barriers and
+ * pivot exchanges of the multi-CTA factorization, flag waits of the block
+ * triangular solves); polls <= 0 restores the default (2^26).  A wait that
+ * gives up makes the call return NQG_ERR_TIMEOUT; the plan stays usable.
+ * The shared-memory barrier waits of the tensor-core kernels keep their
+ * fixed bound.  Synchronizes the plan's stream. */
+int nqg_set_wait_limit(nqg_plan *plan, long long polls);
 int nqg_get_symbolic(const nqg_plan *plan, const nqg_symbolic **sym);
 
 /* Replace all matrix values (same pattern as at creation); host buffer.
@@ -143,8 +158,14 @@ int nqg_set_visibility(nqg_plan *plan, const uint8_t *visible_sn, const uint8_t 
  * (replaces SolverSettings::solve_only, src/QP/linear_solver_wrapper.cpp:
  * 1300-1404, with pmgmres_ldlt_auto(_update), src/gmres/mgmres.cpp:1015-1421). */
 int nqg_solve(nqg_plan *plan, const double *rhs, double *x);
-/* Same with device buffers (n doubles each, may alias). */
+/* Same with device buffers (n doubles each, may alias).  Both return
+ * NQG_ERR_TIMEOUT when a wait of the block solves gave up (x is then not a
+ * solution). */
 int nqg_solve_device(nqg_plan *plan, const double *d_rhs, double *d_x);
+/* Refinement only (reference SolverSettings::iterative_ref_only,
+ * src/QP/linear_solver_wrapper.cpp:1406-1430): GMRES on K x = rhs,
+ * preconditioned by the current factor, started from x = rhs; host buffers. */
+int nqg_refine_only(nqg_plan *plan, const double *rhs, double *x);
 /* Only the LDL^T solve of an ordered vector in place on the device
  * (reference solve_phase_ldl_blocked_parallel, src/linear_solver/
  * solve_phase.cpp:88-111). */
@@ -219,6 +240,11 @@ typedef struct nqg_qp_settings {
   int max_iter;         /* refinement iterations (reference max_iter) */
   int max_iter_nas;     /* active-set iteration cap (reference max_iter_nas) */
   int precision;        /* NQG_FP64 or NQG_FP32 factorization */
+  /* > 0: rounds of Ruiz equilibration of H, A, B, q, a, b before the solve,
+   * undone on the data and the solution after it (reference Nasoq::scaling,
+   * src/nasoq.cpp:662-703); 0: none.  Single-problem solver only: the
+   * batched solver rejects a nonzero value. */
+  int scaling;
 } nqg_qp_settings;
 
 typedef struct nqg_qp_result {
@@ -353,6 +379,32 @@ int nqg_mlp_train(nqg_mlp *m, int epochs, int batch, float lr, float pos_weight,
                   double *epoch_loss);
 const char *nqg_mlp_last_error(const nqg_mlp *m);
 int nqg_mlp_destroy(nqg_mlp *m);
+
+/* ---- SMP QP files (reference smp-format) -------------------------------- */
+/* A QP read from an SMP file (reference SMP::load, smp-format/smp_format.h:
+ * 174-233) and converted to  min 1/2 x'Hx + q'x  s.t.  A x = b, C x <= d
+ * (QPFormatConverter::smp_to_ie, smp-format/mp_format_converter.h:681-712):
+ * rows l <= c'x <= u become c'x <= u and/or -c'x <= -l, infinite sides
+ * (|bound| = 1e20) dropped, in row order (find_inequalities_by_bounds,
+ * :264-433).  H is lower-stored with a zero diagonal in empty columns.
+ * Host only; no GPU needed. */
+typedef struct nqg_qp_data nqg_qp_data;
+/* Returns NQG_OK, or NQG_ERR_ARG for an unreadable or invalid file; *out is
+ * set either way (nqg_qp_data_error explains a failure) and must be freed
+ * with nqg_qp_data_destroy. */
+int nqg_smp_load(const char *path, nqg_qp_data **out);
+const char *nqg_qp_data_error(const nqg_qp_data *qp);
+/* n, equality rows, inequality rows; nnz[3] = entries of H, A, C. */
+int nqg_qp_data_sizes(const nqg_qp_data *qp, int *n, int *meq, int *mineq, int64_t *nnz);
+/* CSC arrays (H lower, A meq x n, C mineq x n) and vectors; any may be NULL. */
+int nqg_qp_data_export(const nqg_qp_data *qp, int *Hp, int *Hi, double *Hx, double *q, int *Ap, int *Ai, double *Ax,
+                       double *b, int *Cp, int *Ci, double *Cx, double *d);
+/* The constant objective term, the stated optimum and the stated solution
+ * (counts 0 when the file holds none); any pointer may be NULL. */
+int nqg_qp_data_extras(const nqg_qp_data *qp, double *fixed, double *optimal_obj, int *n_primals, double *primals,
+                       int *n_duals, double *duals);
+const char *nqg_qp_data_description(const nqg_qp_data *qp);
+int nqg_qp_data_destroy(nqg_qp_data *qp);
 
 #ifdef __cplusplus
 }

@@ -17,6 +17,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libnasoq_gb300.so")
 
 NQG_OK = 0
+NQG_WARN_ZERO_PIVOT = 1
+NQG_WARN_NONFINITE = 2
+NQG_ERR_TIMEOUT = -5
 NQG_FP64 = 0
 NQG_FP32 = 1
 
@@ -30,7 +33,7 @@ class Settings(C.Structure):
     _fields_ = [("precision", C.c_int), ("req_ref_iter", C.c_int), ("max_inner_iter", C.c_int),
                 ("tol_abs", C.c_double), ("tol_rel", C.c_double), ("reg_diag", C.c_double),
                 ("regularization", C.c_int), ("n_relax", C.c_int * 3), ("z_relax", C.c_double * 3),
-                ("reg_diag_fp32", C.c_double), ("solve_precision", C.c_int)]
+                ("reg_diag_fp32", C.c_double), ("solve_precision", C.c_int), ("perturb_plus_cols", C.c_int)]
 
 
 class SymbolicInfo(C.Structure):
@@ -56,7 +59,8 @@ KERNEL_CLASSES = {"update": 0, "wide_panel": 1, "wide_trailing": 2, "bk": 3, "so
 
 class QPSettings(C.Structure):
     _fields_ = [("variant", C.c_int), ("eps_abs", C.c_double), ("diag_perturb", C.c_double),
-                ("stop_tol", C.c_double), ("max_iter", C.c_int), ("max_iter_nas", C.c_int), ("precision", C.c_int)]
+                ("stop_tol", C.c_double), ("max_iter", C.c_int), ("max_iter_nas", C.c_int), ("precision", C.c_int),
+                ("scaling", C.c_int)]
 
 
 class QPResult(C.Structure):
@@ -110,6 +114,7 @@ def lib():
                                   C.POINTER(C.c_void_p)]
     L.nqg_plan_destroy.argtypes = [C.c_void_p]
     L.nqg_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+    L.nqg_set_wait_limit.argtypes = [C.c_void_p, C.c_longlong]
     L.nqg_get_symbolic.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
     L.nqg_set_values.argtypes = [C.c_void_p, _f64p]
     L.nqg_edit_values.argtypes = [C.c_void_p, C.c_int, _i64p, _f64p]
@@ -118,6 +123,7 @@ def lib():
     L.nqg_set_visibility.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     L.nqg_solve.argtypes = [C.c_void_p, _f64p, _f64p]
     L.nqg_solve_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.nqg_refine_only.argtypes = [C.c_void_p, _f64p, _f64p]
     L.nqg_ldlt_solve_ordered_device.argtypes = [C.c_void_p, C.c_void_p]
     L.nqg_spmv_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
     L.nqg_get_timings.argtypes = [C.c_void_p, C.POINTER(Timings)]
@@ -166,6 +172,15 @@ def lib():
     L.nqg_mlp_destroy.argtypes = [C.c_void_p]
     L.nqg_batch_set_profiling.argtypes = [C.c_void_p, C.c_int]
     L.nqg_batch_get_profile.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+    L.nqg_smp_load.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+    L.nqg_qp_data_error.argtypes = [C.c_void_p]
+    L.nqg_qp_data_error.restype = C.c_char_p
+    L.nqg_qp_data_description.argtypes = [C.c_void_p]
+    L.nqg_qp_data_description.restype = C.c_char_p
+    L.nqg_qp_data_sizes.argtypes = [C.c_void_p] + [C.c_void_p] * 4
+    L.nqg_qp_data_export.argtypes = [C.c_void_p] + [C.c_void_p] * 12
+    L.nqg_qp_data_extras.argtypes = [C.c_void_p] + [C.c_void_p] * 6
+    L.nqg_qp_data_destroy.argtypes = [C.c_void_p]
     _lib = L
     return L
 
@@ -289,11 +304,22 @@ class Plan:
         _check(lib().nqg_solve(self._h, rhs, x), "solve")
         return x
 
+    def refine_only(self, rhs):
+        """GMRES refinement alone, started from x = rhs (iterative_ref_only)."""
+        rhs = np.ascontiguousarray(rhs, np.float64)
+        x = np.empty(self.n, np.float64)
+        _check(lib().nqg_refine_only(self._h, rhs, x), "refine only")
+        return x
+
     def solve_device(self, d_rhs_ptr, d_x_ptr):
         _check(lib().nqg_solve_device(self._h, C.c_void_p(d_rhs_ptr), C.c_void_p(d_x_ptr)), "solve")
 
     def set_stream(self, stream_ptr):
         _check(lib().nqg_set_stream(self._h, C.c_void_p(stream_ptr)), "set stream")
+
+    def set_wait_limit(self, polls=0):
+        """Polls before a cross-CTA wait gives up (<= 0: the default)."""
+        _check(lib().nqg_set_wait_limit(self._h, C.c_longlong(int(polls))), "set wait limit")
 
     def timings(self) -> Timings:
         t = Timings()
@@ -351,6 +377,44 @@ def qp_settings(**kw) -> QPSettings:
             v = VARIANTS[v.lower()]
         setattr(s, k, v)
     return s
+
+
+def load_smp(path):
+    """Reads an SMP QP file (the reference's smp-format) into a
+    problems.QP  min 1/2 x'Hx + q'x  s.t.  A x = b, C x <= d, with the file's
+    constant term, stated optimum, primals, duals and description in
+    QP.meta.  Two-sided rows l <= c'x <= u become c'x <= u, -c'x <= -l."""
+    from nasoq_gb300 import problems as P
+    L = lib()
+    h = C.c_void_p()
+    rc = L.nqg_smp_load(os.fsencode(path), C.byref(h))
+    try:
+        if rc < 0:
+            msg = L.nqg_qp_data_error(h).decode() if h else "cannot open file"
+            raise NasoqError(f"load_smp({path}): {msg}")
+        n, meq, mineq = C.c_int(), C.c_int(), C.c_int()
+        nnz = np.zeros(3, np.int64)
+        L.nqg_qp_data_sizes(h, C.byref(n), C.byref(meq), C.byref(mineq), _ptr(nnz))
+        n, meq, mineq = n.value, meq.value, mineq.value
+        Hp, Ap, Cp = (np.zeros(n + 1, np.int32) for _ in range(3))
+        Hi, Ai, Ci = (np.zeros(max(int(k), 1), np.int32) for k in nnz)
+        Hx, Ax, Cx = (np.zeros(max(int(k), 1), np.float64) for k in nnz)
+        q, b, d = np.zeros(max(n, 1)), np.zeros(max(meq, 1)), np.zeros(max(mineq, 1))
+        L.nqg_qp_data_export(h, *[_ptr(a) for a in (Hp, Hi, Hx, q, Ap, Ai, Ax, b, Cp, Ci, Cx, d)])
+        fixed, opt = C.c_double(), C.c_double()
+        npr, ndu = C.c_int(), C.c_int()
+        L.nqg_qp_data_extras(h, C.byref(fixed), C.byref(opt), C.byref(npr), None, C.byref(ndu), None)
+        prim, dual = np.zeros(max(npr.value, 1)), np.zeros(max(ndu.value, 1))
+        L.nqg_qp_data_extras(h, None, None, None, _ptr(prim), None, _ptr(dual))
+        meta = {"kind": "smp", "path": os.fspath(path), "fixed": fixed.value, "optimal_objective": opt.value,
+                "primals": prim[:npr.value], "duals": dual[:ndu.value],
+                "description": L.nqg_qp_data_description(h).decode()}
+    finally:
+        if h:
+            L.nqg_qp_data_destroy(h)
+    k0, k1, k2 = (int(k) for k in nnz)
+    return P.QP(P.CSC(n, n, Hp, Hi[:k0], Hx[:k0]), q[:n], P.CSC(meq, n, Ap, Ai[:k1], Ax[:k1]), b[:meq],
+                P.CSC(mineq, n, Cp, Ci[:k2], Cx[:k2]), d[:mineq], meta)
 
 
 def qp_solve(H, q, A, b, Cm, d, settings: QPSettings | None = None, warm=None):

@@ -1605,6 +1605,12 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
       for (int e = c.eq_ptr[r]; e < c.eq_ptr[r + 1]; ++e) t += c.kv[c.eq_q[e]] * xv[c.eq_var[e]];
       cons = fmax(cons, fabs(t - c.bq[r]));
     }
+    // a non-finite solution (non-finite data, or a breakdown the loop could
+    // not recover from) is never reported as converged
+    int nonfin = 0;
+    for (int i = tid; i < N; i += nt)
+      if (!isfinite(c.tmp[i]) || !isfinite(c.w[i])) nonfin = 1;
+    nonfin = block_sum_int(nonfin, redi);
     quad = block_sum(quad, red);
     lin = block_sum(lin, red);
     dual_obj = block_sum(dual_obj, red);
@@ -1630,7 +1636,7 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
       BResult &R = a.res[pi];
       R.num_iter = num_iter;
       R.active_size = nact;
-      R.flags = s_status;
+      R.flags = s_status | (nonfin ? ST_NONFINITE : 0);
       R.refine_steps = steps;
       R.solves = solves;
       R.warm_dropped = warm_dropped;
@@ -1642,7 +1648,8 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
       R.non_negativity_infn = mx[2];
       R.complementarity_infn = mx[3];
       int st;
-      if (!converged) st = 0;  // check_solve_status: Infeasible when the loop did not converge
+      if (nonfin) st = 3;      // NotConverged
+      else if (!converged) st = 0;  // check_solve_status: Infeasible when the loop did not converge
       else if (mx[0] <= P.eps_abs && mx[1] <= P.eps_abs && mx[2] <= P.eps_abs) st = 1;
       else if (mx[1] <= P.eps_abs) st = 2;
       else st = 3;
@@ -1661,10 +1668,14 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
 // threshold, in ascending order, except one parallel to a constraint it
 // already proposed (same variables, proportional coefficients -- the two
 // sides of a box): both active would make the KKT matrix singular.  A
-// problem with no proposal keeps a cold start.  One thread per problem.
+// problem with no proposal keeps a cold start.  One warp per problem: lanes
+// read 32 scores at a time (coalesced); the candidates of a chunk are taken
+// in constraint order, each checked by all lanes at once against the
+// constraints already proposed.
 __global__ void k_ws_scores(int nprob, BProb *probs, const BPat *pats, const int *ipool, const double *dpool,
                             int *iout, const float *scores, int ld, float thr) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= nprob) return;
   BProb &P = probs[i];
   const BPat &pt = pats[P.pat];
@@ -1674,23 +1685,32 @@ __global__ void k_ws_scores(int nprob, BProb *probs, const BPat *pats, const int
   const float *sc = scores + (size_t)i * ld;
   int cnt = 0;
   const int mi = min(pt.mineq, ld);
-  for (int k = 0; k < mi; ++k) {
-    if (!(sc[k] > thr)) continue;
-    const int ka = bt_ptr[k], kn = bt_ptr[k + 1] - ka;
-    bool parallel = false;
-    for (int t = 0; t < cnt && !parallel; ++t) {
-      const int j = as[t], ja = bt_ptr[j], jn = bt_ptr[j + 1] - ja;
-      if (jn != kn || kn == 0) continue;
-      bool same = true;
-      const double r = kv[bt_q[ka]] / kv[bt_q[ja]];
-      for (int e = 0; e < kn && same; ++e)
-        same = bt_var[ka + e] == bt_var[ja + e] && fabs(kv[bt_q[ka + e]] - r * kv[bt_q[ja + e]]) <=
-                                                        1e-12 * fabs(kv[bt_q[ka + e]]);
-      parallel = same;
+  for (int c0 = 0; c0 < mi; c0 += 32) {
+    const int kk = c0 + lane;
+    unsigned cand = __ballot_sync(0xffffffffu, kk < mi && sc[kk] > thr);
+    while (cand) {
+      const int k = c0 + __ffs(cand) - 1;
+      cand &= cand - 1;
+      const int ka = bt_ptr[k], kn = bt_ptr[k + 1] - ka;
+      bool parallel = false;
+      for (int t = lane; t < cnt; t += 32) {
+        const int j = as[t], ja = bt_ptr[j], jn = bt_ptr[j + 1] - ja;
+        if (jn != kn || kn == 0) continue;
+        bool same = true;
+        const double r = kv[bt_q[ka]] / kv[bt_q[ja]];
+        for (int e = 0; e < kn && same; ++e)
+          same = bt_var[ka + e] == bt_var[ja + e] &&
+                 fabs(kv[bt_q[ka + e]] - r * kv[bt_q[ja + e]]) <= 1e-12 * fabs(kv[bt_q[ka + e]]);
+        parallel = parallel || same;
+      }
+      if (!__any_sync(0xffffffffu, parallel)) {
+        if (lane == 0) as[cnt] = k;
+        ++cnt;
+        __syncwarp();
+      }
     }
-    if (!parallel) as[cnt++] = k;
   }
-  P.ws_n = cnt > 0 ? cnt : -1;
+  if (lane == 0) P.ws_n = cnt > 0 ? cnt : -1;
 }
 
 __global__ void k_ws_clear(int nprob, BProb *probs) {
@@ -1700,7 +1720,7 @@ __global__ void k_ws_clear(int nprob, BProb *probs) {
 
 int batch_ws_from_scores(int nprob, BProb *probs, const BPat *pats, const int *ipool, const double *dpool, int *iout,
                          const float *scores, int ld, float thr, cudaStream_t st) {
-  k_ws_scores<<<(nprob + 127) / 128, 128, 0, st>>>(nprob, probs, pats, ipool, dpool, iout, scores, ld, thr);
+  k_ws_scores<<<(nprob + 7) / 8, 256, 0, st>>>(nprob, probs, pats, ipool, dpool, iout, scores, ld, thr);
   return cudaGetLastError() == cudaSuccess ? NQG_OK : NQG_ERR_CUDA;
 }
 

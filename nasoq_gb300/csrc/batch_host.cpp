@@ -465,7 +465,7 @@ extern "C" int nqg_batch_create(const nqg_batch_settings *s, nqg_batch **out) {
   auto *b = new nqg_batch;
   if (s) b->set = *s;
   else nqg_batch_default_settings(&b->set);
-  if (b->set.qp.precision != NQG_FP64 && b->set.qp.precision != NQG_FP32) {
+  if ((b->set.qp.precision != NQG_FP64 && b->set.qp.precision != NQG_FP32) || b->set.qp.scaling != 0) {
     delete b;
     return NQG_ERR_ARG;
   }

@@ -38,6 +38,7 @@ extern "C" void nqg_default_settings(nqg_settings *s) {
   s->z_relax[2] = 0.05;
   s->reg_diag_fp32 = 0.0;
   s->solve_precision = NQG_FP64;
+  s->perturb_plus_cols = -1;
 }
 
 extern "C" const char *nqg_status_str(int st) {
@@ -509,9 +510,14 @@ static void free_plan(Plan &P) {
   if (P.own_stream) cudaStreamDestroy(P.own_stream);
 }
 
-// Perturbation of tiny diagonals (reference find_perturbation,
-// src/QP/linear_solver_wrapper.cpp:352-363): the factorization sees
-// reg_diag, the refinement matrix sees 0 there (set_diags(0), :1524-1533).
+// Diagonal perturbation of the factored matrix.  regularization 1
+// (reference find_perturbation, src/QP/linear_solver_wrapper.cpp:352-363):
+// tiny diagonals become reg_diag, and the refinement matrix sees 0 there
+// (set_diags(0), :1524-1533).  regularization 0 (apply_perturbation,
+// :365-372): +reg_diag on the leading perturb_plus_cols diagonals, -reg_diag
+// on the rest, and the refinement matrix keeps the unperturbed values
+// (remove_perturbation before the refinement, :1362).  Every column's first
+// stored entry is its diagonal (checked at plan creation).
 static void apply_perturbation(Plan &P) {
   P.pert_idx.clear();
   P.Kx_spmv = P.K.x;
@@ -524,6 +530,13 @@ static void apply_perturbation(Plan &P) {
         P.Kx_spmv[q] = 0.0;
         P.pert_idx.push_back(q);
       }
+    }
+  } else if (P.set.reg_diag != 0.0) {
+    const int plus = P.set.perturb_plus_cols < 0 ? P.n : std::min(P.set.perturb_plus_cols, P.n);
+    for (int j = 0; j < P.n; ++j) {
+      int q = P.K.p[j];
+      if (q >= P.K.p[j + 1]) continue;
+      P.K.x[q] += j < plus ? P.set.reg_diag : -P.set.reg_diag;
     }
   }
   // FP32 factor: a larger, sign-keeping floor on the diagonal of the matrix
@@ -750,10 +763,30 @@ extern "C" int nqg_solve_device(nqg_plan *h, const double *d_rhs, double *d_x) {
   int rc = dev_solve(P, d_rhs, d_x);
   if (rc) return rc;
   NQG_CUDA(cudaEventRecord(P.ev1, P.stream));
+  int st = 0;
+  NQG_CUDA(cudaMemcpyAsync(&st, P.d_status, sizeof(int), cudaMemcpyDeviceToHost, P.stream));
   NQG_CUDA(cudaEventSynchronize(P.ev1));
+  NQG_CUDA(cudaStreamSynchronize(P.stream));
   float ms = 0;
   cudaEventElapsedTime(&ms, P.ev0, P.ev1);
   P.tm.solve_ms = ms;
+  if (st & ST_TIMEOUT) {  // a block-solve wait gave up: x is not a solution
+    st &= ~ST_TIMEOUT;
+    NQG_CUDA(cudaMemcpy(P.d_status, &st, sizeof(int), cudaMemcpyHostToDevice));
+    P.last_error = "a cross-CTA wait of the triangular solves gave up";
+    return NQG_ERR_TIMEOUT;
+  }
+  return NQG_OK;
+}
+
+extern "C" int nqg_set_wait_limit(nqg_plan *h, long long polls) {
+  if (!h) return NQG_ERR_ARG;
+  Plan &P = h->P;
+  if (!P.d_wide_ctl) return NQG_ERR_STATE;
+  const long long v = polls > 0 ? polls : 0;
+  NQG_CUDA(cudaStreamSynchronize(P.stream));
+  NQG_CUDA(cudaMemcpy(static_cast<char *>(P.d_wide_ctl) + wide_ctl_limit_offset(), &v, sizeof(v),
+                      cudaMemcpyHostToDevice));
   return NQG_OK;
 }
 
@@ -766,6 +799,31 @@ extern "C" int nqg_solve(nqg_plan *h, const double *rhs, double *x) {
   if (rc) return rc;
   NQG_CUDA(cudaMemcpyAsync(x, P.d_out, P.n * sizeof(double), cudaMemcpyDeviceToHost, P.stream));
   NQG_CUDA(cudaStreamSynchronize(P.stream));
+  return NQG_OK;
+}
+
+extern "C" int nqg_refine_only(nqg_plan *h, const double *rhs, double *x) {
+  if (!h || (!rhs && h->P.n > 0) || (!x && h->P.n > 0)) return NQG_ERR_ARG;
+  Plan &P = h->P;
+  if (!P.factored) return NQG_ERR_STATE;
+  NQG_CUDA(cudaMemcpyAsync(P.d_in, rhs, P.n * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  NQG_CUDA(cudaEventRecord(P.ev0, P.stream));
+  int rc = dev_refine_only(P, P.d_in, P.d_out);
+  if (rc) return rc;
+  NQG_CUDA(cudaEventRecord(P.ev1, P.stream));
+  int st = 0;
+  NQG_CUDA(cudaMemcpyAsync(&st, P.d_status, sizeof(int), cudaMemcpyDeviceToHost, P.stream));
+  NQG_CUDA(cudaMemcpyAsync(x, P.d_out, P.n * sizeof(double), cudaMemcpyDeviceToHost, P.stream));
+  NQG_CUDA(cudaStreamSynchronize(P.stream));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, P.ev0, P.ev1);
+  P.tm.solve_ms = ms;
+  if (st & ST_TIMEOUT) {
+    st &= ~ST_TIMEOUT;
+    NQG_CUDA(cudaMemcpy(P.d_status, &st, sizeof(int), cudaMemcpyHostToDevice));
+    P.last_error = "a cross-CTA wait of the triangular solves gave up";
+    return NQG_ERR_TIMEOUT;
+  }
   return NQG_OK;
 }
 

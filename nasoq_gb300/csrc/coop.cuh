@@ -3,6 +3,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstddef>
+
 #include "plan.hpp"
 
 namespace nqg {
@@ -26,9 +28,17 @@ struct WideCtl {
   unsigned long long pslot[2][1024];
   // fast panels: up to four candidate words per CTA and exchange
   unsigned long long mslot[2][4][1024];
+  // polls before a cross-CTA wait gives up (0: SPIN_LIMIT); kept across the
+  // per-supernode resets, which clear the fields above only
+  long long spin_limit;
 };
 
-constexpr long long SPIN_LIMIT = 1ll << 26;  // polls before a barrier gives up
+constexpr long long SPIN_LIMIT = 1ll << 26;  // default polls before a wait gives up
+
+__device__ __forceinline__ long long wait_limit(const WideCtl *ctl) {
+  const long long v = *(volatile const long long *)&ctl->spin_limit;
+  return v > 0 ? v : SPIN_LIMIT;
+}
 
 // Grid-wide barrier for a cooperative launch, sense-reversing on ctl->gen.
 // Returns false once any CTA has timed out (all CTAs then unwind).
@@ -48,12 +58,13 @@ __device__ __forceinline__ bool grid_sync(WideCtl *ctl, int *status) {
       atomicAdd(&ctl->gen, 1u);
     } else {
       long long it = 0;
+      const long long lim = wait_limit(ctl);
       while (*vgen == my) {
         if (*vab) {
           ok = 0;
           break;
         }
-        if (++it > SPIN_LIMIT) {
+        if (++it > lim) {
           atomicOr(status, ST_TIMEOUT);
           atomicExch(&ctl->abort, 1);
           ok = 0;

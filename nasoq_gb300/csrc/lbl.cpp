@@ -141,6 +141,20 @@ SolverSettings::~SolverSettings() {
   delete[] child_sn_ptr;
   delete[] child_sn_no;
   delete[] num_sn_child;
+  delete[] etree_mod;
+  delete[] child_ptr;
+  delete[] child_no;
+  delete[] num_child;
+  delete[] s_level_ptr;
+  delete[] s_level_set;
+  delete[] ws;
+  delete[] ws_int;
+  delete[] ws_zeroed;
+  if (own_simplicial) {
+    delete[] l_pb;
+    delete[] l_pe;
+    delete[] l_i;
+  }
   if (remove_trans) free_csc(BT);
   if (solver_mode == 1) {
     delete[] sm_rhs;
@@ -214,6 +228,7 @@ void SolverSettings::default_setting() {
   gpu_precision = 0;
   plan = nullptr;
   last_gpu_status = 0;
+  own_simplicial = false;
 }
 
 int SolverSettings::build_super_matrix() {
@@ -281,6 +296,52 @@ void SolverSettings::find_perturbation(double tol) {
   }
 }
 
+void SolverSettings::apply_perturbation(double tol) {
+  // reference :365-372 (quasi-definite shift of the caller's matrix)
+  for (size_t i = 0; i < AorSM->ncol; ++i) AorSM->x[AorSM->p[i]] += i < A->ncol ? tol : -tol;
+}
+
+// On the host ordered copy, with the reference's arithmetic (:374-394): the
+// sign follows the ordered column index.  The plan's own refinement matrix
+// is the exactly unperturbed one.
+void SolverSettings::add_perturbation(double tol) {
+  for (size_t i = 0; i < A_ord->ncol; ++i) {
+    const size_t ord_col = (size_t)L->IPerm[i];
+    A_ord->x[A_ord->p[ord_col]] += ord_col < A->ncol ? tol : -tol;
+  }
+}
+
+void SolverSettings::remove_perturbation(double tol) {
+  for (size_t i = 0; i < A_ord->ncol; ++i) {
+    const size_t ord_col = (size_t)L->IPerm[i];
+    A_ord->x[A_ord->p[ord_col]] -= ord_col < A->ncol ? tol : -tol;
+  }
+}
+
+// Lower-stored P K P^T of the caller's matrix (current host values) under
+// the current L->IPerm, as the reference's double transpose builds A_ord.
+static CSC *ordered_copy(const CSC *K, const int *iperm) {
+  const int N = (int)K->ncol;
+  nqg::Csc k, lo;
+  k.n = N;
+  k.p.assign(K->p, K->p + N + 1);
+  k.i.assign(K->i, K->i + K->p[N]);
+  k.x.assign(K->x, K->x + K->p[N]);
+  std::vector<int> ip(iperm, iperm + N);
+  nqg::sym_permute(k, ip, &lo, nullptr);
+  CSC *O = new CSC;
+  O->ncol = O->nrow = N;
+  O->nzmax = lo.nnz();
+  O->p = new int[N + 1];
+  O->i = new int[std::max<int64_t>(lo.nnz(), 1)];
+  O->x = new double[std::max<int64_t>(lo.nnz(), 1)];
+  std::copy(lo.p.begin(), lo.p.end(), O->p);
+  std::copy(lo.i.begin(), lo.i.end(), O->i);
+  std::copy(lo.x.begin(), lo.x.end(), O->x);
+  O->stype = -1;
+  return O;
+}
+
 int SolverSettings::symbolic_analysis() {
   psi->start = psi->tic();
   if (solver_mode == 0) {
@@ -301,6 +362,7 @@ int SolverSettings::symbolic_analysis() {
     for (int j = (int)base; j < N; ++j) extra_cols[j] = 1;
   std::vector<double> orig(AorSM->x, AorSM->x + AorSM->p[N]);
   if (regularization == 1) find_perturbation(reg_diag);
+  else apply_perturbation(reg_diag);
   nqg_settings st;
   nqg_default_settings(&st);
   st.precision = gpu_precision ? NQG_FP32 : NQG_FP64;
@@ -310,6 +372,7 @@ int SolverSettings::symbolic_analysis() {
   st.tol_rel = tol_rel;
   st.reg_diag = reg_diag;
   st.regularization = regularization == 1 ? 1 : 0;
+  st.perturb_plus_cols = (int)A->ncol;
   std::copy(n_relax, n_relax + 3, st.n_relax);
   std::copy(z_relax, z_relax + 3, st.z_relax);
   last_gpu_status = nqg_plan_create(N, AorSM->p, AorSM->i, orig.data(), extra_cols, &st, &plan);
@@ -356,26 +419,8 @@ int SolverSettings::symbolic_analysis() {
   perm_piv = new int[std::max(N, 1)];
   marked = new bool[std::max<int64_t>(std::max<int64_t>(N, info.nsuper), 1)]();
   // ordered copy of the matrix (fill-reducing ordering of the analysis)
-  {
-    nqg::Csc K;
-    K.n = N;
-    K.p.assign(AorSM->p, AorSM->p + N + 1);
-    K.i.assign(AorSM->i, AorSM->i + AorSM->p[N]);
-    K.x.assign(AorSM->x, AorSM->x + AorSM->p[N]);
-    nqg::Csc lo;
-    std::vector<int> ip(L->IPerm, L->IPerm + N);
-    nqg::sym_permute(K, ip, &lo, nullptr);
-    A_ord = new CSC;
-    A_ord->ncol = A_ord->nrow = N;
-    A_ord->nzmax = lo.nnz();
-    A_ord->p = new int[N + 1];
-    A_ord->i = new int[std::max<int64_t>(lo.nnz(), 1)];
-    A_ord->x = new double[std::max<int64_t>(lo.nnz(), 1)];
-    std::copy(lo.p.begin(), lo.p.end(), A_ord->p);
-    std::copy(lo.i.begin(), lo.i.end(), A_ord->i);
-    std::copy(lo.x.begin(), lo.x.end(), A_ord->x);
-    A_ord->stype = -1;
-  }
+  A_ord = ordered_copy(AorSM, L->IPerm);
+  allocate_workspace();
   if (solver_mode == 1) {
     const int ns = info.nsuper;
     atree = new int[std::max(ns, 1)];
@@ -404,6 +449,7 @@ int SolverSettings::symbolic_analysis() {
       if (marked[m]) modified_sns.push_back(m);
       visible_sn[m] = marked[m];
     }
+    architecture_related_params();
     // SM value index of every entry of every inequality constraint, in BT order
     const int mineq = B ? (int)B->nrow : 0;
     const_val_idx.assign(mineq, {});
@@ -417,6 +463,55 @@ int SolverSettings::symbolic_analysis() {
 void SolverSettings::reset_symbolic_factor() {
   if (sm_rhs && SM) std::fill(sm_rhs, sm_rhs + SM->ncol, 0.0);
   if (sm_solution && SM) std::fill(sm_solution, sm_solution + SM->ncol, 0.0);
+}
+
+void SolverSettings::architecture_related_params() {
+  // level sets of the supernodal tree for many-thread schedules (reference
+  // :553-561): level of a supernode = longest path from a leaf below it,
+  // supernodes of a level in increasing order (parents follow children in
+  // the numbering, so one forward pass settles every level)
+  delete[] s_level_ptr;
+  delete[] s_level_set;
+  s_level_ptr = s_level_set = nullptr;
+  s_level_no = -1;
+  if (num_thread <= thread_thresh || !L) return;
+  const int ns = (int)L->nsuper;
+  std::vector<int> lev(ns, 0);
+  int nlev = ns > 0 ? 1 : 0;
+  for (int k = 0; k < ns; ++k) {
+    const int p = L->sParent[k];
+    if (p >= 0) lev[p] = std::max(lev[p], lev[k] + 1);
+    nlev = std::max(nlev, lev[k] + 1);
+  }
+  s_level_ptr = new int[nlev + 1]();
+  s_level_set = new int[std::max(ns, 1)];
+  for (int k = 0; k < ns; ++k) s_level_ptr[lev[k] + 1]++;
+  for (int l = 0; l < nlev; ++l) s_level_ptr[l + 1] += s_level_ptr[l];
+  std::vector<int> fill(s_level_ptr, s_level_ptr + nlev);
+  for (int k = 0; k < ns; ++k) s_level_set[fill[lev[k]]++] = k;
+  s_level_no = nlev;
+}
+
+void SolverSettings::allocate_workspace() {
+  // the reference's sizes (:563-600): the update routine's integer and
+  // dense scratch, two n-vectors, and the solve + GMRES scratch
+  const size_t n = AorSM->ncol, ns = L ? L->nsuper : 0;
+  const size_t upd_int = 4 * (size_t)(max_sup_wid + 1) + 2 * n + 3 * ns;
+  const size_t upd_dbl = 2 * (size_t)(max_sup_wid + 1) * (size_t)(max_col + 1);
+  ws_int_size = std::max(upd_int, 3 * n);
+  ws_dbl_size = std::max(upd_dbl, 2 * n);
+  size_t slve = 2 * n;
+  if (max_iter > 0) {
+    const size_t mi = (size_t)max_inner_iter;
+    slve += 4 * (mi + 1) + (mi + 1) * (mi + 2) + 1 + n + (mi + 1) * n + 1;
+  }
+  ws_dbl_size = std::max(slve, ws_dbl_size);
+  delete[] ws;
+  delete[] ws_int;
+  delete[] ws_zeroed;
+  ws = new double[ws_dbl_size]();
+  ws_int = new int[ws_int_size]();
+  ws_zeroed = new double[(size_t)std::max(num_thread, 1) * n]();
 }
 
 int SolverSettings::numerical_factorization() {
@@ -521,6 +616,75 @@ int SolverSettings::add_node_tree_simple(int k) {
   return 1;
 }
 
+// etree_mod / child_ptr / child_no / num_child of the column elimination
+// tree (children in increasing order), and a private assembly tree in the
+// plain-solve mode, built when a column-tree edit first needs them
+static void ensure_column_tree(SolverSettings &S) {
+  const int N = (int)S.AorSM->ncol, ns = (int)S.L->nsuper;
+  if (!S.etree_mod) {
+    S.etree_mod = new int[std::max(N, 1)];
+    std::copy(S.L->Parent, S.L->Parent + N, S.etree_mod);
+  }
+  if (!S.child_ptr) {
+    S.child_ptr = new int[N + 1]();
+    S.child_no = new int[std::max(N, 1)];
+    S.num_child = new int[std::max(N, 1)]();
+    for (int j = 0; j < N; ++j)
+      if (S.L->Parent[j] >= 0) S.num_child[S.L->Parent[j]]++;
+    for (int j = 0; j < N; ++j) S.child_ptr[j + 1] = S.child_ptr[j] + S.num_child[j];
+    std::vector<int> fill(S.child_ptr, S.child_ptr + N);
+    for (int j = 0; j < N; ++j)
+      if (S.L->Parent[j] >= 0) S.child_no[fill[S.L->Parent[j]]++] = j;
+  }
+  if (!S.atree) {
+    S.atree = new int[std::max(ns, 1)];
+    std::copy(S.L->sParent, S.L->sParent + ns, S.atree);
+  }
+}
+
+int SolverSettings::delete_node_tree(int k) {
+  // reference :937-964: children of column k move to k's parent, k hidden;
+  // its supernode is hidden once all of its columns are
+  ensure_column_tree(*this);
+  const int ord_nod = L->IPerm[k];
+  const int par_k = etree_mod[ord_nod];
+  const int cur_par_sn = par_k >= 0 ? L->col2Sup[par_k] : ROOT;
+  for (int q = child_ptr[ord_nod]; q < child_ptr[ord_nod + 1]; ++q) {
+    const int c = child_no[q];
+    if (etree_mod[c] == INVISIBLE) continue;
+    etree_mod[c] = par_k;
+    const int csn = L->col2Sup[c];
+    if (csn != cur_par_sn) atree[csn] = cur_par_sn;
+  }
+  etree_mod[ord_nod] = INVISIBLE;
+  const int cur_sn = L->col2Sup[ord_nod];
+  visible_cnt[cur_sn]++;
+  if (L->super[cur_sn + 1] - L->super[cur_sn] == visible_cnt[cur_sn]) {
+    atree[cur_sn] = INVISIBLE;
+    marked[cur_sn] = false;
+  }
+  return 1;
+}
+
+int SolverSettings::add_node_tree(int k) {
+  // reference :966-993: column k re-attaches below its first visible
+  // ancestor and takes its visible children back
+  ensure_column_tree(*this);
+  const int ord_nod = L->IPerm[k];
+  int k_par = etree[ord_nod];
+  while (k_par != -1 && etree_mod[k_par] == INVISIBLE) k_par = etree[k_par];
+  etree_mod[ord_nod] = k_par;
+  const int cur_sn = L->col2Sup[ord_nod];
+  for (int q = child_ptr[ord_nod]; q < child_ptr[ord_nod + 1]; ++q) {
+    const int c = child_no[q];
+    if (etree_mod[c] == INVISIBLE) continue;
+    etree_mod[c] = ord_nod;
+    const int csn = L->col2Sup[c];
+    if (csn != cur_sn) atree[csn] = cur_sn;
+  }
+  return 1;
+}
+
 int SolverSettings::update_somod(std::vector<int> add_drp_const, const int n_rhs, const double *new_rhs) {
   const int dim = (int)AorSM->nrow;
   for (int k : add_drp_const)
@@ -582,6 +746,12 @@ int SolverSettings::update_factorization() {
   return last_gpu_status >= 0 ? 1 : 0;
 }
 
+int SolverSettings::edit_matrix() { return 1; }
+int SolverSettings::edit_rhs() { return 1; }
+double *SolverSettings::edit_solve_rhs() { return nullptr; }
+int SolverSettings::edit_update_factorization(int, std::vector<int>) { return 1; }
+double *SolverSettings::update_solve() { return nullptr; }
+
 double *SolverSettings::solve_only(const int n_rhs, double *rhs_in) {
   std::copy(rhs_in, rhs_in + AorSM->ncol, rhs);
   return solve_only();
@@ -609,6 +779,73 @@ double *SolverSettings::solve_only() {
   psi->end = psi->toc();
   psi->solve_time += psi->elapsed_time(psi->start, psi->end);
   return x;
+}
+
+double *SolverSettings::iterative_ref_only() {
+  const int N = (int)AorSM->ncol;
+  if (solver_mode == 1) {
+    const int ns = (int)L->nsuper;
+    std::vector<uint8_t> vis(ns), hid(N);
+    for (int s = 0; s < ns; ++s) vis[s] = visible_sn[s] ? 1 : 0;
+    for (int j = 0; j < N; ++j) hid[j] = extra_cols[j] ? 1 : 0;
+    nqg_set_visibility(plan, vis.data(), hid.data());
+  }
+  last_gpu_status = nqg_refine_only(plan, rhs, x);
+  if (last_gpu_status < 0) std::cerr << "nasoq_gb300: refinement failed: " << nqg_status_str(last_gpu_status) << "\n";
+  nqg_timings t;
+  nqg_get_timings(plan, &t);
+  num_ref_iter = t.num_ref_iter;
+  return x;
+}
+
+void SolverSettings::reorder_matrix() {
+  if (!plan || !L) return;
+  const int N = (int)AorSM->ncol;
+  nqg_get_factor(plan, nullptr, nullptr, L->Perm, nullptr);
+  for (int i = 0; i < N; ++i) L->IPerm[L->Perm[i]] = i;
+  free_csc(A_ord);
+  A_ord = ordered_copy(AorSM, L->IPerm);
+  for (int i = 0; i < N; ++i) perm_piv[i] = i;  // the pivots are part of L->Perm now
+}
+
+void SolverSettings::convert_supernode_to_simplicial() {
+  // per column j of supernode s: its values start (j - first column) rows
+  // into the supernode's column and use the supernode's row list from there
+  if (!L) return;
+  const int N = (int)L->n;
+  if (!l_pb) {
+    l_pb = new int[std::max(N, 1)];
+    l_pe = new int[std::max(N, 1)];
+    l_i = new int[std::max<size_t>(L->xsize, 1)];
+    own_simplicial = true;
+  }
+  for (size_t sn = 0; sn < L->nsuper; ++sn) {
+    const int c0 = L->super[sn], c1 = L->super[sn + 1];
+    for (int j = c0; j < c1; ++j) {
+      l_pb[j] = (int)L->p[j] + (j - c0);
+      l_pe[j] = (int)L->p[j + 1];
+      size_t kk = L->i_ptr[c0] + (size_t)(j - c0);
+      for (int k = l_pb[j]; k < l_pe[j]; ++k, ++kk) l_i[k] = L->s[kk];
+    }
+  }
+}
+
+void SolverSettings::copy_lsuper_to_l() {}  // an empty routine in the reference too (:1519-1521)
+
+int SolverSettings::check_ldlt_factor() {
+  if (!download_factor()) return 0;
+  const size_t N = L->n;
+  for (size_t i = 0; i < L->xsize; ++i)
+    if (!std::isfinite(valL[i])) return 0;
+  for (size_t i = 0; i < 2 * N; ++i)
+    if (!std::isfinite(d_val[i])) return 0;
+  std::vector<char> seen(N, 0);
+  for (size_t i = 0; i < N; ++i) {
+    const int p = L->Perm[i];
+    if (p < 0 || (size_t)p >= N || seen[p]) return 0;
+    seen[p] = 1;
+  }
+  return 1;
 }
 
 void SolverSettings::set_diags(double d) {

@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <fstream>
 #include <iostream>
 #include <limits>
 
@@ -156,6 +157,12 @@ Nasoq::Nasoq(size_t H_size, int *Hp, int *Hi, double *Hx, double *q_in, size_t B
   used_constraints = 0;
   ret_val = NotConverged;
   gpu_precision = 0;
+  eTree = col2const = const2col = etree = pinv = col2sup = as0 = nullptr;
+  sKKTt = nullptr;
+  D = E = F = Dinv = Einv = Finv = rec_length = nullptr;
+  c = cinv = 1.0;
+  qp_scalar = inv_qp_scalar = 1.0;
+  dual_FB_a = dual_FB_b = dual_FB = primal_FB_a = primal_FB_b = primal_FB = nullptr;
   default_setting();
 }
 
@@ -178,6 +185,7 @@ Nasoq::Nasoq(size_t H_size, int *Hp, int *Hi, double *Hx, double *q_in, size_t A
 }
 
 Nasoq::~Nasoq() {
+  for (double *v : {D, E, F, Dinv, Einv, Finv}) delete[] v;
   delete[] workspace;
   delete[] primal_vars;
   delete[] dual_vars_eq;
@@ -224,6 +232,36 @@ void Nasoq::auto_perturbation2(size_t dim, size_t total_nnz, double H_norm2, dou
 
 void Nasoq::determine_iterations(size_t total_nnz, double acc_thresh, int &outer, int &inner) {
   nqg::qp_determine_iterations(total_nnz, acc_thresh, outer, inner);
+}
+
+void Nasoq::reset_symbolic_info() {}  // an empty routine in the reference too (:280-281)
+
+void Nasoq::auto_perturbation(size_t total_nnz, double H_norm2, size_t dim, double &reg, int &outer, int &inner) {
+  // the reference's first tuning table (:283-312): small problems refine
+  // 2x2 with 1e-11 (1e-7 when ||H||_F < 1); large ones pick by ||H||_F
+  if (total_nnz < 3e4 || dim < 4100) {
+    reg = H_norm2 < 1 ? 1e-7 : 1e-11;
+    outer = inner = 2;
+    return;
+  }
+  if (H_norm2 < 1) {
+    reg = 1e-7;
+    outer = inner = 1;
+  } else if (H_norm2 < 1e3) {
+    reg = 1e-11;
+    outer = inner = 9;
+  } else if (H_norm2 < 5e5) {
+    reg = 1e-8;
+    outer = inner = 0;
+  } else {
+    reg = 1e-11;
+    outer = inner = 1;
+  }
+}
+
+void Nasoq::allocate_workspace() {
+  // the reference sizes its scratch here without allocating it (:400-411);
+  // `workspace` (B rows + 4 n doubles) is allocated by the constructor
 }
 
 int Nasoq::symbolic_QP() {
@@ -397,6 +435,8 @@ int Nasoq::solve() {
   warm_start = 0;
   qi->tot_st = qi->tic();
   int status = 0;
+  if (scaling > 0) scale_data();
+  if (scaling < 0) scale_data_2();
   if (variant == Tuned) {
     if (symbolic_QP() < 0) return ret_val = Infeasible;
     for (int i = 0; i < 4; i++) {
@@ -408,6 +448,14 @@ int Nasoq::solve() {
     if (symbolic_QP() < 0) return ret_val = Infeasible;
     initialize_x();
     status = numeric_QP();
+  }
+  if (scaling > 0) {
+    unscale_data();
+    unscale_solution();
+  }
+  if (scaling < 0) {
+    unscale_data_2();
+    unscale_solution_2();
   }
   qi->tot_end = qi->toc();
   qi->tot = qi->elapsed_time(qi->tot_st, qi->tot_end);
@@ -439,10 +487,15 @@ void Nasoq::detect_solver_name() {
 int Nasoq::solve(double *primal_in, double *dual_in, const std::vector<int> &as) {
   warm_start = 1;
   qi->tot_st = qi->tic();
+  if (scaling > 0) scale_data();
   int rv = symbolic_QP();
   if (rv < 0) return rv;
   set_warm_start(primal_in, dual_in, as);
   rv = numeric_QP();
+  if (scaling > 0) {
+    unscale_data();
+    unscale_solution();
+  }
   qi->tot_end = qi->toc();
   qi->tot = qi->elapsed_time(qi->tot_st, qi->tot_end);
   compute_objective();
@@ -454,10 +507,15 @@ int Nasoq::solve(double *primal_in, double *dual_in, const std::vector<int> &as)
 int Nasoq::solve(double *primal_in) {
   warm_start = 1;
   qi->tot_st = qi->tic();
+  if (scaling > 0) scale_data();
   int rv = symbolic_QP();
   if (rv < 0) return rv;
   set_warm_start_primal(primal_in);
   rv = numeric_QP();
+  if (scaling > 0) {
+    unscale_data();
+    unscale_solution();
+  }
   qi->tot_end = qi->toc();
   qi->tot = qi->elapsed_time(qi->tot_st, qi->tot_end);
   compute_objective();
@@ -484,6 +542,13 @@ int Nasoq::primal_feasibility(int &nxt_add) {
     }
   }
   return violated_no;
+}
+
+int Nasoq::dual_feasibility() {
+  int neg = 0;
+  for (int i = 0; i < num_active; ++i)
+    if (dual_vars[i] < 0) neg++;
+  return neg;
 }
 
 double Nasoq::dual_step_length(int &nxt_drop) {
@@ -517,6 +582,58 @@ int Nasoq::update_rhs(int nxt_active) {
   return 1;
 }
 
+int Nasoq::solve_kkt_from_scratch() {
+  // [H A' B_S'; A 0 0; B_S 0 0] of the active set S as one lower CSC, the
+  // rhs entries of its rows, solved by a plain-mode solver (reference :890-919)
+  const int n = (int)H->ncol, me = (int)A->nrow, ns = (int)active_set.size(), N = n + me + ns;
+  for (int i = 0; i < me; ++i) lagrange_mult_eq[i] = 0;
+  for (size_t i = 0; i < B->nrow; ++i) lagrange_mult[i] = 0;
+  std::vector<int> slot(B->nrow, -1);
+  for (int t = 0; t < ns; ++t) slot[active_set[t]] = t;
+  std::vector<std::vector<std::pair<int, double>>> cols(N);
+  for (int j = 0; j < n; ++j) {
+    for (int q = H->p[j]; q < H->p[j + 1]; ++q)
+      if (H->i[q] >= j) cols[j].push_back({H->i[q], H->x[q]});
+    if (me > 0)
+      for (int q = A->p[j]; q < A->p[j + 1]; ++q) cols[j].push_back({n + A->i[q], A->x[q]});
+    for (int q = B->p[j]; q < B->p[j + 1]; ++q)
+      if (slot[B->i[q]] >= 0) cols[j].push_back({n + me + slot[B->i[q]], B->x[q]});
+    std::sort(cols[j].begin(), cols[j].end());
+  }
+  for (int k = n; k < N; ++k) cols[k].push_back({k, 0.0});
+  std::vector<int> Kp(N + 1, 0), Ki;
+  std::vector<double> Kx, rhs(N);
+  for (int j = 0; j < N; ++j) {
+    for (auto &e : cols[j]) {
+      Ki.push_back(e.first);
+      Kx.push_back(e.second);
+    }
+    Kp[j + 1] = (int)Ki.size();
+  }
+  for (int i = 0; i < n + me; ++i) rhs[i] = sKKTrhs[i];
+  for (int t = 0; t < ns; ++t) rhs[n + me + t] = sKKTrhs[n + me + active_set[t]];
+  CSC K;
+  K.nrow = K.ncol = N;
+  K.nzmax = Kx.size();
+  K.p = Kp.data();
+  K.i = Ki.data();
+  K.x = Kx.data();
+  K.stype = -1;
+  SolverSettings lin(&K, rhs.data());
+  lin.req_ref_iter = outer_iter_ref;
+  lin.max_inner_iter = inner_iter_ref;
+  lin.tol_abs = lin.tol_rel = stop_tol;
+  lin.reg_diag = diag_perturb;
+  lin.gpu_precision = gpu_precision;
+  if (!lin.symbolic_analysis() || lin.numerical_factorization() < 0) return 0;
+  const double *sol = lin.solve_only();
+  for (int i = 0; i < n; ++i) descent[i] = sol[i];
+  for (int i = 0; i < me; ++i) lagrange_mult_eq[i] = sol[n + i];
+  for (int t = 0; t < ns; ++t) lagrange_mult[active_set[t]] = sol[n + me + t];
+  delete[] lin.x;
+  return 1;
+}
+
 int Nasoq::solve_kkt(solve_type s_type) {
   qi->fct_st = qi->tic();
   if (s_type == SOLVE) {
@@ -546,6 +663,18 @@ double Nasoq::compute_primal_obj() {
   for (size_t i = 0; i < H->ncol; ++i) lin += q[i] * primal_vars[i];
   primal_obj = 0.5 * quad + lin;
   return primal_obj;
+}
+
+double Nasoq::quad_form(const CSC *P, const double *x) {
+  double v = 0.0;
+  for (size_t j = 0; j < P->ncol; ++j)
+    for (int q = P->p[j]; q < P->p[j + 1]; ++q) {
+      const int i = P->i[q];
+      if (i == (int)j) v += 0.5 * P->x[q] * x[i] * x[i];
+      else if (i < (int)j) v += P->x[q] * x[i] * x[j];
+      else return -1;
+    }
+  return v;
 }
 
 double Nasoq::compute_dual_obj() {
@@ -598,6 +727,47 @@ double Nasoq::constraint_sat_norm() {
   return cons_sat_norm;
 }
 
+// a + b - sqrt(a^2 + b^2): zero exactly when a >= 0, b >= 0 and a b = 0
+static void fischer_burmeister(size_t m, const double *a, const double *b, double *f) {
+  for (size_t i = 0; i < m; ++i) f[i] = a[i] + b[i] - std::sqrt(a[i] * a[i] + b[i] * b[i]);
+}
+
+double Nasoq::dual_FB_norm() {
+  // the dual complementarity at z with x(z) = H^{-1} (B' z), H^{-1} q through
+  // a plain-mode solver on H (reference :1108-1160)
+  const size_t n = H->ncol, m = B->nrow;
+  std::vector<double> Bz(n), t1(m), t2(m), fa(m), fb(m), f(m);
+  spmv_small(BT->nrow, BT->ncol, BT->p, BT->i, BT->x, dual_vars, Bz.data());
+  SolverSettings hs(H, Bz.data());
+  hs.gpu_precision = gpu_precision;
+  hs.symbolic_analysis();
+  hs.numerical_factorization();
+  double *hx = hs.solve_only();
+  spmv_small(m, B->ncol, B->p, B->i, B->x, hx, t1.data());
+  for (size_t j = 0; j < n; ++j) hs.rhs[j] = q[j];
+  hx = hs.solve_only();
+  spmv_small(m, B->ncol, B->p, B->i, B->x, hx, t2.data());
+  for (size_t i = 0; i < m; ++i) {
+    fa[i] = dual_vars[i];
+    fb[i] = t1[i] + t2[i] + b[i];
+  }
+  fischer_burmeister(m, fa.data(), fb.data(), f.data());
+  delete[] hs.x;
+  return inf_norm(m, f.data());
+}
+
+double Nasoq::primal_FB_norm() {
+  const size_t m = B->nrow;
+  std::vector<double> bx(m), fa(m), fb(m), f(m);
+  spmv_small(m, B->ncol, B->p, B->i, B->x, primal_vars, bx.data());
+  for (size_t i = 0; i < m; ++i) {
+    fa[i] = dual_vars[i];
+    fb[i] = b[i] - bx[i];
+  }
+  fischer_burmeister(m, fa.data(), fb.data(), f.data());
+  return inf_norm(m, f.data());
+}
+
 double Nasoq::non_negativity_norm() {
   double *tmp = workspace;
   for (size_t i = 0; i < B->nrow; ++i) tmp[i] = dual_vars[i] > 0.0 ? 0 : dual_vars[i];
@@ -611,12 +781,360 @@ void Nasoq::print(int) {
             << "\n";
 }
 
+// the header, then one value per line at 30 significant digits
+static void write_values(const std::string &path, size_t n, const double *v, const std::string &head) {
+  if (n == 0) return;
+  std::ofstream f(path);
+  f.precision(30);
+  f << head;
+  for (size_t i = 0; i < n; ++i) {
+    f << v[i];
+    if (i + 1 < n) f << "\n";
+  }
+}
+
+void Nasoq::export_to_file(std::string p_name, std::string vec_head) {
+  write_values(p_name + "_primal.txt", H->ncol, primal_vars, vec_head);
+  write_values(p_name + "_dual.txt", B->nrow, dual_vars, "");
+  const double info[5] = {(double)num_iter, primal_obj, dual_obj, objective, qi->tot};
+  write_values(p_name + "_info.txt", 5, info, "");
+}
+
+// largest |v|, smallest |v| above 0 among entries that are not a new maximum,
+// mean and variance of |v| (the reference's max_min_vector rule)
+static void abs_range(size_t n, const double *v, double &mx, double &mn, double &avg, double &var) {
+  mx = -std::numeric_limits<double>::max();
+  mn = std::numeric_limits<double>::max();
+  avg = var = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const double t = std::abs(v[i]);
+    if (t > mx) mx = t;
+    else if (t < mn && t > 0) mn = t;
+    avg += t / n;
+  }
+  for (size_t i = 0; i < n; ++i) {
+    const double t = std::abs(v[i]) - avg;
+    var += t * t / n;
+  }
+}
+
+void Nasoq::print_qp_range(int verbose) {
+  // data arrays bound both ends of the range, solution arrays only the top
+  struct Item {
+    size_t n;
+    const double *v;
+    bool both;
+  };
+  const Item items[] = {{H->nzmax, H->x, true},           {H->ncol, q, true},
+                        {H->ncol, primal_vars, false},    {A->nzmax, A->x, true},
+                        {A->nrow, a, true},               {A->nrow, dual_vars_eq, false},
+                        {B->nzmax, B->x, true},           {B->nrow, b, true},
+                        {B->nrow, dual_vars, false}};
+  double max_max = -std::numeric_limits<double>::max(), min_min = std::numeric_limits<double>::max();
+  for (const Item &it : items) {
+    double mx = 0, mn = 0, avg = 0, var = 0;
+    if (it.v) abs_range(it.n, it.v, mx, mn, avg, var);
+    else abs_range(0, nullptr, mx, mn, avg, var);
+    if (verbose) std::cout << mx << "," << mn << "," << avg << "," << var << ",";
+    if (it.both) min_min = std::min(min_min, mn);
+    max_max = std::max(max_max, mx);
+  }
+  std::cout << min_min << "," << max_max << "," << max_max / min_min << ",";
+}
+
 void Nasoq::print_log() {
   std::cout << eps_abs << "," << outer_iter_ref << "," << inner_iter_ref << ",";
   std::cout << stop_tol << "," << diag_perturb << "," << ret_val << "," << num_iter << ",";
   std::cout << qi->tot << "," << active_set.size() << "," << cons_sat_norm << ",";
   std::cout << lag_res << "," << primal_obj << "," << dual_obj << "," << objective << ",";
   std::cout << non_negativity_infn << "," << complementarity_infn << ",";
+}
+
+// ---- scaling -----------------------------------------------------------------
+// diag(row) M diag(col), the row factor applied first (the products are
+// rounded in the reference's order)
+static void scale_rows_cols(CSC *M, const double *row, const double *col) {
+  if (!M || !M->p) return;
+  for (size_t j = 0; j < M->ncol; ++j)
+    for (int q = M->p[j]; q < M->p[j + 1]; ++q) {
+      if (row) M->x[q] *= row[M->i[q]];
+      if (col) M->x[q] *= col[j];
+    }
+}
+
+static void scale_all(CSC *M, double s) {
+  if (!M || !M->p) return;
+  for (int q = 0; q < M->p[M->ncol]; ++q) M->x[q] *= s;
+}
+
+// column infinity norms of a lower- or upper-stored symmetric matrix
+static void sym_col_norms(const CSC *M, double *e) {
+  std::fill(e, e + M->ncol, 0.0);
+  for (size_t j = 0; j < M->ncol; ++j)
+    for (int q = M->p[j]; q < M->p[j + 1]; ++q) {
+      const int i = M->i[q];
+      const double v = std::abs(M->x[q]);
+      e[j] = std::max(e[j], v);
+      if (i != (int)j) e[i] = std::max(e[i], v);
+    }
+}
+
+// a norm below 1e-4 counts as 1 (no scaling), one above 1e4 is capped there
+static double clamp_norm(double v) { return v < 1e-4 ? 1.0 : (v > 1e4 ? 1e4 : v); }
+
+int Nasoq::scale_data_2() {
+  // a single scalar on the data (reference :1319-1332, where the scalar is
+  // fixed at 1)
+  inv_qp_scalar = 1.0;
+  qp_scalar = 1.0 / inv_qp_scalar;
+  scale_all(H, qp_scalar * qp_scalar);
+  for (size_t i = 0; i < H->ncol; ++i) q[i] *= qp_scalar;
+  scale_all(A, qp_scalar);
+  scale_all(B, qp_scalar);
+  return 1;
+}
+
+int Nasoq::unscale_data_2() {
+  scale_all(H, inv_qp_scalar * inv_qp_scalar);
+  for (size_t i = 0; i < H->ncol; ++i) q[i] *= inv_qp_scalar;
+  scale_all(A, inv_qp_scalar);
+  scale_all(AT, inv_qp_scalar);
+  scale_all(B, inv_qp_scalar);
+  scale_all(BT, inv_qp_scalar);
+  return 1;
+}
+
+int Nasoq::unscale_solution_2() {
+  for (size_t i = 0; i < H->ncol; ++i) primal_vars[i] *= qp_scalar;
+  return 1;
+}
+
+int Nasoq::scale_data() {
+  // Modified Ruiz equilibration of the KKT matrix [H A' B'; A 0 0; B 0 0]
+  // with S = diag(D, E, F), plus the cost scaling c, `scaling` rounds
+  // (reference :1352-1483, the OSQP data scaling): each round divides every
+  // row and column by the square root of its infinity norm, then scales H
+  // and q by 1 / max(mean column norm of H, |q|_inf).
+  const size_t n = H->ncol, me = A->nrow, m = B->nrow;
+  auto fresh = [](double *&v, size_t k) {
+    delete[] v;
+    v = new double[std::max<size_t>(k, 1)];
+    std::fill(v, v + std::max<size_t>(k, 1), 1.0);
+  };
+  fresh(D, n), fresh(E, me), fresh(F, m), fresh(Dinv, n), fresh(Einv, me), fresh(Finv, m);
+  c = 1.0;
+  std::vector<double> dt(n), dc(n), et(me), ft(m);
+  for (int r = 0; r < scaling; ++r) {
+    sym_col_norms(H, dt.data());
+    for (const CSC *M : {(const CSC *)A, (const CSC *)B}) {
+      if (!M->p) continue;
+      for (size_t j = 0; j < M->ncol; ++j) {
+        double mx = 0;
+        for (int q2 = M->p[j]; q2 < M->p[j + 1]; ++q2) mx = std::max(mx, std::abs(M->x[q2]));
+        dt[j] = std::max(dt[j], mx);
+      }
+    }
+    std::fill(et.begin(), et.end(), 0.0);
+    std::fill(ft.begin(), ft.end(), 0.0);
+    if (A->p)
+      for (size_t j = 0; j < A->ncol; ++j)
+        for (int q2 = A->p[j]; q2 < A->p[j + 1]; ++q2) et[A->i[q2]] = std::max(et[A->i[q2]], std::abs(A->x[q2]));
+    if (B->p)
+      for (size_t j = 0; j < B->ncol; ++j)
+        for (int q2 = B->p[j]; q2 < B->p[j + 1]; ++q2) ft[B->i[q2]] = std::max(ft[B->i[q2]], std::abs(B->x[q2]));
+    for (double &v : dt) v = 1.0 / std::sqrt(clamp_norm(v));
+    for (double &v : et) v = 1.0 / std::sqrt(clamp_norm(v));
+    for (double &v : ft) v = 1.0 / std::sqrt(clamp_norm(v));
+    scale_rows_cols(H, dt.data(), dt.data());
+    scale_rows_cols(A, et.data(), dt.data());
+    scale_rows_cols(B, ft.data(), dt.data());
+    for (size_t i = 0; i < n; ++i) {
+      q[i] *= dt[i];
+      D[i] *= dt[i];
+    }
+    for (size_t i = 0; i < me; ++i) E[i] *= et[i];
+    for (size_t i = 0; i < m; ++i) F[i] *= ft[i];
+    // cost scaling
+    sym_col_norms(H, dc.data());
+    double mean = 0;
+    for (double v : dc) mean += v;
+    mean /= (double)n;
+    const double qn = clamp_norm(inf_norm(n, q));
+    const double ct = 1.0 / clamp_norm(std::max(mean, qn));
+    scale_all(H, ct);
+    for (size_t i = 0; i < n; ++i) q[i] *= ct;
+    c *= ct;
+  }
+  cinv = 1.0 / c;
+  for (size_t i = 0; i < n; ++i) Dinv[i] = 1.0 / D[i];
+  for (size_t i = 0; i < me; ++i) Einv[i] = 1.0 / E[i];
+  for (size_t i = 0; i < m; ++i) Finv[i] = 1.0 / F[i];
+  for (size_t i = 0; i < me; ++i) a[i] *= E[i];
+  for (size_t i = 0; i < m; ++i) b[i] *= F[i];
+  return 0;
+}
+
+int Nasoq::unscale_data() {
+  scale_all(H, cinv);
+  scale_rows_cols(H, Dinv, Dinv);
+  for (size_t i = 0; i < H->ncol; ++i) {
+    q[i] *= cinv;
+    q[i] *= Dinv[i];
+  }
+  if (A->nrow > 0) {
+    scale_rows_cols(A, Einv, Dinv);
+    scale_rows_cols(AT, Dinv, Einv);
+    for (size_t i = 0; i < A->nrow; ++i) a[i] *= Einv[i];
+  }
+  scale_rows_cols(B, Finv, Dinv);
+  scale_rows_cols(BT, Dinv, Finv);
+  for (size_t i = 0; i < B->nrow; ++i) b[i] *= Finv[i];
+  return 0;
+}
+
+int Nasoq::unscale_solution() {
+  for (size_t i = 0; i < H->ncol; ++i) primal_vars[i] *= D[i];
+  for (size_t i = 0; i < A->nrow; ++i) {
+    dual_vars_eq[i] *= E[i];
+    dual_vars_eq[i] *= cinv;
+  }
+  for (size_t i = 0; i < B->nrow; ++i) {
+    dual_vars[i] *= F[i];
+    dual_vars[i] *= cinv;
+  }
+  return 0;
+}
+
+// ---- the batched-addition variant (reference :1540-1735) -----------------------
+idx_val::idx_val() : val(0.0), idx(-1) {}
+idx_val::idx_val(int i, double v) : val(v), idx(i) {}
+bool CMP(idx_val x, idx_val y) { return x.val < y.val; }
+int remove_from_list(std::vector<idx_val> &list_const, int c_no) {
+  for (size_t i = 0; i < list_const.size(); ++i)
+    if (list_const[i].idx == c_no) {
+      list_const.erase(list_const.begin() + i);
+      return 1;
+    }
+  return 0;
+}
+
+int Nasoq::numeric_QP_batch() {
+  // every violated row enters at once (all but the most violated through a
+  // row edit); rows whose multiplier turns negative leave again before the
+  // step; then the usual primal / dual step on the most violated row
+  int nxt_active = -1, nxt_drop = -1, to_add = 1;
+  std::vector<idx_val> nxt_list;
+  solve_type typ = SOLVE;
+  while (true) {
+    if (num_iter > max_iter_nas) return is_converged = 0;
+    if (to_add == 1) {
+      const int nviol = primal_feasibility_batch(nxt_list);
+      if (nviol == 0) {
+        compute_objective();
+        return is_converged = 1;
+      }
+      if (nxt_list.empty()) return is_converged = 0;
+      edit_kkt_batch(to_add, nxt_list);
+      nxt_active = nxt_list.back().idx;
+      update_rhs(nxt_active);
+      typ = UPDATE;
+      to_add = 0;
+    }
+    while (!to_add) {
+      int neg = -1;
+      solve_kkt(typ);
+      if (dual_feasibility_inner(neg) == 0) break;
+      edit_kkt(to_add, neg);
+      typ = UPDATE;
+      remove_from_list(nxt_list, neg);
+    }
+    update_active_set_batch(0, nxt_list);
+    const double prime_step = primal_step_length_batch(nxt_list);
+    const double dual_step = dual_step_length(nxt_drop);
+    const double step = prime_step > dual_step ? dual_step : prime_step;
+    if (step == std::numeric_limits<double>::max()) return is_converged = 0;
+    if (prime_step == std::numeric_limits<double>::max() && step == dual_step) {
+      to_add = 0;
+      edit_kkt(to_add, nxt_drop);
+      typ = UPDATE;
+      update_active_set(to_add, nxt_drop);
+    } else {
+      update_primal(step);
+      update_dual(step);
+      dual_vars[nxt_active] += step;
+      if (step == prime_step) {
+        to_add = 1;
+        edit_kkt(to_add, nxt_active);
+        update_active_set(to_add, nxt_active);
+      } else if (step == dual_step) {
+        to_add = 0;
+        edit_kkt(to_add, nxt_drop);
+        typ = UPDATE;
+        update_active_set(to_add, nxt_drop);
+      }
+    }
+    num_iter++;
+  }
+}
+
+int Nasoq::edit_kkt_batch(int add_del, std::vector<idx_val> nxt_list) {
+  std::vector<int> rows;
+  for (size_t i = 0; i + 1 < nxt_list.size(); ++i) rows.push_back(nxt_list[i].idx);
+  ss->add_del_matrix_qp(add_del, rows);
+  return 1;
+}
+
+double Nasoq::primal_step_length_batch(const std::vector<idx_val> &nxt_list) {
+  double step = std::numeric_limits<double>::max();
+  for (const idx_val &p : nxt_list) {
+    double bdotx = 0, ddotb = 0;
+    for (int i = BT->p[p.idx]; i < BT->p[p.idx + 1]; ++i) {
+      bdotx += BT->x[i] * primal_vars[BT->i[i]];
+      ddotb += BT->x[i] * descent[BT->i[i]];
+    }
+    if (ddotb < zero_thresh) return std::numeric_limits<double>::max();
+    step = std::min(step, -(b[p.idx] - bdotx) / ddotb);
+  }
+  return step;
+}
+
+int Nasoq::primal_feasibility_batch(std::vector<idx_val> &pair_list) {
+  pair_list.clear();
+  double *tmp = workspace;
+  spmv_small(B->nrow, B->ncol, B->p, B->i, B->x, primal_vars, tmp);
+  for (size_t i = 0; i < B->nrow; ++i) {
+    tmp[i] -= b[i];
+    if (tmp[i] > zero_thresh) pair_list.emplace_back((int)i, tmp[i]);
+  }
+  std::sort(pair_list.begin(), pair_list.end(), CMP);
+  return (int)pair_list.size();
+}
+
+int Nasoq::dual_feasibility_inner(int &most_neg) {
+  int neg = 0;
+  most_neg = -1;
+  double mn = std::numeric_limits<double>::max();
+  for (size_t i = 0; i < B->nrow; ++i)
+    if (lagrange_mult[i] < 0) {
+      neg++;
+      if (lagrange_mult[i] < mn) {
+        mn = lagrange_mult[i];
+        most_neg = (int)i;
+      }
+    }
+  return neg;
+}
+
+int Nasoq::update_active_set_batch(int add_drop, const std::vector<idx_val> nxt_lst) {
+  // adds every listed row but the last; the reference leaves removal
+  // unimplemented (returns 0)
+  if (!add_drop) return 0;
+  for (size_t i = 0; i + 1 < nxt_lst.size(); ++i) {
+    n_active++;
+    active_set.push_back(nxt_lst[i].idx);
+    used_const[nxt_lst[i].idx] = 1;
+  }
+  return 1;
 }
 
 }  // namespace nasoq
@@ -631,6 +1149,7 @@ extern "C" void nqg_qp_default_settings(nqg_qp_settings *s) {
   s->max_iter = 0;
   s->max_iter_nas = 4000;
   s->precision = NQG_FP64;
+  s->scaling = 0;
 }
 
 extern "C" int nqg_qp_solve(int n, const int *Hp, const int *Hi, const double *Hx, const double *q, int meq,
@@ -681,6 +1200,7 @@ extern "C" int nqg_qp_solve(int n, const int *Hp, const int *Hi, const double *H
   qm->max_iter_nas = st.max_iter_nas;
   qm->variant = (nasoq::nasoq_mode)st.variant;
   qm->gpu_precision = st.precision == NQG_FP32 ? 1 : 0;
+  qm->scaling = st.scaling;
   int status;
   const bool warm = x0 && z0 && as0 && n_as >= 0;
   if (!warm) {
@@ -690,15 +1210,25 @@ extern "C" int nqg_qp_solve(int n, const int *Hp, const int *Hi, const double *H
     qm->warm_start = 1;
     qm->qi->tot_st = qm->qi->tic();
     qm->auto_reg_en = qm->variant == nasoq::AUTO ? 2 : (qm->variant == nasoq::Fixed ? 1 : 0);
+    if (qm->scaling > 0) qm->scale_data();
     if (qm->symbolic_QP() < 0) {
       delete qm;
       return NQG_ERR_SYMBOLIC;
     }
     std::vector<double> xw(x0, x0 + n), zw(z0, z0 + mineq), yw(meq, 0.0);
     if (y0) yw.assign(y0, y0 + meq);
+    if (qm->scaling > 0) {  // the starting point in the scaled variables
+      for (int i = 0; i < n; ++i) xw[i] *= qm->Dinv[i];
+      for (int k = 0; k < mineq; ++k) zw[k] *= qm->Finv[k] * qm->c;
+      for (int r = 0; r < meq; ++r) yw[r] *= qm->Einv[r] * qm->c;
+    }
     std::vector<int> asw(as0, as0 + n_as);
     qm->set_warm_start(xw.data(), zw.data(), asw, meq > 0 ? yw.data() : nullptr);
     int conv = qm->numeric_QP();
+    if (qm->scaling > 0) {
+      qm->unscale_data();
+      qm->unscale_solution();
+    }
     qm->qi->tot_end = qm->qi->toc();
     qm->qi->tot = qm->qi->elapsed_time(qm->qi->tot_st, qm->qi->tot_end);
     qm->compute_objective();

@@ -198,6 +198,7 @@ int dev_factor(Plan &P, const std::vector<int> *subset);
 // wide.cu
 struct WideCtl;
 size_t wide_ctl_bytes();
+size_t wide_ctl_limit_offset();  // byte offset of the wait limit in the control block
 template <class T> int factor_wide(Plan &P, int s, T *L, T *Dg, int nb, T *Wb, WideCtl *ctl, int num_sms);
 // Schur update of target s by descendant pair q on the persistent tcgen05
 // kernel (FP32 plans).
@@ -210,6 +211,7 @@ int dev_ldlt_solve_ord(Plan &P, double *d_x);
 int dev_spmv_ord(Plan &P, const double *d_x_ord, double *d_y_ord);
 int dev_spmv_orig(Plan &P, const double *d_x, double *d_y);
 int dev_solve(Plan &P, const double *d_rhs, double *d_x);
+int dev_refine_only(Plan &P, const double *d_rhs, double *d_x);
 int dev_assemble_upload(Plan &P);
 
 #define NQG_CUDA(call)                                                                   \

@@ -578,4 +578,26 @@ int dev_solve(Plan &P, const double *d_rhs, double *d_x) {
   return NQG_OK;
 }
 
+// Refinement alone from x0 = rhs (reference iterative_ref_only,
+// src/QP/linear_solver_wrapper.cpp:1406-1430): no initial triangular solve.
+int dev_refine_only(Plan &P, const double *d_rhs, double *d_x) {
+  const int n = P.n;
+  int rc;
+  k_gather<<<grid_for(n), 256, 0, P.stream>>>(n, P.d_perm, d_rhs, P.d_bo);
+  P.nlaunch++;
+  NQG_CUDA(cudaGetLastError());
+  NQG_CUDA(cudaMemcpyAsync(P.d_xo, P.d_bo, n * sizeof(double), cudaMemcpyDeviceToDevice, P.stream));
+  int used = 0;
+  double rho = 0;
+  const bool flex = P.set.precision == NQG_FP32 && P.set.solve_precision == NQG_FP32;
+  if ((rc = flex ? fgmres_refine(P, P.d_xo, P.d_bo, used, rho) : gmres_refine(P, P.d_xo, P.d_bo, used, rho)))
+    return rc;
+  P.tm.num_ref_iter = used;
+  P.tm.last_residual = rho;
+  k_scatter<<<grid_for(n), 256, 0, P.stream>>>(n, P.d_perm, P.d_xo, d_x);
+  P.nlaunch++;
+  NQG_CUDA(cudaGetLastError());
+  return NQG_OK;
+}
+
 }  // namespace nqg

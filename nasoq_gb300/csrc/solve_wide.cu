@@ -187,6 +187,7 @@ __device__ int wait_up(const unsigned *fl, unsigned epoch, int j, int lim, int f
                        const unsigned long long *xws = nullptr, int w = 0) {
   const int lane = threadIdx.x & 31;
   long long it = 0;
+  const long long lim_ = wait_limit(ctl);
   volatile int *vab = &ctl->abort;
   while (true) {
     const int k = front + lane;
@@ -200,7 +201,7 @@ __device__ int wait_up(const unsigned *fl, unsigned epoch, int j, int lim, int f
     if (lead == 32 && front < lim) continue;  // more ready flags to scan
     if (front > j) break;
     if (*vab) return -1;
-    if (++it > SPIN_LIMIT) {
+    if (++it > lim_) {
       if (lane == 0) {
         atomicOr(status, ST_TIMEOUT);
         atomicExch(&ctl->abort, 1);
@@ -219,6 +220,7 @@ __device__ int wait_down(const unsigned *fl, unsigned epoch, int i, int lo, int 
                          const unsigned long long *xws = nullptr, int w = 0) {
   const int lane = threadIdx.x & 31;
   long long it = 0;
+  const long long lim_ = wait_limit(ctl);
   volatile int *vab = &ctl->abort;
   while (true) {
     const int k = front - 1 - lane;
@@ -232,7 +234,7 @@ __device__ int wait_down(const unsigned *fl, unsigned epoch, int i, int lo, int 
     if (lead == 32 && front > lo) continue;
     if (front <= i) break;
     if (*vab) return -1;
-    if (++it > SPIN_LIMIT) {
+    if (++it > lim_) {
       if (lane == 0) {
         atomicOr(status, ST_TIMEOUT);
         atomicExch(&ctl->abort, 1);
@@ -259,6 +261,7 @@ template <int N>
 __device__ __forceinline__ bool wait_words(const unsigned long long *wp, int n, unsigned epoch, float (&xv)[N],
                                            WideCtl *ctl, int *status) {
   long long it = 0;
+  const long long lim_ = wait_limit(ctl);
   while (true) {
     bool ok = true;
 #pragma unroll
@@ -272,7 +275,7 @@ __device__ __forceinline__ bool wait_words(const unsigned long long *wp, int n, 
     }
     if (__all_sync(0xffffffffu, ok)) return true;
     if (*(volatile int *)&ctl->abort) return false;
-    if (++it > SPIN_LIMIT) {
+    if (++it > lim_) {
       if ((threadIdx.x & 31) == 0) {
         atomicOr(status, ST_TIMEOUT);
         atomicExch(&ctl->abort, 1);
@@ -301,6 +304,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
   __shared__ int s_front;
   const int t = threadIdx.x, r = t & (TB - 1), cg = t / TB;
   int cur_s = -1, front = 0;
+  bool failed = false;  // FP32 words: this thread saw a wait give up
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int s = items[it].x, q = items[it].y;
     if (visible && !visible[s]) continue;
@@ -355,7 +359,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
           if (front < 0) return;
         }
         float xv[CPT];
-        if (!wait_words(xw + c0 + cb, min(CPT, w - cb), epoch, xv, ctl, status)) return;
+        if (!wait_words(xw + c0 + cb, min(CPT, w - cb), epoch, xv, ctl, status)) failed = true;
 #pragma unroll
         for (int cc = 0; cc < CPT; ++cc) acc += V(v[cc]) * xv[cc];
       } else {
@@ -399,7 +403,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
           // polled directly by every warp
           const int cb = (q - 1) * TB + cg * CPT;
           float xv[CPT];
-          if (!wait_words(xw + c0 + cb, CPT, epoch, xv, ctl, status)) return;
+          if (!wait_words(xw + c0 + cb, CPT, epoch, xv, ctl, status)) failed = true;
           a = V(0);
 #pragma unroll
           for (int cc = 0; cc < CPT; ++cc) a += mlink[cc] * xv[cc];
@@ -422,7 +426,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_fwd_blk(const int2 *items, int n
       const int *rows = ls + lpi[s];
       if (t < m) atomicAdd(&x[rows[r0 + t]], -yb[t]);
     }
-    __syncthreads();
+    if (__syncthreads_or(failed)) return;  // a wait gave up (all warps leave together)
   }
 }
 
@@ -442,6 +446,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
   __shared__ int s_front;
   const int t = threadIdx.x, r = t & (TB - 1), cg = t / TB, lane = t & 31;
   int cur_s = -1, front = 0;
+  bool failed = false;  // FP32 words: this thread saw a wait give up
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int s = items[it].x, q = items[it].y;
     if (visible && !visible[s]) continue;
@@ -523,7 +528,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
           if (front < 0) return;
         }
         float xw1[1];
-        if (!wait_words(xw + c0 + row, row < w ? 1 : 0, epoch, xw1, ctl, status)) return;
+        if (!wait_words(xw + c0 + row, row < w ? 1 : 0, epoch, xw1, ctl, status)) failed = true;
         xv = xw1[0];
       } else {
         if (i < front) {
@@ -590,7 +595,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
         // polled directly by every warp
         const int cb1 = (j + 1) * TB + cg * CPT;
         float xv[CPT];
-        if (!wait_words(xw + c0 + cb1, min(CPT, w - cb1), epoch, xv, ctl, status)) return;
+        if (!wait_words(xw + c0 + cb1, min(CPT, w - cb1), epoch, xv, ctl, status)) failed = true;
         a = V(0);
 #pragma unroll
         for (int cc = 0; cc < CPT; ++cc) a += mlink[cc] * xv[cc];
@@ -609,7 +614,7 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_blk(const int2 *items, int n
       __syncthreads();
       if (t == 0) publish(fl + j, epoch);
     }
-    __syncthreads();
+    if (__syncthreads_or(failed)) return;  // a wait gave up (all warps leave together)
   }
 }
 

@@ -135,6 +135,7 @@ __device__ bool grid_exchange(WideCtl *ctl, unsigned &epoch, unsigned long long 
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
     long long it = 0;
+    const long long lim_ = wait_limit(ctl);
     int ok = 1;
     unsigned long long m = 0;
     while (true) {
@@ -152,7 +153,7 @@ __device__ bool grid_exchange(WideCtl *ctl, unsigned &epoch, unsigned long long 
         ok = 0;
         break;
       }
-      if (++it > SPIN_LIMIT) {
+      if (++it > lim_) {
         if (lane == 0) {
           atomicOr(status, ST_TIMEOUT);
           atomicExch(&ctl->abort, 1);
@@ -260,6 +261,7 @@ __device__ bool grid_max_nofence(WideCtl *ctl, unsigned &epoch, unsigned long lo
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
     long long it = 0;
+    const long long lim_ = wait_limit(ctl);
     int ok = 1;
     unsigned long long m = 0;
     while (true) {
@@ -277,7 +279,7 @@ __device__ bool grid_max_nofence(WideCtl *ctl, unsigned &epoch, unsigned long lo
         ok = 0;
         break;
       }
-      if (++it > SPIN_LIMIT) {
+      if (++it > lim_) {
         if (lane == 0) {
           atomicOr(status, ST_TIMEOUT);
           atomicExch(&ctl->abort, 1);
@@ -313,6 +315,7 @@ __device__ bool grid_max_multi(WideCtl *ctl, unsigned &epoch, const unsigned lon
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
     long long it = 0;
+    const long long lim_ = wait_limit(ctl);
     int ok = 1;
     unsigned long long m[FP_COLS];
     while (true) {
@@ -334,7 +337,7 @@ __device__ bool grid_max_multi(WideCtl *ctl, unsigned &epoch, const unsigned lon
         ok = 0;
         break;
       }
-      if (++it > SPIN_LIMIT) {
+      if (++it > lim_) {
         if (lane == 0) {
           atomicOr(status, ST_TIMEOUT);
           atomicExch(&ctl->abort, 1);
@@ -716,6 +719,7 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
     const int G = (int)gridDim.x;
     const int q = tid % WP_NB, p = tid / WP_NB;
     long long it = 0;
+    const long long lim_ = wait_limit(ctl);
     bool fail = false;
     // first every CTA's word of column 0, then every word (each re-checked)
     for (int phase = 0; phase < 2 && !fail; ++phase) {
@@ -748,7 +752,7 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
           fail = true;
           break;
         }
-        if (++it > SPIN_LIMIT) {
+        if (++it > lim_) {
           if (tid == 0) {
             atomicOr(status, ST_TIMEOUT);
             atomicExch(&ctl->abort, 1);
@@ -1671,7 +1675,7 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   if (nb > WP_NB || nb < 1) return NQG_ERR_ARG;
   k_wide_init_perm<T><<<(w + 255) / 256, 256, 0, st>>>(perm, w);
   if (P) P->nlaunch++;
-  if (cudaMemsetAsync(ctl, 0, sizeof(WideCtl), st) != cudaSuccess) return NQG_ERR_CUDA;
+  if (cudaMemsetAsync(ctl, 0, offsetof(WideCtl, spin_limit), st) != cudaSuccess) return NQG_ERR_CUDA;
   const size_t smem = (size_t)(WP_NB + 2) * WP_THREADS * sizeof(T);
   // per call: the attribute belongs to the current device
   if (cudaFuncSetAttribute(k_wide_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
@@ -2144,6 +2148,7 @@ int update_pair_persistent(Plan &P, int s, int q, float *L, const float *Dg) {
 }
 
 size_t wide_ctl_bytes() { return sizeof(WideCtl); }
+size_t wide_ctl_limit_offset() { return offsetof(WideCtl, spin_limit); }
 
 // Same panel / trailing-update sequence as factor_wide, on caller-provided
 // buffers (values S, D, E, perm) and caller-provided scratch (Wb, ctl,

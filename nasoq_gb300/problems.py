@@ -195,6 +195,98 @@ def qp_random_convex(seed: int = 0, grid: int = 45, meq: int = 200, mineq: int =
     return QP(H, q, A, b, C, d, {"kind": "random_convex", "seed": seed})
 
 
+def _scale_csc(M: CSC, row: np.ndarray | None, col: np.ndarray | None) -> CSC:
+    x = np.array(M.x, np.float64)
+    cols = np.repeat(np.arange(M.ncol), np.diff(M.p))
+    if row is not None:
+        x *= row[M.i]
+    if col is not None:
+        x *= col[cols]
+    return CSC(M.nrow, M.ncol, M.p, M.i, x)
+
+
+def qp_ill_scaled(seed: int = 0, grid: int = 12, meq: int = 20, mineq: int = 120, spread: float = 3.0) -> QP:
+    """qp_random_convex with its variables and rows rescaled by factors
+    10^U(-spread, spread): x = S x', H' = S H S, q' = S q, A' = E A S,
+    C' = F C S, b' = E b, d' = F d.  The same optimum (through S) with data
+    spanning about 10^(4 spread) in magnitude: the case Ruiz equilibration is
+    for."""
+    base = qp_random_convex(seed, grid=grid, meq=meq, mineq=mineq)
+    rng = np.random.default_rng(seed + 1000)
+    n = base.H.ncol
+    sv = 10.0 ** rng.uniform(-spread, spread, n)
+    se = 10.0 ** rng.uniform(-spread, spread, base.A.nrow)
+    sf = 10.0 ** rng.uniform(-spread, spread, base.C.nrow)
+    H = _scale_csc(base.H, sv, sv)
+    A = _scale_csc(base.A, se, sv)
+    C = _scale_csc(base.C, sf, sv)
+    return QP(H, base.q * sv, A, base.b * se, C, base.d * sf,
+              {"kind": "ill_scaled", "seed": seed, "spread": spread})
+
+
+def bilaplacian_bounded(seed: int = 0, grid: int = 400, pins: int = 2000, jitter: float = 0.2) -> QP:
+    """Large bounded QP of biharmonic-weights type on a grid x grid mesh.
+
+    Vertices sit at (i h, j h) moved by U(-jitter, jitter) h in each
+    coordinate.  L is the 5-point Laplacian of the moved vertices with
+    dimensionless weights h^2 / |p_a - p_b|^2 between grid neighbours (row
+    sums on the diagonal, about 4 on the unjittered grid), M the lumped
+    vertex areas (products of the half spacings), and H = L M^-1 L, a
+    13-point bilaplacian (lower-stored).  q = 0.  `pins` random vertices
+    are fixed to values in {0, 1} (equality rows), and 0 <= x <= 1 on every
+    vertex becomes two inequality rows per vertex, x_i <= 1 then -x_i <= 0
+    (the bounds-to-rows rule of the SMP converter): n = grid^2 variables,
+    `pins` equalities, 2 n inequalities."""
+    rng = np.random.default_rng(seed)
+    g = grid
+    n = g * g
+    h = 1.0 / (g - 1)
+    jx = rng.uniform(-jitter, jitter, (g, g)) * h
+    jy = rng.uniform(-jitter, jitter, (g, g)) * h
+    X = np.arange(g)[:, None] * h + jx  # X[i, j]: vertex (i, j), index i * g + j
+    Y = np.arange(g)[None, :] * h + jy
+    idx = np.arange(n).reshape(g, g)
+    rows, cols, w = [], [], []
+    for di, dj in ((1, 0), (0, 1)):
+        a = idx[:g - di, :g - dj].ravel()
+        b = idx[di:, dj:].ravel()
+        dx = X.ravel()[b] - X.ravel()[a]
+        dy = Y.ravel()[b] - Y.ravel()[a]
+        rows.append(a)
+        cols.append(b)
+        w.append(h * h / (dx * dx + dy * dy))
+    a = np.concatenate(rows)
+    b = np.concatenate(cols)
+    w = np.concatenate(w)
+    diag = np.zeros(n)
+    np.add.at(diag, a, w)
+    np.add.at(diag, b, w)
+    import scipy.sparse as sp
+    Lm = sp.coo_matrix((np.concatenate([-w, -w, diag]), (np.concatenate([a, b, np.arange(n)]),
+                                                          np.concatenate([b, a, np.arange(n)]))), shape=(n, n)).tocsr()
+    # lumped areas: half the spacing to each neighbour in both directions
+    Xr = X.ravel()
+    Yr = Y.ravel()
+    ii, jj = np.divmod(np.arange(n), g)
+    up = np.where(ii < g - 1, Xr[np.minimum(idx.ravel() + g, n - 1)] - Xr, 0.0)
+    dn = np.where(ii > 0, Xr - Xr[np.maximum(idx.ravel() - g, 0)], 0.0)
+    rt = np.where(jj < g - 1, Yr[np.minimum(idx.ravel() + 1, n - 1)] - Yr, 0.0)
+    lf = np.where(jj > 0, Yr - Yr[np.maximum(idx.ravel() - 1, 0)], 0.0)
+    area = 0.25 * (up + dn) * (rt + lf)
+    Hm = (Lm @ sp.diags(1.0 / area) @ Lm).tocsc()
+    Hl = sp.tril(Hm).tocsc()
+    Hl.sort_indices()
+    H = CSC(n, n, Hl.indptr.astype(np.int32), Hl.indices.astype(np.int32), Hl.data.astype(np.float64))
+    pin = np.sort(rng.choice(n, size=pins, replace=False))
+    vals = rng.integers(0, 2, size=pins).astype(np.float64)
+    A = csc_from_coo(pins, n, np.arange(pins), pin, np.ones(pins))
+    r = np.arange(2 * n)
+    C = csc_from_coo(2 * n, n, r, r // 2, np.where(r % 2 == 0, 1.0, -1.0))
+    d = np.where(r % 2 == 0, 1.0, 0.0)
+    return QP(H, np.zeros(n), A, vals, C, d, {"kind": "bilaplacian_bounded", "seed": seed, "grid": grid,
+                                              "pins": pins, "jitter": jitter})
+
+
 def _matvec(M: CSC, x: np.ndarray) -> np.ndarray:
     y = np.zeros(M.nrow)
     cols = np.repeat(np.arange(M.ncol), np.diff(M.p))

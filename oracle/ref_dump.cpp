@@ -121,14 +121,20 @@ static int run_qp(const nqa::File &in, nqa::File &out) {
   qm->max_iter_nas = (int)in.scalar("max_iter_nas", 200000);
   int variant = (int)in.scalar("variant", 0);
   qm->variant = (nasoq_mode)variant;
+  qm->scaling = (int)in.scalar("scaling", 0);
   // Nasoq::solve() for Fixed/AUTO/PREDET, unrolled so the symbolic state can
   // be dumped between symbolic_QP and initialize_x.
   qm->warm_start = 0;
   qm->auto_reg_en = variant == AUTO ? 2 : (variant == Fixed ? 1 : 0);
+  if (qm->scaling > 0) qm->scale_data();
   qm->symbolic_QP();
   dump_symbolic(out, "sym_", qm->ss, qm->ss->SM->ncol);
   qm->initialize_x();
   int status = qm->numeric_QP();
+  if (qm->scaling > 0) {
+    qm->unscale_data();
+    qm->unscale_solution();
+  }
   qm->compute_objective();
   int ret = qm->check_solve_status(status);
   qm->detect_solver_name();

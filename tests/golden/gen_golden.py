@@ -31,6 +31,7 @@ import nqa  # noqa: E402
 from nasoq_gb300 import problems as P  # noqa: E402
 
 REF_DUMP = os.path.join(ROOT, "oracle", "_ref", "ref_dump")
+ONLY = None  # --only PREFIX: regenerate just the cases whose name starts with it
 
 
 def run(cmd, inp, extra_env=None):
@@ -47,6 +48,10 @@ def run(cmd, inp, extra_env=None):
         return nqa.load(out)
 
 
+def wanted(name):
+    return ONLY is None or name.startswith(ONLY)
+
+
 def save_case(name, inp, out):
     arrs = {"in_" + k: np.asarray(v) for k, v in inp.items()}
     arrs.update({"out_" + k: np.asarray(v) for k, v in out.items()})
@@ -55,6 +60,8 @@ def save_case(name, inp, out):
 
 
 def lbl_case(name, K, rhs, **settings):
+    if not wanted(name):
+        return
     inp = {"Ap": K.p, "Ai": K.i, "Ax": K.x, "rhs": rhs}
     for k, v in settings.items():
         inp[k] = np.array([float(v)])
@@ -75,6 +82,8 @@ def qp_inputs(qp: P.QP, **settings):
 
 
 def qp_case(name, qp, **settings):
+    if not wanted(name):
+        return
     inp = qp_inputs(qp, **settings)
     out = run("qp", inp)
     save_case(name, inp, out)
@@ -142,12 +151,13 @@ def main(ref):
         # data/out_correct.csv rows: NASOQ-Fixed and NASOQ (PREDET) at eps 1e-3
         qp_case(f"qp_{pname}_fixed", qp, variant=0, eps_abs=1e-3, max_iter=2, diag_perturb=1e-9)
         qp_case(f"qp_{pname}_predet", qp, variant=3, eps_abs=1e-3, max_iter=2, diag_perturb=1e-9)
-    qp, x, y, z = json_qp(os.path.join(ref, "tests", "1.json"))
-    inp = qp_inputs(qp, variant=3, eps_abs=1e-3, max_iter=0, diag_perturb=1e-9, stop_tol=1e-15,
-                    max_iter_nas=4000)
-    out = run("qp", inp)
-    out.update({"json_x": x, "json_y": y, "json_z": z})
-    save_case("qp_test1json", inp, out)
+    if wanted("qp_test1json"):
+        qp, x, y, z = json_qp(os.path.join(ref, "tests", "1.json"))
+        inp = qp_inputs(qp, variant=3, eps_abs=1e-3, max_iter=0, diag_perturb=1e-9, stop_tol=1e-15,
+                        max_iter_nas=4000)
+        out = run("qp", inp)
+        out.update({"json_x": x, "json_y": y, "json_z": z})
+        save_case("qp_test1json", inp, out)
     qp = P.qp_random_convex(seed=0)
     qp_case("qp_random_c1_predet", qp, variant=3, eps_abs=1e-8, max_iter=2, diag_perturb=1e-9)
     qp_case("qp_random_c1_fixed", qp, variant=0, eps_abs=1e-8, max_iter=2, diag_perturb=1e-9)
@@ -157,6 +167,18 @@ def main(ref):
         qp = P.qp_mpc(seed=11 + N, horizon=N)
         qp_case(f"qp_mpc_N{N}", qp, variant=3, eps_abs=1e-8, max_iter=2, diag_perturb=1e-9)
 
+    # Ruiz equilibration (Nasoq::scaling > 0, src/nasoq.cpp:1352-1483)
+    qp = P.qp_ill_scaled(seed=21)
+    qp_case("qp_scaled_ill_ruiz", qp, variant=3, eps_abs=1e-8, max_iter=2, diag_perturb=1e-9, scaling=10)
+    qp_case("qp_scaled_ill_none", qp, variant=3, eps_abs=1e-8, max_iter=2, diag_perturb=1e-9)
+    qp = P.qp_random_convex(seed=7, grid=12, meq=20, mineq=120)
+    qp_case("qp_scaled_random_ruiz", qp, variant=0, eps_abs=1e-8, max_iter=2, diag_perturb=1e-9, scaling=5)
+
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NASOQ_REFERENCE", "/root/reference"))
+    args = sys.argv[1:]
+    if "--only" in args:
+        k = args.index("--only")
+        ONLY = args[k + 1]
+        del args[k:k + 2]
+    main(args[0] if args else os.environ.get("NASOQ_REFERENCE", "/root/reference"))

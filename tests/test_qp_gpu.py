@@ -3,7 +3,8 @@ against the reference on its own known-answer problems (tests/1.json and
 data/*.yml with data/out_correct.csv) and on seeded QPs.
 
 The active-set loop is replayed with the same decisions, so status, the
-number of iterations and the final active set must be identical; primal and
+number of iterations and the final active set must be identical (with Ruiz
+equilibration too, on the qp_scaled_* fixtures); primal and
 dual solutions agree to 1e-7 relative (the refinement-free PREDET settings of
 tests/1.json reach 1e-12), the objective to 1e-9 relative, and the KKT norms
 must meet eps_abs."""
@@ -35,7 +36,8 @@ def run(d, precision=nq.NQG_FP64):
                         diag_perturb=float(d["in_diag_perturb"][0]),
                         max_iter=int(d["in_max_iter"][0]),
                         stop_tol=float(d.get("in_stop_tol", [1e-15])[0]),
-                        max_iter_nas=int(d.get("in_max_iter_nas", [200000])[0]), precision=precision)
+                        max_iter_nas=int(d.get("in_max_iter_nas", [200000])[0]), precision=precision,
+                        scaling=int(d.get("in_scaling", [0])[0]))
     return nq.qp_solve(*load_qp(d), settings=st)
 
 
@@ -94,6 +96,8 @@ def test_qp_fp32_factor_matches_reference(path, record_property):
     reference's; the rounding of the FP32 factor may change a decision at a
     near-tie, so it is reported rather than required equal."""
     d = nqa.load(path)
+    if int(d["out_status"][0]) != 1:
+        pytest.skip("FP32 parity is pinned on the problems the reference solves to Optimal")
     x, y, z, act, res = run(d, precision=nq.NQG_FP32)
     ref_it = int(d["out_num_iter"][0])
     record_property("iterations_fp32", res.num_iter)
