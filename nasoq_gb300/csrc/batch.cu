@@ -384,7 +384,7 @@ __device__ bool bk_factor_warp(T *a, int lda, int w, T *D, T *E, int *perm, int 
       }
     }
     const int kk = k + kstep - 1;
-    if (zero && lane == 0) atomicOr(status, ST_ZERO_PIVOT);
+    if (zero && lane == 0) atomicOr(status, absakk == absakk ? ST_ZERO_PIVOT : ST_NONFINITE);
     if (kp != kk) {  // symmetric interchange of kk and kp (kp > kk)
       pivoted = true;
       for (int i = kp + 1 + lane; i < w; i += 32) {

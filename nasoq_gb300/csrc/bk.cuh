@@ -136,7 +136,8 @@ __device__ void bk_factor(T *a, int lda, int w, T *D, T *E, int *perm, int *stat
     kstep = s_kstep;
     zero = s_zero;
     const int kk = k + kstep - 1;
-    if (zero && tid == 0) flag_status(status, ST_ZERO_PIVOT);
+    // a NaN pivot is reported by the non-finite check, not as a zero pivot
+    if (zero && tid == 0 && absakk == absakk) flag_status(status, ST_ZERO_PIVOT);
     // ---- symmetric interchange of kk and kp (kp > kk)
     if (kp != kk) {
       pivoted = true;

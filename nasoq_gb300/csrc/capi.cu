@@ -708,8 +708,10 @@ static int finish_factor(Plan &P) {
   }
   if (st & ST_TIMEOUT) return NQG_ERR_TIMEOUT;
   P.factored = true;
-  if (st & ST_NONFINITE) return NQG_WARN_NONFINITE;
+  // a singular pivot block comes first: the non-finite values that follow
+  // from it (divisions by its zero D entry) are its consequence
   if (st & ST_ZERO_PIVOT) return NQG_WARN_ZERO_PIVOT;
+  if (st & ST_NONFINITE) return NQG_WARN_NONFINITE;
   return NQG_OK;
 }
 

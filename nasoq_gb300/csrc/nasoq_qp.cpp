@@ -292,11 +292,12 @@ int Nasoq::symbolic_QP() {
     outer_iter_ref = inner_iter_ref = max_iter;
   }
   // An FP32 factorization is only the preconditioner of the FP64 refinement:
-  // without refinement its solutions carry FP32 rounding into every
-  // active-set decision, so at least two restarts of two steps run.
+  // without enough refinement its solutions carry FP32 rounding into every
+  // active-set decision (on degenerate problems enough to make the loop
+  // cycle), so at least three restarts of eight steps run.
   if (gpu_precision) {
-    outer_iter_ref = std::max(outer_iter_ref, 2);
-    inner_iter_ref = std::max(inner_iter_ref, 2);
+    outer_iter_ref = std::max(outer_iter_ref, 3);
+    inner_iter_ref = std::max(inner_iter_ref, 8);
   }
   ss->tol_abs = ss->tol_rel = stop_tol;
   ss->req_ref_iter = outer_iter_ref;

@@ -1021,7 +1021,7 @@ __global__ void __launch_bounds__(WP_THREADS) k_wide_panel(T *S, int nrow, int w
         if (r == gt) lc[j * WP_THREADS + tid] = l;
       }
       if (gt == 0) {
-        if (zero) atomicOr(status, ST_ZERO_PIVOT);
+        if (zero && absakk == absakk) atomicOr(status, ST_ZERO_PIVOT);
         S[c + (size_t)c * nrow] = T(1);
         Dd[c] = d;
         De[c] = T(0);

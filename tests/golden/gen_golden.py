@@ -174,6 +174,13 @@ def main(ref):
     qp = P.qp_random_convex(seed=7, grid=12, meq=20, mineq=120)
     qp_case("qp_scaled_random_ruiz", qp, variant=0, eps_abs=1e-8, max_iter=2, diag_perturb=1e-9, scaling=5)
 
+    # the large bounded bilaplacian QP family at a size the reference solves in a second
+    qp = P.bilaplacian_bounded(seed=0, grid=40, pins=20)
+    qp_case("qp_bilap_g40", qp, variant=0, eps_abs=1e-8, max_iter=2, diag_perturb=1e-9)
+    # supernodes wider than the 192-column multi-CTA threshold
+    qp = P.bilaplacian_bounded(seed=1, grid=80, pins=80)
+    qp_case("qp_bilap_g80", qp, variant=0, eps_abs=1e-8, max_iter=2, diag_perturb=1e-9)
+
 
 if __name__ == "__main__":
     args = sys.argv[1:]
