@@ -24,8 +24,10 @@ factor, the reference's refinement schedule, cold start) on the same GPU;
 `plain_fp64_single`: the per-QP FP64 GPU path (one problem at a time, host
 loop over the C ABI) on a sample; `cpu_baseline`: the oracle restatement of
 the reference's method on the host cores.  Secondary sections: `c3`, the
-uneven MPC batch (4096 problems, horizons 10..100), and `lbl_c2`, the
-symmetric-indefinite KKT solve of the 64^3 Laplacian workload.  For N > 1
+uneven MPC batch (4096 problems, horizons 10..100, launch shape from the
+autotuner), `lbl_c2`, the symmetric-indefinite KKT solve of the 64^3
+Laplacian workload, and `c5`, the 400 x 400 bounded bilaplacian QP through
+the single-QP path (time-boxed; --c5-full solves it to the end).  For N > 1
 (torchrun) every rank solves its own batches (no data exchange).
 """
 from __future__ import annotations
@@ -421,13 +423,17 @@ def _family_symbolic(nq, fam):
 
 
 def c3_section(nq, P):
+    from nasoq_gb300 import tune
     qps = P.mpc_batch(BATCH, seed=0)
     probs = [(q.H, q.q, q.A, q.b, q.C, q.d) for q in qps]
     out = {"workload": "qp_mpc_uneven_horizon10-100_b4096"}
     for name, kw in (("mixed", dict(precision=nq.NQG_FP32, refine=1, refine_tol=REFINE_TOL)),
                      ("plain_fp64", dict(precision=nq.NQG_FP64, refine=0))):
+        # launch shape from the autotuner (timed on this batch, or the cached choice)
+        tuned, trep = tune.autotune_batch(probs, cache=os.path.join(ROOT, "gpurun_out", "batch_tune.json"),
+                                          variant=0, eps_abs=EPS, **kw)
         t0 = time.perf_counter()
-        b = nq.QPBatch(probs, settings=nq.batch_settings(variant=0, eps_abs=EPS, **kw))
+        b = nq.QPBatch(probs, settings=tuned)
         fin = time.perf_counter() - t0
         b.solve()
         b.solve()
@@ -436,8 +442,53 @@ def c3_section(nq, P):
         out[name] = {"value": BATCH / (ms / 1e3), "unit": "QP solves/s", "ms": ms,
                      "optimal_fraction": float(np.mean([s.status == 1 for s in st])),
                      "iterations_total": int(sum(s.num_iter for s in st)), "patterns": b.info().npatterns,
-                     "setup_seconds": fin}
+                     "setup_seconds": fin,
+                     "launch": {"threads": tuned.threads, "stage": tuned.stage, "cached": trep["cached"],
+                                "trials": trep.get("trials")}}
         b.close()
+    return out
+
+
+def c5_section(args, nq, P):
+    """The large bounded QP: 400 x 400 jittered bilaplacian, 2000 pins, box
+    rows (n = 160,000, 2000 equalities, 320,000 inequalities), through the
+    single-QP path (host loop, every factorization / partial refactorization
+    / solve on the GPU, FP64).  The reference's method adds one bound per
+    iteration, so the full solve takes thousands of iterations: by default
+    the run is time-boxed at --c5-iters iterations and reports the rate;
+    --c5-full runs it to the end."""
+    t0 = time.perf_counter()
+    qp = P.bilaplacian_bounded(seed=0)
+    gen_s = time.perf_counter() - t0
+    out = {"workload": "bilaplacian_400x400_jitter0.2_pins2000_box", "n": qp.H.ncol, "meq": qp.A.nrow,
+           "mineq": qp.C.nrow, "generate_seconds": gen_s}
+
+    def run(cap):
+        st = nq.qp_settings(variant=0, eps_abs=EPS, precision=nq.NQG_FP64, max_iter_nas=cap)
+        t = time.perf_counter()
+        x, y, z, act, r = nq.qp_solve(qp.H, qp.q, qp.A, qp.b, qp.C, qp.d, settings=st)
+        wall = time.perf_counter() - t
+        return {"iterations": r.num_iter, "seconds": wall, "status": r.status,
+                "ms_per_iteration": 1e3 * wall / max(r.num_iter, 1), "gpu_factor_solve_seconds": r.factor_seconds,
+                "active_set": r.active_size, "lag_res": r.lag_res, "cons_sat_norm": r.cons_sat_norm}
+
+    out["gpu_time_boxed"] = run(args.c5_iters)
+    out["gpu_time_boxed"]["note"] = ("stopped by max_iter_nas (the reference reports such a stop as status 0); "
+                                     "rate = iterations / wall time including the host analysis")
+    if args.c5_full:
+        out["gpu_full"] = run(200000)
+    if args.c5_cpu_iters > 0:
+        # the reference's method restated on the host (oracle), same start, time-boxed
+        try:
+            from oracle import port
+            t = time.perf_counter()
+            r = port.qp_solve(qp, variant=0, eps_abs=EPS, max_iter_nas=args.c5_cpu_iters)
+            wall = time.perf_counter() - t
+            out["cpu_time_boxed"] = {"iterations": int(r["num_iter"]), "seconds": wall,
+                                     "ms_per_iteration": 1e3 * wall / max(int(r["num_iter"]), 1),
+                                     "kind": "port", "cores": os.cpu_count()}
+        except Exception as e:
+            out["cpu_time_boxed"] = {"unavailable": str(e)[:200]}
     return out
 
 
@@ -504,6 +555,11 @@ def main():
     ap.add_argument("--batch", type=int, default=BATCH, help="QPs per step (smaller cases for profiler captures)")
     ap.add_argument("--profile-once", action="store_true",
                     help="train, then exactly one measured step and nothing else (profiler launch lists)")
+    ap.add_argument("--no-c5", action="store_true")
+    ap.add_argument("--c5-iters", type=int, default=150, help="active-set iterations of the time-boxed C5 run")
+    ap.add_argument("--c5-full", action="store_true", help="also solve C5 to the end")
+    ap.add_argument("--c5-cpu-iters", type=int, default=0, help="time-boxed oracle iterations on C5 (0: skip)")
+    ap.add_argument("--c5-only", action="store_true", help="run the C5 section alone")
     ap.add_argument("--save-model", default=None, help="write the trained model's weights (.npz)")
     ap.add_argument("--load-model", default=None, help="use saved weights instead of training")
     args = ap.parse_args()
@@ -523,11 +579,16 @@ def main():
         dist.init_process_group("nccl")
     pk, pk_src = peaks()
     set_batch(args.batch)
+    if args.c5_only:
+        if rank == 0:
+            print(json.dumps({"c5": c5_section(args, nq, P)}), flush=True)
+        return 0
     qp = qp_section(args, world, rank, local, torch, nq, P, learn, pk, pk_src)
     if qp is None:
         return 0
     c3 = None if args.no_c3 else c3_section(nq, P)
     lbl = None if args.no_lbl else lbl_section(args, torch, nq, P, pk)
+    c5 = None if args.no_c5 else c5_section(args, nq, P)
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -550,7 +611,7 @@ def main():
             "mixed_cold_batched": qp["mixed_cold_batched"], "plain_fp64_batched": qp["plain_fp64_batched"],
             "plain_fp64_single": qp["plain_fp64_single"], "model": qp["model"], "roofline": qp["roofline"],
             "cpu_baseline": cpu, "clocks": qp["clocks"], "gpu_launches": qp["gpu_launches"], "c3": c3,
-            "lbl_c2": lbl,
+            "lbl_c2": lbl, "c5": c5,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -225,10 +225,9 @@ int nqg_get_launch_count(const nqg_plan *plan, long long *count);
  * every GPU loading this library holds until the process exits, shared by
  * all calls, so calls whose GPU work overlaps (e.g. on two streams) race.
  * Every call looks up that array's device address (cudaGetSymbolAddress,
- * which allocates nothing), so a device reset between calls is safe; the
- * first call on each device also loads the module and should come before any
- * stream capture.  Work runs on `stream` (NULL = default stream) and the call
- * returns when it has finished. */
+ * which allocates nothing), so a device reset between calls is safe.  Work
+ * runs on `stream` (NULL = default stream); the call is synchronous: it waits
+ * for that work and reads the status word back before it returns. */
 int nqg_dense_ldlt_noalloc(int nrow, int w, double *d_A, int lda, double *d_D, int *d_perm, void *stream);
 
 /* ---- QP solve (dual active-set NASOQ over the GPU LBL) ------------------- */

@@ -294,12 +294,15 @@ int Nasoq::symbolic_QP() {
   // An FP32 factorization is only the preconditioner of the FP64 refinement:
   // without enough refinement its solutions carry FP32 rounding into every
   // active-set decision (on degenerate problems enough to make the loop
-  // cycle), so at least three restarts of eight steps run.
-  if (gpu_precision) {
-    outer_iter_ref = std::max(outer_iter_ref, 3);
-    inner_iter_ref = std::max(inner_iter_ref, 8);
-  }
+  // cycle).  Its refinement therefore runs up to 4 restarts of 10 steps and
+  // stops once the preconditioned residual is below 1e-10, absolute and
+  // relative to the first one.
   ss->tol_abs = ss->tol_rel = stop_tol;
+  if (gpu_precision) {
+    outer_iter_ref = std::max(outer_iter_ref, 4);
+    inner_iter_ref = std::max(inner_iter_ref, 10);
+    ss->tol_abs = ss->tol_rel = std::max(stop_tol, 1e-10);
+  }
   ss->req_ref_iter = outer_iter_ref;
   ss->max_inner_iter = inner_iter_ref;
   ss->reg_diag = diag_perturb;
