@@ -472,21 +472,32 @@ def c5_section(args, nq, P):
                 "ms_per_iteration": 1e3 * wall / max(r.num_iter, 1), "gpu_factor_solve_seconds": r.factor_seconds,
                 "active_set": r.active_size, "lag_res": r.lag_res, "cons_sat_norm": r.cons_sat_norm}
 
-    out["gpu_time_boxed"] = run(args.c5_iters)
-    out["gpu_time_boxed"]["note"] = ("stopped by max_iter_nas (the reference reports such a stop as status 0); "
-                                     "rate = iterations / wall time including the host analysis")
+    # setup (analysis, first factorization, one iteration) and a time-boxed
+    # run; the per-iteration time is the difference between the two
+    first = run(0)
+    boxed = run(args.c5_iters)
+    boxed["ms_per_active_set_iteration"] = 1e3 * (boxed["seconds"] - first["seconds"]) / max(
+        boxed["iterations"] - first["iterations"], 1)
+    boxed["setup_seconds"] = first["seconds"]
+    boxed["note"] = "stopped by max_iter_nas (the reference reports such a stop as status 0)"
+    out["gpu_time_boxed"] = boxed
     if args.c5_full:
         out["gpu_full"] = run(200000)
     if args.c5_cpu_iters > 0:
         # the reference's method restated on the host (oracle), same start, time-boxed
         try:
             from oracle import port
-            t = time.perf_counter()
-            r = port.qp_solve(qp, variant=0, eps_abs=EPS, max_iter_nas=args.c5_cpu_iters)
-            wall = time.perf_counter() - t
-            out["cpu_time_boxed"] = {"iterations": int(r["num_iter"]), "seconds": wall,
-                                     "ms_per_iteration": 1e3 * wall / max(int(r["num_iter"]), 1),
-                                     "kind": "port", "cores": os.cpu_count()}
+
+            def cpu(cap):
+                t = time.perf_counter()
+                r = port.qp_solve(qp, variant=0, eps_abs=EPS, max_iter_nas=cap)
+                return int(r["num_iter"]), time.perf_counter() - t
+
+            i0, t0c = cpu(0)
+            i1, t1c = cpu(args.c5_cpu_iters)
+            out["cpu_time_boxed"] = {"iterations": i1, "seconds": t1c, "setup_seconds": t0c,
+                                     "ms_per_active_set_iteration": 1e3 * (t1c - t0c) / max(i1 - i0, 1),
+                                     "kind": "port", "threads": "OpenBLAS default"}
         except Exception as e:
             out["cpu_time_boxed"] = {"unavailable": str(e)[:200]}
     return out

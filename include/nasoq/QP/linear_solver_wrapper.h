@@ -100,7 +100,7 @@ struct SolverSettings {
   double bwd_err;
 
   // ---- GPU-specific (not in the reference header)
-  int gpu_precision;          // 0: FP64 factor (default), 1: FP32 factor + FP64 refinement
+  int gpu_precision;          // 0: FP64 factor (default), 1: FP32 factor and solves + FP64 flexible GMRES
   nqg_plan *plan;             // device plan, created by symbolic_analysis()
   std::vector<std::vector<long long>> const_val_idx;  // QP mode: SM value index of every entry of each constraint
   int last_gpu_status;        // status of the last C-ABI call

@@ -37,7 +37,13 @@ namespace nqg {
 
 namespace {
 
-constexpr int BT_MAX_THREADS = 256;
+// At most 128 threads per CTA and at least 6 CTAs per SM: the compiler keeps
+// the kernel within 80 registers (no spills in FP32), so 24 warps are
+// resident per SM instead of 16 at its natural 128 registers.  The kernel is
+// bound by block barriers and dependent loads, and more resident QPs hide
+// more of that latency.
+constexpr int BT_MAX_THREADS = 128;
+constexpr int BT_MIN_BLOCKS = 6;
 constexpr int MR_CAP = BATCH_MR_CAP;  // Krylov steps per restart held in shared memory
 
 template <class T> struct Ctx {
@@ -1072,7 +1078,7 @@ template <class T> __device__ void load_state(Ctx<T> &c) {
 }  // namespace
 
 template <class T>
-__global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
+__global__ void __launch_bounds__(BT_MAX_THREADS, BT_MIN_BLOCKS) k_nasoq_batch(BArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double red[32];
   __shared__ int redi[32];

@@ -689,7 +689,7 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
   int smem_optin = 0;
   BQ_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   b->threads = b->set.threads > 0 ? b->set.threads : 128;
-  if (b->threads % 32 || b->threads > 256) return fail(b, NQG_ERR_ARG, "threads must be a multiple of 32, at most 256");
+  if (b->threads % 32 || b->threads > 128) return fail(b, NQG_ERR_ARG, "threads must be a multiple of 32, at most 128");
   nqg::BArgs base_args{};
   base_args.N_max = N_max;
   base_args.w_max = w_max;

@@ -366,6 +366,11 @@ int SolverSettings::symbolic_analysis() {
   nqg_settings st;
   nqg_default_settings(&st);
   st.precision = gpu_precision ? NQG_FP32 : NQG_FP64;
+  // FP32 factor: FP32 triangular solves inside flexible GMRES, whose residual
+  // is the true FP64 one (left-preconditioned GMRES stops on the
+  // preconditioned residual, which an FP32 factor can make small while the
+  // true residual is not)
+  st.solve_precision = gpu_precision ? NQG_FP32 : NQG_FP64;
   st.req_ref_iter = std::max(req_ref_iter, 0);
   st.max_inner_iter = std::max(max_inner_iter, 0);
   st.tol_abs = tol_abs;
