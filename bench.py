@@ -313,7 +313,10 @@ def qp_section(args, world, rank, local, torch, nq, P, learn, pk, pk_src):
         return min(times), x, z, s
 
     cold_ms, xc, zc, sc = cold_run(mixed)
-    f64_ms, x64, z64, s64 = cold_run(dict(variant=0, eps_abs=EPS, precision=nq.NQG_FP64, refine=0))
+    # the plain FP64 GPU path: FP64 factor, the reference's refinement schedule,
+    # cold start, every QP factoring its own KKT matrix
+    f64_ms, x64, z64, s64 = cold_run(dict(variant=0, eps_abs=EPS, precision=nq.NQG_FP64, refine=0,
+                                          share_factor=0))
     xr = np.abs(xw - x64).reshape(BATCH, n).max(axis=1) / np.maximum(np.abs(x64).reshape(BATCH, n).max(axis=1), 1)
 
     # plain FP64 single-QP path (host loop over the C ABI) on a sample
@@ -390,7 +393,8 @@ def qp_section(args, world, rank, local, torch, nq, P, learn, pk, pk_src):
                                "optimal_fraction": float(np.mean([s.status == 1 for s in sc]))},
         "plain_fp64_batched": {"value": BATCH / (f64_ms / 1e3), "unit": "QP solves/s",
                                "optimal_fraction": float(np.mean([s.status == 1 for s in s64])),
-                               "precision": "FP64 factor and solves, the reference's GMRES schedule, cold start"},
+                               "precision": "FP64 factor and solves, the reference's GMRES schedule, cold start, "
+                                            "one factorization per QP (share_factor=0)"},
         "plain_fp64_single": single,
         "model": {"sizes": list(model.sizes), "n_train": rep.n_train, "label_seconds": rep.label_seconds,
                   "train_seconds": rep.train_seconds, "loss_first": rep.losses[0], "loss_last": rep.losses[-1],

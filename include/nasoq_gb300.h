@@ -289,10 +289,15 @@ typedef struct nqg_batch_settings {
   int refine;           /* 0: the reference's GMRES schedule (restarts x steps from the variant);
                            1: adaptive flexible GMRES to refine_tol */
   double refine_tol;    /* refine == 1: stop once ||b - Kx||_2 <= refine_tol * ||b||_2 */
-  int threads;          /* CTA size, a multiple of 32 up to 128 (0: 128) */
+  int threads;          /* CTA size, a multiple of 32 up to 256 (0: 128) */
   int use_graph;        /* 1: the queue resets and the kernels are replayed from a captured CUDA graph */
   int stage;            /* 1: a problem's factor and row lists stay in shared memory when they fit
                            (problems grouped into shared-memory tiers, one launch per tier) */
+  int share_factor;     /* 1 (default): problems with identical matrices (same H, A, C values, e.g. a
+                           parametric family whose q / b / d change) share the factorization with every
+                           inequality hidden, computed once at finalize; each solve starts from a copy
+                           and refactors only the paths of its active rows.  0: every solve factors its
+                           own KKT matrix from scratch. */
 } nqg_batch_settings;
 
 typedef struct nqg_batch_stats {

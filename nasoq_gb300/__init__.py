@@ -73,7 +73,7 @@ class QPResult(C.Structure):
 
 class BatchSettings(C.Structure):
     _fields_ = [("qp", QPSettings), ("refine", C.c_int), ("refine_tol", C.c_double), ("threads", C.c_int),
-                ("use_graph", C.c_int), ("stage", C.c_int)]
+                ("use_graph", C.c_int), ("stage", C.c_int), ("share_factor", C.c_int)]
 
 
 class BatchStats(C.Structure):

@@ -37,13 +37,10 @@ namespace nqg {
 
 namespace {
 
-// At most 128 threads per CTA and at least 6 CTAs per SM: the compiler keeps
-// the kernel within 80 registers (no spills in FP32), so 24 warps are
-// resident per SM instead of 16 at its natural 128 registers.  The kernel is
-// bound by block barriers and dependent loads, and more resident QPs hide
-// more of that latency.
-constexpr int BT_MAX_THREADS = 128;
-constexpr int BT_MIN_BLOCKS = 6;
+// Up to 256 threads per CTA; the kernel's natural 128 registers leave 4 CTAs
+// of 128 threads per SM.  (Capping it at 80 registers for 6 CTAs per SM was
+// measured slower: 7-12 % on cold and FP64 batches, +2 % on warm ones.)
+constexpr int BT_MAX_THREADS = 256;
 constexpr int MR_CAP = BATCH_MR_CAP;  // Krylov steps per restart held in shared memory
 
 template <class T> struct Ctx {
@@ -1053,6 +1050,42 @@ template <class T> __device__ void sort_mlist(Ctx<T> &c) {
   __syncthreads();
 }
 
+// Slot state of a problem whose group shares one factorization: the factor,
+// its pivoting state and both value copies of K with every inequality
+// hidden, copied from the group's base slot; visibility likewise.
+template <class T> __device__ void copy_base(Ctx<T> &c, const unsigned char *bs, const BSlot &L, const BPat &pt) {
+  const int tid = threadIdx.x, nt = blockDim.x, N = c.N;
+  const T *bL = reinterpret_cast<const T *>(bs + L.o_L);
+  const T *bD = reinterpret_cast<const T *>(bs + L.o_D);
+  const int *bls = reinterpret_cast<const int *>(bs + L.o_ls);
+  const int *bperm = reinterpret_cast<const int *>(bs + L.o_perm);
+  const int *biperm = reinterpret_cast<const int *>(bs + L.o_iperm);
+  const int *blperm = reinterpret_cast<const int *>(bs + L.o_lperm);
+  const double *bF = reinterpret_cast<const double *>(bs + L.o_Fv);
+  const double *bR = reinterpret_cast<const double *>(bs + L.o_Rv);
+  const unsigned long long *bmask = reinterpret_cast<const unsigned long long *>(bs + L.o_cmask);
+  for (int i = tid; i < pt.xsize; i += nt) c.L[i] = bL[i];
+  for (int i = tid; i < 2 * N; i += nt) c.D[i] = bD[i];
+  for (int i = tid; i < pt.ssize; i += nt) c.ls[i] = bls[i];
+  for (int i = tid; i < N; i += nt) {
+    c.perm[i] = bperm[i];
+    c.iperm[i] = biperm[i];
+    c.lperm[i] = blperm[i];
+  }
+  for (int i = tid; i < c.nnzR; i += nt) {
+    c.Fv[i] = bF[i];
+    c.Rv[i] = bR[i];
+  }
+  for (int s = tid; s < c.ns; s += nt) {
+    c.piv[s] = bs[L.o_piv + s];
+    c.cmask[s] = bmask[s];
+    c.mark[s] = 0;
+    c.vis[s] = c.sn_con[s] < 0 ? 1 : 0;
+  }
+  if (tid == 0) *c.nmark = 0;
+  __syncthreads();
+}
+
 // Visibility, descendant masks and both value copies of K from the active set.
 template <class T> __device__ void load_state(Ctx<T> &c) {
   for (int s = threadIdx.x; s < c.ns; s += blockDim.x) {
@@ -1078,7 +1111,7 @@ template <class T> __device__ void load_state(Ctx<T> &c) {
 }  // namespace
 
 template <class T>
-__global__ void __launch_bounds__(BT_MAX_THREADS, BT_MIN_BLOCKS) k_nasoq_batch(BArgs a) {
+__global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double red[32];
   __shared__ int redi[32];
@@ -1122,17 +1155,23 @@ __global__ void __launch_bounds__(BT_MAX_THREADS, BT_MIN_BLOCKS) k_nasoq_batch(B
   sp += up16((size_t)a.mi_max);
   unsigned char *stage = sp;  // the factor and row lists of a problem that fits
 
-  unsigned char *slot = a.slots + (size_t)blockIdx.x * a.slot.bytes;
+  unsigned char *const own_slot = a.slots + (size_t)blockIdx.x * a.slot.bytes;
+  const bool build_bases = a.mode == 1;
   for (;;) {
     if (tid == 0) {
       const int qi = atomicAdd(a.head, 1);
-      s_prob = qi < a.nprob ? a.order[qi] : -1;
+      if (build_bases) s_prob = qi < a.nbase ? qi : -1;  // a group
+      else s_prob = qi < a.nprob ? a.order[qi] : -1;
       s_status = 0;
       s_nmark = 0;
     }
     __syncthreads();
-    const int pi = s_prob;
-    if (pi < 0) break;
+    if (s_prob < 0) break;
+    // mode 1: the group's shared factorization is built in its base slot,
+    // for the group's representative problem
+    const int grp = build_bases ? s_prob : -1;
+    const int pi = build_bases ? a.base_rep[grp] : s_prob;
+    unsigned char *const slot = build_bases ? a.bases + (size_t)grp * a.slot.bytes : own_slot;
     const BProb &P = a.probs[pi];
     const BPat &pt = a.pats[P.pat];
     Ctx<T> &c = sc;
@@ -1182,7 +1221,7 @@ __global__ void __launch_bounds__(BT_MAX_THREADS, BT_MIN_BLOCKS) k_nasoq_batch(B
       c.reg32 = P.reg32;
       // the factor and the row lists live in shared memory when they fit
       const size_t lbytes = ((size_t)pt.xsize * sizeof(T) + 15) / 16 * 16;
-      if (lbytes + (size_t)pt.ssize * sizeof(int) <= (size_t)a.stage_bytes) {
+      if (!build_bases && lbytes + (size_t)pt.ssize * sizeof(int) <= (size_t)a.stage_bytes) {
         c.L = reinterpret_cast<T *>(stage);
         c.ls = reinterpret_cast<int *>(stage + lbytes);
       } else {
@@ -1237,22 +1276,33 @@ __global__ void __launch_bounds__(BT_MAX_THREADS, BT_MIN_BLOCKS) k_nasoq_batch(B
     const bool adaptive = a.refine == 1;
     int steps = 0, solves = 0, warm_dropped = 0;
 
-    // ---- set-up: pattern state into the slot
-    for (int i = tid; i < N; i += nt) {
-      const int p0 = ip[pt.o_perm0 + i];
-      c.perm[i] = p0;
-      c.iperm[p0] = i;
-      c.D[i] = T(0);
-      c.D[N + i] = T(0);
-    }
-    for (int i = tid; i < pt.ssize; i += nt) c.ls[i] = ip[pt.o_ls0 + i];
-    for (int i = tid; i < pt.xsize; i += nt) c.L[i] = T(0);
-    for (int s = tid; s < c.ns; s += nt) {
-      c.mark[s] = 0;
-      c.piv[s] = 0;
+    // ---- set-up: pattern state into the slot (a problem of a group starts
+    // from the group's factorization instead, below)
+    if (build_bases || P.base < 0) {
+      for (int i = tid; i < N; i += nt) {
+        const int p0 = ip[pt.o_perm0 + i];
+        c.perm[i] = p0;
+        c.iperm[p0] = i;
+        c.D[i] = T(0);
+        c.D[N + i] = T(0);
+      }
+      for (int i = tid; i < pt.ssize; i += nt) c.ls[i] = ip[pt.o_ls0 + i];
+      for (int i = tid; i < pt.xsize; i += nt) c.L[i] = T(0);
+      for (int s = tid; s < c.ns; s += nt) {
+        c.mark[s] = 0;
+        c.piv[s] = 0;
+      }
     }
     for (int k = tid; k < mineq; k += nt) c.act[k] = 0;
     __syncthreads();
+    if (build_bases) {  // every inequality hidden: the cold start's factorization
+      load_state(c);
+      build_vlist(c);
+      mark_all(c, true);
+      factor_marked(c);
+      continue;
+    }
+    const unsigned char *const bslot = P.base >= 0 ? a.bases + (size_t)P.base * a.slot.bytes : nullptr;
     int nact = 0;
     // warm start: proposed active set (constraints listed in as_out), then
     // the equality-constrained solution on it (below)
@@ -1272,7 +1322,18 @@ __global__ void __launch_bounds__(BT_MAX_THREADS, BT_MIN_BLOCKS) k_nasoq_batch(B
     // constraints are hidden by the partial refactorization of their paths.
     bool cold = !warm, full = true;
     for (int round = 0; round < 5; ++round) {
-      if (full) {
+      if (full && bslot) {
+        // the group's cold factorization, then the active rows made visible
+        // by partial refactorization of their paths
+        copy_base(c, bslot, a.slot, pt);
+        if (tid == 0)
+          for (int k = 0; k < mineq; ++k)
+            if (c.act[k]) edit_constraint(c, k, true);
+        __syncthreads();
+        sort_mlist(c);
+        factor_marked(c);
+        build_vlist(c);
+      } else if (full) {
         load_state(c);
         build_vlist(c);
         mark_all(c, true);
@@ -1717,6 +1778,29 @@ __global__ void k_ws_scores(int nprob, BProb *probs, const BPat *pats, const int
     }
   }
   if (lane == 0) P.ws_n = cnt > 0 ? cnt : -1;
+}
+
+// One block per problem: its q, b and d from the stacked staging buffer.
+__global__ void k_scatter_vectors(int nprob, const BProb *probs, const BPat *pats, const int64_t *voff,
+                                  const double *stage, double *dpool) {
+  const int i = blockIdx.x;
+  if (i >= nprob) return;
+  const BProb &P = probs[i];
+  const BPat &pt = pats[P.pat];
+  const int64_t oq = voff[3 * i], ob = voff[3 * i + 1], od = voff[3 * i + 2];
+  if (oq >= 0)
+    for (int t = threadIdx.x; t < pt.n; t += blockDim.x) dpool[P.o_q + t] = stage[oq + t];
+  if (ob >= 0)
+    for (int t = threadIdx.x; t < pt.meq; t += blockDim.x) dpool[P.o_b + t] = stage[ob + t];
+  if (od >= 0)
+    for (int t = threadIdx.x; t < pt.mineq; t += blockDim.x) dpool[P.o_d + t] = stage[od + t];
+}
+
+int batch_scatter_vectors(int nprob, const BProb *probs, const BPat *pats, const int64_t *voff, const double *stage,
+                          double *dpool, cudaStream_t st) {
+  if (nprob <= 0) return NQG_OK;
+  k_scatter_vectors<<<nprob, 128, 0, st>>>(nprob, probs, pats, voff, stage, dpool);
+  return cudaGetLastError() == cudaSuccess ? NQG_OK : NQG_ERR_CUDA;
 }
 
 __global__ void k_ws_clear(int nprob, BProb *probs) {

@@ -59,6 +59,7 @@ struct BProb {
   int outer, inner;          // refinement restarts x inner steps
   int max_iter_nas;
   int ws_n;                  // warm start: size of the proposed active set (-1: cold start)
+  int base;                  // group of problems with identical K (shared cold factorization), -1: none
   int64_t o_kv;              // nnzK values of K (original, every constraint entry present)
   int64_t o_pert;            // N bytes: diagonal replaced by the regularization
   int64_t o_q, o_b, o_d;     // n, meq, mineq
@@ -105,12 +106,25 @@ struct BArgs {
   int N_max, w_max, nr_max, ns_max, mi_max, nlev_max;  // shared-memory sizing
   unsigned long long *prof;  // per-phase SM cycles summed over CTAs, or null
   int stage_bytes;           // shared memory for the factor and row lists of problems that fit
+  // Problems with identical matrix values (same pattern, values,
+  // regularization) share the factorization with every inequality hidden: a
+  // launch with mode = 1 computes it once per group into `bases` (one slot
+  // layout each, for problem base_rep[g]); mode = 0 starts every member from
+  // a copy of it and refactors only the paths of its warm-start rows.
+  unsigned char *bases;
+  const int *base_rep;
+  int nbase;
+  int mode;
 };
 
 size_t batch_smem_bytes(const BArgs &a, size_t tsize);
 int batch_ws_from_scores(int nprob, BProb *probs, const BPat *pats, const int *ipool, const double *dpool, int *iout,
                          const float *scores, int ld, float thr, cudaStream_t st);
 int batch_ws_clear(int nprob, BProb *probs, cudaStream_t st);
+// Copies stacked q / b / d (offsets per problem in voff[3 i + 0..2], -1: not
+// given) from a staging buffer into the value pool.
+int batch_scatter_vectors(int nprob, const BProb *probs, const BPat *pats, const int64_t *voff, const double *stage,
+                          double *dpool, cudaStream_t st);
 template <class T> int batch_prepare(int threads, size_t smem_attr, size_t smem, int *blocks_per_sm);
 template <class T> int launch_batch(const BArgs &a, int grid, int threads, size_t smem, cudaStream_t st);
 

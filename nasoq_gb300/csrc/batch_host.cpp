@@ -335,6 +335,14 @@ struct nqg_batch {
   int64_t n_dbl = 0, n_pert_bytes = 0, n_dout = 0, n_iout = 0;
   int grid = 0, threads = 128, blocks_per_sm = 0, num_sms = 0;
   size_t smem = 0;
+  // groups of problems with identical matrices: one shared factorization each
+  unsigned char *d_bases = nullptr;
+  int *d_base_rep = nullptr;
+  int nbase = 0;
+  // staging of set_vectors: stacked q / b / d and their offsets per problem
+  double *d_vstage = nullptr;
+  int64_t *d_voff = nullptr;
+  int64_t n_vstage = 0;
   cudaGraphExec_t gexec = nullptr;
   cudaGraph_t graph = nullptr;
   double last_ms = 0.0;
@@ -364,8 +372,13 @@ void free_device(nqg_batch *b) {
   if (b->d_prof) cudaFree(b->d_prof);
   b->d_prof = nullptr;
   for (void *p : {(void *)b->d_pats, (void *)b->d_probs, (void *)b->d_ipool, (void *)b->d_order, (void *)b->d_head,
-                  (void *)b->d_iout, (void *)b->d_dpool, (void *)b->d_dout, (void *)b->d_res, (void *)b->d_slots})
+                  (void *)b->d_iout, (void *)b->d_dpool, (void *)b->d_dout, (void *)b->d_res, (void *)b->d_slots,
+                  (void *)b->d_bases, (void *)b->d_base_rep, (void *)b->d_vstage, (void *)b->d_voff})
     if (p) cudaFree(p);
+  b->d_bases = nullptr;
+  b->d_base_rep = nullptr;
+  b->d_vstage = nullptr;
+  b->d_voff = nullptr;
   b->d_pats = nullptr;
   b->d_probs = nullptr;
   b->d_ipool = b->d_order = b->d_head = b->d_iout = nullptr;
@@ -458,6 +471,7 @@ extern "C" void nqg_batch_default_settings(nqg_batch_settings *s) {
   s->threads = 0;
   s->use_graph = 1;
   s->stage = 0;
+  s->share_factor = 1;
 }
 
 extern "C" int nqg_batch_create(const nqg_batch_settings *s, nqg_batch **out) {
@@ -646,6 +660,50 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
   b->h_dpool.assign(od, 0.0);
   std::vector<unsigned char> pert(std::max<int64_t>(pb, 1), 0);
   for (int i = 0; i < np; ++i) fill_values(b, i, pert);
+  // ---- groups of problems with identical matrices (pattern, K values,
+  // perturbation flags, regularization): one shared cold factorization each
+  std::vector<int> base_rep;
+  for (int i = 0; i < np; ++i) b->h_probs[i].base = -1;
+  if (b->set.share_factor) {
+    auto kv_of = [&](int i) { return b->h_dpool.data() + b->h_probs[i].o_kv; };
+    auto pf_of = [&](int i) { return pert.data() + (b->h_probs[i].o_pert - od * (int64_t)sizeof(double)); };
+    std::unordered_map<uint64_t, std::vector<int>> cand;  // key -> representatives
+    std::vector<int> members(np, 0), first_of(np, -1);
+    for (int i = 0; i < np; ++i) {
+      const BProb &R = b->h_probs[i];
+      const BPat &Pp = b->pats[R.pat].P;
+      uint64_t h = 1469598103934665603ull ^ (uint64_t)R.pat;
+      const unsigned char *kb = reinterpret_cast<const unsigned char *>(kv_of(i));
+      for (int64_t t = 0; t < (int64_t)Pp.nnzK * 8; ++t) h = (h ^ kb[t]) * 1099511628211ull;
+      int rep = -1;
+      for (int r : cand[h]) {
+        const BProb &Q = b->h_probs[r];
+        if (Q.pat == R.pat && Q.reg == R.reg && Q.reg32 == R.reg32 && Q.outer == R.outer && Q.inner == R.inner &&
+            std::memcmp(kv_of(r), kv_of(i), (size_t)Pp.nnzK * sizeof(double)) == 0 &&
+            std::memcmp(pf_of(r), pf_of(i), (size_t)Pp.N) == 0) {
+          rep = r;
+          break;
+        }
+      }
+      if (rep < 0) {
+        cand[h].push_back(i);
+        rep = i;
+      }
+      first_of[i] = rep;
+      members[rep]++;
+    }
+    std::vector<int> gid(np, -1);
+    for (int i = 0; i < np; ++i) {
+      const int rep = first_of[i];
+      if (members[rep] < 2) continue;  // alone: nothing to share
+      if (gid[rep] < 0) {
+        gid[rep] = (int)base_rep.size();
+        base_rep.push_back(rep);
+      }
+      b->h_probs[i].base = gid[rep];
+    }
+  }
+  b->nbase = (int)base_rep.size();
   // ---- slot layout (one problem at a time per CTA)
   const size_t ts = b->set.qp.precision == NQG_FP32 ? sizeof(float) : sizeof(double);
   nqg::BSlot sl{};
@@ -689,7 +747,7 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
   int smem_optin = 0;
   BQ_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   b->threads = b->set.threads > 0 ? b->set.threads : 128;
-  if (b->threads % 32 || b->threads > 128) return fail(b, NQG_ERR_ARG, "threads must be a multiple of 32, at most 128");
+  if (b->threads % 32 || b->threads > 256) return fail(b, NQG_ERR_ARG, "threads must be a multiple of 32, at most 256");
   nqg::BArgs base_args{};
   base_args.N_max = N_max;
   base_args.w_max = w_max;
@@ -778,6 +836,11 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
   BQ_CUDA(cudaMemcpy(b->d_order, order.data(), np * sizeof(int), cudaMemcpyHostToDevice));
   BQ_CUDA(cudaMalloc(&b->d_head, std::max<size_t>(b->tiers.size(), 1) * sizeof(int)));
   BQ_CUDA(cudaMalloc(&b->d_slots, (size_t)std::max<int64_t>(nslots, 1) * sl.bytes));
+  if (b->nbase > 0) {
+    BQ_CUDA(cudaMalloc(&b->d_bases, (size_t)b->nbase * sl.bytes));
+    BQ_CUDA(cudaMalloc(&b->d_base_rep, (size_t)b->nbase * sizeof(int)));
+    BQ_CUDA(cudaMemcpy(b->d_base_rep, base_rep.data(), (size_t)b->nbase * sizeof(int), cudaMemcpyHostToDevice));
+  }
   BQ_CUDA(cudaMemcpy(b->d_probs, b->h_probs.data(), np * sizeof(BProb), cudaMemcpyHostToDevice));
   BQ_CUDA(cudaEventCreateWithFlags(&b->e0, cudaEventDefault));
   BQ_CUDA(cudaEventCreateWithFlags(&b->e1, cudaEventDefault));
@@ -803,8 +866,28 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
     A.refine_tol = b->set.refine_tol;
     A.mr_max = mr_max;
     A.prof = nullptr;
+    A.bases = b->d_bases;
+    A.base_rep = b->d_base_rep;
+    A.nbase = b->nbase;
+    A.mode = 0;
   }
   b->args.slot = sl;
+  // ---- the groups' shared factorizations (once: the matrices never change)
+  if (b->nbase > 0) {
+    TierLaunch &T0 = b->tiers.front();
+    nqg::BArgs A = T0.args;
+    A.mode = 1;
+    A.stage_bytes = 0;
+    A.slots = b->d_slots;
+    A.head = b->d_head;
+    BQ_CUDA(cudaMemsetAsync(A.head, 0, sizeof(int), b->stream));
+    const int grid = std::min(b->nbase, T0.bps * b->num_sms);
+    const size_t smem = base_smem;
+    const int rc = b->set.qp.precision == NQG_FP32 ? nqg::launch_batch<float>(A, grid, b->threads, smem, b->stream)
+                                                   : nqg::launch_batch<double>(A, grid, b->threads, smem, b->stream);
+    if (rc) return fail(b, rc, "launch of the shared factorizations failed");
+    BQ_CUDA(cudaStreamSynchronize(b->stream));
+  }
   b->finalized = true;
   return NQG_OK;
 }
@@ -813,31 +896,50 @@ extern "C" int nqg_batch_set_vectors(nqg_batch *b, const double *q_all, const do
                                      const double *d_all) {
   // New q / b / d for every problem, concatenated in problem order (any may
   // be NULL: unchanged).
+  // One copy per given vector into a staging buffer, then one kernel
+  // scatters every problem's segment into the value pool.
   if (!b || !b->finalized) return NQG_ERR_STATE;
   const int np = (int)b->qp.size();
-  int64_t oq = 0, ob = 0, odd = 0;
+  int64_t tq = 0, tb = 0, td = 0;
+  for (const HostQP &Q : b->qp) {
+    tq += Q.n;
+    tb += Q.meq;
+    td += Q.mineq;
+  }
+  if (!b->d_vstage) {
+    b->n_vstage = tq + tb + td;
+    BQ_CUDA(cudaMalloc(&b->d_vstage, std::max<int64_t>(b->n_vstage, 1) * sizeof(double)));
+    BQ_CUDA(cudaMalloc(&b->d_voff, (size_t)np * 3 * sizeof(int64_t)));
+  }
+  std::vector<int64_t> off((size_t)np * 3, -1);
+  int64_t oq = 0, ob = tq, odd = tq + tb;
   for (int i = 0; i < np; ++i) {
     HostQP &Q = b->qp[i];
-    const BProb &P = b->h_probs[i];
     if (q_all) {
       std::copy(q_all + oq, q_all + oq + Q.n, Q.q.begin());
-      BQ_CUDA(cudaMemcpyAsync(b->d_dpool + P.o_q, q_all + oq, Q.n * sizeof(double), cudaMemcpyHostToDevice,
-                              b->stream));
+      off[3 * i] = oq;
     }
-    if (beq_all && Q.meq) {
-      std::copy(beq_all + ob, beq_all + ob + Q.meq, Q.b.begin());
-      BQ_CUDA(cudaMemcpyAsync(b->d_dpool + P.o_b, beq_all + ob, Q.meq * sizeof(double), cudaMemcpyHostToDevice,
-                              b->stream));
+    if (beq_all) {
+      std::copy(beq_all + (ob - tq), beq_all + (ob - tq) + Q.meq, Q.b.begin());
+      off[3 * i + 1] = ob;
     }
-    if (d_all && Q.mineq) {
-      std::copy(d_all + odd, d_all + odd + Q.mineq, Q.d.begin());
-      BQ_CUDA(cudaMemcpyAsync(b->d_dpool + P.o_d, d_all + odd, Q.mineq * sizeof(double), cudaMemcpyHostToDevice,
-                              b->stream));
+    if (d_all) {
+      std::copy(d_all + (odd - tq - tb), d_all + (odd - tq - tb) + Q.mineq, Q.d.begin());
+      off[3 * i + 2] = odd;
     }
     oq += Q.n;
     ob += Q.meq;
     odd += Q.mineq;
   }
+  if (q_all && tq)
+    BQ_CUDA(cudaMemcpyAsync(b->d_vstage, q_all, tq * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  if (beq_all && tb)
+    BQ_CUDA(cudaMemcpyAsync(b->d_vstage + tq, beq_all, tb * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  if (d_all && td)
+    BQ_CUDA(cudaMemcpyAsync(b->d_vstage + tq + tb, d_all, td * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  BQ_CUDA(cudaMemcpyAsync(b->d_voff, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, b->stream));
+  const int rc = nqg::batch_scatter_vectors(np, b->d_probs, b->d_pats, b->d_voff, b->d_vstage, b->d_dpool, b->stream);
+  if (rc) return fail(b, rc, "vector scatter failed");
   BQ_CUDA(cudaStreamSynchronize(b->stream));
   return NQG_OK;
 }

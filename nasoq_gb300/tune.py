@@ -19,7 +19,7 @@ from collections import Counter
 
 import nasoq_gb300 as nq
 
-CANDIDATES = ((128, 0), (64, 0), (96, 0), (128, 1))
+CANDIDATES = ((128, 0), (64, 0), (256, 0), (128, 1))
 DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "nasoq_gb300", "batch_tune.json")
 
 

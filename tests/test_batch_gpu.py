@@ -156,3 +156,41 @@ def test_batch_warm_start_from_solution():
         assert rel(x, part(d, "x", i)) <= 1e-7, f"problem {i}"
         assert res.lag_res <= eps and res.cons_sat_norm <= eps
     b.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [nq.NQG_FP64, nq.NQG_FP32])
+def test_shared_factorization_matches_private(precision):
+    """Problems with identical matrices start from one shared factorization
+    (share_factor = 1) and refactor only their active rows' paths: the same
+    status, iteration counts and solutions as factoring each KKT matrix
+    privately, cold and warm-started."""
+    fam = P.mpc_parametric(0)
+    thetas = np.random.default_rng(77).standard_normal((96, fam.P.shape[1]))
+    base = fam.base
+    one = (base.H, base.q, base.A, base.b, base.C, base.d)
+    kw = dict(variant=0, eps_abs=1e-8, precision=precision)
+    if precision == nq.NQG_FP32:
+        kw.update(refine=1, refine_tol=1e-12)
+    runs = {}
+    for share in (0, 1):
+        b = nq.QPBatch([one] * len(thetas), settings=nq.batch_settings(share_factor=share, **kw))
+        b.set_vectors(q_all=(thetas @ fam.P.T).ravel(), d_all=(fam.d0[None, :] + thetas @ fam.S.T).ravel())
+        b.solve()
+        cold = b.results()
+        # warm: every other problem starts from its own optimal active set
+        for i in range(0, len(thetas), 2):
+            act = b.result(i)[3]
+            b.set_warm_start(i, act)
+        b.solve()
+        warm = b.results()
+        runs[share] = (cold, warm)
+        b.close()
+    tol = 1e-9 if precision == nq.NQG_FP64 else 1e-6
+    for phase in (0, 1):
+        x0, _, z0, s0 = runs[0][phase]
+        x1, _, z1, s1 = runs[1][phase]
+        assert all(a.status == 1 and c.status == 1 for a, c in zip(s0, s1))
+        if precision == nq.NQG_FP64:
+            assert [a.num_iter for a in s0] == [c.num_iter for c in s1]
+        assert rel(x1, x0) <= tol and rel(z1, z0) <= tol

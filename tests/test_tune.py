@@ -21,7 +21,7 @@ def _probs(horizons):
 def test_autotune_picks_fastest_complete_candidate_and_caches(tmp_path):
     probs = _probs([10, 12, 30])
     cache = str(tmp_path / "tune.json")
-    table = {(128, 0): (5.0, 3), (64, 0): (3.0, 2), (96, 0): (4.0, 3), (128, 1): (6.0, 3)}
+    table = {(128, 0): (5.0, 3), (64, 0): (3.0, 2), (256, 0): (4.0, 3), (128, 1): (6.0, 3)}
     calls = []
 
     def timer(problems, s):
@@ -31,18 +31,18 @@ def test_autotune_picks_fastest_complete_candidate_and_caches(tmp_path):
     s, rep = tune.autotune_batch(probs, cache=cache, timer=timer, variant=0, eps_abs=1e-8,
                                  precision=nq.NQG_FP32, refine=1)
     # (64, 0) is fastest but solved fewer QPs
-    assert (s.threads, s.stage) == (96, 0) and not rep["cached"]
+    assert (s.threads, s.stage) == (256, 0) and not rep["cached"]
     assert s.qp.precision == nq.NQG_FP32 and s.refine == 1 and s.qp.eps_abs == 1e-8
     assert len(calls) == 4
     saved = json.load(open(cache))
-    assert saved[rep["key"]]["threads"] == 96
+    assert saved[rep["key"]]["threads"] == 256
 
     def no_timer(problems, s):
         raise AssertionError("cached choice must not be timed again")
 
     s2, rep2 = tune.autotune_batch(probs, cache=cache, timer=no_timer, variant=0, eps_abs=1e-8,
                                    precision=nq.NQG_FP32, refine=1)
-    assert rep2["cached"] and (s2.threads, s2.stage) == (96, 0)
+    assert rep2["cached"] and (s2.threads, s2.stage) == (256, 0)
     # another size profile or other settings: another key
     assert tune.profile_key(_probs([10, 12, 60]), s) != rep["key"]
     assert tune.profile_key(probs, nq.batch_settings(precision=nq.NQG_FP64)) != rep["key"]
