@@ -1562,6 +1562,10 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
     // most twice).  The reference's fixed schedule runs to 1e-15 and needs
     // none of this.
     if (!adaptive || !converged || pol >= 2) break;
+    // no iteration since the initial solution: it already is the solution on
+    // the final active set (negative multipliers were dropped before), so
+    // polishing would repeat the same solve
+    if (pol == 0 && num_iter == 0) break;
     if (*c.nmark > 0) {
       sort_mlist(c);
       factor_marked(c);
