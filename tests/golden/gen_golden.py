@@ -69,6 +69,28 @@ def lbl_case(name, K, rhs, **settings):
     save_case(name, inp, out)
 
 
+def lbl_case_light(name, K, rhs, **settings):
+    """An LBL case too large to keep the reference's factor: inputs, the
+    reference's solutions, the perturbed values, and the condition number and
+    2x2-pivot count of the reference's factorization."""
+    if not wanted(name):
+        return
+    inp = {"Ap": K.p, "Ai": K.i, "Ax": K.x, "rhs": rhs}
+    for k, v in settings.items():
+        inp[k] = np.array([float(v)])
+    out = run("lbl", inp)
+    n = K.ncol
+    Kd = np.zeros((n, n))
+    for j in range(n):
+        for q in range(K.p[j], K.p[j + 1]):
+            Kd[K.i[q], j] = Kd[j, K.i[q]] = out["Ax_perturbed"][q]
+    ev = np.abs(np.linalg.eigvalsh(Kd))
+    keep = {k: out[k] for k in ("x", "x_noref", "Ax_perturbed", "num_ref_iter", "sym_max_sup_wid")}
+    keep["kappa"] = np.array([ev.max() / ev.min()])
+    keep["n2x2"] = np.array([float(np.count_nonzero(out["d_val"][n:]))])
+    save_case(name, inp, keep)
+
+
 def qp_inputs(qp: P.QP, **settings):
     inp = {
         "Hp": qp.H.p, "Hi": qp.H.i, "Hx": qp.H.x, "q": qp.q,
@@ -144,6 +166,12 @@ def main(ref):
     K = P.sym_indefinite(seed=8, n=300, density=0.02)
     lbl_case("lbl_indef_sparse", K, np.random.default_rng(8).standard_normal(300), req_ref_iter=3,
              max_inner_iter=3, reg_diag=1e-9)
+
+    # strongly indefinite KKT (2500 zero-diagonal constraint columns, 2500
+    # negative eigenvalues), kappa ~ 1e4, 2x2 pivots inside supernodes up to
+    # 2545 columns wide: the FP32 multi-CTA kernels at their default thresholds
+    K, rhs = P.lbl_kkt(seed=22, grid3d=16, m=2500, per_row=4, delta=0.0)
+    lbl_case_light("lblw_kkt3d_hard", K, rhs, req_ref_iter=2, reg_diag=1e-9)
 
     # --- NASOQ QPs ---------------------------------------------------------------
     for pname in ("matt_qp1", "test05_0"):
