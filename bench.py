@@ -548,10 +548,28 @@ def lbl_section(args, torch, nq, P, pk):
     step()
     stats = plan.kernel_stats()
     plan.set_profiling(False)
+    oracle = None
+    if args.lbl_oracle:
+        # the reference's FP64 method (oracle restatement, all host cores) on
+        # the same system, same ordering and supernodes; outside the timed region
+        try:
+            from oracle import port
+            port.set_threads(os.cpu_count() or 1)
+            diag = K.p[:-1]
+            axp, axr = K.x.copy(), K.x.copy()
+            small = np.abs(K.x[diag]) < 1e-9
+            axp[diag[small]] = 1e-9
+            axr[diag[small]] = 0.0
+            t = time.perf_counter()
+            o = port.solve(n, K.p, K.i, axp, axr, plan.symbolic, rhs, req_ref_iter=2, max_inner_iter=2)
+            oracle = {"max_rel_x_error": float(np.linalg.norm(x32 - o["x"]) / np.linalg.norm(o["x"])),
+                      "oracle_seconds": time.perf_counter() - t, "threads": os.cpu_count()}
+        except Exception as e:
+            oracle = {"unavailable": str(e)[:200]}
     plan.close()
     return {"workload": f"lbl_kkt_lap3d_{GRID}cube_m{MCON}", "N": n, "value": 1000.0 / ms, "unit": "solves/s",
             "ms_per_step": ms, "relres": rr, "meets_target": bool(rr <= TARGET_RELRES), "analysis_s": analysis_s,
-            "kernels_ms": {k: v["total_ms"] for k, v in stats.items()}}
+            "error_vs_oracle": oracle, "kernels_ms": {k: v["total_ms"] for k, v in stats.items()}}
 
 
 def main():
@@ -567,6 +585,9 @@ def main():
     ap.add_argument("--no-c3", action="store_true")
     ap.add_argument("--no-lbl", action="store_true")
     ap.add_argument("--lbl-steps", type=int, default=3)
+    ap.add_argument("--lbl-oracle", action="store_true",
+                    help="also solve the LBL system with the oracle (FP64, host cores, ~1-2 min) for its error")
+    ap.add_argument("--lbl-only", action="store_true", help="run the LBL section alone")
     ap.add_argument("--batch", type=int, default=BATCH, help="QPs per step (smaller cases for profiler captures)")
     ap.add_argument("--profile-once", action="store_true",
                     help="train, then exactly one measured step and nothing else (profiler launch lists)")
@@ -597,6 +618,10 @@ def main():
     if args.c5_only:
         if rank == 0:
             print(json.dumps({"c5": c5_section(args, nq, P)}), flush=True)
+        return 0
+    if args.lbl_only:
+        if rank == 0:
+            print(json.dumps({"lbl_c2": lbl_section(args, torch, nq, P, pk)}), flush=True)
         return 0
     qp = qp_section(args, world, rank, local, torch, nq, P, learn, pk, pk_src)
     if qp is None:
