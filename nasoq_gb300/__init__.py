@@ -1,5 +1,8 @@
-"""nasoq_gb300: supernodal Bunch-Kaufman LDL^T, supernodal solves and GMRES
-refinement for sparse symmetric-indefinite (KKT) systems on one GB300 GPU.
+"""nasoq_gb300: NASOQ's dual active-set QP solver on one GB300 GPU -- batched
+QPs with the whole active-set loop on the device (QPBatch), the learned
+active-set warm start (MLP), single QPs (qp_solve), SMP files (load_smp) --
+over supernodal Bunch-Kaufman LDL^T, supernodal solves and GMRES refinement
+of sparse symmetric-indefinite (KKT) systems (Plan).
 
 This module is a thin ctypes binding of the C ABI in include/nasoq_gb300.h
 (built in-tree as nasoq_gb300/libnasoq_gb300.so by nasoq_gb300.build).  There
@@ -557,6 +560,12 @@ class QPBatch:
         st = (BatchStats * len(self.sizes))()
         self._raise(lib().nqg_batch_get_all(self._h, _ptr(x), _ptr(y), _ptr(z), C.cast(st, C.c_void_p)), "get all")
         return x[:self.n_tot], y[:self.meq_tot], z[:self.mineq_tot], st
+
+    def stats(self):
+        """Per-problem statistics only (status, iterations, KKT norms, ...)."""
+        st = (BatchStats * len(self.sizes))()
+        self._raise(lib().nqg_batch_get_all(self._h, None, None, None, C.cast(st, C.c_void_p)), "get all")
+        return st
 
     PROFILE_PHASES = ("total", "setup", "refactor", "precond", "spmv", "refine", "select", "update",
                       "supernodes", "iterations", "fwd_wide", "fwd_narrow", "diag", "bwd", "gather")

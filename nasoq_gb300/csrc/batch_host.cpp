@@ -1062,8 +1062,11 @@ extern "C" int nqg_batch_get_all(nqg_batch *b, double *x_all, double *y_all, dou
   // and per-problem statistics (nprob entries).
   if (!b || !b->finalized) return NQG_ERR_STATE;
   const int np = (int)b->qp.size();
-  std::vector<double> out(std::max<int64_t>(b->n_dout, 1));
-  BQ_CUDA(cudaMemcpyAsync(out.data(), b->d_dout, b->n_dout * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  std::vector<double> out;
+  if (x_all || y_all || z_all) {
+    out.resize(std::max<int64_t>(b->n_dout, 1));
+    BQ_CUDA(cudaMemcpyAsync(out.data(), b->d_dout, b->n_dout * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  }
   std::vector<BResult> R(np);
   BQ_CUDA(cudaMemcpyAsync(R.data(), b->d_res, np * sizeof(BResult), cudaMemcpyDeviceToHost, b->stream));
   BQ_CUDA(cudaStreamSynchronize(b->stream));

@@ -88,6 +88,7 @@ def lbl_case_light(name, K, rhs, **settings):
     keep = {k: out[k] for k in ("x", "x_noref", "Ax_perturbed", "num_ref_iter", "sym_max_sup_wid")}
     keep["kappa"] = np.array([ev.max() / ev.min()])
     keep["n2x2"] = np.array([float(np.count_nonzero(out["d_val"][n:]))])
+    keep["gmax"] = np.array([float(np.abs(out["valL"]).max())])  # element growth of the factor
     save_case(name, inp, keep)
 
 

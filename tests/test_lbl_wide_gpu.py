@@ -6,8 +6,9 @@ made by tests/golden/gen_golden.py from the reference).  The multi-CTA
 kernels run at their default widths (192-column threshold, 64-column
 panels), FP64 and every FP32 variant:
 
-  * FP64: 2x2 pivots found, solutions within max(1e-9, 1e-14 kappa) of the
-    reference's (without and with refinement);
+  * FP64: 2x2 pivots found, solutions within max(1e-9, 1e-14 kappa,
+    1e-15 g) of the reference's, g its largest factor entry (without and with
+    refinement);
   * FP32 factor (tcgen05, per-tile tcgen05, mma.sync, SIMT trailing updates;
     FP64 or FP32 triangular solves, level or block kernels) with FP64
     refinement: relative residual 1e-10 and x within 1e-6 of the reference."""
@@ -47,7 +48,9 @@ def test_fp64_hard_pivots_default_thresholds():
     plan = _plan(d, req_ref_iter=0)
     assert plan.factor() == nq.NQG_OK
     assert plan.timings().num_2x2 > 0
-    tol = max(1e-9, 1e-14 * kappa)
+    # unrefined solutions differ by rounding amplified by the element growth
+    # that block-restricted pivoting leaves (pivots as small as reg_diag)
+    tol = max(1e-9, 1e-14 * kappa, 1e-15 * float(d["out_gmax"][0]))
     x0 = plan.solve(d["in_rhs"])
     xr = d["out_x_noref"]
     assert np.linalg.norm(x0 - xr) <= tol * np.linalg.norm(xr)
