@@ -354,7 +354,9 @@ int nqg_batch_get_stream(const nqg_batch *b, void **stream);
  * [5] refinement (solves included), [6] entering-constraint selection,
  * [7] steps and edits, [8] supernodes factored, [9] active-set iterations,
  * and inside [3]: [10] forward sweeps of wide levels, [11] of narrow levels,
- * [12] diagonal solves, [13] backward sweeps, [14] gathers and scatters. */
+ * [12] diagonal solves, [13] backward sweeps, [14] gathers and scatters;
+ * inside [1]: [15] the factorizations of the set-up rounds (a shared
+ * factorization's copy and the active rows' refactorization included). */
 int nqg_batch_set_profiling(nqg_batch *b, int on);
 int nqg_batch_get_profile(nqg_batch *b, unsigned long long *counters, int n);
 const char *nqg_batch_last_error(const nqg_batch *b);

@@ -568,7 +568,7 @@ class QPBatch:
         return st
 
     PROFILE_PHASES = ("total", "setup", "refactor", "precond", "spmv", "refine", "select", "update",
-                      "supernodes", "iterations", "fwd_wide", "fwd_narrow", "diag", "bwd", "gather")
+                      "supernodes", "iterations", "fwd_wide", "fwd_narrow", "diag", "bwd", "gather", "init_factor")
 
     def set_profiling(self, on=True):
         self._raise(lib().nqg_batch_set_profiling(self._h, 1 if on else 0), "set profiling")

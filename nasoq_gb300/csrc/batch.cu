@@ -86,7 +86,7 @@ template <class T> struct Ctx {
 
 // Counters of nqg_batch_get_profile.
 enum { PH_TOTAL, PH_INIT, PH_FACTOR, PH_PRECOND, PH_SPMV, PH_REFINE, PH_SELECT, PH_UPDATE, PH_SN, PH_ITER,
-       PH_FWD_WIDE, PH_FWD_NARROW, PH_DIAG, PH_BWD, PH_GATHER, PH_N };
+       PH_FWD_WIDE, PH_FWD_NARROW, PH_DIAG, PH_BWD, PH_GATHER, PH_INIT_FACTOR, PH_N };
 static_assert(PH_N <= BATCH_PROFILE_COUNTERS, "profile counters");
 #define BQ_T0(c) const long long t0_ = (c).cyc ? clock64() : 0
 #define BQ_T1(c, ph) \
@@ -1322,6 +1322,7 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
     // constraints are hidden by the partial refactorization of their paths.
     bool cold = !warm, full = true;
     for (int round = 0; round < 5; ++round) {
+      const long long tf0 = c.cyc ? clock64() : 0;
       if (full && bslot) {
         // the group's cold factorization, then the active rows made visible
         // by partial refactorization of their paths
@@ -1343,6 +1344,7 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
         factor_marked(c);
         build_vlist(c);
       }
+      if (c.cyc && tid == 0) c.cyc[PH_INIT_FACTOR] += (unsigned long long)(clock64() - tf0);
       for (int i = tid; i < N; i += nt) {
         double v = 0.0;
         if (i < n) v = -c.q[i];
@@ -1566,6 +1568,10 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
     // the final active set (negative multipliers were dropped before), so
     // polishing would repeat the same solve
     if (pol == 0 && num_iter == 0) break;
+    // the final solution is refined further than the loop's solves: after a
+    // long trajectory its active set is settled, and its KKT norms decide the
+    // status
+    const double polish_tol = fmin(a.refine_tol, 1e-12);
     if (*c.nmark > 0) {
       sort_mlist(c);
       factor_marked(c);
@@ -1582,7 +1588,7 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
     __syncthreads();
     precond(c, c.rhs, c.sol);
     solves++;
-    steps += refine(c, c.rhs, c.sol, P.outer, P.inner, flexible, adaptive, a.refine_tol, P.tol_abs, P.tol_rel, gs);
+    steps += refine(c, c.rhs, c.sol, P.outer, P.inner, flexible, adaptive, polish_tol, P.tol_abs, P.tol_rel, gs);
     // a negative multiplier: that constraint does not belong to the active
     // set of this point; drop it and solve again (at most three times)
     for (int rep = 0; rep < 3; ++rep) {
@@ -1613,7 +1619,7 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
       __syncthreads();
       precond(c, c.rhs, c.sol);
       solves++;
-      steps += refine(c, c.rhs, c.sol, P.outer, P.inner, flexible, adaptive, a.refine_tol, P.tol_abs, P.tol_rel, gs);
+      steps += refine(c, c.rhs, c.sol, P.outer, P.inner, flexible, adaptive, polish_tol, P.tol_abs, P.tol_rel, gs);
     }
     for (int k = tid; k < mineq; k += nt)
       if (!c.act[k]) zv[k] = 0.0;
