@@ -8,8 +8,10 @@ available): the parametric MPC family at horizon 50 (n = 450, 300 equality
 rows, 900 box rows), q = P theta, box shifts S theta, theta in R^32 ~ N(0, I),
 P and S dense N(0, 0.1) (nasoq_gb300.problems.mpc_parametric).  One step = one
 batch of 4096 fresh theta: model logits on the GPU, warm-start sets, and the
-batched NASOQ solve (one CTA per QP), FP32 factorization with FP64 flexible
-GMRES refinement, every QP checked at eps_abs = 1e-8.  The active-set model is
+batched NASOQ solve (one CTA per QP; the batch's QPs share one cold
+factorization of their common KKT matrix), FP32 factorization with FP64
+flexible GMRES refinement, every QP checked at eps_abs = 1e-8 and only those
+that meet it counted.  The active-set model is
 trained at start-up by the library's own kernels on plain-NASOQ solves of
 200k random theta (outside the timed region; reported).
 
@@ -650,7 +652,7 @@ def main():
             "vs_baseline": None, "dtype": "fp32-factor+fp64-refine", "data": "synthetic",
             "config": {"workload": "qp_mpc50_parametric_theta32", "batch": BATCH, "n": 450, "meq": 300,
                        "mineq": 900, "eps_abs": EPS, "variant": "Fixed",
-                       "precision": "FP32 factor and triangular solves, FP64 flexible GMRES to 1e-12 relative "
+                       "precision": f"FP32 factor and triangular solves, FP64 flexible GMRES to {REFINE_TOL:g} relative "
                                     "residual, final polish on the active set",
                        "warm_start": f"learned (MLP 32-256-256-900, BF16 weights, FP32 accumulation; logit > "
                                      f"{WS_THRESHOLD:g} proposes a constraint)",
