@@ -55,7 +55,8 @@ EPS = 1e-8
 N_TRAIN = 200_000
 REFINE_TOL = 1e-10  # FGMRES target of the mixed path: swept 1e-12..1e-10, every QP Optimal, max lag ~1e-9
 THETA_SEED = 20261204
-WS_THRESHOLD = 1.0  # logit above which a constraint is proposed (swept 0..5: 1.0 fastest, every QP optimal)
+WS_THRESHOLD = 1.5  # logit above which a constraint is proposed (swept 0..5: 1.0-1.5 fastest, every QP optimal)
+TRAIN_EPOCHS = 60   # swept 20 / 60: 60 epochs (10 s) cut warm-start drops from 5.0 to 2.9 per QP
 CPU_SAMPLE_PER_PROC = 48
 # DRAM bytes (read + write) of one batch-kernel launch on this workload, from
 # an ncu capture of the measured step of --profile-once (4096 QPs):
@@ -225,7 +226,8 @@ def qp_section(args, world, rank, local, torch, nq, P, learn, pk, pk_src):
         model.set_weights(z["w"], z["b"])
         rep = learn.TrainReport(int(z["n_train"]), 0.0, 0.0, [float(v) for v in z["losses"]], float(z["active"]))
     else:
-        model, rep = learn.train_model(fam, n_train=args.n_train, seed=11 + rank, epochs=20, batch=1024, lr=1e-3,
+        model, rep = learn.train_model(fam, n_train=args.n_train, seed=11 + rank, epochs=TRAIN_EPOCHS, batch=1024,
+                                       lr=1e-3,
                                        solver=dict(variant=0, eps_abs=EPS, precision=nq.NQG_FP32, refine=1,
                                                    refine_tol=REFINE_TOL))
         if args.save_model and rank == 0:

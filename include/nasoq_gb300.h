@@ -356,7 +356,10 @@ int nqg_batch_get_stream(const nqg_batch *b, void **stream);
  * and inside [3]: [10] forward sweeps of wide levels, [11] of narrow levels,
  * [12] diagonal solves, [13] backward sweeps, [14] gathers and scatters;
  * inside [1]: [15] the factorizations of the set-up rounds (a shared
- * factorization's copy and the active rows' refactorization included). */
+ * factorization's copy and the active rows' refactorization included);
+ * every supernode factorization split into [16] assembly, [17] descendant
+ * updates, [18] Bunch-Kaufman, [19] rows below, [20] inverse of the
+ * diagonal block, [21] stores; [22] pivot renaming after a factorization. */
 int nqg_batch_set_profiling(nqg_batch *b, int on);
 int nqg_batch_get_profile(nqg_batch *b, unsigned long long *counters, int n);
 const char *nqg_batch_last_error(const nqg_batch *b);

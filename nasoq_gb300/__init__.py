@@ -568,7 +568,8 @@ class QPBatch:
         return st
 
     PROFILE_PHASES = ("total", "setup", "refactor", "precond", "spmv", "refine", "select", "update",
-                      "supernodes", "iterations", "fwd_wide", "fwd_narrow", "diag", "bwd", "gather", "init_factor")
+                      "supernodes", "iterations", "fwd_wide", "fwd_narrow", "diag", "bwd", "gather", "init_factor",
+                      "sn_assemble", "sn_updates", "sn_bk", "sn_rows", "sn_inverse", "sn_store", "rename")
 
     def set_profiling(self, on=True):
         self._raise(lib().nqg_batch_set_profiling(self._h, 1 if on else 0), "set profiling")

@@ -86,7 +86,8 @@ template <class T> struct Ctx {
 
 // Counters of nqg_batch_get_profile.
 enum { PH_TOTAL, PH_INIT, PH_FACTOR, PH_PRECOND, PH_SPMV, PH_REFINE, PH_SELECT, PH_UPDATE, PH_SN, PH_ITER,
-       PH_FWD_WIDE, PH_FWD_NARROW, PH_DIAG, PH_BWD, PH_GATHER, PH_INIT_FACTOR, PH_N };
+       PH_FWD_WIDE, PH_FWD_NARROW, PH_DIAG, PH_BWD, PH_GATHER, PH_INIT_FACTOR,
+       PH_SN_ASSEMBLE, PH_SN_UPDATES, PH_SN_BK, PH_SN_ROWS, PH_SN_INVERSE, PH_SN_STORE, PH_RENAME, PH_N };
 static_assert(PH_N <= BATCH_PROFILE_COUNTERS, "profile counters");
 #define BQ_T0(c) const long long t0_ = (c).cyc ? clock64() : 0
 #define BQ_T1(c, ph) \
@@ -489,6 +490,14 @@ template <class T> __device__ void factor_sn(Ctx<T> &c, int s) {
   const int c0 = r0.x, w = r0.y, nr = r0.z;
   const int *rows = c.ls + r1.x;
   T *B = c.B;
+  long long tq = c.cyc ? clock64() : 0;
+  auto lap = [&](int ph) {
+    if (c.cyc && tid == 0) {
+      const long long now = clock64();
+      c.cyc[ph] += (unsigned long long)(now - tq);
+      tq = now;
+    }
+  };
   for (int p = tid; p < nr; p += nt) c.map[rows[p]] = p;
   for (int e = tid; e < nr * w; e += nt) B[e] = T(0);
   __syncthreads();
@@ -511,6 +520,7 @@ template <class T> __device__ void factor_sn(Ctx<T> &c, int s) {
     }
   }
   __syncthreads();
+  lap(PH_SN_ASSEMBLE);
   // descendant updates: descendants that never hide, then the active
   // constraint columns; warp wi takes every num_warps()-th of them
   {
@@ -521,6 +531,7 @@ template <class T> __device__ void factor_sn(Ctx<T> &c, int s) {
     });
   }
   __syncthreads();
+  lap(PH_SN_UPDATES);
   // Bunch-Kaufman on the diagonal block (one warp up to 32 columns), then the rows below
   bool pivoted = false;
   if (w <= 32) {
@@ -535,8 +546,10 @@ template <class T> __device__ void factor_sn(Ctx<T> &c, int s) {
     bk_factor<T>(B, nr, w, c.Dsm, c.Esm, c.lp, c.status, &pivoted);
   }
   __syncthreads();
+  lap(PH_SN_BK);
   if (nr > w) panel_rows_warp0(c, B, nr, w, pivoted);
   __syncthreads();
+  lap(PH_SN_ROWS);
   // The solves apply the diagonal block through the inverse of its unit
   // lower triangle (one product instead of w dependent steps); nothing else
   // reads L11 once the rows below are solved, so the inverse replaces it.
@@ -556,6 +569,7 @@ template <class T> __device__ void factor_sn(Ctx<T> &c, int s) {
     if (i > j) B[i + (size_t)j * nr] = c.Binv[i + j * w];
   }
   __syncthreads();
+  lap(PH_SN_INVERSE);
   T *Ls = c.L + r0.w;
   for (int e = tid; e < nr * w; e += nt) {
     T v = B[e];
@@ -569,6 +583,7 @@ template <class T> __device__ void factor_sn(Ctx<T> &c, int s) {
   }
   if (tid == 0) c.piv[s] = pivoted ? 1 : 0;
   __syncthreads();
+  lap(PH_SN_STORE);
 }
 
 // Factor the supernodes of mlist (ascending ids: children before parents,
@@ -578,6 +593,7 @@ template <class T> __device__ void factor_sn(Ctx<T> &c, int s) {
 template <class T> __device__ void factor_marked(Ctx<T> &c) {
   const int m = *c.nmark;
   for (int t = 0; t < m; ++t) factor_sn(c, c.mlist[t]);
+  BQ_T0(c);
   // renaming: rows of descendants that fall into a pivoted supernode
   for (int t = 0; t < m; ++t) {
     const int s = c.mlist[t];
@@ -609,6 +625,7 @@ template <class T> __device__ void factor_marked(Ctx<T> &c) {
   __syncthreads();
   if (threadIdx.x == 0) *c.nmark = 0;
   __syncthreads();
+  BQ_T1(c, PH_RENAME);
 }
 
 // ---- triangular solves (factor order, vector in shared memory) ---------------

@@ -18,7 +18,7 @@
 namespace nqg {
 
 constexpr int BATCH_MR_CAP = 10;  // largest number of Krylov steps per restart
-constexpr int BATCH_PROFILE_COUNTERS = 16;
+constexpr int BATCH_PROFILE_COUNTERS = 24;
 
 struct BPat {
   int n, meq, mineq, N, base;  // N = n + meq + mineq; base = n + meq (first constraint column)
