@@ -287,31 +287,43 @@ template <class T> __device__ void sub_update_warp(Ctx<T> &c, int pq, int d, int
   const T *Dd = c.D + cd, *Ed = c.D + c.N + cd;
   const int m = nrd - lb, nc = ub - lb + 1;
   T *B = c.B;
-  for (int e = lane; e < m * nc; e += 32) {
-    const int i = e % m, jj = e / m;
-    const int ri = rd[lb + i];
-    const int ti = c.map[ri];
-    const int tj = rd[lb + jj] - c0;
-    if (ti < 0 || ti >= nr || rows[ti] != ri || tj < 0 || tj >= w) {
-      atomicOr(c.status, ST_BOUNDS);
-      continue;
-    }
-    if (ti < tj) continue;  // lower triangle of the target only
-    double acc = 0.0;
-    for (int k = 0; k < wd; ++k) {
-      const double lik = (double)Ld[lb + i + (size_t)k * nrd];
-      const double ek = (double)Ed[k];
-      if (ek == 0.0 || k + 1 >= wd) {
-        acc += lik * (double)Dd[k] * (double)Ld[lb + jj + (size_t)k * nrd];
-      } else {
-        // 2x2 block (k, k+1): (D L^T)_k,j = d1 L_jk + e L_j,k+1; (D L^T)_k+1,j = e L_jk + d2 L_j,k+1
-        const double ljk = (double)Ld[lb + jj + (size_t)k * nrd], ljk1 = (double)Ld[lb + jj + (size_t)(k + 1) * nrd];
-        const double lik1 = (double)Ld[lb + i + (size_t)(k + 1) * nrd];
-        acc += lik * ((double)Dd[k] * ljk + ek * ljk1) + lik1 * (ek * ljk + (double)Dd[k + 1] * ljk1);
-        ++k;
+  // lanes over the descendant's rows (each lane's target row found once),
+  // the target columns in turn; the products accumulate in the factor's
+  // precision, in the order of the descendant's columns
+  for (int i0 = 0; i0 < m; i0 += 32) {
+    const int i = i0 + lane;
+    int ti = -1;
+    if (i < m) {
+      const int ri = rd[lb + i];
+      ti = c.map[ri];
+      if (ti < 0 || ti >= nr || rows[ti] != ri) {
+        atomicOr(c.status, ST_BOUNDS);
+        ti = -1;
       }
     }
-    atomicAdd(&B[ti + tj * nr], T(-acc));
+    for (int jj = 0; jj < nc; ++jj) {
+      const int tj = rd[lb + jj] - c0;
+      if (tj < 0 || tj >= w) {
+        if (lane == 0) atomicOr(c.status, ST_BOUNDS);
+        continue;
+      }
+      if (ti < tj) continue;  // lower triangle of the target only (and rows out of bounds)
+      T acc = T(0);
+      for (int k = 0; k < wd; ++k) {
+        const T lik = Ld[lb + i + (size_t)k * nrd];
+        const T ek = Ed[k];
+        if (ek == T(0) || k + 1 >= wd) {
+          acc += lik * Dd[k] * Ld[lb + jj + (size_t)k * nrd];
+        } else {
+          // 2x2 block (k, k+1): (D L^T)_k,j = d1 L_jk + e L_j,k+1; (D L^T)_k+1,j = e L_jk + d2 L_j,k+1
+          const T ljk = Ld[lb + jj + (size_t)k * nrd], ljk1 = Ld[lb + jj + (size_t)(k + 1) * nrd];
+          const T lik1 = Ld[lb + i + (size_t)(k + 1) * nrd];
+          acc += lik * (Dd[k] * ljk + ek * ljk1) + lik1 * (ek * ljk + Dd[k + 1] * ljk1);
+          ++k;
+        }
+      }
+      atomicAdd(&B[ti + tj * nr], -acc);
+    }
   }
 }
 
@@ -420,12 +432,11 @@ __device__ bool bk_factor_warp(T *a, int lda, int w, T *D, T *E, int *perm, int 
     if (kstep == 1) {
       if (!zero) {
         const T r1 = T(1) / a[k + (size_t)k * lda];
-        const int m = w - k - 1;
-        for (int e = lane; e < m * m; e += 32) {
-          const int jj = e / m, ii = e % m;
-          if (ii < jj) continue;
-          const int i = k + 1 + ii, j = k + 1 + jj;
-          a[i + (size_t)j * lda] -= r1 * a[j + (size_t)k * lda] * a[i + (size_t)k * lda];
+        // trailing update of the lower triangle, a column at a time (lanes over
+        // rows i >= j; column k is read only)
+        for (int j = k + 1; j < w; ++j) {
+          const T rj = r1 * a[j + (size_t)k * lda];
+          for (int i = j + lane; i < w; i += 32) a[i + (size_t)j * lda] -= rj * a[i + (size_t)k * lda];
         }
         __syncwarp();
         for (int i = k + 1 + lane; i < w; i += 32) a[i + (size_t)k * lda] *= r1;
@@ -449,11 +460,11 @@ __device__ bool bk_factor_warp(T *a, int lda, int w, T *D, T *E, int *perm, int 
         wk[2 * q + 1] = d21 * (d22 * ajk1 - ajk);
       }
       __syncwarp();
-      for (int e = lane; e < m * m; e += 32) {
-        const int q = e / m, ii = e % m;
-        const int j = k + 2 + q, i = k + 2 + ii;
-        if (i < j) continue;
-        a[i + (size_t)j * lda] -= a[i + (size_t)k * lda] * wk[2 * q] + a[i + (size_t)(k + 1) * lda] * wk[2 * q + 1];
+      for (int q = 0; q < m; ++q) {
+        const int j = k + 2 + q;
+        const T w0 = wk[2 * q], w1 = wk[2 * q + 1];
+        for (int i = j + lane; i < w; i += 32)
+          a[i + (size_t)j * lda] -= a[i + (size_t)k * lda] * w0 + a[i + (size_t)(k + 1) * lda] * w1;
       }
       __syncwarp();
       for (int q = lane; q < m; q += 32) {
