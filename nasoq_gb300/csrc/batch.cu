@@ -348,7 +348,8 @@ template <class T> __device__ __forceinline__ void s_flag_store(Ctx<T> &c, bool 
 // unit diagonal, D / E the diagonal and 2x2 sub-diagonals, perm[m] = original
 // local column at position m) on a w <= 32 wide lower-stored block, by one
 // warp: the steps and the arithmetic of each entry are those of the CTA-wide
-// bk_factor.  wk holds 2 (w - 2) multipliers of a 2x2 step.  Returns whether
+// bk_factor.  wk holds the multipliers of a step (w - 1 of a 1x1, 2 (w - 2) of a
+// 2x2).  Returns whether
 // any interchange happened.
 template <class T>
 __device__ bool bk_factor_warp(T *a, int lda, int w, T *D, T *E, int *perm, int *status, T *wk) {
@@ -432,11 +433,17 @@ __device__ bool bk_factor_warp(T *a, int lda, int w, T *D, T *E, int *perm, int 
     if (kstep == 1) {
       if (!zero) {
         const T r1 = T(1) / a[k + (size_t)k * lda];
-        // trailing update of the lower triangle, a column at a time (lanes over
-        // rows i >= j; column k is read only)
-        for (int j = k + 1; j < w; ++j) {
-          const T rj = r1 * a[j + (size_t)k * lda];
-          for (int i = j + lane; i < w; i += 32) a[i + (size_t)j * lda] -= rj * a[i + (size_t)k * lda];
+        // trailing update of the lower triangle: lane owns row i = k + 1 + lane
+        // (w <= 32) and walks its columns j <= i, independent updates; the
+        // multipliers r1 a_jk are staged once per column
+        for (int j = k + 1 + lane; j < w; j += 32) wk[j] = r1 * a[j + (size_t)k * lda];
+        __syncwarp();
+        {
+          const int i = k + 1 + lane;
+          if (i < w) {
+            const T aik = a[i + (size_t)k * lda];
+            for (int j = k + 1; j <= i; ++j) a[i + (size_t)j * lda] -= wk[j] * aik;
+          }
         }
         __syncwarp();
         for (int i = k + 1 + lane; i < w; i += 32) a[i + (size_t)k * lda] *= r1;
@@ -460,11 +467,14 @@ __device__ bool bk_factor_warp(T *a, int lda, int w, T *D, T *E, int *perm, int 
         wk[2 * q + 1] = d21 * (d22 * ajk1 - ajk);
       }
       __syncwarp();
-      for (int q = 0; q < m; ++q) {
-        const int j = k + 2 + q;
-        const T w0 = wk[2 * q], w1 = wk[2 * q + 1];
-        for (int i = j + lane; i < w; i += 32)
-          a[i + (size_t)j * lda] -= a[i + (size_t)k * lda] * w0 + a[i + (size_t)(k + 1) * lda] * w1;
+      {
+        // lane owns row i = k + 2 + lane (w <= 32), independent updates over its columns
+        const int i = k + 2 + lane;
+        if (i < w) {
+          const T aik = a[i + (size_t)k * lda], aik1 = a[i + (size_t)(k + 1) * lda];
+          for (int q = 0; q <= i - k - 2; ++q)
+            a[i + (size_t)(k + 2 + q) * lda] -= aik * wk[2 * q] + aik1 * wk[2 * q + 1];
+        }
       }
       __syncwarp();
       for (int q = lane; q < m; q += 32) {
