@@ -556,6 +556,7 @@ def lbl_section(args, torch, nq, P, pk):
     off = K.i != cols
     np.add.at(y, cols[off], K.x[off] * x32[K.i[off]])
     rr = float(np.linalg.norm(rhs - y) / np.linalg.norm(rhs))
+    ref_iter = int(plan.timings().num_ref_iter)
     plan.set_profiling(True)
     step()
     stats = plan.kernel_stats()
@@ -581,6 +582,8 @@ def lbl_section(args, torch, nq, P, pk):
     plan.close()
     return {"workload": f"lbl_kkt_lap3d_{GRID}cube_m{MCON}", "N": n, "value": 1000.0 / ms, "unit": "solves/s",
             "ms_per_step": ms, "relres": rr, "meets_target": bool(rr <= TARGET_RELRES), "analysis_s": analysis_s,
+            "refine_iterations": ref_iter,
+            "operand_split": "bf16" if os.environ.get("NASOQ_GB300_SPLIT") == "bf16" else "tf32",
             "error_vs_oracle": oracle, "kernels_ms": {k: v["total_ms"] for k, v in stats.items()}}
 
 

@@ -24,6 +24,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <string>
+#include <type_traits>
 
 #include "coop.cuh"
 #include "plan.hpp"
@@ -33,6 +34,37 @@
 namespace nqg {
 
 namespace {
+
+// Packed operands of the tcgen05 updates: blocks of 128 rows x one chunk of K,
+// swizzled K-major, hi part then lo part.  A chunk is 128 bytes of a row:
+// 32 K entries of split TF32, or 64 of split BF16 (NASOQ_GB300_SPLIT=bf16:
+// half the operand bytes per product, 2^-16 instead of 2^-22 relative
+// representation error).
+__host__ __device__ constexpr int pk_chunk(bool bf) { return bf ? 64 : 32; }
+bool pk_bf16() {
+  const char *e = std::getenv("NASOQ_GB300_SPLIT");
+  return e && std::string(e) == "bf16";
+}
+
+// One 16-byte unit of a packed row: 4 K entries (TF32) or 8 (BF16, two per
+// word, lower K in the low half), split into hi / lo, at unit position
+// c ^ (r % 8) of row r of the hi and lo blocks.
+template <bool BF>
+__device__ __forceinline__ void pk_store_unit(unsigned char *hi, unsigned char *lo, int r, int c, const float *x) {
+  uint32_t h[4], l[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    if constexpr (BF) {
+      t5::bf16_split2(x[2 * q], x[2 * q + 1], h[q], l[q]);
+    } else {
+      h[q] = t5::tf32_rna(x[q]);
+      l[q] = t5::tf32_rna(x[q] - __uint_as_float(h[q]));
+    }
+  }
+  const int off = r * 128 + ((c ^ (r & 7)) << 4);
+  *reinterpret_cast<uint4 *>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+  *reinterpret_cast<uint4 *>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+}
 
 constexpr int WP_THREADS = 256;
 constexpr int WP_NB = 64;  // widest panel; the row cache holds WP_NB + 2 columns
@@ -563,7 +595,7 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
                                                                int ldw, float *Dd, float *De, WideCtl *ctl,
                                                                int slot, unsigned seq, int *status,
                                                                unsigned char *pack_a, unsigned char *pack_b,
-                                                               int nkc_stride, int kcs) {
+                                                               int nkc_stride, int kcs, int pk_bf) {
   extern __shared__ __align__(16) unsigned char fb_raw[];
   __shared__ float rinv[WP_NB];
   __shared__ unsigned cpart[FB_THREADS / WP_NB][WP_NB];
@@ -791,37 +823,36 @@ __global__ void __launch_bounds__(FB_THREADS) k_wide_panel_blk(float *S, int nro
       S[r_own + (size_t)(k0 + j) * nrow] = wv * rinv[j];
     }
   // operands of the trailing updates (pack_a non-null): the thread's row of
-  // L (A) and, inside the diagonal block, of W (B) as split-TF32 blocks in the
-  // layout of k_pack_split, chunks kcs .. of row block r_own / 128, columns
-  // from kept on zero.  Rows of the panel itself are never read by a later
-  // update (they lie above every updated column) and are not written.
+  // L (A) and, inside the diagonal block, of W (B) as split blocks (TF32, or
+  // BF16 when pk_bf) in the layout of k_pack_split, chunks kcs .. of row
+  // block r_own / 128, columns from kept on zero.  Rows of the panel itself
+  // are never read by a later update (they lie above every updated column)
+  // and are not written.
   if (pack_a && own) {
     const int rb = r_own / t5::TM, rr = r_own % t5::TM;
-    for (int c = 0; c * t5::TK < nbR; ++c) {
-      const size_t blk = ((size_t)rb * nkc_stride + kcs + c) * (2 * t5::OPND_BYTES);
-      unsigned char *ah = pack_a + blk, *bh = r_own < w ? pack_b + blk : nullptr;
+    auto pack_row = [&](auto bf_tag) {
+      constexpr bool BF = decltype(bf_tag)::value;
+      constexpr int KC = pk_chunk(BF), UE = KC / 8;
+      for (int c = 0; c * KC < nbR; ++c) {
+        const size_t blk = ((size_t)rb * nkc_stride + kcs + c) * (2 * t5::OPND_BYTES);
+        unsigned char *ah = pack_a + blk, *bh = r_own < w ? pack_b + blk : nullptr;
 #pragma unroll 2
-      for (int cc = 0; cc < t5::TK / 4; ++cc) {
-        uint32_t lh[4], ll[4], wh[4], wl[4];
+        for (int cc = 0; cc < 8; ++cc) {
+          float lx[UE], wx[UE];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int j = c * t5::TK + cc * 4 + q;
-          const float wv = j < kept ? wsm[j * FB_THREADS + tid] : 0.f;
-          const float lv = j < kept ? wv * rinv[j] : 0.f;
-          lh[q] = t5::tf32_rna(lv);
-          ll[q] = t5::tf32_rna(lv - __uint_as_float(lh[q]));
-          wh[q] = t5::tf32_rna(wv);
-          wl[q] = t5::tf32_rna(wv - __uint_as_float(wh[q]));
-        }
-        const int off = rr * 128 + ((cc ^ (rr & 7)) << 4);
-        *reinterpret_cast<uint4 *>(ah + off) = make_uint4(lh[0], lh[1], lh[2], lh[3]);
-        *reinterpret_cast<uint4 *>(ah + t5::OPND_BYTES + off) = make_uint4(ll[0], ll[1], ll[2], ll[3]);
-        if (bh) {
-          *reinterpret_cast<uint4 *>(bh + off) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
-          *reinterpret_cast<uint4 *>(bh + t5::OPND_BYTES + off) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
+          for (int q = 0; q < UE; ++q) {
+            const int j = c * KC + cc * UE + q;
+            const float wv = j < kept ? wsm[j * FB_THREADS + tid] : 0.f;
+            wx[q] = wv;
+            lx[q] = j < kept ? wv * rinv[j] : 0.f;
+          }
+          pk_store_unit<BF>(ah, ah + t5::OPND_BYTES, rr, cc, lx);
+          if (bh) pk_store_unit<BF>(bh, bh + t5::OPND_BYTES, rr, cc, wx);
         }
       }
-    }
+    };
+    if (pk_bf) pack_row(std::true_type{});
+    else pack_row(std::false_type{});
   }
   if (blockIdx.x == 0) {
     for (int e = tid; e < kept * nbR; e += FB_THREADS) {
@@ -1290,14 +1321,17 @@ constexpr int TP_THREADS = 320;  // producer warp, MMA warp, 8 epilogue warps
 __host__ __device__ constexpr size_t tp_smem_bytes() { return (size_t)TP_STAGES * t5::STAGE_BYTES + 1024; }
 
 // Blocks of rows [rb_first * 128, row_hi) x columns [0, kb) of src (element
-// (r, k) at src[r + k * ld]) into chunks kc0 .. of the pack buffer.
+// (r, k) at src[r + k * ld]) into chunks kc0 .. of the pack buffer (a chunk
+// holds pk_chunk(BF) columns).
+template <bool BF>
 __global__ void __launch_bounds__(256) k_pack_split(const float *src, int ld, int row_hi, int kb, unsigned char *dst,
                                                     int nkc_stride, int kc0, int rb_first, const int *halt) {
-  __shared__ float tk[t5::TK][t5::TM + 1];
+  constexpr int KC = pk_chunk(BF), UE = KC / 8;  // K per chunk, entries per 16-byte unit
+  __shared__ float tk[KC][t5::TM + 1];
   if (halt && *(volatile const int *)halt) return;  // queued behind a fast panel that stopped early
   const int rb = rb_first + blockIdx.x, kcl = blockIdx.y;
-  const int r0 = rb * t5::TM, k0 = kcl * t5::TK;
-  for (int e = threadIdx.x; e < t5::TK * t5::TM; e += blockDim.x) {
+  const int r0 = rb * t5::TM, k0 = kcl * KC;
+  for (int e = threadIdx.x; e < KC * t5::TM; e += blockDim.x) {
     const int k = e / t5::TM, r = e % t5::TM, gr = r0 + r;
     tk[k][r] = (gr < row_hi && k0 + k < kb) ? __ldcg(src + gr + (size_t)(k0 + k) * ld) : 0.f;
   }
@@ -1307,16 +1341,10 @@ __global__ void __launch_bounds__(256) k_pack_split(const float *src, int ld, in
 #pragma unroll
   for (int cc = 0; cc < 4; ++cc) {
     const int c = (threadIdx.x & 1) * 4 + cc;
-    uint32_t h[4], l[4];
+    float x[UE];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const float x = tk[4 * c + q][r];
-      h[q] = t5::tf32_rna(x);
-      l[q] = t5::tf32_rna(x - __uint_as_float(h[q]));
-    }
-    const int off = r * 128 + ((c ^ (r & 7)) << 4);
-    *reinterpret_cast<uint4 *>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<uint4 *>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+    for (int q = 0; q < UE; ++q) x[q] = tk[UE * c + q][r];
+    pk_store_unit<BF>(hi, lo, r, c, x);
   }
 }
 
@@ -1324,12 +1352,14 @@ __global__ void __launch_bounds__(256) k_pack_split(const float *src, int ld, in
 // L(i, k-1) for rows [0, row_hi) and columns [0, kb) of src (element (i, t)
 // at src[i + t * ld]; d, e the descendant's diagonal and 2 x 2 sub-diagonal),
 // in the layout of k_pack_split, chunk kc of row block rb at rb * nkc + kc.
+template <bool BF>
 __global__ void __launch_bounds__(256) k_pack_ld(const float *src, int ld, int row_hi, int kb, const float *Dd,
                                                  const float *Ed, unsigned char *dst, int nkc) {
-  __shared__ float tk[t5::TK + 2][t5::TM + 1];
+  constexpr int KC = pk_chunk(BF), UE = KC / 8;
+  __shared__ float tk[KC + 2][t5::TM + 1];
   const int rb = blockIdx.x, kc = blockIdx.y;
-  const int r0 = rb * t5::TM, k0 = kc * t5::TK;
-  for (int e = threadIdx.x; e < (t5::TK + 2) * t5::TM; e += blockDim.x) {
+  const int r0 = rb * t5::TM, k0 = kc * KC;
+  for (int e = threadIdx.x; e < (KC + 2) * t5::TM; e += blockDim.x) {
     const int q = e / t5::TM, r = e % t5::TM, t = k0 - 1 + q, gr = r0 + r;
     tk[q][r] = (gr < row_hi && t >= 0 && t < kb) ? __ldcg(src + gr + (size_t)t * ld) : 0.f;
   }
@@ -1339,19 +1369,15 @@ __global__ void __launch_bounds__(256) k_pack_ld(const float *src, int ld, int r
 #pragma unroll
   for (int cc = 0; cc < 4; ++cc) {
     const int c = (threadIdx.x & 1) * 4 + cc;
-    uint32_t h[4], l[4];
+    float x[UE];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int k = 4 * c + q, t = k0 + k;
+    for (int q = 0; q < UE; ++q) {
+      const int k = UE * c + q, t = k0 + k;
       const float dk = t < kb ? Dd[t] : 0.f, ek = t < kb ? Ed[t] : 0.f;
       const float em = (t >= 1 && t - 1 < kb) ? Ed[t - 1] : 0.f;
-      const float x = dk * tk[k + 1][r] + ek * tk[k + 2][r] + em * tk[k][r];
-      h[q] = t5::tf32_rna(x);
-      l[q] = t5::tf32_rna(x - __uint_as_float(h[q]));
+      x[q] = dk * tk[k + 1][r] + ek * tk[k + 2][r] + em * tk[k][r];
     }
-    const int off = r * 128 + ((c ^ (r & 7)) << 4);
-    *reinterpret_cast<uint4 *>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<uint4 *>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+    pk_store_unit<BF>(hi, lo, r, c, x);
   }
 }
 
@@ -1438,7 +1464,7 @@ __device__ __forceinline__ bool tp_wait(uint32_t mbar, uint32_t parity, volatile
 //     nrow): at S[i, j] for j in [cb, ce), i >= j, i < nrow;
 //   MAPPED = true (descendant pair, i, j relative to its first row): at
 //     S[prow[i] + pcol[j] * nrow] for i < mrows, j < ncols, j <= i.
-template <bool MAPPED>
+template <bool MAPPED, bool BF>
 __global__ void __launch_bounds__(TP_THREADS, 1) k_tc_persistent(float *S, int nrow, int cb, int ce,
                                                                  const unsigned char *pack_a,
                                                                  const unsigned char *pack_b, int nkc_stride, int kc0,
@@ -1513,8 +1539,12 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_tc_persistent(float *S, int n
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      // MMA issue: 3 split-TF32 products per K step of 8
-      constexpr uint32_t IDESC = t5::idesc_tf32(t5::TM, t5::TN);
+      // MMA issue: 3 split products per 32-byte K step (8 TF32 or 16 BF16 entries)
+      constexpr uint32_t IDESC = BF ? t5::idesc_bf16(t5::TM, t5::TN) : t5::idesc_tf32(t5::TM, t5::TN);
+      auto mma = [](uint32_t d_, uint64_t a_, uint64_t b_, uint32_t acc_) {
+        if constexpr (BF) t5::mma_bf16(d_, a_, b_, IDESC, acc_);
+        else t5::mma_tf32(d_, a_, b_, IDESC, acc_);
+      };
       uint32_t it = 0, last_bar = 0, last_par = 0;
       bool ok = true, any = false;
       int i = 0;
@@ -1537,12 +1567,12 @@ __global__ void __launch_bounds__(TP_THREADS, 1) k_tc_persistent(float *S, int n
           const uint32_t a_hi = t5::smem_u32(base + (size_t)s * t5::STAGE_BYTES), a_lo = a_hi + t5::OPND_BYTES;
           const uint32_t b_hi = a_hi + 2 * t5::OPND_BYTES, b_lo = a_hi + 3 * t5::OPND_BYTES;
 #pragma unroll
-          for (int ks = 0; ks < t5::TK / 8; ++ks) {
+          for (int ks = 0; ks < 4; ++ks) {
             const uint32_t off = ks * 32;
             const uint32_t acc0 = (kc > kc0 || ks > 0) ? 1u : 0u;
-            t5::mma_tf32(d, t5::desc_sw128(a_lo + off), t5::desc_sw128(b_hi + off), IDESC, acc0);
-            t5::mma_tf32(d, t5::desc_sw128(a_hi + off), t5::desc_sw128(b_lo + off), IDESC, 1u);
-            t5::mma_tf32(d, t5::desc_sw128(a_hi + off), t5::desc_sw128(b_hi + off), IDESC, 1u);
+            mma(d, t5::desc_sw128(a_lo + off), t5::desc_sw128(b_hi + off), acc0);
+            mma(d, t5::desc_sw128(a_hi + off), t5::desc_sw128(b_lo + off), 1u);
+            mma(d, t5::desc_sw128(a_hi + off), t5::desc_sw128(b_hi + off), 1u);
           }
           t5::mma_commit(t5::smem_u32(&empty[s]));
           last_bar = t5::smem_u32(&empty[s]);
@@ -1693,15 +1723,17 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   const char *te = std::getenv("NASOQ_GB300_TRAILING");
   const int trail = !te ? 2 : std::string(te) == "simt" ? 0 : std::string(te) == "mma" ? 1 : 2;
   const bool tile_only = te && std::string(te) == "tile";
-  // packed split-TF32 operands: row blocks of A (L rows) then of B (W rows),
+  // packed split operands: row blocks of A (L rows) then of B (W rows),
   // nkc_stride chunks each (every pending panel starts on a new chunk)
   unsigned char *pack_a = (sizeof(T) == 4 && trail == 2 && !tile_only && P) ? P->d_wide_pack : nullptr;
-  const int nch_panel = (nb + 1 + t5::TK - 1) / t5::TK;
+  const bool bf = pk_bf16();
+  const int kchunk = pk_chunk(bf);
+  const int nch_panel = (nb + 1 + kchunk - 1) / kchunk;
   const int nkc_stride = (std::max(depth, 1) + 1) * nch_panel;  // room for depth + 1 panels
   const int nrb_all = (nrow + t5::TM - 1) / t5::TM, ncb_all = (w + t5::TN - 1) / t5::TN;
   unsigned char *pack_b = pack_a ? pack_a + (size_t)nrb_all * nkc_stride * PK_BLOCK : nullptr;
-  if (pack_a && cudaFuncSetAttribute(k_tc_persistent<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)tp_smem_bytes()) != cudaSuccess)
+  if (pack_a && cudaFuncSetAttribute(bf ? k_tc_persistent<false, true> : k_tc_persistent<false, false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tp_smem_bytes()) != cudaSuccess)
     return NQG_ERR_CUDA;
   if (sizeof(T) == 4 && trail == 1 &&
       cudaFuncSetAttribute(k_wide_trailing_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM) !=
@@ -1795,28 +1827,26 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   int spec_limit = SPEC_MAX;  // batch size: 1 after a rewind, doubling after each clean batch
   const int *halt = &ctl->halt;
   // chunks of a panel of kb columns in the pack buffer
-  auto nch = [&](int kb) { return (kb + t5::TK - 1) / t5::TK; };
-  // split-TF32 blocks of a finished panel (columns k0 .. k0+kb-1, W at
-  // column woff of Wb) into chunks kcs .. of the pack buffer, rows from the
-  // block holding k0 + kb on (the rows every later update of it touches)
+  auto nch = [&](int kb) { return (kb + kchunk - 1) / kchunk; };
+  // split blocks of a finished panel (columns k0 .. k0+kb-1, W at column
+  // woff of Wb) into chunks kcs .. of the pack buffer, rows from the block
+  // holding k0 + kb on (the rows every later update of it touches)
   auto pack_panel = [&](int k0, int kb, int woff, int kcs) -> int {
     const int k1 = k0 + kb;
     if (!pack_a || k1 >= w || kb <= 0) return NQG_OK;
     cudaEvent_t e1 = P ? P->prof_begin() : nullptr;
     const int rb_first = k1 / t5::TM;
     int ld = nrow;
-    k_pack_split<<<dim3(nrb_all - rb_first, nch(kb)), 256, 0, st>>>(reinterpret_cast<const float *>(S) +
-                                                                         (size_t)k0 * nrow,
-                                                                     ld, nrow, kb, pack_a, nkc_stride, kcs,
-                                                                     rb_first, halt);
-    k_pack_split<<<dim3(ncb_all - rb_first, nch(kb)), 256, 0, st>>>(reinterpret_cast<const float *>(Wb) +
-                                                                         (size_t)woff * nrow,
-                                                                     ld, w, kb, pack_b, nkc_stride, kcs, rb_first,
-                                                                     halt);
+    auto pk = bf ? k_pack_split<true> : k_pack_split<false>;
+    pk<<<dim3(nrb_all - rb_first, nch(kb)), 256, 0, st>>>(reinterpret_cast<const float *>(S) + (size_t)k0 * nrow, ld,
+                                                          nrow, kb, pack_a, nkc_stride, kcs, rb_first, halt);
+    pk<<<dim3(ncb_all - rb_first, nch(kb)), 256, 0, st>>>(reinterpret_cast<const float *>(Wb) + (size_t)woff * nrow,
+                                                          ld, w, kb, pack_b, nkc_stride, kcs, rb_first, halt);
     if (cudaGetLastError() != cudaSuccess) return NQG_ERR_CUDA;
     if (P) {
       P->nlaunch += 2;
-      const double bytes = (double)kb * ((nrow - rb_first * t5::TM) + (w - rb_first * t5::TM)) * 12.0;
+      // FP32 read once, hi + lo written
+      const double bytes = (double)kb * ((nrow - rb_first * t5::TM) + (w - rb_first * t5::TM)) * (bf ? 8.0 : 12.0);
       P->prof_end(NQG_K_PACK, e1, 0.0, bytes);
     }
     return NQG_OK;
@@ -1832,9 +1862,9 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       const int ntile = ncb * nrb - ncb * (ncb - 1) / 2;
       const int G = std::max(1, std::min(ntile, num_sms));
       float *Sf = reinterpret_cast<float *>(S);
-      k_tc_persistent<false><<<G, TP_THREADS, tp_smem_bytes(), st>>>(Sf, nrow, cb, ce, pack_a, pack_b, nkc_stride,
-                                                                     kca, kcb, blk0, nrb, ncb, ntile, halt, status,
-                                                                     nullptr, nullptr, 0, 0);
+      auto kt = bf ? k_tc_persistent<false, true> : k_tc_persistent<false, false>;
+      kt<<<G, TP_THREADS, tp_smem_bytes(), st>>>(Sf, nrow, cb, ce, pack_a, pack_b, nkc_stride, kca, kcb, blk0, nrb,
+                                                 ncb, ntile, halt, status, nullptr, nullptr, 0, 0);
     } else {
       const int tm = (nrow - cb + t5::TM - 1) / t5::TM, tn = (ce - cb + t5::TN - 1) / t5::TN;
       k_wide_trailing_t5<<<tm * tn, t5::THREADS, t5::smem_bytes(1), st>>>(
@@ -1947,9 +1977,9 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
       if (++blk_seq == 0) blk_seq = 1;
       unsigned seq = blk_seq;
       unsigned char *pa = k0 + kb_want < w ? pack_a : nullptr, *pb = pack_b;
-      int nkcs = nkc_stride;
+      int nkcs = nkc_stride, pkbf = bf ? 1 : 0;
       void *args[] = {&Sf, &nrow, &w, &k0, &kb_want, &Wf, &ldw, &Df, &Ef, &ctl, &slot, &seq, &status, &pa, &pb,
-                      &nkcs, &kcs};
+                      &nkcs, &kcs, &pkbf};
       cudaEvent_t e0 = P ? P->prof_begin() : nullptr;
       if (cudaLaunchCooperativeKernel((void *)k_wide_panel_blk, dim3(Gb), dim3(FB_THREADS), args, fast_blk_smem(),
                                       st) != cudaSuccess)
@@ -2118,29 +2148,32 @@ int update_pair_persistent(Plan &P, int s, int q, float *L, const float *Dg) {
   const int nrs = (int)(P.sym.lpi[s + 1] - P.sym.lpi[s]);
   const int m = nrd - lb, nc = ub - lb + 1;
   if (m <= 0 || nc <= 0 || wd <= 0) return NQG_OK;
-  const int nkc = (wd + t5::TK - 1) / t5::TK, nrb = (m + t5::TM - 1) / t5::TM, ncb = (nc + t5::TN - 1) / t5::TN;
+  const bool bf = pk_bf16();
+  const int nkc = (wd + pk_chunk(bf) - 1) / pk_chunk(bf), nrb = (m + t5::TM - 1) / t5::TM,
+            ncb = (nc + t5::TN - 1) / t5::TN;
   unsigned char *pa = P.d_wide_pack, *pb = pa + (size_t)nrb * nkc * PK_BLOCK;
   int *prow = P.d_pers_map, *pcol = prow + m;
   if (!pa || !prow) return NQG_ERR_ARG;
   cudaStream_t st = P.stream;
-  if (cudaFuncSetAttribute(k_tc_persistent<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)tp_smem_bytes()) != cudaSuccess)
+  auto kt = bf ? k_tc_persistent<true, true> : k_tc_persistent<true, false>;
+  if (cudaFuncSetAttribute(kt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tp_smem_bytes()) != cudaSuccess)
     return NQG_ERR_CUDA;
   cudaEvent_t ep = P.prof_begin();
   k_pair_map<<<std::min((m + 255) / 256, 1024), 256, 0, st>>>(P.d_ls + P.sym.lpi[d] + lb, m, nc,
                                                               P.d_ls + P.sym.lpi[s], nrs, cs0, ws, prow, pcol,
                                                               P.d_status);
   const float *Ld = L + P.sym.lpx[d] + lb;
-  k_pack_ld<<<dim3(nrb, nkc), 256, 0, st>>>(Ld, nrd, m, wd, Dg + c0, Dg + P.n + c0, pa, nkc);
-  k_pack_split<<<dim3(ncb, nkc), 256, 0, st>>>(Ld, nrd, nc, wd, pb, nkc, 0, 0, nullptr);
-  P.prof_end(NQG_K_PACK, ep, 0.0, (double)(m + nc) * wd * 12.0);
+  (bf ? k_pack_ld<true> : k_pack_ld<false>)<<<dim3(nrb, nkc), 256, 0, st>>>(Ld, nrd, m, wd, Dg + c0, Dg + P.n + c0,
+                                                                           pa, nkc);
+  (bf ? k_pack_split<true> : k_pack_split<false>)<<<dim3(ncb, nkc), 256, 0, st>>>(Ld, nrd, nc, wd, pb, nkc, 0, 0,
+                                                                                 nullptr);
+  P.prof_end(NQG_K_PACK, ep, 0.0, (double)(m + nc) * wd * (bf ? 8.0 : 12.0));
   cudaEvent_t e0 = P.prof_begin();
   const int ntile = ncb * nrb - ncb * (ncb - 1) / 2;
   const int G = std::max(1, std::min(ntile, P.num_sms));
   const int nflat = (int)tp_flat_count(nrb, ncb);
-  k_tc_persistent<true><<<G, TP_THREADS, tp_smem_bytes(), st>>>(L + P.sym.lpx[s], nrs, 0, 0, pa, pb, nkc, 0, nkc, 0,
-                                                                nrb, ncb, nflat, nullptr, P.d_status, prow, pcol, m,
-                                                                nc);
+  kt<<<G, TP_THREADS, tp_smem_bytes(), st>>>(L + P.sym.lpx[s], nrs, 0, 0, pa, pb, nkc, 0, nkc, 0, nrb, ncb, nflat,
+                                             nullptr, P.d_status, prow, pcol, m, nc);
   if (cudaGetLastError() != cudaSuccess) return NQG_ERR_CUDA;
   P.nlaunch += 4;
   P.prof_end(NQG_K_UPDATE, e0, P.pair_flops[q], 0.0);
