@@ -195,7 +195,7 @@ int nqg_get_device_status(const nqg_plan *plan, int *status_bits);
 #define NQG_K_SPMV 5            /* refinement residual SpMV */
 #define NQG_K_OTHER 6           /* assembly, row renaming, vector kernels */
 #define NQG_K_WIDE_PIVOT 7      /* wide supernode: BK panel with pivot search */
-#define NQG_K_PACK 8            /* split-TF32 operand packing of the tcgen05 updates */
+#define NQG_K_PACK 8            /* split-BF16 / split-TF32 operand packing of the tcgen05 updates */
 #define NQG_K_CLASSES 9
 typedef struct nqg_kernel_stats {
   long long launches;

@@ -459,8 +459,9 @@ static int upload_plan(Plan &P) {
     if (wide_rows > 0)
       NQG_CUDA(cudaMalloc(&P.d_wide_W,
                           (size_t)wide_rows * ((P.wide_depth + 1) * (P.wide_nb + 1) + 2) * P.val_size()));
-    // FP32: packed split-TF32 operands of the persistent tcgen05 updates,
-    // blocks of 128 rows x 32 columns (hi + lo TF32 halves of 16 KB each).
+    // FP32: packed split operands of the persistent tcgen05 updates, blocks
+    // of 128 rows x one chunk of K (hi + lo halves of 16 KB each; counted
+    // here in 32-entry TF32 chunks, at least as many as 64-entry BF16 ones).
     // Trailing updates of a wide supernode: row blocks of L then of W, each
     // wide_depth panels of chunks; a persistent descendant pair: row blocks
     // of L D then of L, the descendant's width in chunks.  One buffer serves

@@ -140,7 +140,7 @@ struct Plan {
   // wide supernodes (blocked cooperative BK)
   void *d_wide_W = nullptr;         // panel buffer, max nrow x (nb+2)
   void *d_wide_ctl = nullptr;       // barrier / reduction control block
-  unsigned char *d_wide_pack = nullptr;  // FP32: split-TF32 operand blocks of the tcgen05 updates
+  unsigned char *d_wide_pack = nullptr;  // FP32: split operand blocks of the tcgen05 updates
   int *d_pers_map = nullptr;              // target positions of a persistent pair's rows and columns
   int *d_pair_map = nullptr;              // target row positions of the pairs' rows (pair_moff)
   int64_t *d_pair_moff = nullptr;

@@ -1,6 +1,8 @@
 // Fifth-generation tensor cores (sm_100a family): TMEM accumulators,
 // single-thread MMA issue with operands described in shared memory, mbarrier
 // completion, and the split-TF32 128 x 128 tile product built on them.
+// kind::f16 MMAs on BF16 operands use the same layout with 64 entries per
+// 128-byte row (K = 16 per MMA, the same 32-byte step).
 //
 // Operand layout: K-major, 128-byte swizzle.  A 128 x 32 FP32 tile is 128 rows
 // of 128 bytes; 16-byte chunk c of row r is stored at chunk position

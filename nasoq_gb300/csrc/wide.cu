@@ -37,13 +37,13 @@ namespace {
 
 // Packed operands of the tcgen05 updates: blocks of 128 rows x one chunk of K,
 // swizzled K-major, hi part then lo part.  A chunk is 128 bytes of a row:
-// 32 K entries of split TF32, or 64 of split BF16 (NASOQ_GB300_SPLIT=bf16:
-// half the operand bytes per product, 2^-16 instead of 2^-22 relative
-// representation error).
+// 64 K entries of split BF16 (the default), or 32 of split TF32
+// (NASOQ_GB300_SPLIT=tf32: twice the operand bytes and MMA steps per
+// product, 2^-22 instead of 2^-16 relative representation error).
 __host__ __device__ constexpr int pk_chunk(bool bf) { return bf ? 64 : 32; }
 bool pk_bf16() {
   const char *e = std::getenv("NASOQ_GB300_SPLIT");
-  return e && std::string(e) == "bf16";
+  return !(e && std::string(e) == "tf32");
 }
 
 // One 16-byte unit of a packed row: 4 K entries (TF32) or 8 (BF16, two per
@@ -1302,19 +1302,19 @@ __global__ void __launch_bounds__(t5::THREADS) k_wide_trailing_t5(float *S, int 
 // Persistent trailing update on the tcgen05 tensor cores.
 //
 // Operands are packed once per panel: k_pack_split writes the panel's L rows
-// (A) and W rows (B) as split-TF32 blocks of 128 rows x 32 columns of K (hi
-// then lo, 16 KB each, in the swizzled K-major layout of
+// (A) and W rows (B) as split blocks of 128 rows x one chunk of K (64 BF16 or
+// 32 TF32 entries; hi then lo, 16 KB each, in the swizzled K-major layout of
 // t5::store_row_split), block (rb, kc) at rb * nkc_stride + kc, row blocks at
 // absolute 128-row positions of the supernode, every panel starting on a new
 // chunk (zeros pad a partial chunk).  k_tc_persistent then runs one CTA
 // per SM over the lower-triangular set of 128 x 128 tiles: warp 0 streams
 // both operand blocks of each K chunk into a three-stage shared-memory ring
-// with bulk copies, warp 1 issues the split-TF32 MMAs (the same three
-// products per K step as t5::tile_tf32x3) into one of two TMEM accumulators,
+// with bulk copies, warp 1 issues the split MMAs (lo.hi, hi.lo, hi.hi per
+// 32-byte K step, as t5::tile_tf32x3) into one of two TMEM accumulators,
 // and warps 2-9 (two per TMEM lane quarter, 64 columns each) subtract the
 // finished accumulator from S while the next tile accumulates in the other
 // one; they load their S values before the accumulator is ready.
-constexpr int PK_BLOCK = 2 * t5::OPND_BYTES;  // hi + lo of one 128 x 32 block
+constexpr int PK_BLOCK = 2 * t5::OPND_BYTES;  // hi + lo of one 128-row block of a chunk
 constexpr int TP_STAGES = 3;
 constexpr int TP_THREADS = 320;  // producer warp, MMA warp, 8 epilogue warps
 
@@ -1714,7 +1714,8 @@ static int run_wide(T *S, int nrow, int w, T *Dd, T *De, int *perm, T *Wb, WideC
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_wide_panel<T>, WP_THREADS, smem) != cudaSuccess)
     return NQG_ERR_CUDA;
   const int maxG = std::max(1, std::min(occ * num_sms, 1024));
-  // FP32 trailing updates: tcgen05 split-TF32 tiles by default;
+  // FP32 trailing updates: the persistent tcgen05 kernel on packed split
+  // operands (BF16; NASOQ_GB300_SPLIT=tf32 for TF32) by default;
   // NASOQ_GB300_TRAILING=mma selects the mma.sync split-TF32 kernel and
   // =simt the CUDA-core kernel
   // NASOQ_GB300_TRAILING=tile keeps the tcgen05 updates on one CTA per tile

@@ -211,7 +211,7 @@ def test_fp64_blocked_wide_kernels(path, monkeypatch):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("trailing", ["tcgen05", "tcgen05-bf16", "tcgen05-depth1", "tcgen05-depth2", "tcgen05-tile",
+@pytest.mark.parametrize("trailing", ["tcgen05", "tcgen05-tf32", "tcgen05-depth1", "tcgen05-depth2", "tcgen05-tile",
                                       "mma", "simt", "general-panels"])
 @pytest.mark.parametrize("path", CASES, ids=os.path.basename)
 def test_fp32_blocked_wide_kernels(path, trailing, monkeypatch):
@@ -219,13 +219,13 @@ def test_fp32_blocked_wide_kernels(path, trailing, monkeypatch):
     kernels (fast panels where no pivot search is needed, or every panel on
     the general kernel), trailing updates on the tcgen05 tensor cores (one,
     two or four panels per delayed update; the persistent kernel on packed
-    split-TF32 or split-BF16 operands, or one CTA per tile) or with mma.sync
-    (split TF32) or on CUDA cores:
+    split-BF16 or split-TF32 operands, or one CTA per tile with split TF32)
+    or with mma.sync (split TF32) or on CUDA cores:
     the refined solution meets the FP32 bar of the single-CTA kernels."""
     for k, v in WIDE_ENV.items():
         monkeypatch.setenv(k, v)
-    if trailing == "tcgen05-bf16":
-        monkeypatch.setenv("NASOQ_GB300_SPLIT", "bf16")
+    if trailing == "tcgen05-tf32":
+        monkeypatch.setenv("NASOQ_GB300_SPLIT", "tf32")
     elif trailing == "general-panels":
         monkeypatch.setenv("NASOQ_GB300_PANEL", "general")
     elif trailing.startswith("tcgen05-depth"):
@@ -249,12 +249,12 @@ def test_fp32_blocked_wide_kernels(path, trailing, monkeypatch):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("update", ["tcgen05", "tcgen05-persistent", "tcgen05-persistent-bf16", "simt"])
+@pytest.mark.parametrize("update", ["tcgen05", "tcgen05-persistent", "tcgen05-persistent-tf32", "simt"])
 @pytest.mark.parametrize("path", CASES, ids=os.path.basename)
 def test_fp32_update_kernels(path, update, monkeypatch):
     """FP32 factor with every Schur update between supernodes on the tcgen05
     tiles (any descendant width), every one as a persistent tcgen05 launch
-    on packed split-TF32 or split-BF16 operands, or every one on the
+    on packed split-BF16 or split-TF32 operands, or every one on the
     CUDA-core tiles: the refined solution meets the FP32 bar."""
     if update == "tcgen05":
         monkeypatch.setenv("NASOQ_GB300_UPDATE_TC_MIN", "1")
@@ -262,8 +262,8 @@ def test_fp32_update_kernels(path, update, monkeypatch):
     elif update.startswith("tcgen05-persistent"):
         monkeypatch.setenv("NASOQ_GB300_UPDATE_TC_MIN", "1")
         monkeypatch.setenv("NASOQ_GB300_UPDATE_PERSIST_MIN", "0")
-        if update.endswith("bf16"):
-            monkeypatch.setenv("NASOQ_GB300_SPLIT", "bf16")
+        if update.endswith("tf32"):
+            monkeypatch.setenv("NASOQ_GB300_SPLIT", "tf32")
     else:
         monkeypatch.setenv("NASOQ_GB300_UPDATE", "simt")
     d = nqa.load(path)
@@ -359,13 +359,14 @@ def test_fast_panel_kernels_agree(n, pivots, monkeypatch):
 @pytest.mark.parametrize("n,pivots", [(1024, False), (1100, True)])
 def test_trailing_kernels_agree(n, pivots, monkeypatch):
     """One dense FP32 supernode: the persistent tcgen05 trailing update on
-    packed split-TF32 operands against the one-CTA-per-tile kernel that
-    splits its operands while loading them.  With full 64-column panels both
+    packed split-TF32 operands (NASOQ_GB300_SPLIT=tf32) against the
+    one-CTA-per-tile kernel that splits its operands while loading them.  With full 64-column panels both
     sum the same products in the same chunks of 32, so the factors agree bit
     for bit; with pivot searches (panels of any width, padded chunks) both
     factors reach a backward error of 1e-4 max(|L||D||L|^T) (no diagonal
     floor) and the refined solution the FP32 bar.  The persistent kernel on
-    split-BF16 operands (64 K entries per chunk) reaches 1e-4 too."""
+    split-BF16 operands (the default, 64 K entries per chunk) reaches 1e-4
+    too."""
     rng = np.random.default_rng(7 * n + pivots)
     M = rng.standard_normal((n, n))
     M = (M + M.T) / 2
@@ -381,13 +382,14 @@ def test_trailing_kernels_agree(n, pivots, monkeypatch):
     monkeypatch.setenv("NASOQ_GB300_TRAILING", "tile")
     assert plan.factor() == 0
     out = {}
+    monkeypatch.setenv("NASOQ_GB300_SPLIT", "tf32")
     for mode in ("tile", "persistent", "persistent-bf16"):
         if mode == "tile":
             monkeypatch.setenv("NASOQ_GB300_TRAILING", "tile")
         else:
             monkeypatch.delenv("NASOQ_GB300_TRAILING", raising=False)
         if mode == "persistent-bf16":
-            monkeypatch.setenv("NASOQ_GB300_SPLIT", "bf16")
+            monkeypatch.delenv("NASOQ_GB300_SPLIT", raising=False)
         assert plan.factor() == 0
         out[mode] = plan.factor_arrays()
         vals, dv, perm, ls = out[mode]

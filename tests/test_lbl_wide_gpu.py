@@ -9,7 +9,7 @@ panels), FP64 and every FP32 variant:
   * FP64: 2x2 pivots found, solutions within max(1e-9, 1e-14 kappa,
     1e-15 g) of the reference's, g its largest factor entry (without and with
     refinement);
-  * FP32 factor (tcgen05 on split-TF32 or split-BF16 operands, per-tile
+  * FP32 factor (tcgen05 on split-BF16 or split-TF32 operands, per-tile
     tcgen05, mma.sync, SIMT trailing updates;
     FP64 or FP32 triangular solves, level or block kernels) with FP64
     refinement: relative residual 1e-10 and x within 1e-6 of the reference."""
@@ -65,11 +65,11 @@ def test_fp64_hard_pivots_default_thresholds():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("trailing", ["tcgen05", "tcgen05-bf16", "tile", "mma", "simt"])
+@pytest.mark.parametrize("trailing", ["tcgen05", "tcgen05-tf32", "tile", "mma", "simt"])
 @pytest.mark.parametrize("solves", ["fp64", "fp32-level", "fp32-block"])
 def test_fp32_hard_pivots_default_thresholds(trailing, solves, monkeypatch):
-    if trailing == "tcgen05-bf16":
-        monkeypatch.setenv("NASOQ_GB300_SPLIT", "bf16")
+    if trailing == "tcgen05-tf32":
+        monkeypatch.setenv("NASOQ_GB300_SPLIT", "tf32")
     elif trailing != "tcgen05":
         monkeypatch.setenv("NASOQ_GB300_TRAILING", trailing)
     if solves == "fp32-block":
