@@ -444,9 +444,9 @@ def c3_section(nq, P):
     out = {"workload": "qp_mpc_uneven_horizon10-100_b4096"}
     for name, kw in (("mixed", dict(precision=nq.NQG_FP32, refine=1, refine_tol=REFINE_TOL)),
                      ("plain_fp64", dict(precision=nq.NQG_FP64, refine=0))):
-        # launch shape from the autotuner (timed on this batch, or the cached choice)
-        tuned, trep = tune.autotune_batch(probs, cache=os.path.join(ROOT, "gpurun_out", "batch_tune.json"),
-                                          variant=0, eps_abs=EPS, **kw)
+        # launch shape from the autotuner (timed on this batch, or the choice
+        # cached under the user's cache directory)
+        tuned, trep = tune.autotune_batch(probs, variant=0, eps_abs=EPS, **kw)
         t0 = time.perf_counter()
         b = nq.QPBatch(probs, settings=tuned)
         fin = time.perf_counter() - t0
