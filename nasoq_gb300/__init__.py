@@ -317,6 +317,12 @@ class Plan:
     def solve_device(self, d_rhs_ptr, d_x_ptr):
         _check(lib().nqg_solve_device(self._h, C.c_void_p(d_rhs_ptr), C.c_void_p(d_x_ptr)), "solve")
 
+    def spmv_device(self, d_x_ptr, d_y_ptr):
+        """y = K x (original ordering, the values given at creation or by
+        set_values, without perturbation); device buffers of n doubles,
+        queued on the plan's stream."""
+        _check(lib().nqg_spmv_device(self._h, C.c_void_p(d_x_ptr), C.c_void_p(d_y_ptr)), "spmv")
+
     def set_stream(self, stream_ptr):
         _check(lib().nqg_set_stream(self._h, C.c_void_p(stream_ptr)), "set stream")
 

@@ -26,6 +26,7 @@ def lib():
         L = C.CDLL(_build.build())
         L.nqp_init.argtypes = [C.c_char_p]
         L.nqp_set_threads.argtypes = [C.c_int]
+        L.nqp_spmv.argtypes = [C.c_int] + [C.c_void_p] * 5
         L.nqp_solve.argtypes = [C.c_int] + [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 8 + \
             [C.c_int, C.c_int, C.c_double, C.c_double] + [C.c_void_p] * 7
         rc = L.nqp_init(openblas_path().encode())
@@ -41,6 +42,18 @@ def set_threads(t):
 
 def _p(a):
     return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def spmv(n, Ap, Ai, Ax, x):
+    """y = K x, K symmetric given by its lower triangle in CSC (the
+    reference's spmv_csc_sym_one_int, src/matrixVector/spmv_CSC.cpp:26-102,
+    with alpha = 1, beta = 0)."""
+    a = lambda v, t: np.ascontiguousarray(v, t)
+    Ap, Ai, Ax, x = a(Ap, np.int32), a(Ai, np.int32), a(Ax, np.float64), a(x, np.float64)
+    y = np.zeros(n)
+    if lib().nqp_spmv(int(n), _p(Ap), _p(Ai), _p(Ax), _p(x), _p(y)) != 0:
+        raise ValueError("oracle spmv: bad arguments")
+    return y
 
 
 def solve(n, Ap, Ai, Ax, Ax_ref, sym, rhs, req_ref_iter=2, max_inner_iter=2, tol_abs=1e-15, tol_rel=1e-15,

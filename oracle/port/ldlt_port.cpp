@@ -952,6 +952,16 @@ void nqp_set_threads(int t) {
   if (B.setthreads) B.setthreads(t);
 }
 
+// y = K x for K lower-stored symmetric CSC (n columns), the column sweep of
+// spmv_sym (alpha = 1, beta = 0).
+int nqp_spmv(int n, const int *Ap, const int *Ai, const double *Ax, const double *x, double *y) {
+  if (n < 0 || !Ap || (n > 0 && (!Ai || !Ax || !x || !y))) return -1;
+  std::vector<int> Kp(Ap, Ap + n + 1), Ki(Ai, Ai + Ap[n]);
+  std::vector<double> Kx(Ax, Ax + Ap[n]);
+  spmv_sym(n, Kp, Ki, Kx, x, y);
+  return 0;
+}
+
 // Factor (perturbed values Ax) + solve with refinement on Ax_ref.  Symbolic
 // arrays as produced by the analysis (perm, super, lpi, ls, colp, sparent,
 // col2sup).  Outputs x (original ordering) and, when non-NULL, the factor

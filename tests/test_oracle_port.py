@@ -44,6 +44,23 @@ def refine_matrix(d):
     return ax
 
 
+def test_port_spmv_is_the_symmetric_product():
+    """The oracle's SpMV (the reference's column sweep over the lower
+    triangle) equals the dense symmetric product on the smallest LBL fixture,
+    to the bound of a different summation order."""
+    path = min(CASES, key=os.path.getsize)
+    d = nqa.load(path)
+    n = len(d["in_rhs"])
+    Ap, Ai, Ax = d["in_Ap"], d["in_Ai"], d["in_Ax"]
+    cols = np.repeat(np.arange(n), np.diff(Ap))
+    M = np.zeros((n, n))
+    M[Ai, cols] = Ax
+    M[cols, Ai] = Ax
+    x = np.random.default_rng(1).standard_normal(n)
+    y = port.spmv(n, Ap, Ai, Ax, x)
+    assert np.all(np.abs(y - M @ x) <= n * 2.0 ** -52 * (np.abs(M) @ np.abs(x)))
+
+
 @pytest.mark.parametrize("path", CASES, ids=os.path.basename)
 def test_port_reproduces_reference_factor(path):
     port.set_threads(FIXTURE_BLAS_THREADS)
