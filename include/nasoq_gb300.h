@@ -307,7 +307,8 @@ typedef struct nqg_batch_stats {
 } nqg_batch_stats;
 
 typedef struct nqg_batch_info {
-  int nprob, npatterns, grid, threads, blocks_per_sm, pad;
+  int nprob, npatterns, grid, threads, blocks_per_sm;
+  int warp_factor;      /* 1: small supernodes factored a warp each, level by level */
   int64_t smem_bytes, slot_bytes;
   double last_ms;       /* device time of the last nqg_batch_solve */
 } nqg_batch_info;

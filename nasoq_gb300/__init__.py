@@ -88,7 +88,7 @@ class BatchStats(C.Structure):
 
 class BatchInfo(C.Structure):
     _fields_ = [("nprob", C.c_int), ("npatterns", C.c_int), ("grid", C.c_int), ("threads", C.c_int),
-                ("blocks_per_sm", C.c_int), ("pad", C.c_int), ("smem_bytes", C.c_int64), ("slot_bytes", C.c_int64),
+                ("blocks_per_sm", C.c_int), ("warp_factor", C.c_int), ("smem_bytes", C.c_int64), ("slot_bytes", C.c_int64),
                 ("last_ms", C.c_double)]
 
 

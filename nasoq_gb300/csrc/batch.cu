@@ -27,6 +27,7 @@
 //    them into shared memory in the factor's order.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 
@@ -41,6 +42,7 @@ namespace {
 // of 128 threads per SM.  (Capping it at 80 registers for 6 CTAs per SM was
 // measured slower: 7-12 % on cold and FP64 batches, +2 % on warm ones.)
 constexpr int BT_MAX_THREADS = 256;
+constexpr int WF_WARPS = 4;  // warps of the level-parallel factorization
 constexpr int MR_CAP = BATCH_MR_CAP;  // Krylov steps per restart held in shared memory
 
 template <class T> struct Ctx {
@@ -72,6 +74,12 @@ template <class T> struct Ctx {
   int *map;
   T *xs, *B, *rowbuf, *Dsm, *Esm, *Binv;
   int *lp;
+  // per-warp scratch of the level-parallel factorization (WF_WARPS warps):
+  // block wcap x rcap, D, E, local pivot order, Bunch-Kaufman multipliers
+  T *wB, *wD, *wE, *wwk;
+  int *wlp;
+  int wcap, rcap;  // widest / tallest supernode a warp takes (<= 32)
+  int wf;          // level-parallel factorization on
   uint8_t *vis;  // per supernode: visible (structural, or the column of an active constraint)
   uint8_t *act;  // per constraint: active
   int *vlvl;     // visible supernodes of each level: vlist[vlvl[l] .. vlvl[l+1]),
@@ -607,13 +615,213 @@ template <class T> __device__ void factor_sn(Ctx<T> &c, int s) {
   lap(PH_SN_STORE);
 }
 
+// ---- factorization of one supernode (warp scope) -----------------------------
+// The steps and the per-entry arithmetic of factor_sn for a supernode of at
+// most wcap columns and rcap rows (both <= 32), by warp wi in its own
+// scratch: target rows found by a search of the row list held one per lane,
+// descendant updates applied in list order (no atomics), the rows below
+// permuted in place along the cycles of the pivot order, and the inverse of
+// the unit L11 formed in the block's upper triangle (zero otherwise) before
+// it replaces L11.
+template <class T> __device__ void factor_sn_warp(Ctx<T> &c, int s, int wi) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = lane_id();
+  if (c.cyc && lane == 0) atomicAdd(&c.cyc[PH_SN], 1ull);
+  const int4 r0 = c.snrec[2 * s], r1 = c.snrec[2 * s + 1];
+  const int c0 = r0.x, w = r0.y, nr = r0.z;
+  const int *rows = c.ls + r1.x;
+  T *B = c.wB + (size_t)wi * c.wcap * c.rcap;
+  T *Dw = c.wD + wi * c.wcap, *Ew = c.wE + wi * c.wcap, *wk = c.wwk + wi * 64;
+  int *lpw = c.wlp + wi * c.wcap;
+  const int myrow = lane < nr ? rows[lane] : -1;
+  // position of row r in the row list, -1 when absent (every lane calls)
+  auto find = [&](int r) {
+    int pos = -1;
+    for (int k = 0; k < nr; ++k)
+      if (__shfl_sync(FULL, myrow, k) == r) pos = k;
+    return pos;
+  };
+  for (int e = lane; e < nr * w; e += 32) B[e] = T(0);
+  __syncwarp();
+  // matrix columns (entries of rows >= the column)
+  for (int m = 0; m < w; ++m) {
+    const int col = c0 + m, j = c.perm[col];
+    const int qb = c.Rp[j], qe = c.Rp[j + 1];
+    for (int q0 = qb; q0 < qe; q0 += 32) {
+      const int qq = q0 + lane;
+      const int oi = qq < qe ? c.iperm[c.Rj[qq]] : -1;
+      const int pos = find(oi);
+      if (qq < qe && oi >= col) {
+        if (pos < 0) atomicOr(c.status, ST_BOUNDS);  // not in the row list: corrupted structure
+        else B[pos + m * nr] = T(c.Fv[qq]);
+      }
+    }
+  }
+  __syncwarp();
+  // descendant updates (sub_update_warp's arithmetic, one pair after another)
+  for_visible_pairs(c, s, r1.y, r1.z, r1.w, [&](int pq) {
+    const int4 pr = c.prec[pq], d0 = c.snrec[2 * pr.x];
+    const int lb = pr.y, ub = pr.z;
+    const int cd = d0.x, wd = d0.y, nrd = d0.z;
+    const int *rd = c.ls + pr.w;
+    const T *Ld = c.L + d0.w;
+    const T *Dd = c.D + cd, *Ed = c.D + c.N + cd;
+    const int md = nrd - lb, nc = ub - lb + 1;
+    for (int i0 = 0; i0 < md; i0 += 32) {
+      const int i = i0 + lane;
+      const int ri = i < md ? rd[lb + i] : -1;
+      int ti = find(ri);
+      if (i < md && ti < 0) atomicOr(c.status, ST_BOUNDS);
+      for (int jj = 0; jj < nc; ++jj) {
+        const int tj = rd[lb + jj] - c0;
+        if (tj < 0 || tj >= w) {
+          if (lane == 0) atomicOr(c.status, ST_BOUNDS);
+          continue;
+        }
+        if (ti < tj) continue;  // lower triangle of the target only (and absent rows)
+        T acc = T(0);
+        for (int k = 0; k < wd; ++k) {
+          const T lik = Ld[lb + i + (size_t)k * nrd];
+          const T ek = Ed[k];
+          if (ek == T(0) || k + 1 >= wd) {
+            acc += lik * Dd[k] * Ld[lb + jj + (size_t)k * nrd];
+          } else {
+            const T ljk = Ld[lb + jj + (size_t)k * nrd], ljk1 = Ld[lb + jj + (size_t)(k + 1) * nrd];
+            const T lik1 = Ld[lb + i + (size_t)(k + 1) * nrd];
+            acc += lik * (Dd[k] * ljk + ek * ljk1) + lik1 * (ek * ljk + Dd[k + 1] * ljk1);
+            ++k;
+          }
+        }
+        B[ti + tj * nr] -= acc;
+      }
+    }
+    __syncwarp();
+  });
+  const bool pivoted = bk_factor_warp<T>(B, nr, w, Dw, Ew, lpw, c.status, wk);
+  // rows below: lane owns row r; new column j takes old column lpw[j]
+  // (cycles of the pivot order, in place), solve with the unit L11^T, scale
+  // by D^-1 (panel_rows_warp0's arithmetic)
+  for (int rb0 = w; rb0 < nr; rb0 += 32) {
+    const int r = rb0 + lane;
+    if (r < nr) {
+      T *br = B + r;
+      if (pivoted) {
+        unsigned done = 0u;
+        for (int j0 = 0; j0 < w; ++j0) {
+          if ((done >> j0) & 1u) continue;
+          const T first = br[(size_t)j0 * nr];
+          int j = j0;
+          for (int guard = 0; guard < w; ++guard) {
+            done |= 1u << j;
+            const int src = lpw[j];
+            if (src == j0 || src < 0 || src >= w) {
+              br[(size_t)j * nr] = first;
+              break;
+            }
+            br[(size_t)j * nr] = br[(size_t)src * nr];
+            j = src;
+          }
+        }
+      }
+      for (int j = 0; j < w; ++j) {
+        T x = br[(size_t)j * nr];
+        for (int t = 0; t < j; ++t) x -= br[(size_t)t * nr] * B[j + (size_t)t * nr];
+        br[(size_t)j * nr] = x;
+      }
+      for (int j = 0; j < w; ++j) {
+        if (Ew[j] == T(0) || j + 1 >= w) {
+          br[(size_t)j * nr] = br[(size_t)j * nr] * (T(1) / Dw[j]);
+        } else {
+          const T e = Ew[j];
+          const T inv = T(1) / (Dw[j] * Dw[j + 1] - e * e);
+          const T x1 = br[(size_t)j * nr], x2 = br[(size_t)(j + 1) * nr];
+          br[(size_t)j * nr] = (x1 * Dw[j + 1] - x2 * e) * inv;
+          br[(size_t)(j + 1) * nr] = (x2 * Dw[j] - x1 * e) * inv;
+          ++j;
+        }
+      }
+    }
+  }
+  __syncwarp();
+  // inverse of the unit L11: X(i, j), i > j, at B[j + i nr] (lane j owns row j
+  // of the upper triangle), then moved below the diagonal
+  if (lane < w) {
+    const int j = lane;
+    for (int i = j + 1; i < w; ++i) {
+      T acc = B[i + (size_t)j * nr];
+      for (int k = j + 1; k < i; ++k) acc += B[i + (size_t)k * nr] * B[j + (size_t)k * nr];
+      B[j + (size_t)i * nr] = -acc;
+    }
+  }
+  __syncwarp();
+  for (int e = lane; e < w * w; e += 32) {
+    const int i = e % w, j = e / w;
+    if (i > j) B[i + (size_t)j * nr] = B[j + (size_t)i * nr];
+  }
+  __syncwarp();
+  for (int e = lane; e < w * w; e += 32) {
+    const int i = e % w, j = e / w;
+    if (i > j) B[j + (size_t)i * nr] = T(0);
+  }
+  __syncwarp();
+  T *Ls = c.L + r0.w;
+  for (int e = lane; e < nr * w; e += 32) {
+    const T v = B[e];
+    if (!(v == v) || isinf((double)v)) atomicOr(c.status, ST_NONFINITE);
+    Ls[e] = v;
+  }
+  for (int m = lane; m < w; m += 32) {
+    c.D[c0 + m] = Dw[m];
+    c.D[c.N + c0 + m] = Ew[m];
+    c.lperm[c0 + m] = lpw[m];
+  }
+  if (lane == 0) c.piv[s] = pivoted ? 1 : 0;
+  __syncwarp();
+}
+
 // Factor the supernodes of mlist (ascending ids: children before parents,
 // the reference's order of mod_indices), then fold the pivots into the row
 // lists of the descendants (row_reordering, Sym_BLAS.cpp:327-490) and into
 // the ordering (reorder_matrix, linear_solver_wrapper.cpp:1432-1460).
+// Level-parallel form: supernodes of one level of the tree are independent
+// (each reads only descendants on lower levels and writes only itself), so
+// per level the first WF_WARPS warps take the ones that fit a warp, in turn
+// by their rank among the level's marked supernodes, and the CTA then
+// factors the rest of the level one at a time.
 template <class T> __device__ void factor_marked(Ctx<T> &c) {
   const int m = *c.nmark;
-  for (int t = 0; t < m; ++t) factor_sn(c, c.mlist[t]);
+  if (c.wf) {
+    const unsigned FULL = 0xffffffffu;
+    const int wi = warp_id(), lane = lane_id(), nwf = min(num_warps(), WF_WARPS);
+    auto fits = [&](int s) { return c.snrec[2 * s].y <= c.wcap && c.snrec[2 * s].z <= c.rcap; };
+    for (int l = 0; l < c.nlev; ++l) {
+      bool big = false;  // the level has supernodes for the CTA path (uniform over the CTA)
+      if (wi < nwf) {
+        int seen = 0;
+        for (int t0 = 0; t0 < m; t0 += 32) {
+          const int t = t0 + lane;
+          const int s = t < m ? c.mlist[t] : -1;
+          const bool at = s >= 0 && c.lev[s] == l;
+          const bool hit = at && fits(s);
+          big = big || __any_sync(FULL, at && !hit);
+          unsigned bal = __ballot_sync(FULL, hit);
+          while (bal) {
+            const int b = __ffs(bal) - 1;
+            bal &= bal - 1u;
+            const int sb = __shfl_sync(FULL, s, b);
+            if (seen++ % nwf == wi) factor_sn_warp(c, sb, wi);
+          }
+        }
+      }
+      if (__syncthreads_or(big ? 1 : 0))
+        for (int t = 0; t < m; ++t) {
+          const int s = c.mlist[t];
+          if (c.lev[s] == l && !fits(s)) factor_sn(c, s);
+        }
+    }
+  } else {
+    for (int t = 0; t < m; ++t) factor_sn(c, c.mlist[t]);
+  }
   BQ_T0(c);
   // renaming: rows of descendants that fall into a pivoted supernode
   for (int t = 0; t < m; ++t) {
@@ -1191,6 +1399,21 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
   sp += up16((size_t)a.ns_max);
   uint8_t *act = sp;
   sp += up16((size_t)a.mi_max);
+  const int wcap = min(a.w_max, 32), rcap = min(a.nr_max, 32);
+  T *wB = nullptr, *wD = nullptr, *wE = nullptr, *wwk = nullptr;
+  int *wlp = nullptr;
+  if (a.warp_factor) {
+    wB = reinterpret_cast<T *>(sp);
+    sp += up16((size_t)WF_WARPS * wcap * rcap * sizeof(T));
+    wD = reinterpret_cast<T *>(sp);
+    sp += up16((size_t)WF_WARPS * wcap * sizeof(T));
+    wE = reinterpret_cast<T *>(sp);
+    sp += up16((size_t)WF_WARPS * wcap * sizeof(T));
+    wlp = reinterpret_cast<int *>(sp);
+    sp += up16((size_t)WF_WARPS * wcap * sizeof(int));
+    wwk = reinterpret_cast<T *>(sp);
+    sp += up16((size_t)WF_WARPS * 64 * sizeof(T));
+  }
   unsigned char *stage = sp;  // the factor and row lists of a problem that fits
 
   unsigned char *const own_slot = a.slots + (size_t)blockIdx.x * a.slot.bytes;
@@ -1293,6 +1516,14 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
       c.Esm = Esm;
       c.Binv = Binv;
       c.lp = lp;
+      c.wB = wB;
+      c.wD = wD;
+      c.wE = wE;
+      c.wlp = wlp;
+      c.wwk = wwk;
+      c.wcap = wcap;
+      c.rcap = rcap;
+      c.wf = a.warp_factor ? 1 : 0;
       c.vis = vis;
       c.act = act;
       c.vlvl = vlvl;
@@ -1869,10 +2100,16 @@ int batch_ws_clear(int nprob, BProb *probs, cudaStream_t st) {
 
 size_t batch_smem_bytes(const BArgs &a, size_t tsize) {
   auto up = [](size_t b) { return (b + 15) / 16 * 16; };
+  size_t wf = 0;
+  if (a.warp_factor) {
+    const size_t wcap = (size_t)std::min(a.w_max, 32), rcap = (size_t)std::min(a.nr_max, 32);
+    wf = up(WF_WARPS * wcap * rcap * tsize) + 2 * up(WF_WARPS * wcap * tsize) + up(WF_WARPS * wcap * sizeof(int)) +
+         up((size_t)WF_WARPS * 64 * tsize);
+  }
   return up((size_t)a.N_max * sizeof(int)) + up((size_t)a.N_max * tsize) + up((size_t)a.nr_max * a.w_max * tsize) +
          up((size_t)a.w_max * 32 * tsize) + 2 * up((size_t)a.w_max * tsize) + up((size_t)a.w_max * sizeof(int)) +
          up((size_t)a.w_max * a.w_max * tsize) + 4 * up((size_t)(a.nlev_max + 1) * sizeof(int)) + up((size_t)a.ns_max) +
-         up((size_t)a.mi_max) + (size_t)a.stage_bytes;
+         up((size_t)a.mi_max) + wf + (size_t)a.stage_bytes;
 }
 
 // Raises the kernel's dynamic shared-memory limit to smem_attr (outside any

@@ -106,6 +106,7 @@ struct BArgs {
   int N_max, w_max, nr_max, ns_max, mi_max, nlev_max;  // shared-memory sizing
   unsigned long long *prof;  // per-phase SM cycles summed over CTAs, or null
   int stage_bytes;           // shared memory for the factor and row lists of problems that fit
+  int warp_factor;           // level-parallel factorization, a warp per supernode of <= 32 x 32
   // Problems with identical matrix values (same pattern, values,
   // regularization) share the factorization with every inequality hidden: a
   // launch with mode = 1 computes it once per group into `bases` (one slot

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <unordered_map>
@@ -756,8 +757,30 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
   base_args.mi_max = mi_max;
   base_args.nlev_max = nlev_max;
   base_args.stage_bytes = 0;
-  const size_t base_smem = nqg::batch_smem_bytes(base_args, ts);
   const size_t static_smem = 8 * 1024;  // the kernel's own __shared__ variables, rounded up
+  // Level-parallel factorization (a warp per supernode of at most 32 x 32)
+  // where its per-warp scratch keeps as many CTAs per SM as the layout
+  // without it; NASOQ_GB300_BATCH_WARP_FACTOR=0 / 1 turns it off / on.
+  {
+    const char *e = std::getenv("NASOQ_GB300_BATCH_WARP_FACTOR");
+    base_args.warp_factor = 0;
+    if (e && std::string(e) == "1") {
+      base_args.warp_factor = 1;
+    } else if (!(e && std::string(e) == "0")) {
+      nqg::BArgs with = base_args;
+      with.warp_factor = 1;
+      const size_t s0 = nqg::batch_smem_bytes(base_args, ts), s1 = nqg::batch_smem_bytes(with, ts);
+      auto occ = [&](size_t sm, int *bps) {
+        return b->set.qp.precision == NQG_FP32 ? nqg::batch_prepare<float>(b->threads, sm, sm, bps)
+                                               : nqg::batch_prepare<double>(b->threads, sm, sm, bps);
+      };
+      int b0 = 0, b1 = 0;
+      if ((int64_t)s1 + (int64_t)static_smem <= smem_optin && occ(s0, &b0) == NQG_OK && occ(s1, &b1) == NQG_OK &&
+          b1 > 0 && b1 >= b0)
+        base_args.warp_factor = 1;
+    }
+  }
+  const size_t base_smem = nqg::batch_smem_bytes(base_args, ts);
   if ((int64_t)base_smem + (int64_t)static_smem > smem_optin)
     return fail(b, NQG_ERR_SIZE, "largest pattern exceeds the batched solver's shared memory");
   const int64_t stage_max = smem_optin - (int64_t)base_smem - (int64_t)static_smem;
@@ -1106,6 +1129,7 @@ extern "C" int nqg_batch_get_info(const nqg_batch *b, nqg_batch_info *info) {
   info->grid = b->grid;
   info->threads = b->threads;
   info->blocks_per_sm = b->blocks_per_sm;
+  info->warp_factor = b->tiers.empty() ? 0 : b->tiers.front().args.warp_factor;
   info->smem_bytes = (int64_t)b->smem;
   info->slot_bytes = b->args.slot.bytes;
   info->last_ms = b->last_ms;

@@ -73,9 +73,17 @@ def _run(d, qps, **kw):
 
 
 @pytest.mark.gpu
-def test_batch_fp64_matches_reference():
+@pytest.mark.parametrize("factor_path", ["auto", "warp", "cta"])
+def test_batch_fp64_matches_reference(factor_path, monkeypatch):
+    """The reference's status, iteration count, active set and solution for
+    every problem of the batch fixture, with the supernodes factored by the
+    launch's choice, level by level a warp each, or one at a time by the CTA."""
+    if factor_path != "auto":
+        monkeypatch.setenv("NASOQ_GB300_BATCH_WARP_FACTOR", "1" if factor_path == "warp" else "0")
     d, qps = fixture()
     b = _run(d, qps, precision=nq.NQG_FP64, refine=0)
+    if factor_path != "auto":
+        assert b.info().warp_factor == (1 if factor_path == "warp" else 0)
     eps = float(d["set_eps_abs"][0])
     assert b.info().npatterns < len(qps)  # the parametric instances share one pattern
     for i in range(len(qps)):
@@ -94,7 +102,10 @@ def test_batch_fp64_matches_reference():
 
 
 @pytest.mark.gpu
-def test_batch_mixed_precision_meets_tolerance(record_property):
+@pytest.mark.parametrize("factor_path", ["auto", "warp", "cta"])
+def test_batch_mixed_precision_meets_tolerance(factor_path, record_property, monkeypatch):
+    if factor_path != "auto":
+        monkeypatch.setenv("NASOQ_GB300_BATCH_WARP_FACTOR", "1" if factor_path == "warp" else "0")
     d, qps = fixture()
     b = _run(d, qps, precision=nq.NQG_FP32, refine=1, refine_tol=1e-12)
     eps = float(d["set_eps_abs"][0])
