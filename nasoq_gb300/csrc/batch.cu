@@ -785,9 +785,10 @@ template <class T> __device__ void factor_sn_warp(Ctx<T> &c, int s, int wi) {
 // the ordering (reorder_matrix, linear_solver_wrapper.cpp:1432-1460).
 // Level-parallel form: supernodes of one level of the tree are independent
 // (each reads only descendants on lower levels and writes only itself), so
-// per level the first WF_WARPS warps take the ones that fit a warp, in turn
-// by their rank among the level's marked supernodes, and the CTA then
-// factors the rest of the level one at a time.
+// per level with at least two marked supernodes that fit a warp, the first
+// WF_WARPS warps take those in turn by their rank among the level's marked
+// supernodes; the CTA factors the rest one at a time (the ones that do not
+// fit, and a level's single one, which the CTA path spreads over all warps).
 template <class T> __device__ void factor_marked(Ctx<T> &c) {
   const int m = *c.nmark;
   if (c.wf) {
@@ -795,16 +796,23 @@ template <class T> __device__ void factor_marked(Ctx<T> &c) {
     const int wi = warp_id(), lane = lane_id(), nwf = min(num_warps(), WF_WARPS);
     auto fits = [&](int s) { return c.snrec[2 * s].y <= c.wcap && c.snrec[2 * s].z <= c.rcap; };
     for (int l = 0; l < c.nlev; ++l) {
-      bool big = false;  // the level has supernodes for the CTA path (uniform over the CTA)
-      if (wi < nwf) {
+      // every warp counts the level's supernodes the same way (uniform over the CTA)
+      int nfit = 0;
+      bool big = false;
+      for (int t0 = 0; t0 < m; t0 += 32) {
+        const int t = t0 + lane;
+        const int s = t < m ? c.mlist[t] : -1;
+        const bool at = s >= 0 && c.lev[s] == l;
+        nfit += __popc(__ballot_sync(FULL, at && fits(s)));
+        big = big || __any_sync(FULL, at && !fits(s));
+      }
+      const bool warps = nfit >= 2;
+      if (warps && wi < nwf) {
         int seen = 0;
         for (int t0 = 0; t0 < m; t0 += 32) {
           const int t = t0 + lane;
           const int s = t < m ? c.mlist[t] : -1;
-          const bool at = s >= 0 && c.lev[s] == l;
-          const bool hit = at && fits(s);
-          big = big || __any_sync(FULL, at && !hit);
-          unsigned bal = __ballot_sync(FULL, hit);
+          unsigned bal = __ballot_sync(FULL, s >= 0 && c.lev[s] == l && fits(s));
           while (bal) {
             const int b = __ffs(bal) - 1;
             bal &= bal - 1u;
@@ -813,10 +821,11 @@ template <class T> __device__ void factor_marked(Ctx<T> &c) {
           }
         }
       }
-      if (__syncthreads_or(big ? 1 : 0))
+      if (warps) __syncthreads();
+      if (big || (!warps && nfit > 0))
         for (int t = 0; t < m; ++t) {
           const int s = c.mlist[t];
-          if (c.lev[s] == l && !fits(s)) factor_sn(c, s);
+          if (c.lev[s] == l && (!warps || !fits(s))) factor_sn(c, s);
         }
     }
   } else {
