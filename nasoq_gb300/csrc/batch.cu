@@ -785,13 +785,15 @@ template <class T> __device__ void factor_sn_warp(Ctx<T> &c, int s, int wi) {
 // the ordering (reorder_matrix, linear_solver_wrapper.cpp:1432-1460).
 // Level-parallel form: supernodes of one level of the tree are independent
 // (each reads only descendants on lower levels and writes only itself), so
-// per level with at least two marked supernodes that fit a warp, the first
-// WF_WARPS warps take those in turn by their rank among the level's marked
-// supernodes; the CTA factors the rest one at a time (the ones that do not
-// fit, and a level's single one, which the CTA path spreads over all warps).
+// per level the first WF_WARPS warps take the marked supernodes that fit a
+// warp, in turn by their rank among the level's marked supernodes, and the
+// CTA factors the rest one at a time.  A refactorization of one or two paths
+// to the root (at most 2 nlev supernodes, the active-set iterations) keeps
+// the CTA path throughout: its supernodes are the widest, with the most
+// descendant updates, which the CTA path spreads over every warp.
 template <class T> __device__ void factor_marked(Ctx<T> &c) {
   const int m = *c.nmark;
-  if (c.wf) {
+  if (c.wf && m > 2 * c.nlev) {
     const unsigned FULL = 0xffffffffu;
     const int wi = warp_id(), lane = lane_id(), nwf = min(num_warps(), WF_WARPS);
     auto fits = [&](int s) { return c.snrec[2 * s].y <= c.wcap && c.snrec[2 * s].z <= c.rcap; };
@@ -806,8 +808,7 @@ template <class T> __device__ void factor_marked(Ctx<T> &c) {
         nfit += __popc(__ballot_sync(FULL, at && fits(s)));
         big = big || __any_sync(FULL, at && !fits(s));
       }
-      const bool warps = nfit >= 2;
-      if (warps && wi < nwf) {
+      if (nfit > 0 && wi < nwf) {
         int seen = 0;
         for (int t0 = 0; t0 < m; t0 += 32) {
           const int t = t0 + lane;
@@ -821,11 +822,11 @@ template <class T> __device__ void factor_marked(Ctx<T> &c) {
           }
         }
       }
-      if (warps) __syncthreads();
-      if (big || (!warps && nfit > 0))
+      if (nfit > 0) __syncthreads();
+      if (big)
         for (int t = 0; t < m; ++t) {
           const int s = c.mlist[t];
-          if (c.lev[s] == l && (!warps || !fits(s))) factor_sn(c, s);
+          if (c.lev[s] == l && !fits(s)) factor_sn(c, s);
         }
     }
   } else {
