@@ -759,14 +759,15 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
   base_args.stage_bytes = 0;
   const size_t static_smem = 8 * 1024;  // the kernel's own __shared__ variables, rounded up
   // Level-parallel factorization (a warp per supernode of at most 32 x 32)
-  // where its per-warp scratch keeps as many CTAs per SM as the layout
-  // without it; NASOQ_GB300_BATCH_WARP_FACTOR=0 / 1 turns it off / on.
+  // for FP32 factors where its per-warp scratch keeps as many CTAs per SM as
+  // the layout without it (FP64 factors measured faster on the CTA path);
+  // NASOQ_GB300_BATCH_WARP_FACTOR=0 / 1 turns it off / on.
   {
     const char *e = std::getenv("NASOQ_GB300_BATCH_WARP_FACTOR");
     base_args.warp_factor = 0;
     if (e && std::string(e) == "1") {
       base_args.warp_factor = 1;
-    } else if (!(e && std::string(e) == "0")) {
+    } else if (!(e && std::string(e) == "0") && b->set.qp.precision == NQG_FP32) {
       nqg::BArgs with = base_args;
       with.warp_factor = 1;
       const size_t s0 = nqg::batch_smem_bytes(base_args, ts), s1 = nqg::batch_smem_bytes(with, ts);
