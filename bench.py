@@ -61,7 +61,7 @@ CPU_SAMPLE_PER_PROC = 48
 # DRAM bytes (read + write) of one batch-kernel launch on this workload, from
 # an ncu capture of the measured step of --profile-once (4096 QPs):
 # profiles/dram_k_nasoq_batch_mpc50_warm4096.md
-NCU_BATCH_TRAFFIC = 4_458_161_664 + 3_448_829_184
+NCU_BATCH_TRAFFIC = 3_725_971_200 + 2_870_434_304
 # LBL section: K = [H A^T; A -1e-8 I], H 3D 7-point Laplacian on 64^3, A 20000 x n, 6 N(0,1) per row
 GRID, MCON, PER_ROW, DELTA, SEED = 64, 20000, 6, 1e-8, 0
 TARGET_RELRES = 1e-10
