@@ -325,6 +325,12 @@ int nqg_batch_add(nqg_batch *b, int n, const int *Hp, const int *Hi, const doubl
 int nqg_batch_finalize(nqg_batch *b);
 /* New q / a / b of every problem, concatenated in problem order (NULL: unchanged). */
 int nqg_batch_set_vectors(nqg_batch *b, const double *q_all, const double *a_all, const double *b_all);
+/* The same, enqueued on the batch's stream without waiting: ordered before
+ * the next solve on that stream.  Arrays in page-locked memory are copied
+ * asynchronously and must stay unchanged until the stream has passed the
+ * copies (e.g. until the next nqg_batch_get_all); pageable arrays are staged
+ * before the call returns. */
+int nqg_batch_set_vectors_async(nqg_batch *b, const double *q_all, const double *a_all, const double *b_all);
 /* Proposed active set of problem i for the next solve (n_as < 0: cold start).
  * The solve factors the KKT system with these constraints active, drops the
  * ones whose multipliers come out negative (up to three rounds, then a cold
@@ -381,6 +387,9 @@ int nqg_mlp_num_params(const nqg_mlp *m, long *n_weights, long *n_biases);
 int nqg_mlp_set_weights(nqg_mlp *m, const float *w_all, const float *b_all);
 int nqg_mlp_get_weights(nqg_mlp *m, float *w_all, float *b_all);
 int nqg_mlp_forward(nqg_mlp *m, int rows, const float *x, float *logits);
+/* Device buffers, enqueued on `stream` (NULL: the model's own stream, and the
+ * call waits).  The model's activation buffers serve every call: forwards of
+ * one model on different streams must not overlap (use one model per stream). */
 int nqg_mlp_forward_device(nqg_mlp *m, int rows, const float *d_x, float *d_logits, void *stream);
 int nqg_mlp_loss_grad(nqg_mlp *m, int rows, const float *x, const float *y, float pos_weight, double *loss,
                       float *gw_all, float *gb_all);

@@ -147,6 +147,7 @@ def lib():
         [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 4
     L.nqg_batch_finalize.argtypes = [C.c_void_p]
     L.nqg_batch_set_vectors.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.nqg_batch_set_vectors_async.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.nqg_batch_set_warm_start.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
     L.nqg_batch_solve.argtypes = [C.c_void_p]
     L.nqg_batch_solve_async.argtypes = [C.c_void_p]
@@ -518,6 +519,18 @@ class QPBatch:
         conv = lambda a: None if a is None else np.ascontiguousarray(a, np.float64)
         q_all, b_all, d_all = conv(q_all), conv(b_all), conv(d_all)
         self._raise(lib().nqg_batch_set_vectors(self._h, _ptr(q_all), _ptr(b_all), _ptr(d_all)), "set vectors")
+
+    def set_vectors_async(self, q_all=None, b_all=None, d_all=None):
+        """set_vectors enqueued on the batch's stream without waiting.  Arrays
+        in page-locked memory (e.g. numpy views of pinned torch tensors) are
+        copied asynchronously: keep them unchanged until the stream has passed
+        the copies (results() synchronizes it).  The arrays are referenced
+        until then."""
+        conv = lambda a: None if a is None else np.ascontiguousarray(a, np.float64)
+        q_all, b_all, d_all = conv(q_all), conv(b_all), conv(d_all)
+        self._pending = (q_all, b_all, d_all)
+        self._raise(lib().nqg_batch_set_vectors_async(self._h, _ptr(q_all), _ptr(b_all), _ptr(d_all)),
+                    "set vectors")
 
     def set_warm_start(self, i, active_set):
         """Proposed active set of problem i (None: cold start)."""

@@ -343,6 +343,7 @@ struct nqg_batch {
   // staging of set_vectors: stacked q / b / d and their offsets per problem
   double *d_vstage = nullptr;
   int64_t *d_voff = nullptr;
+  std::vector<int64_t> h_voff;  // segment offsets of the last nqg_batch_set_vectors
   int64_t n_vstage = 0;
   cudaGraphExec_t gexec = nullptr;
   cudaGraph_t graph = nullptr;
@@ -916,12 +917,13 @@ extern "C" int nqg_batch_finalize(nqg_batch *b) {
   return NQG_OK;
 }
 
-extern "C" int nqg_batch_set_vectors(nqg_batch *b, const double *q_all, const double *beq_all,
-                                     const double *d_all) {
-  // New q / b / d for every problem, concatenated in problem order (any may
-  // be NULL: unchanged).
-  // One copy per given vector into a staging buffer, then one kernel
-  // scatters every problem's segment into the value pool.
+// New q / b / d for every problem, concatenated in problem order (any may be
+// NULL: unchanged).  One copy per given vector into a staging buffer, then
+// one kernel scatters every problem's segment into the value pool, both on
+// the batch's stream; `sync` waits for them and keeps the host copies of the
+// vectors current (nothing reads those after finalize).
+static int set_vectors_impl(nqg_batch *b, const double *q_all, const double *beq_all, const double *d_all,
+                            bool sync) {
   if (!b || !b->finalized) return NQG_ERR_STATE;
   const int np = (int)b->qp.size();
   int64_t tq = 0, tb = 0, td = 0;
@@ -935,20 +937,23 @@ extern "C" int nqg_batch_set_vectors(nqg_batch *b, const double *q_all, const do
     BQ_CUDA(cudaMalloc(&b->d_vstage, std::max<int64_t>(b->n_vstage, 1) * sizeof(double)));
     BQ_CUDA(cudaMalloc(&b->d_voff, (size_t)np * 3 * sizeof(int64_t)));
   }
-  std::vector<int64_t> off((size_t)np * 3, -1);
+  // segment offsets of every problem (-1: vector not given), kept in the
+  // batch so that an asynchronous copy of them never reads freed memory
+  std::vector<int64_t> &off = b->h_voff;
+  off.assign((size_t)np * 3, -1);
   int64_t oq = 0, ob = tq, odd = tq + tb;
   for (int i = 0; i < np; ++i) {
     HostQP &Q = b->qp[i];
     if (q_all) {
-      std::copy(q_all + oq, q_all + oq + Q.n, Q.q.begin());
+      if (sync) std::copy(q_all + oq, q_all + oq + Q.n, Q.q.begin());
       off[3 * i] = oq;
     }
     if (beq_all) {
-      std::copy(beq_all + (ob - tq), beq_all + (ob - tq) + Q.meq, Q.b.begin());
+      if (sync) std::copy(beq_all + (ob - tq), beq_all + (ob - tq) + Q.meq, Q.b.begin());
       off[3 * i + 1] = ob;
     }
     if (d_all) {
-      std::copy(d_all + (odd - tq - tb), d_all + (odd - tq - tb) + Q.mineq, Q.d.begin());
+      if (sync) std::copy(d_all + (odd - tq - tb), d_all + (odd - tq - tb) + Q.mineq, Q.d.begin());
       off[3 * i + 2] = odd;
     }
     oq += Q.n;
@@ -964,8 +969,18 @@ extern "C" int nqg_batch_set_vectors(nqg_batch *b, const double *q_all, const do
   BQ_CUDA(cudaMemcpyAsync(b->d_voff, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, b->stream));
   const int rc = nqg::batch_scatter_vectors(np, b->d_probs, b->d_pats, b->d_voff, b->d_vstage, b->d_dpool, b->stream);
   if (rc) return fail(b, rc, "vector scatter failed");
-  BQ_CUDA(cudaStreamSynchronize(b->stream));
+  if (sync) BQ_CUDA(cudaStreamSynchronize(b->stream));
   return NQG_OK;
+}
+
+extern "C" int nqg_batch_set_vectors(nqg_batch *b, const double *q_all, const double *beq_all,
+                                     const double *d_all) {
+  return set_vectors_impl(b, q_all, beq_all, d_all, true);
+}
+
+extern "C" int nqg_batch_set_vectors_async(nqg_batch *b, const double *q_all, const double *beq_all,
+                                           const double *d_all) {
+  return set_vectors_impl(b, q_all, beq_all, d_all, false);
 }
 
 extern "C" int nqg_batch_set_warm_start(nqg_batch *b, int i, int n_as, const int *as) {

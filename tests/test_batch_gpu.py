@@ -170,6 +170,37 @@ def test_batch_warm_start_from_solution():
 
 
 @pytest.mark.gpu
+def test_batch_set_vectors_async_matches_sync():
+    """New vectors enqueued without waiting, from page-locked arrays, and an
+    asynchronous solve give the synchronous update's results: every problem
+    Optimal, x and z within rounding of the summation order."""
+    torch = pytest.importorskip("torch")
+    fam = P.mpc_parametric(0)
+    thetas = np.random.default_rng(5).standard_normal((64, fam.P.shape[1]))
+    base = fam.base
+    one = (base.H, base.q, base.A, base.b, base.C, base.d)
+    b = nq.QPBatch([one] * len(thetas), settings=nq.batch_settings(variant=0, eps_abs=1e-8, precision=nq.NQG_FP32,
+                                                                    refine=1, refine_tol=1e-10))
+    q = thetas @ fam.P.T
+    d = fam.d0[None, :] + thetas @ fam.S.T
+    b.set_vectors(q_all=q.ravel(), d_all=d.ravel())
+    b.solve()
+    x0, _, z0, s0 = b.results()
+    b.set_vectors(q_all=(2.0 * q).ravel(), d_all=d.ravel())  # other vectors in between
+    b.solve()
+    qp = torch.empty(q.shape, dtype=torch.float64, pin_memory=True).numpy()
+    dp = torch.empty(d.shape, dtype=torch.float64, pin_memory=True).numpy()
+    qp[:] = q
+    dp[:] = d
+    b.set_vectors_async(q_all=qp.reshape(-1), d_all=dp.reshape(-1))
+    b.solve_async()
+    x1, _, z1, s1 = b.results()
+    assert all(a.status == 1 and c.status == 1 for a, c in zip(s0, s1))
+    assert rel(x1, x0) <= 1e-8 and rel(z1, z0) <= 1e-8
+    b.close()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("precision", [nq.NQG_FP64, nq.NQG_FP32])
 def test_shared_factorization_matches_private(precision):
     """Problems with identical matrices start from one shared factorization
