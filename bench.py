@@ -349,7 +349,12 @@ def qp_section(args, world, rank, local, torch, nq, P, learn, pk, pk_src):
     pipe_ms, (_, _, _, pipe_stats) = pipelined(list(range(kp)))
     pipe_ok = sum(1 for s_ in pipe_stats if s_.status == 1)
     e2e_value = BATCH * kp / (pipe_ms / 1e3) * world
+    # page-locked buffers go before the second batch's stream: torch's host
+    # allocator records the streams a buffer was copied on
+    torch.cuda.synchronize()
+    slots.clear()
     batch2.close()
+    del ws2, model2
     th_last = thetas_for(args.steps - 1, rank)
     warm_it = np.array([s.num_iter for s in warm_stats])
     warm_ok = np.mean([s.status == 1 for s in warm_stats])

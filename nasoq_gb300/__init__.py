@@ -605,6 +605,7 @@ class QPBatch:
         return i
 
     def close(self):
+        self._pending = None
         if getattr(self, "_h", None):
             lib().nqg_batch_destroy(self._h)
             self._h = None
