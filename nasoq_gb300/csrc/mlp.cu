@@ -2,7 +2,7 @@
 // theta -> one logit per inequality constraint (positive: predicted active at
 // the optimum), whose prediction seeds the batched NASOQ solve as a warm start
 // (nqg_batch_warm_start_from_scores); the active-set iteration then corrects
-// it and remains the judge of the final tolerance.  The reference has no
+// it and alone decides whether the final tolerance is met.  The reference has no
 // learned component; its warm-start entry is Nasoq::set_warm_start
 // (src/nasoq.cpp:413-436).
 //
