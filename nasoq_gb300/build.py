@@ -14,6 +14,7 @@ import concurrent.futures as cf
 import glob
 import os
 import platform
+import re
 import shutil
 import subprocess
 import sys
@@ -51,11 +52,19 @@ def sources():
     return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
+def _deps(src):
+    """Files an object depends on: its source, every header of the package
+    and of include/, and the .cu files it includes (batch_fp64.cu)."""
+    deps = [src] + glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.hpp")) \
+        + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(ROOT, "include", "**", "*.h"), recursive=True)
+    with open(src) as f:
+        deps += [os.path.join(CSRC, m) for m in re.findall(r'#include "([^"/]+\.cu)"', f.read())]
+    return deps
+
+
 def _compile(nvcc, src, flags, clean=False):
     obj = os.path.join(OBJ, os.path.basename(src) + ".o")
-    if not clean and os.path.exists(obj) and os.path.getmtime(obj) >= max(
-            [os.path.getmtime(src)] + [os.path.getmtime(h) for h in glob.glob(os.path.join(CSRC, "*.h*"))]
-            + [os.path.getmtime(h) for h in glob.glob(os.path.join(ROOT, "include", "**", "*.h"), recursive=True)]):
+    if not clean and os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in _deps(src)):
         return obj
     lang = ["-x", "cu"] if src.endswith(".cu") else ["-x", "c++"]
     cmd = [nvcc] + lang + flags + ["-c", src, "-o", obj]

@@ -2017,7 +2017,10 @@ __global__ void __launch_bounds__(BT_MAX_THREADS) k_nasoq_batch(BArgs a) {
   if (a.prof && tid < PH_N) atomicAdd(a.prof + tid, s_cyc[tid]);
 }
 
-
+// batch_fp64.cu compiles this file again with NQG_BATCH_FP64_UNIT defined for
+// the FP64 instantiation alone (the two instantiations then build in
+// parallel); the non-template kernels and host functions belong to this unit.
+#ifndef NQG_BATCH_FP64_UNIT
 
 // Warm-start sets from per-constraint scores (e.g. the logits of the active-set
 // model): problem i proposes every constraint k with scores[i * ld + k] >
@@ -2122,6 +2125,8 @@ size_t batch_smem_bytes(const BArgs &a, size_t tsize) {
          up((size_t)a.mi_max) + wf + (size_t)a.stage_bytes;
 }
 
+#endif  // NQG_BATCH_FP64_UNIT
+
 // Raises the kernel's dynamic shared-memory limit to smem_attr (outside any
 // stream capture) and returns how many CTAs of `smem` bytes fit on an SM.
 template <class T> int batch_prepare(int threads, size_t smem_attr, size_t smem, int *blocks_per_sm) {
@@ -2138,9 +2143,12 @@ template <class T> int launch_batch(const BArgs &a, int grid, int threads, size_
   return cudaGetLastError() == cudaSuccess ? NQG_OK : NQG_ERR_CUDA;
 }
 
+#ifdef NQG_BATCH_FP64_UNIT
 template int launch_batch<double>(const BArgs &, int, int, size_t, cudaStream_t);
-template int launch_batch<float>(const BArgs &, int, int, size_t, cudaStream_t);
 template int batch_prepare<double>(int, size_t, size_t, int *);
+#else
+template int launch_batch<float>(const BArgs &, int, int, size_t, cudaStream_t);
 template int batch_prepare<float>(int, size_t, size_t, int *);
+#endif
 
 }  // namespace nqg
