@@ -58,3 +58,15 @@ def test_invalid_arguments_rejected():
     rc = L.nqg_symbolic_create(2, Ap, Ai, None, None, None, ctypes.byref(h))
     assert rc == 0
     L.nqg_symbolic_destroy(h)
+
+
+def test_build_tracks_included_units_and_headers():
+    """The incremental build recompiles an object when a header (.h, .hpp,
+    .cuh) or a .cu file it includes changes: batch_fp64.cu compiles batch.cu
+    again for the FP64 instantiation."""
+    from nasoq_gb300 import build
+    csrc = os.path.join(ROOT, "nasoq_gb300", "csrc")
+    deps = {os.path.basename(d) for d in build._deps(os.path.join(csrc, "batch_fp64.cu"))}
+    assert {"batch_fp64.cu", "batch.cu", "batch.hpp", "bk.cuh", "tcgen05.cuh", "nasoq_gb300.h"} <= deps
+    srcs = {os.path.basename(s) for s in build.sources()}
+    assert {"batch.cu", "batch_fp64.cu"} <= srcs
